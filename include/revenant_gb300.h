@@ -1,0 +1,422 @@
+/*
+ * revenant_gb300.h — the C ABI of the GB300 receive chain.
+ *
+ * This library stands in for the reference's Vulkan operator surface on the
+ * receive path: core/gpu (Context, Buffer, ComputePipeline + record_dispatch)
+ * together with the hot-path shaders in core/shaders. Every launch takes the
+ * same parameter structs the reference's shaders take as push and
+ * specialisation constants, byte for byte, so a caller that builds a
+ * PfbBranchParams / VrxFineParams / ... for the reference can hand the same
+ * bytes here. Host-side planning (prototype and table design, receiver
+ * placement, plan_vrx, per-block parameter derivation) is exported too, so a
+ * caller without the reference's core/dsp can drive the chain.
+ *
+ * Conventions (mirroring core/error.h and core/plugin/engine_plugin_abi.h):
+ *   - every entry point returns int32: RV_OK (0) or a negative RV_ERR_*;
+ *   - the message for the most recent failure on the calling thread is
+ *     returned by rv_last_error();
+ *   - no C++ exception crosses this boundary;
+ *   - pointers named *_dev are CUDA device pointers, all other pointers are
+ *     host pointers; lengths are ELEMENT counts of the pointed-to type;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default);
+ *   - launches are asynchronous on `stream` and never allocate; parameters
+ *     are validated on the host before the launch, with the same rules as the
+ *     reference's validate() twins, and a rejected launch enqueues nothing.
+ */
+#ifndef REVENANT_GB300_H
+#define REVENANT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (core/error.h Status / Error{message, code}) ---------- */
+#define RV_OK 0
+#define RV_ERR_INVALID (-1)     /* parameters rejected by host validation   */
+#define RV_ERR_CUDA (-2)        /* a CUDA runtime call failed               */
+#define RV_ERR_NO_DEVICE (-3)   /* no usable sm_103 device                  */
+#define RV_ERR_NO_MEMORY (-4)   /* allocation failed                        */
+#define RV_ERR_UNSUPPORTED (-5) /* shape outside what this build implements */
+#define RV_ERR_TIMEOUT (-6)     /* a bounded device wait gave up            */
+
+/* Message for the most recent failure on this thread ("" if none). The
+ * pointer stays valid until the next failing call on the same thread. */
+const char* rv_last_error(void);
+
+/* Library version; bumps on any ABI change. */
+#define RV_ABI_VERSION 1
+int32_t rv_abi_version(void);
+
+/* ---- value types ------------------------------------------------------- */
+
+/* std::complex<float> / std430 vec2 (core/dsp/types.h:40-45). */
+typedef struct rv_cf32 {
+    float re;
+    float im;
+} rv_cf32;
+
+/* core/dsp/convert.h:116-143 ConvertParams: four packed uint32. */
+typedef struct rv_convert_params {
+    uint32_t ring_mask;
+    uint32_t dst_offset;
+    uint32_t src_offset; /* in SAMPLES, not bytes */
+    uint32_t count;
+} rv_convert_params;
+
+/* core/dsp/pfb.h:32-71 GridParams (M, L+1, D). */
+typedef struct rv_grid_params {
+    uint32_t channels;
+    uint32_t taps_per_branch;
+    uint32_t decimation;
+} rv_grid_params;
+
+/* core/dsp/pfb_branch_reference.h:28-53 PfbBranchParams. */
+typedef struct rv_pfb_branch_params {
+    uint32_t ring_mask;
+    uint32_t base_offset;
+    uint32_t block_count;
+} rv_pfb_branch_params;
+
+/* core/dsp/pfb_fft_reference.h:36-69 PfbFftParams: the FFT kernel's three
+ * specialisation constants (M, D, log2 M) then its four push constants. */
+typedef struct rv_pfb_fft_params {
+    uint32_t channels;
+    uint32_t decimation;
+    uint32_t stages;
+    uint32_t block_base;
+    uint32_t block_count;
+    uint32_t out_ring_blocks;
+    uint32_t out_ring_mask;
+} rv_pfb_fft_params;
+
+/* core/dsp/spectrum_reference.h SpectrumParams (spec M, N, log2 N; push
+ * chan_blocks, chan_mask, in_offset). */
+typedef struct rv_spectrum_params {
+    uint32_t channels;
+    uint32_t transform;
+    uint32_t stages;
+    uint32_t chan_blocks;
+    uint32_t chan_mask;
+    uint32_t in_offset;
+} rv_spectrum_params;
+
+/* core/dsp/spectrum_levels_reference.h SpectrumLevelsParams. */
+typedef struct rv_spectrum_levels_params {
+    uint32_t bins;
+    uint32_t low_permille;
+    uint32_t high_permille;
+} rv_spectrum_levels_params;
+
+/* core/dsp/vrx_reference.h VrxFineConfig (spec T, P, nco_log2). */
+typedef struct rv_vrx_fine_config {
+    uint32_t taps;
+    uint32_t phases;
+    uint32_t nco_log2;
+} rv_vrx_fine_config;
+
+/* core/dsp/vrx_reference.h:232-271 VrxFineParams: fifteen 32-bit words. */
+typedef struct rv_vrx_fine_params {
+    uint32_t chan_base;
+    uint32_t chan_mask;
+    uint32_t in_offset;
+    uint32_t out_offset;
+    uint32_t out_mask;
+    uint32_t count;
+    uint32_t step_whole;
+    uint32_t step_rem;
+    uint32_t out_rate;
+    uint32_t frac0;
+    uint32_t nco_phase_high;
+    uint32_t nco_phase_low;
+    uint32_t nco_delta_high;
+    uint32_t nco_delta_low;
+    float inv_out_rate;
+} rv_vrx_fine_params;
+
+/* Demodulator modes: engine::Demod (core/engine/vrx.h) numbering. */
+#define RV_DEMOD_RAW 0
+#define RV_DEMOD_AM 1
+#define RV_DEMOD_NFM 2
+#define RV_DEMOD_WFM 3
+#define RV_DEMOD_USB 4
+#define RV_DEMOD_LSB 5
+#define RV_DEMOD_DSB 6
+#define RV_DEMOD_CW 7
+#define RV_DEMOD_P25P1 8
+#define RV_DEMOD_DSTAR 9
+#define RV_DEMOD_TETRA 10
+#define RV_DEMOD_DMR 11
+#define RV_DEMOD_SAM 12
+
+/* core/dsp/vrx_reference.h VrxDemodConfig (the demod kernel's seven
+ * specialisation constants minus channel_power). */
+typedef struct rv_vrx_demod_config {
+    uint32_t mode;
+    uint32_t decimation;
+    uint32_t audio_taps;
+    uint32_t dc_taps;
+    uint32_t channels;
+    uint32_t pilot_taps;
+} rv_vrx_demod_config;
+
+/* core/dsp/vrx_reference.h:584 VrxDemodParams: four 32-bit words. */
+typedef struct rv_vrx_demod_params {
+    uint32_t in_mask;
+    uint32_t in_offset;
+    uint32_t count;
+    float gain;
+} rv_vrx_demod_params;
+
+/* core/dsp/vrx_reference.h VrxCarrierConfig; power 1 = PLL, 2 = Costas. */
+typedef struct rv_vrx_carrier_config {
+    uint32_t power;
+    uint32_t nco_log2;
+} rv_vrx_carrier_config;
+
+/* core/dsp/vrx_reference.h:716 VrxCarrierParams: fourteen 32-bit words. */
+typedef struct rv_vrx_carrier_params {
+    uint32_t in_mask;
+    uint32_t in_offset;
+    uint32_t count;
+    uint32_t flags;
+    float shift;
+    float k1_acquire;
+    float k2_acquire;
+    float k1_track;
+    float k2_track;
+    float level_alpha;
+    float lock_alpha;
+    float clamp_radians;
+    uint32_t hold_in;
+    uint32_t hold_out;
+} rv_vrx_carrier_params;
+
+#define RV_CARRIER_STATE_WORDS 8
+
+/* ---- receiver requests and plans (core/engine/vrx.h, vrx_reference.h) -- */
+
+/* The planning-relevant subset of engine::VrxParams. */
+typedef struct rv_vrx_request {
+    int64_t center;        /* Hz relative to the source centre */
+    int64_t bandwidth;     /* Hz; 0 = the mode's default passband */
+    int64_t passband_low;  /* explicit edges win when either is non-zero */
+    int64_t passband_high;
+    uint32_t demod;        /* RV_DEMOD_* */
+    uint32_t deemphasis;   /* 0 default, 1 none, 2 75us, 3 50us */
+    uint32_t stereo;       /* 0/1 */
+    uint32_t reserved;
+    int64_t audio_rate;    /* 0 = 48000 */
+    int64_t cw_pitch;      /* Hz, CW only */
+} rv_vrx_request;
+
+/* engine::VrxPlacement (core/engine/vrx.h). */
+typedef struct rv_vrx_placement {
+    uint32_t channel;
+    uint32_t bandwidth_clamped;
+    int64_t centre_numerator;
+    int64_t centre_denominator;
+    int64_t residual_numerator;
+    int64_t residual_denominator;
+    int64_t channel_rate;
+    int64_t granted_low;
+    int64_t granted_high;
+} rv_vrx_placement;
+
+/* The scalar part of dsp::VrxPlan (core/dsp/vrx_reference.h). The two
+ * tables (fine taps, demod weights) are returned separately. */
+typedef struct rv_vrx_plan_info {
+    rv_vrx_placement placement;
+    uint32_t mode;
+    uint32_t bandwidth_clamped;
+    int64_t channel_rate;
+    int64_t audio_rate;
+    int64_t demod_rate;
+    int64_t output_rate;
+    int64_t passband_low;
+    int64_t passband_high;
+    int64_t bandwidth;
+    int64_t filter_numerator;
+    int64_t filter_denominator;
+    int64_t mix_numerator;
+    int64_t mix_denominator;
+    rv_vrx_fine_config fine;
+    uint32_t stereo;
+    uint64_t fine_nco_delta;
+    rv_vrx_demod_config demod;
+    float demod_gain;
+    rv_vrx_carrier_config carrier;
+    rv_vrx_carrier_params carrier_loop;
+    int64_t deviation;
+    uint32_t deemphasis;
+    uint32_t deemphasis_taps;
+    uint32_t audio_decimation_taps;
+    uint32_t reserved;
+    uint64_t fine_tap_count;     /* phases * taps + 1 */
+    uint64_t demod_weight_count; /* audio + dc + 2*pilot (+ 2*audio rotation) */
+} rv_vrx_plan_info;
+
+/* dsp::VrxFineBlock / VrxDemodBlock bookkeeping. */
+typedef struct rv_vrx_fine_block {
+    rv_vrx_fine_params params;
+    uint32_t reserved;
+    uint64_t first_input;
+    uint64_t oldest_input;
+    uint64_t newest_input;
+} rv_vrx_fine_block;
+
+typedef struct rv_vrx_demod_block {
+    rv_vrx_demod_params params;
+    uint64_t first_fine;
+    uint64_t oldest_fine;
+} rv_vrx_demod_block;
+
+/* ===================================================================== *
+ * Runtime: context, buffers, streams  (core/gpu/context.h, buffer.h)     *
+ * ===================================================================== */
+
+typedef struct rv_context rv_context;
+typedef struct rv_buffer rv_buffer;
+
+/* core/gpu/context.h:26-58 DeviceInfo. */
+typedef struct rv_device_info {
+    char name[256];
+    int32_t device_index;
+    int32_t sm_count;
+    int32_t cc_major;
+    int32_t cc_minor;
+    uint64_t total_memory;
+    uint64_t max_shared_per_block; /* opt-in bytes */
+    uint64_t l2_bytes;
+} rv_device_info;
+
+/* Context::create (core/gpu/context.cpp:274). device_index < 0 reads
+ * REVENANT_GPU_INDEX, else 0 (core/gpu/context.cpp:174). */
+int32_t rv_context_create(int32_t device_index, rv_context** out);
+int32_t rv_context_destroy(rv_context* context);
+int32_t rv_context_device_info(const rv_context* context, rv_device_info* out);
+/* The context's own stream (core/gpu Context::submit's queue). */
+void* rv_context_stream(const rv_context* context);
+int32_t rv_context_synchronize(rv_context* context);
+
+/* core/gpu/buffer.h:33-39 MemoryKind. */
+#define RV_MEMORY_DEVICE_LOCAL 0
+#define RV_MEMORY_UPLOAD 1   /* pinned, host-written */
+#define RV_MEMORY_READBACK 2 /* pinned, host-read */
+
+int32_t rv_buffer_create(rv_context* context, uint64_t bytes, int32_t kind, rv_buffer** out);
+int32_t rv_buffer_destroy(rv_buffer* buffer);
+/* Device address (device-local) or host address (pinned kinds). */
+void* rv_buffer_address(const rv_buffer* buffer);
+uint64_t rv_buffer_size(const rv_buffer* buffer);
+/* Synchronous copies on the context stream (core/gpu CommandRunner::copy). */
+int32_t rv_buffer_upload(rv_buffer* buffer, uint64_t offset, const void* src, uint64_t bytes);
+int32_t rv_buffer_download(const rv_buffer* buffer, uint64_t offset, void* dst, uint64_t bytes);
+int32_t rv_buffer_clear(rv_buffer* buffer);
+
+/* ===================================================================== *
+ * Plain kernels: one launch per reference dispatch, bit-identical to the  *
+ * reference's CPU twins (fp32, no contraction, denormals flushed).        *
+ * ===================================================================== */
+
+/* core/shaders/convert_{cu8,cs8,cs16,cs24}_cf32.comp; twins
+ * core/dsp/convert.cpp reference_convert_*. `packed_dev` is the staging
+ * buffer as raw bytes (packed_bytes long, whole 32-bit words are read). */
+#define RV_FORMAT_CU8 0
+#define RV_FORMAT_CS8 1
+#define RV_FORMAT_CS16 2
+#define RV_FORMAT_CS24 3
+int32_t rv_convert(void* stream, int32_t format, const rv_convert_params* params,
+                   const void* packed_dev, uint64_t packed_bytes, rv_cf32* ring_dev,
+                   uint64_t ring_len);
+
+/* core/shaders/pfb_branch.comp; twin core/dsp/pfb_branch_reference.cpp:22. */
+int32_t rv_pfb_branch(void* stream, const rv_grid_params* grid, const rv_pfb_branch_params* params,
+                      const float* taps_dev, uint64_t taps_len, const rv_cf32* ring_dev,
+                      uint64_t ring_len, rv_cf32* branch_dev, uint64_t branch_len);
+
+/* core/shaders/pfb_fft.comp; twin core/dsp/pfb_fft_reference.cpp:152. */
+int32_t rv_pfb_fft(void* stream, const rv_pfb_fft_params* params, const rv_cf32* branch_dev,
+                   uint64_t branch_len, const rv_cf32* twiddles_dev, uint64_t twiddles_len,
+                   rv_cf32* channel_ring_dev, uint64_t channel_ring_len);
+
+/* core/shaders/spectrum.comp; twin core/dsp/spectrum_reference.cpp:286.
+ * window holds N window taps then N/2 correction gains. */
+int32_t rv_spectrum(void* stream, const rv_spectrum_params* params,
+                    const rv_cf32* channel_ring_dev, uint64_t channel_ring_len,
+                    const rv_cf32* twiddles_dev, uint64_t twiddles_len, const float* window_dev,
+                    uint64_t window_len, float* frame_dev, uint64_t frame_len);
+
+/* core/shaders/spectrum_levels.comp; twin
+ * core/dsp/spectrum_levels_reference.cpp:75. levels_dev receives 2 floats. */
+int32_t rv_spectrum_levels(void* stream, const rv_spectrum_levels_params* params,
+                           const float* frame_dev, uint64_t frame_len, float* levels_dev);
+
+/* core/shaders/vrx_fine.comp; twin core/dsp/vrx_reference.cpp:489. */
+int32_t rv_vrx_fine(void* stream, const rv_vrx_fine_config* config,
+                    const rv_vrx_fine_params* params, const rv_cf32* channel_ring_dev,
+                    uint64_t channel_ring_len, const rv_cf32* taps_dev, uint64_t taps_len,
+                    const rv_cf32* nco_dev, uint64_t nco_len, rv_cf32* fine_ring_dev,
+                    uint64_t fine_ring_len);
+
+/* core/shaders/vrx_demod.comp; twin core/dsp/vrx_reference.cpp:714. */
+int32_t rv_vrx_demod(void* stream, const rv_vrx_demod_config* config,
+                     const rv_vrx_demod_params* params, const rv_cf32* fine_ring_dev,
+                     uint64_t fine_ring_len, const float* weights_dev, uint64_t weights_len,
+                     float* audio_dev, uint64_t audio_len);
+
+/* core/shaders/vrx_carrier.comp; twin core/dsp/vrx_reference.cpp:1083.
+ * Rotates the fine ring in place and carries 8 state words. */
+int32_t rv_vrx_carrier(void* stream, const rv_vrx_carrier_config* config,
+                       const rv_vrx_carrier_params* params, const rv_cf32* nco_dev,
+                       uint64_t nco_len, rv_cf32* fine_ring_dev, uint64_t fine_ring_len,
+                       uint32_t* state_dev);
+
+/* ===================================================================== *
+ * Host planning (core/dsp/pfb_design.cpp, vrx_reference.cpp,             *
+ * core/engine/vrx_place.cpp), restated; results equal the reference's.   *
+ * ===================================================================== */
+
+int32_t rv_validate_grid(const rv_grid_params* grid);
+/* design_prototype (core/dsp/pfb_design.cpp:381). taps_len = M*(L+1). */
+int32_t rv_design_prototype(const rv_grid_params* grid, double attenuation_db, float* taps,
+                            uint64_t taps_len, double* stopband_db, uint64_t* group_delay);
+/* build_twiddles (core/dsp/pfb_design.cpp:515); M entries. */
+int32_t rv_build_twiddles(uint32_t channels, rv_cf32* table, uint64_t table_len);
+/* build_nco_table (core/dsp/vrx_reference.cpp:364); 2^log2 entries. */
+int32_t rv_build_nco_table(uint32_t log2_size, rv_cf32* table, uint64_t table_len);
+/* build_spectrum_window (core/dsp/spectrum_reference.cpp:195); 3N/2 floats. */
+int32_t rv_build_spectrum_window(uint32_t transform, uint32_t taps_per_branch,
+                                 double attenuation_db, float* window, uint64_t window_len);
+/* engine::place (core/engine/vrx_place.cpp:199). */
+int32_t rv_place(const rv_grid_params* grid, int64_t rate, const rv_vrx_request* request,
+                 rv_vrx_placement* placement);
+/* engine::channel_count_for (core/engine/vrx_place.cpp:187). */
+uint32_t rv_channel_count_for(int64_t rate, int64_t widest_receiver_hz);
+/* dsp::plan_vrx (core/dsp/vrx_reference.cpp:2568). Fills `info`; when the
+ * table pointers are non-NULL also writes the fine tap table
+ * (info->fine_tap_count entries) and demod weights (info->demod_weight_count).
+ * Call once with NULL tables to learn the sizes. */
+int32_t rv_plan_vrx(const rv_grid_params* grid, int64_t rate, const rv_vrx_request* request,
+                    const rv_vrx_placement* placement, rv_vrx_plan_info* info,
+                    rv_cf32* fine_taps, uint64_t fine_taps_len, float* demod_weights,
+                    uint64_t demod_weights_len);
+/* dsp::fine_block / demod_block / carrier_block (vrx_reference.cpp:2830+). */
+int32_t rv_fine_block(const rv_vrx_plan_info* plan, uint32_t channel_base, uint32_t channel_mask,
+                      uint32_t fine_mask, uint64_t first_output, uint32_t count,
+                      rv_vrx_fine_block* block);
+int32_t rv_demod_block(const rv_vrx_plan_info* plan, uint32_t fine_mask, uint64_t first_audio,
+                       uint32_t count, rv_vrx_demod_block* block);
+int32_t rv_carrier_block(const rv_vrx_plan_info* plan, uint32_t fine_mask, uint64_t first_fine,
+                         uint32_t count, int32_t reset, float shift,
+                         rv_vrx_carrier_params* params);
+/* dsp::demod_fine_history (core/dsp/vrx_reference.h). */
+uint32_t rv_demod_fine_history(const rv_vrx_demod_config* config);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REVENANT_GB300_H */

@@ -1,0 +1,982 @@
+/*
+ * oracle.c — CPU restatement of the reference's receive-chain twins.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT: loaded only by tests/, by
+ * __graft_entry__.smoke() as the checker, and by bench.py's CPU arm. See
+ * oracle.h. Compiled with -ffp-contract=off -fno-fast-math so that every
+ * float expression below rounds once per operation, as the reference's
+ * core/dsp/reference_fp.h pledge requires, and run under a scoped hardware
+ * denormal flush (the reference's ScopedDenormalFlush,
+ * core/dsp/denormal_mode.h), because the device flushes fp32 denormals.
+ */
+#define _GNU_SOURCE
+#include "oracle.h"
+
+#include <fenv.h>
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+/* ------------------------------------------------------------------ */
+/* errors                                                             */
+
+static __thread char g_error[512];
+
+const char* or_last_error(void) { return g_error; }
+
+static int32_t fail(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_error, sizeof g_error, fmt, ap);
+    va_end(ap);
+    return -1;
+}
+
+static int32_t ok(void) {
+    g_error[0] = 0;
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* scoped denormal flush (core/dsp/denormal_mode.h ScopedDenormalFlush) */
+/* Sets the floating-point environment's flush-to-zero bits through   */
+/* <fenv.h> and restores the caller's environment afterwards.          */
+
+typedef struct {
+    fenv_t saved;
+} flush_scope;
+
+static void flush_begin(flush_scope* s) {
+    fegetenv(&s->saved);
+    fenv_t env = s->saved;
+#if defined(__x86_64__)
+    env.__mxcsr |= (1u << 15) | (1u << 6); /* FTZ | DAZ */
+#elif defined(__aarch64__)
+    env.__fpcr |= (1u << 24); /* FZ */
+#else
+#error "oracle: no denormal-flush control for this architecture"
+#endif
+    fesetenv(&env);
+}
+
+static void flush_end(flush_scope* s) { fesetenv(&s->saved); }
+
+static int is_pow2_u64(uint64_t v) { return v != 0 && (v & (v - 1)) == 0; }
+
+static uint32_t bits_of(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+static float float_of(uint32_t u) {
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+/* ------------------------------------------------------------------ */
+/* deterministic transcendentals                                      */
+/* core/dsp/vrx_reference.cpp:227-306 (rsqrt, sqrt, recip, atan),      */
+/* core/dsp/spectrum_reference.cpp det_log2. Newton iterations from a  */
+/* bit-trick seed and a fixed odd polynomial, all correctly-rounded    */
+/* + - * so every IEEE implementation agrees.                          */
+
+static const float kHalfPiF = (float)1.57079632679489661923;
+static const float kPiF = (float)3.14159265358979323846;
+static const float kAtanC[10] = {
+    (float)0.9999999998,  (float)-0.3333331929, (float)0.1999923872, (float)-0.1427217912,
+    (float)0.1099615976,  (float)-0.0853800324, (float)0.0603537785, (float)-0.0336503503,
+    (float)0.0122847765,  (float)-0.0021090222};
+
+static float det_rsqrt(float value) {
+    const float seed = float_of(0x5F375A86u - (bits_of(value) >> 1));
+    const float half_value = 0.5F * value;
+    float r = seed;
+    for (int i = 0; i < 4; ++i) r = r * (1.5F - half_value * (r * r));
+    return r;
+}
+
+static float det_sqrt(float value) {
+    if (!(value > 0.0F)) return 0.0F;
+    return value * det_rsqrt(value);
+}
+
+static float det_recip(float value) {
+    const float seed = float_of(0x7EF311C3u - bits_of(value));
+    float r = seed;
+    for (int i = 0; i < 4; ++i) r = r * (2.0F - value * r);
+    return r;
+}
+
+static float det_atan_unit(float t) {
+    const float u = t * t;
+    float p = kAtanC[9];
+    for (int i = 8; i >= 0; --i) p = p * u + kAtanC[i];
+    return t * p;
+}
+
+static float det_atan2(float y, float x) {
+    const float ay = fabsf(y);
+    const float ax = fabsf(x);
+    if (ay == 0.0F && ax == 0.0F) return 0.0F;
+    const float numerator = (ax < ay) ? ax : ay;
+    const float denominator = (ay < ax) ? ax : ay;
+    const float ratio = numerator * det_recip(denominator);
+    float angle = det_atan_unit(ratio);
+    if (ay > ax) angle = kHalfPiF - angle;
+    if (x < 0.0F) angle = kPiF - angle;
+    return (y < 0.0F) ? -angle : angle;
+}
+
+static const float kLogC[5] = {2.88539008177792681F, 0.96179669392597560F, 0.57707801635558536F,
+                               0.41219858311113240F, 0.32059889797532520F};
+static const float kSqrt2F = 1.41421356237309505F;
+static const float kDecibelsPerOctave = 3.01029995663981195F;
+
+static float det_log2(float value) {
+    const uint32_t bits = bits_of(value);
+    int exponent = (int)((bits >> 23) & 0xFFu) - 127;
+    float mantissa = float_of((bits & 0x007FFFFFu) | 0x3F800000u);
+    if (mantissa > kSqrt2F) {
+        mantissa = mantissa * 0.5F;
+        exponent = exponent + 1;
+    }
+    const float t = (mantissa - 1.0F) * det_recip(mantissa + 1.0F);
+    const float u = t * t;
+    float p = kLogC[4];
+    for (int i = 3; i >= 0; --i) p = p * u + kLogC[i];
+    const float fraction = t * p;
+    return (float)exponent + fraction;
+}
+
+#define WRAP_DET1(name)                \
+    float or_##name(float v) {          \
+        flush_scope s;                 \
+        flush_begin(&s);               \
+        const float r = name(v);       \
+        flush_end(&s);                 \
+        return r;                      \
+    }
+WRAP_DET1(det_rsqrt)
+WRAP_DET1(det_sqrt)
+WRAP_DET1(det_recip)
+WRAP_DET1(det_log2)
+
+float or_det_atan2(float y, float x) {
+    flush_scope s;
+    flush_begin(&s);
+    const float r = det_atan2(y, x);
+    flush_end(&s);
+    return r;
+}
+
+/* ------------------------------------------------------------------ */
+/* convert (core/dsp/convert.cpp reference_convert_*; constants        */
+/* core/dsp/convert.h:43-106)                                          */
+
+static const float kCu8Bias = 127.5F;
+static const float kCu8Scale = 0.00784313772F;      /* 0x3C008081 */
+static const float kCs8Scale = 0.0078125F;          /* 2^-7  */
+static const float kCs16Scale = 0.000030517578125F; /* 2^-15 */
+static const float kCs24Scale = 0.00000011920928955078125F; /* 2^-23 */
+
+static uint32_t load_word(const uint8_t* b, uint64_t word) {
+    const uint8_t* p = b + word * 4;
+    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) |
+           ((uint32_t)p[3] << 24);
+}
+
+static int32_t sign_extend(uint32_t raw, int bits) {
+    const uint32_t shifted = raw << (32 - bits);
+    int32_t s;
+    memcpy(&s, &shifted, 4);
+    return s >> (32 - bits);
+}
+
+int32_t or_convert(int32_t format, const rv_convert_params* p, const void* packed,
+                   uint64_t packed_bytes, rv_cf32* ring, uint64_t ring_len) {
+    uint64_t bytes_per_sample;
+    switch (format) {
+        case RV_FORMAT_CU8:
+        case RV_FORMAT_CS8: bytes_per_sample = 2; break;
+        case RV_FORMAT_CS16: bytes_per_sample = 4; break;
+        case RV_FORMAT_CS24: bytes_per_sample = 6; break;
+        default: return fail("convert: unknown format %d", format);
+    }
+    /* core/dsp/convert.cpp check_request */
+    const uint64_t capacity = (uint64_t)p->ring_mask + 1u;
+    if ((capacity & (uint64_t)p->ring_mask) != 0)
+        return fail("convert: ring_mask %u is not a power of two minus one", p->ring_mask);
+    if (ring_len < capacity)
+        return fail("convert: ring holds %llu samples, mask %u implies %llu",
+                    (unsigned long long)ring_len, p->ring_mask, (unsigned long long)capacity);
+    if (p->count > capacity)
+        return fail("convert: %u samples into a ring of %llu would alias", p->count,
+                    (unsigned long long)capacity);
+    const uint64_t last_sample = (uint64_t)p->src_offset + p->count;
+    if (last_sample > 0xFFFFFFFFull)
+        return fail("convert: src_offset %u plus count %u overflows 32 bits", p->src_offset,
+                    p->count);
+    const uint64_t words_needed = (last_sample * bytes_per_sample + 3u) / 4u;
+    if (words_needed > 0x100000000ull)
+        return fail("convert: request reaches past the 32-bit word index");
+    if (packed_bytes < words_needed * 4u)
+        return fail("convert: reads %llu whole words, source holds %llu bytes",
+                    (unsigned long long)words_needed, (unsigned long long)packed_bytes);
+    if (p->count == 0) return ok();
+
+    const uint8_t* b = (const uint8_t*)packed;
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t index = 0; index < p->count; ++index) {
+        const uint32_t src = p->src_offset + index;
+        float iv, qv;
+        if (format == RV_FORMAT_CU8 || format == RV_FORMAT_CS8) {
+            const uint32_t word = load_word(b, src >> 1);
+            const int shift = (int)((src & 1u) << 4);
+            const uint32_t i_raw = (word >> shift) & 0xFFu;
+            const uint32_t q_raw = (word >> (shift + 8)) & 0xFFu;
+            if (format == RV_FORMAT_CU8) {
+                iv = ((float)i_raw - kCu8Bias) * kCu8Scale;
+                qv = ((float)q_raw - kCu8Bias) * kCu8Scale;
+            } else {
+                iv = (float)sign_extend(i_raw, 8) * kCs8Scale;
+                qv = (float)sign_extend(q_raw, 8) * kCs8Scale;
+            }
+        } else if (format == RV_FORMAT_CS16) {
+            const uint32_t word = load_word(b, src);
+            iv = (float)sign_extend(word & 0xFFFFu, 16) * kCs16Scale;
+            qv = (float)sign_extend(word >> 16, 16) * kCs16Scale;
+        } else {
+            /* six bytes a sample, little-endian, I in bytes 0-2, Q in 3-5 */
+            const uint8_t* q = b + (uint64_t)src * 6u;
+            const uint32_t i_raw = (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16);
+            const uint32_t q_raw = (uint32_t)q[3] | ((uint32_t)q[4] << 8) | ((uint32_t)q[5] << 16);
+            iv = (float)sign_extend(i_raw, 24) * kCs24Scale;
+            qv = (float)sign_extend(q_raw, 24) * kCs24Scale;
+        }
+        rv_cf32* out = &ring[(p->dst_offset + index) & p->ring_mask];
+        out->re = iv;
+        out->im = qv;
+    }
+    flush_end(&s);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* grid validation (core/dsp/pfb_design.cpp validate(GridParams))      */
+
+static int32_t validate_grid(const rv_grid_params* g) {
+    if (g->channels < 2) return fail("grid: channel count %u is below 2", g->channels);
+    if (!is_pow2_u64(g->channels)) return fail("grid: channel count %u is not a power of two", g->channels);
+    if (g->channels > 2048) return fail("grid: channel count %u exceeds 2048", g->channels);
+    if (g->taps_per_branch == 0) return fail("grid: zero taps per branch");
+    if (g->decimation == 0) return fail("grid: zero decimation");
+    if (g->channels % g->decimation != 0)
+        return fail("grid: decimation %u does not divide %u", g->decimation, g->channels);
+    if ((uint64_t)g->channels * g->taps_per_branch > (1u << 20))
+        return fail("grid: prototype exceeds 2^20 taps");
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* branch FIR (core/dsp/pfb_branch_reference.cpp:22-145)               */
+/* y[b][(M-r)&(M-1)] = sum_{q ascending} x[(base - (qM+r)) & mask] * h[qM+r] */
+
+static void branch_block(uint32_t M, uint32_t T, uint32_t base, uint32_t mask, const float* taps,
+                         const rv_cf32* ring, rv_cf32* out_block) {
+    for (uint32_t r = 0; r < M; ++r) {
+        float acc_re = 0.0F, acc_im = 0.0F;
+        for (uint32_t q = 0; q < T; ++q) {
+            const uint32_t n = q * M + r;
+            const rv_cf32 s = ring[(base - n) & mask];
+            const float c = taps[n];
+            acc_re = acc_re + s.re * c;
+            acc_im = acc_im + s.im * c;
+        }
+        rv_cf32* o = &out_block[(M - r) & (M - 1u)];
+        o->re = acc_re;
+        o->im = acc_im;
+    }
+}
+
+int32_t or_pfb_branch(const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                      uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out,
+                      uint64_t out_len) {
+    if (validate_grid(g) != 0) return -1;
+    const uint32_t M = g->channels, T = g->taps_per_branch, D = g->decimation;
+    if (taps_len != (uint64_t)M * T) return fail("pfb_branch: wants %u taps", M * T);
+    if (out_len != (uint64_t)p->block_count * M) return fail("pfb_branch: output length");
+    if (p->block_count == 0) return ok();
+    const uint64_t capacity = (uint64_t)p->ring_mask + 1u;
+    if ((capacity & (uint64_t)p->ring_mask) != 0) return fail("pfb_branch: ring_mask");
+    if (ring_len < capacity) return fail("pfb_branch: ring shorter than mask implies");
+    const uint64_t span = (uint64_t)M * T + (uint64_t)(p->block_count - 1u) * D;
+    if (span > capacity) return fail("pfb_branch: needs %llu samples of history, ring %llu",
+                                     (unsigned long long)span, (unsigned long long)capacity);
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t b = 0; b < p->block_count; ++b)
+        branch_block(M, T, p->base_offset + b * D, p->ring_mask, taps, ring, out + (uint64_t)b * M);
+    flush_end(&s);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* radix-2 DIT FFT (core/dsp/pfb_fft_reference.cpp:54-102)             */
+/* bit-reversed load, stage s: half span h=2^s, twiddle W[j*(M>>(s+1))],*/
+/* ia = ((b>>s)<<(s+1)) + j, value = b*w, a+value / a-value            */
+
+static uint32_t reverse_bits(uint32_t v, uint32_t stages) {
+    uint32_t r = 0;
+    for (uint32_t bit = 0; bit < stages; ++bit) r |= ((v >> bit) & 1u) << (stages - 1u - bit);
+    return r;
+}
+
+static void fft_block(const rv_cf32* in, const rv_cf32* tw, rv_cf32* x, uint32_t n,
+                      uint32_t stages) {
+    for (uint32_t i = 0; i < n; ++i) x[i] = in[reverse_bits(i, stages)];
+    const uint32_t butterflies = n >> 1;
+    for (uint32_t st = 0; st < stages; ++st) {
+        const uint32_t half = 1u << st;
+        const uint32_t step = n >> (st + 1u);
+        for (uint32_t b = 0; b < butterflies; ++b) {
+            const uint32_t j = b & (half - 1u);
+            const uint32_t ia = ((b >> st) << (st + 1u)) + j;
+            const uint32_t ib = ia + half;
+            const float ar = x[ia].re, ai = x[ia].im, br = x[ib].re, bi = x[ib].im;
+            const float wr = tw[j * step].re, wi = tw[j * step].im;
+            const float vr = br * wr - bi * wi;
+            const float vi = br * wi + bi * wr;
+            x[ia].re = ar + vr;
+            x[ia].im = ai + vi;
+            x[ib].re = ar - vr;
+            x[ib].im = ai - vi;
+        }
+    }
+}
+
+static uint32_t log2_u32(uint32_t v) {
+    uint32_t s = 0;
+    while (s < 31 && (1u << s) < v) ++s;
+    return s;
+}
+
+int32_t or_fft_radix2(const rv_cf32* tw, const rv_cf32* in, rv_cf32* out, uint32_t size,
+                      uint32_t batch) {
+    if (!is_pow2_u64(size) || size < 2) return fail("fft_radix2: size %u", size);
+    const uint32_t stages = log2_u32(size);
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t b = 0; b < batch; ++b)
+        fft_block(in + (uint64_t)b * size, tw, out + (uint64_t)b * size, size, stages);
+    flush_end(&s);
+    return ok();
+}
+
+/* core/dsp/pfb_fft_reference.cpp validate(PfbFftParams) */
+static int32_t validate_fft(const rv_pfb_fft_params* p) {
+    if (!is_pow2_u64(p->channels) || p->channels < 2) return fail("pfb_fft: channels %u", p->channels);
+    if (p->stages >= 32 || (1u << p->stages) != p->channels) return fail("pfb_fft: stages");
+    if (p->decimation == 0 || p->decimation > p->channels || p->channels % p->decimation != 0)
+        return fail("pfb_fft: decimation must divide channels");
+    if (!is_pow2_u64(p->out_ring_blocks)) return fail("pfb_fft: out_ring_blocks");
+    if (p->out_ring_mask != p->out_ring_blocks - 1u) return fail("pfb_fft: out_ring_mask");
+    if (p->block_count > p->out_ring_blocks) return fail("pfb_fft: dispatch overruns the ring");
+    return 0;
+}
+
+/* Phase correction exp(-j 2 pi k m D / M) from the twiddle circle and the
+ * channel-major scatter (core/dsp/pfb_fft_reference.cpp:185-228). */
+static void fft_finish(const rv_pfb_fft_params* p, const rv_cf32* x, const rv_cf32* tw,
+                       uint32_t m_abs, rv_cf32* ring) {
+    const uint32_t M = p->channels;
+    const uint32_t slot = m_abs & p->out_ring_mask;
+    const uint32_t dm = ((m_abs & (M - 1u)) * p->decimation) & (M - 1u);
+    for (uint32_t k = 0; k < M; ++k) {
+        float vr = x[k].re, vi = x[k].im;
+        if (p->decimation != M) {
+            const rv_cf32 c = tw[(k * dm) & (M - 1u)];
+            const float pr = vr * c.re - vi * c.im;
+            const float pi = vr * c.im + vi * c.re;
+            vr = pr;
+            vi = pi;
+        }
+        rv_cf32* o = &ring[(uint64_t)k * p->out_ring_blocks + slot];
+        o->re = vr;
+        o->im = vi;
+    }
+}
+
+int32_t or_pfb_fft(const rv_pfb_fft_params* p, const rv_cf32* branch, uint64_t branch_len,
+                   const rv_cf32* tw, uint64_t tw_len, rv_cf32* ring, uint64_t ring_len) {
+    if (validate_fft(p) != 0) return -1;
+    const uint32_t M = p->channels;
+    if (tw_len != M) return fail("pfb_fft: needs %u twiddles", M);
+    if (branch_len < (uint64_t)p->block_count * M) return fail("pfb_fft: branch values");
+    if (ring_len < (uint64_t)M * p->out_ring_blocks) return fail("pfb_fft: channel ring");
+    rv_cf32* x = (rv_cf32*)malloc(sizeof(rv_cf32) * M);
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t b = 0; b < p->block_count; ++b) {
+        fft_block(branch + (uint64_t)b * M, tw, x, M, p->stages);
+        fft_finish(p, x, tw, p->block_base + b, ring);
+    }
+    flush_end(&s);
+    free(x);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* coarse chain over host threads (convert -> branch -> FFT)           */
+
+typedef struct {
+    const rv_grid_params* g;
+    const float* taps;
+    const rv_cf32* tw;
+    const uint8_t* packed;
+    uint64_t samples;
+    uint64_t first_block;
+    uint32_t b0, b1;
+    uint32_t out_ring_blocks;
+    rv_cf32* ring;
+} coarse_job;
+
+static void* coarse_worker(void* arg) {
+    const coarse_job* j = (const coarse_job*)arg;
+    const uint32_t M = j->g->channels, T = j->g->taps_per_branch, D = j->g->decimation;
+    const uint32_t stages = log2_u32(M);
+    const uint32_t support = M * T;
+    if (j->b1 <= j->b0) return NULL;
+    /* Block b is centred on absolute input n0 = (first_block + b) * D and
+     * reads x[n0 - (M*T - 1) .. n0]; samples before the capture read as zero.
+     * The worker converts its whole input span once, then filters from it. */
+    const int64_t first = (int64_t)((j->first_block + j->b0) * (uint64_t)D) - (int64_t)(support - 1u);
+    const uint64_t span = (uint64_t)(j->b1 - j->b0 - 1u) * D + support;
+    rv_cf32* x_lin = (rv_cf32*)malloc(sizeof(rv_cf32) * span);
+    rv_cf32* br = (rv_cf32*)malloc(sizeof(rv_cf32) * M);
+    rv_cf32* x = (rv_cf32*)malloc(sizeof(rv_cf32) * M);
+    rv_pfb_fft_params fp = {M, D, stages, 0, 1, j->out_ring_blocks, j->out_ring_blocks - 1u};
+    flush_scope s;
+    flush_begin(&s);
+    for (uint64_t w = 0; w < span; ++w) {
+        const int64_t n = first + (int64_t)w;
+        rv_cf32 v = {0.0F, 0.0F};
+        if (n >= 0 && (uint64_t)n < j->samples) {
+            const uint32_t word = load_word(j->packed, (uint64_t)n);
+            v.re = (float)sign_extend(word & 0xFFFFu, 16) * kCs16Scale;
+            v.im = (float)sign_extend(word >> 16, 16) * kCs16Scale;
+        }
+        x_lin[w] = v;
+    }
+    for (uint32_t b = j->b0; b < j->b1; ++b) {
+        /* x_lin[(b - b0) * D + support - 1] is x[n0]; index it as a ring with
+         * an all-ones mask so (base - n) & mask is the linear offset. */
+        const uint32_t base = (b - j->b0) * D + support - 1u;
+        branch_block(M, T, base, 0xFFFFFFFFu, j->taps, x_lin, br);
+        fft_block(br, j->tw, x, M, stages);
+        fft_finish(&fp, x, j->tw, (uint32_t)(j->first_block + b), j->ring);
+    }
+    flush_end(&s);
+    free(x_lin);
+    free(br);
+    free(x);
+    return NULL;
+}
+
+int32_t or_coarse_cs16(const rv_grid_params* g, const float* taps, const rv_cf32* tw,
+                       const void* packed, uint64_t samples, uint64_t first_block,
+                       uint32_t block_count, uint32_t out_ring_blocks, rv_cf32* ring,
+                       int32_t threads) {
+    if (validate_grid(g) != 0) return -1;
+    if (!is_pow2_u64(out_ring_blocks) || block_count > out_ring_blocks)
+        return fail("coarse: out_ring_blocks must be a power of two >= block_count");
+    int n = threads > 0 ? threads : (int)sysconf(_SC_NPROCESSORS_ONLN);
+    if (n < 1) n = 1;
+    if ((uint32_t)n > block_count) n = block_count ? (int)block_count : 1;
+    pthread_t* tid = (pthread_t*)calloc((size_t)n, sizeof(pthread_t));
+    coarse_job* jobs = (coarse_job*)calloc((size_t)n, sizeof(coarse_job));
+    for (int t = 0; t < n; ++t) {
+        coarse_job* j = &jobs[t];
+        j->g = g;
+        j->taps = taps;
+        j->tw = tw;
+        j->packed = (const uint8_t*)packed;
+        j->samples = samples;
+        j->first_block = first_block;
+        j->b0 = (uint32_t)(((uint64_t)block_count * t) / n);
+        j->b1 = (uint32_t)(((uint64_t)block_count * (t + 1)) / n);
+        j->out_ring_blocks = out_ring_blocks;
+        j->ring = ring;
+        if (n == 1) coarse_worker(j);
+        else pthread_create(&tid[t], NULL, coarse_worker, j);
+    }
+    if (n > 1)
+        for (int t = 0; t < n; ++t) pthread_join(tid[t], NULL);
+    free(tid);
+    free(jobs);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 channelizer yardstick                                          */
+
+int32_t or_pfb_f64(const rv_grid_params* g, const float* taps, const rv_cf32* ring,
+                   uint32_t ring_mask, uint32_t base_offset, uint32_t block_count,
+                   uint32_t block_base, double* out_re, double* out_im) {
+    if (validate_grid(g) != 0 && g->channels <= 2048) return -1;
+    const uint32_t M = g->channels, T = g->taps_per_branch, D = g->decimation;
+    double* br = (double*)malloc(sizeof(double) * 2 * M);
+    double* cs = (double*)malloc(sizeof(double) * 2 * M);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (uint32_t j = 0; j < M; ++j) {
+        cs[2 * j] = cos(two_pi * j / M);
+        cs[2 * j + 1] = -sin(two_pi * j / M);
+    }
+    for (uint32_t b = 0; b < block_count; ++b) {
+        const uint32_t base = base_offset + b * D;
+        for (uint32_t r = 0; r < M; ++r) {
+            double ar = 0, ai = 0;
+            for (uint32_t q = 0; q < T; ++q) {
+                const uint32_t n = q * M + r;
+                const rv_cf32 s = ring[(base - n) & ring_mask];
+                ar += (double)s.re * taps[n];
+                ai += (double)s.im * taps[n];
+            }
+            const uint32_t slot = (M - r) & (M - 1u);
+            br[2 * slot] = ar;
+            br[2 * slot + 1] = ai;
+        }
+        const uint32_t m_abs = block_base + b;
+        const uint32_t dm = ((m_abs & (M - 1u)) * D) & (M - 1u);
+        for (uint32_t k = 0; k < M; ++k) {
+            double yr = 0, yi = 0;
+            for (uint32_t n = 0; n < M; ++n) {
+                const uint32_t e = (uint32_t)(((uint64_t)k * n) & (M - 1u));
+                yr += br[2 * n] * cs[2 * e] - br[2 * n + 1] * cs[2 * e + 1];
+                yi += br[2 * n] * cs[2 * e + 1] + br[2 * n + 1] * cs[2 * e];
+            }
+            const uint32_t e = (k * dm) & (M - 1u);
+            const double zr = yr * cs[2 * e] - yi * cs[2 * e + 1];
+            const double zi = yr * cs[2 * e + 1] + yi * cs[2 * e];
+            out_re[(uint64_t)k * block_count + b] = zr;
+            out_im[(uint64_t)k * block_count + b] = zi;
+        }
+    }
+    free(br);
+    free(cs);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* spectrum (core/dsp/spectrum_reference.cpp:286-390)                  */
+
+int32_t or_spectrum(const rv_spectrum_params* p, const rv_cf32* ring, uint64_t ring_len,
+                    const rv_cf32* tw, uint64_t tw_len, const float* window, uint64_t window_len,
+                    float* frame, uint64_t frame_len) {
+    if (!is_pow2_u64(p->channels) || p->channels < 2) return fail("spectrum: channels");
+    if (!is_pow2_u64(p->transform) || p->transform < 4) return fail("spectrum: transform");
+    if (p->transform > 2048) return fail("spectrum: transform above 2048");
+    if (p->stages >= 32 || (1u << p->stages) != p->transform) return fail("spectrum: stages");
+    if (!is_pow2_u64(p->chan_blocks)) return fail("spectrum: chan_blocks");
+    if (p->chan_mask != p->chan_blocks - 1u) return fail("spectrum: chan_mask");
+    if (p->transform > p->chan_blocks) return fail("spectrum: window longer than the ring");
+    const uint32_t N = p->transform, M = p->channels, half = N / 2;
+    if (tw_len != N) return fail("spectrum: twiddles");
+    if (window_len != (uint64_t)N + half) return fail("spectrum: window length");
+    if (ring_len < (uint64_t)M * p->chan_blocks) return fail("spectrum: ring");
+    if (frame_len < (uint64_t)M * half) return fail("spectrum: frame");
+    rv_cf32* w = (rv_cf32*)malloc(sizeof(rv_cf32) * N);
+    rv_cf32* x = (rv_cf32*)malloc(sizeof(rv_cf32) * N);
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t ch = 0; ch < M; ++ch) {
+        const uint64_t origin = (uint64_t)ch * p->chan_blocks;
+        for (uint32_t n = 0; n < N; ++n) {
+            const rv_cf32 v = ring[origin + ((p->in_offset + n) & p->chan_mask)];
+            const float gain = window[n];
+            w[n].re = v.re * gain;
+            w[n].im = v.im * gain;
+        }
+        fft_block(w, tw, x, N, p->stages);
+        const uint64_t out_origin = (uint64_t)((ch + M / 2) & (M - 1u)) * half;
+        for (uint32_t bin = 0; bin < half; ++bin) {
+            const rv_cf32 v = x[(bin + N - N / 4) & (N - 1u)];
+            const float power = v.re * v.re + v.im * v.im;
+            const float flattened = power * window[N + bin];
+            const float floored = (flattened < 1.0e-20F) ? 1.0e-20F : flattened;
+            frame[out_origin + bin] = det_log2(floored) * kDecibelsPerOctave;
+        }
+    }
+    flush_end(&s);
+    free(w);
+    free(x);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* spectrum levels (core/dsp/spectrum_levels_reference.cpp:75-135)     */
+
+static uint32_t rank_of(uint32_t count, uint32_t permille) {
+    return (count / 1000u) * permille + ((count % 1000u) * permille) / 1000u;
+}
+
+int32_t or_spectrum_levels(const rv_spectrum_levels_params* p, const float* frame,
+                           uint64_t frame_len, float* levels) {
+    if (p->bins == 0) return fail("levels: no bins");
+    if (p->low_permille > 1000 || p->high_permille > 1000) return fail("levels: permille");
+    if (p->low_permille >= p->high_permille) return fail("levels: low must sit below high");
+    if (frame_len < p->bins) return fail("levels: frame shorter than bins");
+    static __thread uint32_t histogram[1024];
+    memset(histogram, 0, sizeof histogram);
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t i = 0; i < p->bins; ++i) {
+        float t = (frame[i] - (-200.0F)) * 4.26666666666666666F;
+        t = (t < 0.0F) ? 0.0F : t;
+        t = (t > 1023.0F) ? 1023.0F : t;
+        ++histogram[(uint32_t)t];
+    }
+    uint32_t lo = rank_of(p->bins, p->low_permille), hi = rank_of(p->bins, p->high_permille);
+    if (lo > p->bins - 1u) lo = p->bins - 1u;
+    if (hi > p->bins - 1u) hi = p->bins - 1u;
+    uint32_t lb = 0, hb = 0, cum = 0;
+    int lf = 0, hf = 0;
+    for (uint32_t b = 0; b < 1024; ++b) {
+        cum += histogram[b];
+        if (!lf && cum > lo) { lb = b; lf = 1; }
+        if (!hf && cum > hi) { hb = b; hf = 1; }
+    }
+    levels[0] = -200.0F + ((float)lb + 0.5F) * 0.234375F;
+    levels[1] = -200.0F + ((float)hb + 0.5F) * 0.234375F;
+    flush_end(&s);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* fine stage (core/dsp/vrx_reference.cpp:489-620)                     */
+
+static int32_t validate_fine(const rv_vrx_fine_config* c, const rv_vrx_fine_params* p) {
+    if (c->taps < 2 || c->taps > 256) return fail("vrx fine: %u taps outside [2, 256]", c->taps);
+    if (c->phases < 1 || c->phases > 4096) return fail("vrx fine: phases");
+    if (c->nco_log2 > 24) return fail("vrx fine: nco_log2");
+    if (p->out_rate == 0) return fail("vrx fine: output rate is zero");
+    if (p->frac0 >= p->out_rate) return fail("vrx fine: frac0 must be below the output rate");
+    const uint64_t cap = (uint64_t)p->chan_mask + 1u;
+    if ((cap & (uint64_t)p->chan_mask) != 0) return fail("vrx fine: chan_mask");
+    const uint64_t ocap = (uint64_t)p->out_mask + 1u;
+    if ((ocap & (uint64_t)p->out_mask) != 0) return fail("vrx fine: out_mask");
+    if ((uint64_t)p->frac0 + (uint64_t)p->count * p->step_rem > 0xFFFFFFFFull)
+        return fail("vrx fine: recurrence overflows 32 bits");
+    if ((uint64_t)(p->out_rate - 1u) * c->phases > 0xFFFFFFFFull)
+        return fail("vrx fine: phase selection overflows 32 bits");
+    return 0;
+}
+
+int32_t or_vrx_fine(const rv_vrx_fine_config* c, const rv_vrx_fine_params* p, const rv_cf32* chan,
+                    uint64_t chan_len, const rv_cf32* taps, uint64_t taps_len, const rv_cf32* nco,
+                    uint64_t nco_len, rv_cf32* fine, uint64_t fine_len) {
+    if (validate_fine(c, p) != 0) return -1;
+    if (taps_len != (uint64_t)c->phases * c->taps + 1u) return fail("vrx fine: tap table size");
+    if (nco_len != (1ull << c->nco_log2)) return fail("vrx fine: nco size");
+    if (chan_len < (uint64_t)p->chan_base + p->chan_mask + 1u) return fail("vrx fine: channel ring");
+    if (fine_len < (uint64_t)p->out_mask + 1u) return fail("vrx fine: output ring");
+    if (p->count > (uint64_t)p->out_mask + 1u) return fail("vrx fine: count exceeds output ring");
+    if (p->count == 0) return ok();
+    flush_scope s;
+    flush_begin(&s);
+    const uint64_t delta = ((uint64_t)p->nco_delta_high << 32) | p->nco_delta_low;
+    const uint64_t phase0 = ((uint64_t)p->nco_phase_high << 32) | p->nco_phase_low;
+    for (uint32_t i = 0; i < p->count; ++i) {
+        const uint32_t acc = p->frac0 + i * p->step_rem;
+        const uint32_t carry = acc / p->out_rate;
+        const uint32_t frac = acc - carry * p->out_rate;
+        const uint32_t n_rel = i * p->step_whole + carry;
+        const uint32_t scaled = frac * c->phases;
+        const uint32_t phase = scaled / p->out_rate;
+        const uint32_t blend_num = scaled - phase * p->out_rate;
+        const float blend = (float)blend_num * p->inv_out_rate;
+        const float blend_c = 1.0F - blend;
+        const uint32_t base = p->in_offset + n_rel;
+        float ar = 0.0F, ai = 0.0F;
+        for (uint32_t k = 0; k < c->taps; ++k) {
+            const uint32_t slot = phase + k * c->phases;
+            const rv_cf32 g0 = taps[slot], g1 = taps[slot + 1u];
+            const float tr = g0.re * blend_c + g1.re * blend;
+            const float ti = g0.im * blend_c + g1.im * blend;
+            const rv_cf32 x = chan[(uint64_t)p->chan_base + ((base - k) & p->chan_mask)];
+            ar = ar + (x.re * tr - x.im * ti);
+            ai = ai + (x.re * ti + x.im * tr);
+        }
+        /* phi(i) = phase0 + i * delta mod 2^64 (the kernel's umulExtended /
+         * uaddCarry chain is this 64-bit product and sum) */
+        const uint64_t phi = phase0 + (uint64_t)i * delta;
+        const uint32_t idx = (c->nco_log2 == 0) ? 0u : (uint32_t)(phi >> 32) >> (32u - c->nco_log2);
+        const rv_cf32 rot = nco[idx];
+        rv_cf32* o = &fine[(p->out_offset + i) & p->out_mask];
+        o->re = ar * rot.re - ai * rot.im;
+        o->im = ar * rot.im + ai * rot.re;
+    }
+    flush_end(&s);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* demodulators (core/dsp/vrx_reference.cpp:620-917)                   */
+
+static int is_known_mode(uint32_t m) { return m <= 12; }
+static int is_complex_mode(uint32_t m) {
+    return m == RV_DEMOD_RAW || m == RV_DEMOD_P25P1 || m == RV_DEMOD_DSTAR ||
+           m == RV_DEMOD_TETRA || m == RV_DEMOD_DMR;
+}
+
+static uint32_t fine_history(const rv_vrx_demod_config* c) {
+    const uint32_t det = (c->mode == RV_DEMOD_AM || c->mode == RV_DEMOD_SAM) ? c->dc_taps - 1u
+                         : (c->mode == RV_DEMOD_NFM || c->mode == RV_DEMOD_WFM) ? 1u
+                                                                                 : 0u;
+    const uint32_t audio = c->audio_taps - 1u;
+    const uint32_t pilot = c->pilot_taps == 0 ? 0u : c->audio_taps / 2u + c->pilot_taps - 1u;
+    return (audio > pilot ? audio : pilot) + det;
+}
+
+static int32_t validate_demod(const rv_vrx_demod_config* c, const rv_vrx_demod_params* p) {
+    if (!is_known_mode(c->mode)) return fail("vrx demod: unknown mode %u", c->mode);
+    const int cx = is_complex_mode(c->mode);
+    if (c->decimation == 0) return fail("vrx demod: decimation is zero");
+    if (c->audio_taps == 0 || c->audio_taps > 4096) return fail("vrx demod: audio taps");
+    if (c->dc_taps == 0 || c->dc_taps > 4096) return fail("vrx demod: dc taps");
+    if (cx && (c->decimation != 1u || c->audio_taps != 1u)) return fail("vrx demod: complex tap with a filter");
+    if (c->channels != 1u && c->channels != 2u) return fail("vrx demod: channels");
+    if (cx && c->channels != 2u) return fail("vrx demod: complex tap is two channels");
+    if (c->pilot_taps > 2048) return fail("vrx demod: pilot taps");
+    if (c->pilot_taps != 0 && c->mode != RV_DEMOD_WFM) return fail("vrx demod: pilot without WFM");
+    if (c->pilot_taps != 0 && c->channels != 2u) return fail("vrx demod: pilot with one channel");
+    if (c->channels == 2u && !cx && c->pilot_taps == 0) return fail("vrx demod: stereo without pilot");
+    const uint64_t cap = (uint64_t)p->in_mask + 1u;
+    if ((cap & (uint64_t)p->in_mask) != 0) return fail("vrx demod: in_mask");
+    const uint64_t span = p->count == 0 ? 0 : (uint64_t)(p->count - 1u) * c->decimation + fine_history(c) + 1u;
+    if (span > cap) return fail("vrx demod: history does not fit the input ring");
+    return 0;
+}
+
+typedef struct {
+    const rv_vrx_demod_config* c;
+    const rv_cf32* ring;
+    uint32_t mask;
+    const float* w;
+} demod_ctx;
+
+static rv_cf32 at(const demod_ctx* d, uint32_t i) { return d->ring[i & d->mask]; }
+
+static float magnitude_at(const demod_ctx* d, uint32_t i) {
+    const rv_cf32 z = at(d, i);
+    return det_sqrt(z.re * z.re + z.im * z.im);
+}
+
+static float detect(const demod_ctx* d, uint32_t index) {
+    const rv_vrx_demod_config* c = d->c;
+    if (c->mode == RV_DEMOD_AM) {
+        float dc = 0.0F;
+        for (uint32_t w = 0; w < c->dc_taps; ++w) {
+            const float term = magnitude_at(d, index - w) * d->w[c->audio_taps + w];
+            dc = dc + term;
+        }
+        return magnitude_at(d, index) - dc;
+    }
+    if (c->mode == RV_DEMOD_SAM) {
+        float dc = 0.0F;
+        for (uint32_t w = 0; w < c->dc_taps; ++w) {
+            const float term = at(d, index - w).re * d->w[c->audio_taps + w];
+            dc = dc + term;
+        }
+        return at(d, index).re - dc;
+    }
+    if (c->mode == RV_DEMOD_NFM || c->mode == RV_DEMOD_WFM) {
+        const rv_cf32 z = at(d, index), q = at(d, index - 1u);
+        const float pr = z.re * q.re + z.im * q.im;
+        const float pi = z.im * q.re - z.re * q.im;
+        return det_atan2(pi, pr);
+    }
+    return at(d, index).re;
+}
+
+int32_t or_vrx_demod(const rv_vrx_demod_config* c, const rv_vrx_demod_params* p,
+                     const rv_cf32* fine, uint64_t fine_len, const float* weights,
+                     uint64_t weights_len, float* audio, uint64_t audio_len) {
+    if (validate_demod(c, p) != 0) return -1;
+    const uint64_t pilot_base = (uint64_t)c->audio_taps + c->dc_taps;
+    const uint64_t rotation_base = pilot_base + 2ull * c->pilot_taps;
+    const uint64_t wanted = c->pilot_taps == 0 ? pilot_base : rotation_base + 2ull * c->audio_taps;
+    if (weights_len != wanted) return fail("vrx demod: wants %llu weights", (unsigned long long)wanted);
+    if (fine_len < (uint64_t)p->in_mask + 1u) return fail("vrx demod: fine ring");
+    if (audio_len != (uint64_t)p->count * c->channels) return fail("vrx demod: audio length");
+    if (p->count == 0) return ok();
+    demod_ctx d = {c, fine, p->in_mask, weights};
+    const float kPilotLockPower = 2.0e-5F;
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t i = 0; i < p->count; ++i) {
+        const uint32_t index = p->in_offset + i * c->decimation;
+        if (is_complex_mode(c->mode)) {
+            const rv_cf32 z = at(&d, index);
+            audio[2u * i] = z.re * p->gain;
+            audio[2u * i + 1u] = z.im * p->gain;
+            continue;
+        }
+        if (c->channels == 2u) {
+            const uint32_t pilot_at = index - c->audio_taps / 2u;
+            float pr = 0.0F, pi = 0.0F;
+            for (uint32_t k = 0; k < c->pilot_taps; ++k) {
+                const float comp = detect(&d, pilot_at - k);
+                const float tr = comp * weights[pilot_base + 2u * k];
+                const float ti = comp * weights[pilot_base + 2u * k + 1u];
+                pr = pr + tr;
+                pi = pi + ti;
+            }
+            const float sr = pr * p->gain, si = pi * p->gain;
+            const float rr = sr * sr, ii = si * si;
+            const float power = rr + ii;
+            const float inverse = det_recip((power < kPilotLockPower) ? kPilotLockPower : power);
+            const float cross = sr * si;
+            const float cos_two = (ii - rr) * inverse;
+            const float sin_two = (-2.0F * cross) * inverse;
+            const float locked = (power >= kPilotLockPower) ? 1.0F : 0.0F;
+            float sum = 0.0F, diff = 0.0F;
+            for (uint32_t t = 0; t < c->audio_taps; ++t) {
+                const float weighted = detect(&d, index - t) * weights[t];
+                sum = sum + weighted;
+                const float ref = sin_two * weights[rotation_base + 2u * t] -
+                                  cos_two * weights[rotation_base + 2u * t + 1u];
+                const float term = weighted * ref;
+                diff = diff + term;
+            }
+            const float gated = diff * locked;
+            audio[2u * i] = (sum + gated) * p->gain;
+            audio[2u * i + 1u] = (sum - gated) * p->gain;
+            continue;
+        }
+        float acc = 0.0F;
+        for (uint32_t t = 0; t < c->audio_taps; ++t) {
+            const float term = detect(&d, index - t) * weights[t];
+            acc = acc + term;
+        }
+        audio[i] = acc * p->gain;
+    }
+    flush_end(&s);
+    return ok();
+}
+
+/* ------------------------------------------------------------------ */
+/* carrier loop (core/dsp/vrx_reference.cpp:1040-1187)                 */
+
+static float clampf3(float v, float lo, float hi) {
+    const float m = (v < lo) ? lo : v; /* std::max(v, lo) */
+    return (hi < m) ? hi : m;          /* std::min(m, hi) */
+}
+
+int32_t or_vrx_carrier(const rv_vrx_carrier_config* c, const rv_vrx_carrier_params* p,
+                       const rv_cf32* nco, uint64_t nco_len, rv_cf32* fine, uint64_t fine_len,
+                       uint32_t* state) {
+    if (c->power != 1u && c->power != 2u) return fail("vrx carrier: power");
+    if (c->nco_log2 == 0 || c->nco_log2 > 24) return fail("vrx carrier: nco_log2");
+    const uint64_t cap = (uint64_t)p->in_mask + 1u;
+    if ((cap & (uint64_t)p->in_mask) != 0) return fail("vrx carrier: in_mask");
+    if (p->count > cap) return fail("vrx carrier: count exceeds the ring");
+    if ((p->flags & ~1u) != 0) return fail("vrx carrier: unknown flags");
+    if (!isfinite(p->shift)) return fail("vrx carrier: shift not finite");
+    if (!(p->clamp_radians > 0.0F) || !((double)p->clamp_radians <= 0.5 * 3.14159265358979323846))
+        return fail("vrx carrier: clamp");
+    if (!(p->k1_acquire > 0.0F && p->k1_acquire < 1.0F) || !(p->k1_track > 0.0F && p->k1_track < 1.0F))
+        return fail("vrx carrier: proportional gain");
+    if (!(p->k2_acquire > 0.0F && p->k2_acquire < 1.0F) || !(p->k2_track > 0.0F && p->k2_track < 1.0F))
+        return fail("vrx carrier: integral gain");
+    if (!(p->level_alpha > 0.0F && p->level_alpha <= 1.0F) || !(p->lock_alpha > 0.0F && p->lock_alpha <= 1.0F))
+        return fail("vrx carrier: one-pole coefficient");
+    if (p->hold_in == 0 || p->hold_out == 0) return fail("vrx carrier: zero hold");
+    if (nco_len != (1ull << c->nco_log2)) return fail("vrx carrier: nco size");
+    if (fine_len < cap) return fail("vrx carrier: fine ring");
+
+    const float kTurnsPerRadian = (float)683565275.576431632;
+    const float kLevelFloor = (float)1.0e-24;
+    flush_scope s;
+    flush_begin(&s);
+    const int reset = (p->flags & 1u) != 0;
+    uint32_t phase = reset ? 0u : state[0];
+    float integrator = reset ? 0.0F : float_of(state[1]);
+    float level = reset ? 0.0F : float_of(state[2]);
+    float lock_re = reset ? 0.0F : float_of(state[3]);
+    float lock_im = reset ? 0.0F : float_of(state[4]);
+    uint32_t locked = reset ? 0u : state[5];
+    uint32_t held = reset ? 0u : state[6];
+    uint32_t primed = reset ? 0u : state[7];
+    integrator = clampf3(integrator + p->shift, -p->clamp_radians, p->clamp_radians);
+    const uint32_t down = 32u - c->nco_log2;
+    for (uint32_t i = 0; i < p->count; ++i) {
+        rv_cf32* zp = &fine[(p->in_offset + i) & p->in_mask];
+        const rv_cf32 z = *zp;
+        const rv_cf32 r = nco[phase >> down];
+        const float yr = z.re * r.re - z.im * r.im;
+        const float yi = z.re * r.im + z.im * r.re;
+        zp->re = yr;
+        zp->im = yi;
+        const float rr = yr * yr, ii = yi * yi;
+        const float power = rr + ii;
+        const float cross = yr * yi;
+        float wr, wi, mag;
+        if (c->power == 1u) {
+            wr = yr;
+            wi = yi;
+            mag = det_sqrt(power);
+        } else {
+            wr = rr - ii;
+            wi = cross + cross;
+            mag = power;
+        }
+        if (primed == 0u) {
+            level = mag;
+            primed = 1u;
+        } else {
+            const float step = p->level_alpha * (mag - level);
+            level = level + step;
+        }
+        {
+            const float sr = p->lock_alpha * (wr - lock_re);
+            const float si = p->lock_alpha * (wi - lock_im);
+            lock_re = lock_re + sr;
+            lock_im = lock_im + si;
+        }
+        const float bound = 2.0F * fabsf(lock_im);
+        const int inside = lock_re > bound;
+        if (locked != 0u) {
+            held = inside ? (held > 0u ? held - 1u : 0u) : held + 1u;
+            if (held >= p->hold_out) { locked = 0u; held = 0u; }
+        } else {
+            held = inside ? held + 1u : 0u;
+            if (held >= p->hold_in) { locked = 1u; held = 0u; }
+        }
+        const float inverse = det_recip((level < kLevelFloor) ? kLevelFloor : level);
+        const float detected = ((c->power == 1u) ? yi : cross) * inverse;
+        const float error = clampf3(detected, -1.0F, 1.0F);
+        const float k1 = locked ? p->k1_track : p->k1_acquire;
+        const float k2 = locked ? p->k2_track : p->k2_acquire;
+        integrator = clampf3(integrator + k2 * error, -p->clamp_radians, p->clamp_radians);
+        const float advance = k1 * error + integrator;
+        const float turns = advance * kTurnsPerRadian;
+        phase = phase + (uint32_t)(int32_t)turns;
+    }
+    state[0] = phase;
+    state[1] = bits_of(integrator);
+    state[2] = bits_of(level);
+    state[3] = bits_of(lock_re);
+    state[4] = bits_of(lock_im);
+    state[5] = locked;
+    state[6] = held;
+    state[7] = primed;
+    flush_end(&s);
+    return ok();
+}

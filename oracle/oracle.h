@@ -1,0 +1,87 @@
+/*
+ * oracle.h — CPU restatement of the reference's receive-chain twins.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT. Only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline / reference leg may load this library, and only as
+ * the checker (or the timed CPU arm). The GPU library never links it and has
+ * no CPU fallback.
+ *
+ * Each function restates, in plain C, the reference CPU twin cited beside it,
+ * in the same operation order: fp32 with no contraction and denormals flushed
+ * to zero, so that results are bit-identical to the twin (and to the CUDA
+ * kernels). Parity of this restatement with the reference itself is pinned in
+ * tests/test_oracle_pin.py against the reference's own twins compiled from
+ * source (oracle/ref), and by the committed fixtures in tests/golden/.
+ *
+ * The *_f64 functions are double-precision restatements of the same maths
+ * (not of the fp32 operation order), used as the error yardstick for the
+ * reordered / split-precision paths.
+ *
+ * Return value: 0 on success, -1 on rejected parameters (message from
+ * or_last_error()), mirroring the twins' Status.
+ */
+#ifndef REVENANT_ORACLE_H
+#define REVENANT_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/revenant_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+const char* or_last_error(void);
+
+float or_det_rsqrt(float v);
+float or_det_sqrt(float v);
+float or_det_recip(float v);
+float or_det_atan2(float y, float x);
+float or_det_log2(float v);
+
+int32_t or_convert(int32_t format, const rv_convert_params* p, const void* packed,
+                   uint64_t packed_bytes, rv_cf32* ring, uint64_t ring_len);
+int32_t or_pfb_branch(const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                      uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out,
+                      uint64_t out_len);
+int32_t or_pfb_fft(const rv_pfb_fft_params* p, const rv_cf32* branch, uint64_t branch_len,
+                   const rv_cf32* twiddles, uint64_t tw_len, rv_cf32* ring, uint64_t ring_len);
+int32_t or_fft_radix2(const rv_cf32* twiddles, const rv_cf32* in, rv_cf32* out, uint32_t size,
+                      uint32_t batch);
+int32_t or_spectrum(const rv_spectrum_params* p, const rv_cf32* ring, uint64_t ring_len,
+                    const rv_cf32* twiddles, uint64_t tw_len, const float* window,
+                    uint64_t window_len, float* frame, uint64_t frame_len);
+int32_t or_spectrum_levels(const rv_spectrum_levels_params* p, const float* frame,
+                           uint64_t frame_len, float* levels);
+int32_t or_vrx_fine(const rv_vrx_fine_config* c, const rv_vrx_fine_params* p, const rv_cf32* chan,
+                    uint64_t chan_len, const rv_cf32* taps, uint64_t taps_len, const rv_cf32* nco,
+                    uint64_t nco_len, rv_cf32* fine, uint64_t fine_len);
+int32_t or_vrx_demod(const rv_vrx_demod_config* c, const rv_vrx_demod_params* p,
+                     const rv_cf32* fine, uint64_t fine_len, const float* weights,
+                     uint64_t weights_len, float* audio, uint64_t audio_len);
+int32_t or_vrx_carrier(const rv_vrx_carrier_config* c, const rv_vrx_carrier_params* p,
+                       const rv_cf32* nco, uint64_t nco_len, rv_cf32* fine, uint64_t fine_len,
+                       uint32_t* state);
+
+/* Whole coarse chain for a contiguous cs16 capture: convert -> branch -> FFT,
+ * block by block, over `threads` host threads (0 = all). Output is the
+ * channel-major ring [M][out_ring_blocks]. Used as the timed CPU arm and as
+ * the checker of the fused GPU coarse kernel. */
+int32_t or_coarse_cs16(const rv_grid_params* g, const float* taps, const rv_cf32* twiddles,
+                       const void* packed, uint64_t samples, uint64_t first_block,
+                       uint32_t block_count, uint32_t out_ring_blocks, rv_cf32* channel_ring,
+                       int32_t threads);
+
+/* FP64 yardstick: PFB channelizer (branch FIR + exact M-point DFT + phase
+ * correction) of cf32 input x (as double), for blocks [0, block_count):
+ * y[k][m] = sum_r branch_r(m) * exp(-2 pi i k (M - r mod M)/M) * exp(-2 pi i k m D / M).
+ * Output channel-major [M][block_count] complex double. */
+int32_t or_pfb_f64(const rv_grid_params* g, const float* taps, const rv_cf32* ring,
+                   uint32_t ring_mask, uint32_t base_offset, uint32_t block_count,
+                   uint32_t block_base, double* out_re, double* out_im);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

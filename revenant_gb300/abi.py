@@ -1,0 +1,154 @@
+"""ctypes mirror of include/revenant_gb300.h (structs and constants).
+
+Field order and widths match the C header exactly; tests/test_abi.py checks
+sizes and that the shared library exports every declared entry point.
+"""
+import ctypes as C
+
+U32, U64, I32, I64, F32 = C.c_uint32, C.c_uint64, C.c_int32, C.c_int64, C.c_float
+
+RV_OK = 0
+RV_ERR_INVALID = -1
+RV_ERR_CUDA = -2
+RV_ERR_NO_DEVICE = -3
+RV_ERR_NO_MEMORY = -4
+RV_ERR_UNSUPPORTED = -5
+RV_ERR_TIMEOUT = -6
+
+FORMAT_CU8, FORMAT_CS8, FORMAT_CS16, FORMAT_CS24 = 0, 1, 2, 3
+BYTES_PER_SAMPLE = {FORMAT_CU8: 2, FORMAT_CS8: 2, FORMAT_CS16: 4, FORMAT_CS24: 6}
+
+DEMOD = dict(raw=0, am=1, nfm=2, wfm=3, usb=4, lsb=5, dsb=6, cw=7, p25p1=8, dstar=9, tetra=10,
+             dmr=11, sam=12)
+
+MEMORY_DEVICE_LOCAL, MEMORY_UPLOAD, MEMORY_READBACK = 0, 1, 2
+
+
+class _S(C.Structure):
+    def __repr__(self):
+        return "%s(%s)" % (type(self).__name__,
+                           ", ".join("%s=%r" % (n, getattr(self, n)) for n, _ in self._fields_))
+
+    def as_dict(self):
+        out = {}
+        for n, _ in self._fields_:
+            v = getattr(self, n)
+            out[n] = v.as_dict() if isinstance(v, _S) else v
+        return out
+
+
+class CF32(_S):
+    _fields_ = [("re", F32), ("im", F32)]
+
+
+class ConvertParams(_S):
+    _fields_ = [("ring_mask", U32), ("dst_offset", U32), ("src_offset", U32), ("count", U32)]
+
+
+class GridParams(_S):
+    _fields_ = [("channels", U32), ("taps_per_branch", U32), ("decimation", U32)]
+
+
+class PfbBranchParams(_S):
+    _fields_ = [("ring_mask", U32), ("base_offset", U32), ("block_count", U32)]
+
+
+class PfbFftParams(_S):
+    _fields_ = [("channels", U32), ("decimation", U32), ("stages", U32), ("block_base", U32),
+                ("block_count", U32), ("out_ring_blocks", U32), ("out_ring_mask", U32)]
+
+
+class SpectrumParams(_S):
+    _fields_ = [("channels", U32), ("transform", U32), ("stages", U32), ("chan_blocks", U32),
+                ("chan_mask", U32), ("in_offset", U32)]
+
+
+class SpectrumLevelsParams(_S):
+    _fields_ = [("bins", U32), ("low_permille", U32), ("high_permille", U32)]
+
+
+class VrxFineConfig(_S):
+    _fields_ = [("taps", U32), ("phases", U32), ("nco_log2", U32)]
+
+
+class VrxFineParams(_S):
+    _fields_ = [("chan_base", U32), ("chan_mask", U32), ("in_offset", U32), ("out_offset", U32),
+                ("out_mask", U32), ("count", U32), ("step_whole", U32), ("step_rem", U32),
+                ("out_rate", U32), ("frac0", U32), ("nco_phase_high", U32), ("nco_phase_low", U32),
+                ("nco_delta_high", U32), ("nco_delta_low", U32), ("inv_out_rate", F32)]
+
+
+class VrxDemodConfig(_S):
+    _fields_ = [("mode", U32), ("decimation", U32), ("audio_taps", U32), ("dc_taps", U32),
+                ("channels", U32), ("pilot_taps", U32)]
+
+
+class VrxDemodParams(_S):
+    _fields_ = [("in_mask", U32), ("in_offset", U32), ("count", U32), ("gain", F32)]
+
+
+class VrxCarrierConfig(_S):
+    _fields_ = [("power", U32), ("nco_log2", U32)]
+
+
+class VrxCarrierParams(_S):
+    _fields_ = [("in_mask", U32), ("in_offset", U32), ("count", U32), ("flags", U32),
+                ("shift", F32), ("k1_acquire", F32), ("k2_acquire", F32), ("k1_track", F32),
+                ("k2_track", F32), ("level_alpha", F32), ("lock_alpha", F32),
+                ("clamp_radians", F32), ("hold_in", U32), ("hold_out", U32)]
+
+
+class VrxRequest(_S):
+    _fields_ = [("center", I64), ("bandwidth", I64), ("passband_low", I64), ("passband_high", I64),
+                ("demod", U32), ("deemphasis", U32), ("stereo", U32), ("reserved", U32),
+                ("audio_rate", I64), ("cw_pitch", I64)]
+
+
+class VrxPlacement(_S):
+    _fields_ = [("channel", U32), ("bandwidth_clamped", U32), ("centre_numerator", I64),
+                ("centre_denominator", I64), ("residual_numerator", I64),
+                ("residual_denominator", I64), ("channel_rate", I64), ("granted_low", I64),
+                ("granted_high", I64)]
+
+
+class VrxPlanInfo(_S):
+    _fields_ = [("placement", VrxPlacement), ("mode", U32), ("bandwidth_clamped", U32),
+                ("channel_rate", I64), ("audio_rate", I64), ("demod_rate", I64),
+                ("output_rate", I64), ("passband_low", I64), ("passband_high", I64),
+                ("bandwidth", I64), ("filter_numerator", I64), ("filter_denominator", I64),
+                ("mix_numerator", I64), ("mix_denominator", I64), ("fine", VrxFineConfig),
+                ("stereo", U32), ("fine_nco_delta", U64), ("demod", VrxDemodConfig),
+                ("demod_gain", F32), ("carrier", VrxCarrierConfig),
+                ("carrier_loop", VrxCarrierParams), ("deviation", I64), ("deemphasis", U32),
+                ("deemphasis_taps", U32), ("audio_decimation_taps", U32), ("reserved", U32),
+                ("fine_tap_count", U64), ("demod_weight_count", U64)]
+
+
+class VrxFineBlock(_S):
+    _fields_ = [("params", VrxFineParams), ("reserved", U32), ("first_input", U64),
+                ("oldest_input", U64), ("newest_input", U64)]
+
+
+class VrxDemodBlock(_S):
+    _fields_ = [("params", VrxDemodParams), ("first_fine", U64), ("oldest_fine", U64)]
+
+
+class DeviceInfo(_S):
+    _fields_ = [("name", C.c_char * 256), ("device_index", I32), ("sm_count", I32),
+                ("cc_major", I32), ("cc_minor", I32), ("total_memory", U64),
+                ("max_shared_per_block", U64), ("l2_bytes", U64)]
+
+
+def request(center=0, bandwidth=0, demod="nfm", deemphasis=0, stereo=True, audio_rate=0,
+            passband_low=0, passband_high=0, cw_pitch=700):
+    r = VrxRequest()
+    r.center = center
+    r.bandwidth = bandwidth
+    r.passband_low = passband_low
+    r.passband_high = passband_high
+    r.demod = DEMOD[demod] if isinstance(demod, str) else demod
+    r.deemphasis = deemphasis
+    r.stereo = 1 if stereo else 0
+    r.audio_rate = audio_rate
+    r.cw_pitch = cw_pitch
+    return r

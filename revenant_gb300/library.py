@@ -1,0 +1,173 @@
+"""Build and load librevenant_gb300.so (CUDA for sm_103a + C++ host code).
+
+``build()`` compiles every translation unit under csrc/ with nvcc for
+sm_103a only (``-gencode arch=compute_103a,code=sm_103a``), in parallel, into
+an in-tree shared library. ``lib()`` loads it once and declares the C
+signatures from include/revenant_gb300.h. Nothing here implements a kernel;
+if the library cannot be loaded every entry point raises.
+"""
+import ctypes as C
+import os
+import subprocess
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+SO = os.path.join(OUT, "librevenant_gb300.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-ffp-contract=off", "--fmad=false", "-ftz=true", "-prec-div=true",
+              "-prec-sqrt=true", "-I" + INCLUDE, "-I" + CSRC]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
+             "-I" + INCLUDE, "-I" + CSRC]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def _sources():
+    cu, cpp = [], []
+    for name in sorted(os.listdir(CSRC)):
+        path = os.path.join(CSRC, name)
+        if name.endswith(".cu"):
+            cu.append(path)
+        elif name.endswith(".cpp"):
+            cpp.append(path)
+    return cu, cpp
+
+
+def _headers():
+    hs = [os.path.join(INCLUDE, n) for n in os.listdir(INCLUDE)]
+    hs += [os.path.join(CSRC, n) for n in os.listdir(CSRC) if n.endswith((".h", ".cuh"))]
+    return hs
+
+
+def build(force=False, verbose=False):
+    """Compile csrc/ into _build/librevenant_gb300.so (sm_103a only)."""
+    cu, cpp = _sources()
+    os.makedirs(os.path.join(OUT, "obj"), exist_ok=True)
+    headers_mtime = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(__file__)])
+    nvcc = _nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(OUT, "obj", os.path.basename(src) + ".o")
+        if (not force and os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
+                and os.path.getmtime(obj) >= headers_mtime):
+            return obj
+        if src.endswith(".cu"):
+            cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj + ".tmp"]
+        else:
+            cmd = ["g++"] + CXX_FLAGS + ["-c", src, "-o", obj + ".tmp"]
+        if verbose:
+            print(" ".join(cmd))
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("compile failed: %s\n%s%s" % (src, res.stdout, res.stderr))
+        os.replace(obj + ".tmp", obj)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as pool:
+        objs = list(pool.map(compile_one, cu + cpp))
+    if force or not os.path.exists(SO) or any(os.path.getmtime(o) > os.path.getmtime(SO) for o in objs):
+        cmd = [nvcc] + ARCH + ["-shared", "-o", SO + ".tmp"] + objs + ["-lcudart", "-lpthread"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("link failed\n%s%s" % (res.stdout, res.stderr))
+        os.replace(SO + ".tmp", SO)
+    return SO
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+class LibraryError(RuntimeError):
+    pass
+
+
+def load(path=SO):
+    """Load the shared library and declare its signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise LibraryError("librevenant_gb300.so is not built (%s); run "
+                               "revenant_gb300.build() first" % path)
+        lib = C.CDLL(path)
+        _declare(lib)
+        _lib = lib
+        return lib
+
+
+def lib():
+    return load()
+
+
+P = C.c_void_p
+U32, U64, I32, I64, F32, F64 = C.c_uint32, C.c_uint64, C.c_int32, C.c_int64, C.c_float, C.c_double
+ptr = C.POINTER
+
+# name -> (restype, argtypes); the single list the ABI test walks.
+SIGNATURES = {
+    "rv_last_error": (C.c_char_p, []),
+    "rv_abi_version": (I32, []),
+    "rv_context_create": (I32, [I32, ptr(P)]),
+    "rv_context_destroy": (I32, [P]),
+    "rv_context_device_info": (I32, [P, ptr(abi.DeviceInfo)]),
+    "rv_context_stream": (P, [P]),
+    "rv_context_synchronize": (I32, [P]),
+    "rv_buffer_create": (I32, [P, U64, I32, ptr(P)]),
+    "rv_buffer_destroy": (I32, [P]),
+    "rv_buffer_address": (P, [P]),
+    "rv_buffer_size": (U64, [P]),
+    "rv_buffer_upload": (I32, [P, U64, P, U64]),
+    "rv_buffer_download": (I32, [P, U64, P, U64]),
+    "rv_buffer_clear": (I32, [P]),
+    "rv_convert": (I32, [P, I32, ptr(abi.ConvertParams), P, U64, P, U64]),
+    "rv_pfb_branch": (I32, [P, ptr(abi.GridParams), ptr(abi.PfbBranchParams), P, U64, P, U64, P, U64]),
+    "rv_pfb_fft": (I32, [P, ptr(abi.PfbFftParams), P, U64, P, U64, P, U64]),
+    "rv_spectrum": (I32, [P, ptr(abi.SpectrumParams), P, U64, P, U64, P, U64, P, U64]),
+    "rv_spectrum_levels": (I32, [P, ptr(abi.SpectrumLevelsParams), P, U64, P]),
+    "rv_vrx_fine": (I32, [P, ptr(abi.VrxFineConfig), ptr(abi.VrxFineParams), P, U64, P, U64, P, U64, P, U64]),
+    "rv_vrx_demod": (I32, [P, ptr(abi.VrxDemodConfig), ptr(abi.VrxDemodParams), P, U64, P, U64, P, U64]),
+    "rv_vrx_carrier": (I32, [P, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P]),
+    "rv_validate_grid": (I32, [ptr(abi.GridParams)]),
+    "rv_design_prototype": (I32, [ptr(abi.GridParams), F64, P, U64, ptr(F64), ptr(U64)]),
+    "rv_build_twiddles": (I32, [U32, P, U64]),
+    "rv_build_nco_table": (I32, [U32, P, U64]),
+    "rv_build_spectrum_window": (I32, [U32, U32, F64, P, U64]),
+    "rv_place": (I32, [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), ptr(abi.VrxPlacement)]),
+    "rv_channel_count_for": (U32, [I64, I64]),
+    "rv_plan_vrx": (I32, [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), ptr(abi.VrxPlacement),
+                          ptr(abi.VrxPlanInfo), P, U64, P, U64]),
+    "rv_fine_block": (I32, [ptr(abi.VrxPlanInfo), U32, U32, U32, U64, U32, ptr(abi.VrxFineBlock)]),
+    "rv_demod_block": (I32, [ptr(abi.VrxPlanInfo), U32, U64, U32, ptr(abi.VrxDemodBlock)]),
+    "rv_carrier_block": (I32, [ptr(abi.VrxPlanInfo), U32, U64, U32, I32, F32, ptr(abi.VrxCarrierParams)]),
+    "rv_demod_fine_history": (U32, [ptr(abi.VrxDemodConfig)]),
+}
+
+
+def _declare(lib):
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def check(status):
+    """Raise with rv_last_error() when a call returned a negative status."""
+    if status != abi.RV_OK:
+        raise LibraryError("revenant_gb300 error %d: %s" % (status, lib().rv_last_error().decode()))
+    return status

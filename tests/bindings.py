@@ -1,0 +1,168 @@
+"""ctypes views of the three C libraries the tests compare.
+
+- ``oracle()``  : oracle/_build/liboracle.so, the CPU restatement (or_*).
+- ``reference()``: oracle/_ref/libreftwins.so, the reference's own twins
+  compiled from its sources (ref_*); None where the sources are absent.
+- the GPU library is bound in revenant_gb300 itself (rv_*).
+
+All three share one calling convention, so a test can run the same case
+through each and compare the bytes.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+from revenant_gb300 import abi  # noqa: E402  (struct definitions)
+
+P = C.c_void_p
+U32, U64, I32, I64, F32, F64 = C.c_uint32, C.c_uint64, C.c_int32, C.c_int64, C.c_float, C.c_double
+ptr = C.POINTER
+
+
+def _sig(lib, prefix):
+    def f(name, res, *args):
+        fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = list(args)
+    f("last_error", C.c_char_p)
+    for n in ("det_rsqrt", "det_sqrt", "det_recip", "det_log2"):
+        f(n, F32, F32)
+    f("det_atan2", F32, F32, F32)
+    f("convert", I32, I32, ptr(abi.ConvertParams), P, U64, P, U64)
+    f("pfb_branch", I32, ptr(abi.GridParams), ptr(abi.PfbBranchParams), P, U64, P, U64, P, U64)
+    f("pfb_fft", I32, ptr(abi.PfbFftParams), P, U64, P, U64, P, U64)
+    f("fft_radix2", I32, P, P, P, U32, U32)
+    f("spectrum", I32, ptr(abi.SpectrumParams), P, U64, P, U64, P, U64, P, U64)
+    f("spectrum_levels", I32, ptr(abi.SpectrumLevelsParams), P, U64, P)
+    f("vrx_fine", I32, ptr(abi.VrxFineConfig), ptr(abi.VrxFineParams), P, U64, P, U64, P, U64, P, U64)
+    f("vrx_demod", I32, ptr(abi.VrxDemodConfig), ptr(abi.VrxDemodParams), P, U64, P, U64, P, U64)
+    f("vrx_carrier", I32, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P)
+
+
+_oracle = None
+_reference = None
+
+
+def oracle():
+    global _oracle
+    if _oracle is None:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import build as oracle_build  # oracle/build.py
+        lib = C.CDLL(oracle_build.build())
+        _sig(lib, "or_")
+        lib.or_coarse_cs16.restype = I32
+        lib.or_coarse_cs16.argtypes = [ptr(abi.GridParams), P, P, P, U64, U64, U32, U32, P, I32]
+        lib.or_pfb_f64.restype = I32
+        lib.or_pfb_f64.argtypes = [ptr(abi.GridParams), P, P, U32, U32, U32, U32, P, P]
+        _oracle = Lib(lib, "or_")
+    return _oracle
+
+
+def reference():
+    """The reference's own twins, or None when they were not built here."""
+    global _reference
+    if _reference is None:
+        path = os.path.join(ROOT, "oracle", "_ref", "libreftwins.so")
+        if not os.path.exists(path):
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import build as oracle_build
+            try:
+                built = oracle_build.build_reference()
+            except Exception:
+                built = None
+            if not built or not os.path.exists(path):
+                return None
+        lib = C.CDLL(path)
+        _sig(lib, "ref_")
+        lib.ref_design_prototype.restype = I32
+        lib.ref_design_prototype.argtypes = [ptr(abi.GridParams), F64, P, U64, ptr(F64), ptr(U64)]
+        lib.ref_build_twiddles.restype = I32
+        lib.ref_build_twiddles.argtypes = [U32, P, U64]
+        lib.ref_build_nco_table.restype = I32
+        lib.ref_build_nco_table.argtypes = [U32, P, U64]
+        lib.ref_build_spectrum_window.restype = I32
+        lib.ref_build_spectrum_window.argtypes = [U32, U32, F64, P, U64]
+        lib.ref_place.restype = I32
+        lib.ref_place.argtypes = [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), ptr(abi.VrxPlacement)]
+        lib.ref_channel_count_for.restype = U32
+        lib.ref_channel_count_for.argtypes = [I64, I64]
+        lib.ref_plan_vrx.restype = I32
+        lib.ref_plan_vrx.argtypes = [ptr(abi.GridParams), I64, ptr(abi.VrxRequest),
+                                     ptr(abi.VrxPlacement), ptr(abi.VrxPlanInfo), P, U64, P, U64]
+        lib.ref_fine_block.restype = I32
+        lib.ref_fine_block.argtypes = [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), U32, U32, U32,
+                                       U64, U32, ptr(abi.VrxFineBlock)]
+        lib.ref_demod_block.restype = I32
+        lib.ref_demod_block.argtypes = [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), U32, U64, U32,
+                                        ptr(abi.VrxDemodBlock)]
+        _reference = Lib(lib, "ref_")
+    return _reference
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Lib:
+    """numpy-friendly wrappers; each returns (status, outputs...)."""
+
+    def __init__(self, lib, prefix):
+        self.lib = lib
+        self.prefix = prefix
+
+    def fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    def error(self):
+        return self.fn("last_error")().decode()
+
+    def det(self, name, *args):
+        return self.fn(name)(*args)
+
+    def convert(self, fmt, params, packed, ring):
+        st = self.fn("convert")(fmt, C.byref(params), _p(packed), packed.nbytes, _p(ring), ring.shape[0])
+        return st
+
+    def pfb_branch(self, grid, params, taps, ring, out):
+        return self.fn("pfb_branch")(C.byref(grid), C.byref(params), _p(taps), taps.size,
+                                     _p(ring), ring.shape[0], _p(out), out.shape[0])
+
+    def pfb_fft(self, params, branch, tw, ring):
+        return self.fn("pfb_fft")(C.byref(params), _p(branch), branch.shape[0], _p(tw), tw.shape[0],
+                                  _p(ring), ring.shape[0])
+
+    def fft_radix2(self, tw, x, out, size, batch):
+        return self.fn("fft_radix2")(_p(tw), _p(x), _p(out), size, batch)
+
+    def spectrum(self, params, ring, tw, window, frame):
+        return self.fn("spectrum")(C.byref(params), _p(ring), ring.shape[0], _p(tw), tw.shape[0],
+                                   _p(window), window.size, _p(frame), frame.size)
+
+    def spectrum_levels(self, params, frame, levels):
+        return self.fn("spectrum_levels")(C.byref(params), _p(frame), frame.size, _p(levels))
+
+    def vrx_fine(self, config, params, chan, taps, nco, fine):
+        return self.fn("vrx_fine")(C.byref(config), C.byref(params), _p(chan), chan.shape[0],
+                                   _p(taps), taps.shape[0], _p(nco), nco.shape[0], _p(fine), fine.shape[0])
+
+    def vrx_demod(self, config, params, fine, weights, audio):
+        return self.fn("vrx_demod")(C.byref(config), C.byref(params), _p(fine), fine.shape[0],
+                                    _p(weights), weights.size, _p(audio), audio.size)
+
+    def vrx_carrier(self, config, params, nco, fine, state):
+        return self.fn("vrx_carrier")(C.byref(config), C.byref(params), _p(nco), nco.shape[0],
+                                      _p(fine), fine.shape[0], _p(state))
+
+
+def cf32(n):
+    """Zeroed complex-float buffer as an (n, 2) float32 array."""
+    return np.zeros((n, 2), dtype=np.float32)
+
+
+def same_bits(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
