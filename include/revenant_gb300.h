@@ -375,6 +375,34 @@ int32_t rv_vrx_carrier(void* stream, const rv_vrx_carrier_config* config,
                        uint32_t* state_dev);
 
 /* ===================================================================== *
+ * Fused kernels (same outputs as the plain chain, bit for bit)           *
+ * ===================================================================== */
+
+/* Parameters of the fused coarse chain: PfbBranchParams' ring view of the
+ * raw input plus PfbFftParams' output view. */
+typedef struct rv_coarse_params {
+    uint32_t ring_mask;       /* raw ring capacity in samples, minus one */
+    uint32_t base_offset;     /* ring position of x[mD] for block 0 */
+    uint32_t block_count;
+    uint32_t block_base;      /* absolute output block index of block 0 */
+    uint32_t out_ring_blocks; /* channel ring blocks per channel, power of two */
+    uint32_t out_ring_mask;
+} rv_coarse_params;
+
+/* convert -> pfb_branch -> pfb_fft in one launch, reading the staging ring
+ * in its native format (RV_FORMAT_CS16: one 32-bit word per sample;
+ * RV_FORMAT_CU8: two samples per word) and writing the channel-major ring
+ * [M][out_ring_blocks]. Output is bit-identical to rv_convert (whole ring,
+ * dst_offset 0) followed by rv_pfb_branch and rv_pfb_fft with the same
+ * offsets (core/engine/graph.cpp:5118-5199). Grids without a fused
+ * instantiation return RV_ERR_UNSUPPORTED. */
+int32_t rv_coarse_fused(void* stream, const rv_grid_params* grid, int32_t format,
+                        const rv_coarse_params* params, const void* raw_ring_dev,
+                        uint64_t raw_ring_bytes, const float* taps_dev, uint64_t taps_len,
+                        const rv_cf32* twiddles_dev, uint64_t twiddles_len,
+                        rv_cf32* channel_ring_dev, uint64_t channel_ring_len);
+
+/* ===================================================================== *
  * Host planning (core/dsp/pfb_design.cpp, vrx_reference.cpp,             *
  * core/engine/vrx_place.cpp), restated; results equal the reference's.   *
  * ===================================================================== */

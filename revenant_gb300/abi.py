@@ -98,6 +98,11 @@ class VrxCarrierParams(_S):
                 ("clamp_radians", F32), ("hold_in", U32), ("hold_out", U32)]
 
 
+class CoarseParams(_S):
+    _fields_ = [("ring_mask", U32), ("base_offset", U32), ("block_count", U32), ("block_base", U32),
+                ("out_ring_blocks", U32), ("out_ring_mask", U32)]
+
+
 class VrxRequest(_S):
     _fields_ = [("center", I64), ("bandwidth", I64), ("passband_low", I64), ("passband_high", I64),
                 ("demod", U32), ("deemphasis", U32), ("stereo", U32), ("reserved", U32),
@@ -137,6 +142,9 @@ class DeviceInfo(_S):
     _fields_ = [("name", C.c_char * 256), ("device_index", I32), ("sm_count", I32),
                 ("cc_major", I32), ("cc_minor", I32), ("total_memory", U64),
                 ("max_shared_per_block", U64), ("l2_bytes", U64)]
+
+
+EXTRA_STRUCTS = {"rv_coarse_params": CoarseParams}
 
 
 def request(center=0, bandwidth=0, demod="nfm", deemphasis=0, stereo=True, audio_rate=0,

@@ -1,0 +1,312 @@
+// Fused coarse chain: raw IQ ring -> convert -> polyphase branch FIR ->
+// M-point FFT -> output phase correction -> channel-major ring, in one kernel.
+//
+// Computes exactly what the reference's three dispatches compute
+// (convert_*_cf32.comp, pfb_branch.comp:98-149, pfb_fft.comp:274-363; twins
+// core/dsp/convert.cpp, pfb_branch_reference.cpp:98-141,
+// pfb_fft_reference.cpp:54-228): the same per-output operation order, the
+// same butterfly arithmetic, so the channel ring is bit-identical to the
+// plain path. What changes is the data movement:
+//
+//  * Branch FIR as register sliding windows. For branch r, block b and block
+//    b + M/D share T-1 of their T input samples (the window advances by one
+//    polyphase row). Each thread owns one (branch r, block phase) pair and
+//    slides a T-sample window in registers, so every input sample is loaded
+//    from HBM and converted exactly once per tile (plus a T-1 warm-up), and
+//    each output costs T multiply-adds out of registers. Lanes of a warp own
+//    consecutive r, so each load instruction is one coalesced run of samples.
+//    The raw ring stays in its native width (4 B/sample for cs16), never
+//    widened to cf32 in HBM.
+//  * FFT in registers: radix-2 DIT stages taken three at a time inside one
+//    thread (8 values), with one shared-memory transpose between groups; the
+//    butterfly graph is the reference's, only visited in a different order.
+//  * Output staged in shared memory so each channel's slots for a chunk of
+//    blocks are written as one contiguous run.
+//
+// Per input sample the work is 2*T*M/D complex-by-real multiply-adds plus an
+// (M/D)/M share of one M-point FFT; every multiply and add rounds separately
+// (no FMA contraction, denormals flushed), as the reference twins require.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+#include "common.cuh"
+#include "revenant_gb300.h"
+
+namespace rv {
+int32_t validate_grid(const rv_grid_params* g);
+
+namespace {
+
+constexpr int kChunksPerTile = 8;
+
+__device__ __forceinline__ int32_t sext16(uint32_t raw) { return ((int32_t)(raw << 16)) >> 16; }
+
+// One raw sample at ring position pos (already masked), converted exactly as
+// the plain convert kernel converts it.
+template <int FMT>
+__device__ __forceinline__ float2 load_sample(const uint32_t* __restrict__ raw, uint32_t pos) {
+    if (FMT == RV_FORMAT_CS16) {
+        const uint32_t w = __ldg(&raw[pos]);
+        return make_float2((float)sext16(w & 0xFFFFu) * 0.000030517578125F,
+                           (float)sext16(w >> 16) * 0.000030517578125F);
+    } else {  // RV_FORMAT_CU8
+        const uint32_t w = __ldg(&raw[pos >> 1]);
+        const int shift = (int)((pos & 1u) << 4);
+        const uint32_t i_raw = (w >> shift) & 0xFFu;
+        const uint32_t q_raw = (w >> (shift + 8)) & 0xFFu;
+        return make_float2(((float)i_raw - 127.5F) * 0.00784313772F,
+                           ((float)q_raw - 127.5F) * 0.00784313772F);
+    }
+}
+
+// acc += s * c for both components: a rounded multiply then a rounded add per
+// component (packed f32x2 forms were measured not to reproduce the scalar
+// rounding bit for bit, so they are not used).
+__device__ __forceinline__ void mac(float2& acc, float2 s, float c) {
+    acc.x = acc.x + s.x * c;
+    acc.y = acc.y + s.y * c;
+}
+
+template <int L>
+__device__ __forceinline__ uint32_t brev_c(uint32_t v) {
+    return __brev(v) >> (32 - L);
+}
+
+template <int M>
+struct Log2 {
+    static constexpr int value = (M <= 1) ? 0 : 1 + Log2<M / 2>::value;
+};
+template <>
+struct Log2<1> {
+    static constexpr int value = 0;
+};
+
+// Position of local element u of FFT thread t when bit group g (bits
+// [3g, 3g+3)) is held in registers.
+__device__ __forceinline__ uint32_t group_pos(uint32_t t, uint32_t u, int g) {
+    const uint32_t lo_mask = (1u << (3 * g)) - 1u;
+    return (t & lo_mask) | (u << (3 * g)) | ((t >> (3 * g)) << (3 * g + 3));
+}
+
+template <int M, int T, int D, int FMT, int S>
+__global__ void __launch_bounds__(M*(M / D) * S)
+k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const rv_cf32* __restrict__ tw_g,
+         rv_cf32* __restrict__ ring, rv_coarse_params p, uint32_t tiles) {
+    constexpr int P = M / D;          // block phases sharing no samples
+    constexpr int NT = M * P * S;     // threads
+    constexpr int CB = T * P;         // blocks per chunk per sub-stream
+    constexpr int NB = CB * kChunksPerTile;
+    constexpr int TILE = S * NB;
+    constexpr int L = Log2<M>::value;
+    static_assert(L % 3 == 0, "fused coarse kernel holds three FFT stages per register group");
+    constexpr int G = L / 3;          // register groups of three stages
+    constexpr int FT = M / 8;         // FFT threads per block
+    constexpr int TASKS = S * CB * FT;
+    constexpr int ROUNDS = (TASKS + NT - 1) / NT;
+
+    extern __shared__ float2 smem[];
+    float2* twd = smem;               // [M]
+    float2* A = twd + M;              // [S*CB][M] branch outputs, then transpose scratch
+    float2* B = A + S * CB * M;       // [M][S*CB] channel-major staging
+
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t i = tid; i < (uint32_t)M; i += NT) twd[i] = ld_cf32(&tw_g[i]);
+
+    const uint32_t r = tid % M;
+    const uint32_t par = (tid / M) % P;
+    const uint32_t s = tid / (M * P);
+    float h[T];
+#pragma unroll
+    for (int q = 0; q < T; ++q) h[q] = taps[q * M + r];
+    __syncthreads();
+
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t tile0 = tile * (uint32_t)TILE;
+        // ring position of this thread's q = 0 sample for its first block
+        const uint32_t n0 = p.base_offset + (tile0 + s * NB + par) * (uint32_t)D - r;
+        float2 win[T];
+#pragma unroll
+        for (int q = 1; q < T; ++q) win[T - q] = load_sample<FMT>(raw, (n0 - (uint32_t)(q * M)) & p.ring_mask);
+
+        for (int c = 0; c < kChunksPerTile; ++c) {
+            // ---- branch FIR: T steps, window slot of sample q at step i is (i - q) mod T
+#pragma unroll
+            for (int i = 0; i < T; ++i) {
+                const uint32_t g = (uint32_t)(c * T + i);
+                win[i] = load_sample<FMT>(raw, (n0 + g * (uint32_t)M) & p.ring_mask);
+                float2 acc = make_float2(0.0F, 0.0F);
+#pragma unroll
+                for (int q = 0; q < T; ++q) mac(acc, win[(i - q + T) % T], h[q]);
+                const uint32_t bl = (uint32_t)i * P + par;
+                A[(s * CB + bl) * M + ((M - r) & (M - 1u))] = acc;
+            }
+            __syncthreads();
+
+            // ---- FFT, 8 values per thread, three stages per register group
+#pragma unroll 1
+            for (int round = 0; round < ROUNDS; ++round) {
+                const uint32_t task = (uint32_t)round * NT + tid;
+                const bool valid = task < (uint32_t)TASKS;
+                const uint32_t blk = valid ? task / FT : 0u;
+                const uint32_t t = task % FT;
+                float2* a = A + blk * M;
+                float2 v[8];
+                if (valid) {
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) v[u] = a[brev_c<L>(group_pos(t, u, 0))];
+                }
+#pragma unroll
+                for (int grp = 0; grp < G; ++grp) {
+                    if (grp > 0) {
+                        __syncwarp();
+                        if (valid) {
+#pragma unroll
+                            for (int u = 0; u < 8; ++u) a[group_pos(t, u, grp - 1)] = v[u];
+                        }
+                        __syncwarp();
+                        if (valid) {
+#pragma unroll
+                            for (int u = 0; u < 8; ++u) v[u] = a[group_pos(t, u, grp)];
+                        }
+                    }
+#pragma unroll
+                    for (int l = 0; l < 3; ++l) {
+                        const int st = 3 * grp + l;
+                        const uint32_t half = 1u << st;
+                        const uint32_t step = (uint32_t)M >> (st + 1);
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            if (u & (1 << l)) continue;
+                            const uint32_t j = group_pos(t, (uint32_t)u, grp) & (half - 1u);
+                            butterfly(v[u], v[u | (1 << l)], twd[j * step]);
+                        }
+                    }
+                }
+                if (valid) {
+                    const uint32_t sb = blk / CB, bl = blk % CB;
+                    const uint32_t m_abs = p.block_base + tile0 + sb * NB + (uint32_t)c * CB + bl;
+                    const uint32_t dm = ((m_abs & (M - 1u)) * (uint32_t)D) & (M - 1u);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const uint32_t k = group_pos(t, u, G - 1);
+                        float2 val = v[u];
+                        if (D != M) val = cmul(val, twd[(k * dm) & (M - 1u)]);
+                        B[k * (S * CB) + blk] = val;
+                    }
+                }
+            }
+            __syncthreads();
+
+            // ---- write-out: each channel's run of S*CB slots
+            for (uint32_t e = tid; e < (uint32_t)(M * S * CB); e += NT) {
+                const uint32_t k = e / (S * CB), blk = e % (S * CB);
+                const uint32_t sb = blk / CB, bl = blk % CB;
+                const uint32_t m_local = tile0 + sb * NB + (uint32_t)c * CB + bl;
+                if (m_local < p.block_count) {
+                    const uint32_t slot = (p.block_base + m_local) & p.out_ring_mask;
+                    st_cf32(&ring[(uint64_t)k * p.out_ring_blocks + slot], B[e]);
+                }
+            }
+        }
+    }
+}
+
+template <int M, int T, int D, int FMT, int S>
+int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
+               const rv_coarse_params& p) {
+    constexpr int P = M / D, NT = M * P * S, CB = T * P;
+    constexpr int TILE = S * CB * kChunksPerTile;
+    const size_t shared = sizeof(float2) * (M + 2 * S * CB * M);
+    auto kern = k_coarse<M, T, D, FMT, S>;
+    static int max_grid = 0;
+    if (max_grid == 0) {
+        if (shared > 48 * 1024) {
+            if (int32_t st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared),
+                                         "coarse shared"))
+                return st;
+        }
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (int32_t st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, shared),
+                                     "coarse occupancy"))
+            return st;
+        max_grid = (per_sm > 0 ? per_sm : 1) * sms;
+    }
+    const uint32_t tiles = (p.block_count + TILE - 1) / TILE;
+    const uint32_t grid = tiles < (uint32_t)max_grid ? tiles : (uint32_t)max_grid;
+    kern<<<grid, NT, shared, stream>>>(raw, taps, tw, ring, p, tiles);
+    return cuda_status(cudaGetLastError(), "coarse_fused launch");
+}
+
+}  // namespace
+
+// Dispatch over the instantiated grids. Returns RV_ERR_UNSUPPORTED for a
+// grid this build has no fused kernel for (the plain kernels cover it).
+int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
+                            const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring) {
+    const uint32_t* w = static_cast<const uint32_t*>(raw);
+#define RV_COARSE_CASE(MM, TT, DD, SS)                                                                    \
+    if (g.channels == MM && g.taps_per_branch == TT && g.decimation == DD) {                             \
+        if (format == RV_FORMAT_CS16) return launch<MM, TT, DD, RV_FORMAT_CS16, SS>(stream, w, taps, tw, ring, p); \
+        if (format == RV_FORMAT_CU8) return launch<MM, TT, DD, RV_FORMAT_CU8, SS>(stream, w, taps, tw, ring, p);   \
+    }
+    RV_COARSE_CASE(64, 17, 32, 1)
+    RV_COARSE_CASE(8, 17, 4, 8)
+    RV_COARSE_CASE(64, 17, 64, 2)
+#undef RV_COARSE_CASE
+    return set_error_fmt(RV_ERR_UNSUPPORTED,
+                         "coarse_fused: no fused kernel for M=%u T=%u D=%u format %d in this build (use the plain launches)",
+                         g.channels, g.taps_per_branch, g.decimation, format);
+}
+
+int32_t validate_coarse(const rv_grid_params* g, int32_t format, const rv_coarse_params* p, uint64_t raw_bytes,
+                        uint64_t taps_len, uint64_t tw_len, uint64_t ring_len) {
+    if (int32_t st = validate_grid(g)) return st;
+    if (format != RV_FORMAT_CS16 && format != RV_FORMAT_CU8)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "coarse_fused: format %d (cs16 and cu8 are fused)", format);
+    const uint32_t M = g->channels, T = g->taps_per_branch, D = g->decimation;
+    const uint64_t cap = (uint64_t)p->ring_mask + 1u;
+    if ((cap & (uint64_t)p->ring_mask) != 0 || cap < 2)
+        return set_error_fmt(RV_ERR_INVALID, "coarse_fused: ring_mask %u is not a power of two minus one", p->ring_mask);
+    const uint64_t need_bytes = format == RV_FORMAT_CS16 ? cap * 4u : cap * 2u;
+    if (raw_bytes < need_bytes)
+        return set_error_fmt(RV_ERR_INVALID, "coarse_fused: raw ring holds %llu bytes, mask implies %llu",
+                             (unsigned long long)raw_bytes, (unsigned long long)need_bytes);
+    if (taps_len != (uint64_t)M * T) return set_error_fmt(RV_ERR_INVALID, "coarse_fused: wants %u taps", M * T);
+    if (tw_len != M) return set_error_fmt(RV_ERR_INVALID, "coarse_fused: wants %u twiddles", M);
+    if (p->block_count == 0) return RV_OK;
+    const uint64_t span = (uint64_t)M * T + (uint64_t)(p->block_count - 1u) * D;
+    if (span > cap)
+        return set_error_fmt(RV_ERR_INVALID, "coarse_fused: needs %llu samples of history, ring capacity is %llu",
+                             (unsigned long long)span, (unsigned long long)cap);
+    if (!is_pow2(p->out_ring_blocks) || p->out_ring_mask != p->out_ring_blocks - 1u)
+        return set_error_fmt(RV_ERR_INVALID, "coarse_fused: out_ring_blocks must be a power of two and out_ring_mask one less");
+    if (p->block_count > p->out_ring_blocks)
+        return set_error_fmt(RV_ERR_INVALID, "coarse_fused: %u blocks overrun a %u-block ring", p->block_count,
+                             p->out_ring_blocks);
+    if (ring_len < (uint64_t)M * p->out_ring_blocks)
+        return set_error_fmt(RV_ERR_INVALID, "coarse_fused: channel ring too short");
+    return RV_OK;
+}
+
+}  // namespace rv
+
+extern "C" int32_t rv_coarse_fused(void* stream, const rv_grid_params* grid, int32_t format,
+                                   const rv_coarse_params* params, const void* raw_ring_dev, uint64_t raw_ring_bytes,
+                                   const float* taps_dev, uint64_t taps_len, const rv_cf32* twiddles_dev,
+                                   uint64_t twiddles_len, rv_cf32* channel_ring_dev, uint64_t channel_ring_len) {
+    if (grid == nullptr || params == nullptr || raw_ring_dev == nullptr || taps_dev == nullptr ||
+        twiddles_dev == nullptr || channel_ring_dev == nullptr)
+        return rv::set_error_fmt(RV_ERR_INVALID, "rv_coarse_fused: NULL argument");
+    if (int32_t st = rv::validate_coarse(grid, format, params, raw_ring_bytes, taps_len, twiddles_len, channel_ring_len))
+        return st;
+    if (params->block_count == 0) return rv::clear_error();
+    if (((uintptr_t)raw_ring_dev & 3u) != 0)
+        return rv::set_error_fmt(RV_ERR_INVALID, "rv_coarse_fused: raw ring is not 4-byte aligned");
+    if (int32_t st = rv::launch_coarse_fused(reinterpret_cast<cudaStream_t>(stream), *grid, format, *params,
+                                             raw_ring_dev, taps_dev, twiddles_dev, channel_ring_dev))
+        return st;
+    return rv::clear_error();
+}

@@ -143,6 +143,7 @@ SIGNATURES = {
     "rv_vrx_fine": (I32, [P, ptr(abi.VrxFineConfig), ptr(abi.VrxFineParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_vrx_demod": (I32, [P, ptr(abi.VrxDemodConfig), ptr(abi.VrxDemodParams), P, U64, P, U64, P, U64]),
     "rv_vrx_carrier": (I32, [P, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P]),
+    "rv_coarse_fused": (I32, [P, ptr(abi.GridParams), I32, ptr(abi.CoarseParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_validate_grid": (I32, [ptr(abi.GridParams)]),
     "rv_design_prototype": (I32, [ptr(abi.GridParams), F64, P, U64, ptr(F64), ptr(U64)]),
     "rv_build_twiddles": (I32, [U32, P, U64]),
