@@ -1,0 +1,384 @@
+"""Benchmark: input MS/s through the channelizer + N virtual receivers.
+
+Workload (the batched-receivers configuration): a 2^27-sample cs16 capture at
+20 MS/s, a 64-channel 2x-oversampled polyphase channelizer (T = 17 taps per
+branch) and 256 virtual receivers with seeded offsets, bandwidths uniform in
+12.5-200 kHz and modes uniform over NFM/AM/USB/LSB/WFM (stereo WFM), each
+planned exactly as the reference plans it. One step = the whole capture
+through the chain: fused convert/branch/FFT, then every receiver's fine stage
+(resampler + NCO), detector and audio filter, audio read back to the host.
+
+  value : input samples per second with the capture resident in HBM
+  e2e   : the same through rv_chain_run with the capture in pinned host
+          memory (host->device copy and audio readback inside the timed region)
+  plain_path : the same chain recorded the reference's way (one launch per
+          stage per receiver), timed on a shorter capture
+  roofline   : the dominant stage, from CUDA events on the chain's stream
+
+`--impl reference` times the reference's CPU implementation of the path (the
+oracle restatement of its twins, all host threads) on a bounded sample of the
+same workload and prints the same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import numpy as np  # noqa: E402
+
+RATE = 20_000_000
+GRID = (64, 17, 32)
+LOG2N = 27
+RECEIVERS = 256
+SEED = 3
+RUN_SAMPLES = 1 << 24
+METRIC = "input MS/s through channelizer+N VRX on 1 GB300, % HBM roofline, vs plain path"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--log2n", type=int, default=LOG2N)
+    ap.add_argument("--receivers", type=int, default=RECEIVERS)
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def capture(n, seed=SEED):
+    """Seeded cs16 capture: a few strong carriers of each mode over noise."""
+    import signals
+    rng = np.random.default_rng(seed)
+    chunk = 1 << 22
+    out = np.empty(2 * n, np.int16)
+    emitters = [("wfm", 2_500_000, 1.0), ("nfm", -3_100_000, 0.4), ("am", 5_000_000, 0.4), ("usb", -7_000_000, 0.3),
+                ("lsb", 8_200_000, 0.3), ("wfm", -6_300_000, 0.8)]
+    for at in range(0, n, chunk):
+        m = min(chunk, n - at)
+        z = np.zeros(m, np.complex128)
+        for kind, off, amp in emitters:
+            f = {"wfm": signals.wfm, "nfm": signals.nfm, "am": signals.am, "usb": signals.ssb,
+                 "lsb": lambda n_, r_, o_, amp, t0: signals.ssb(n_, r_, o_, amp=amp, upper=False, t0=t0)}[kind]
+            z += f(m, RATE, off, amp=amp, t0=at)
+        z += signals.noise(m, rng, 0.01)
+        peak = 6.0
+        out[2 * at:2 * (at + m):2] = np.clip(np.round(z.real / peak * 32767), -32768, 32767)
+        out[2 * at + 1:2 * (at + m):2] = np.clip(np.round(z.imag / peak * 32767), -32768, 32767)
+    return out
+
+
+class Clocks:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(s[0]) for s in self.samples if num(s[0])]
+        mx = [num(s[1]) for s in self.samples if num(s[1])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def receivers(count):
+    import signals
+    return signals.random_receivers(count, RATE, seed=SEED, grid=GRID)
+
+
+def algorithmic_bytes(plans, samples):
+    """Compulsory and per-stage algorithmic bytes for `samples` input samples."""
+    M, T, D = GRID
+    blocks = samples // D
+    coarse = samples * 4 + blocks * M * 8  # cs16 in, channel ring out
+    fine = demod = 0
+    for p in plans:
+        fc, fd = p.channel_rate, p.demod_rate
+        n_fine = samples * fd // RATE
+        fine += blocks * 8 + n_fine * 8  # the channel stream read once, fine ring written
+        n_audio = samples * p.output_rate // RATE
+        demod += n_fine * (8 + 4 + 4) + n_audio * 4 * p.demod.channels
+    audio_out = sum(samples * p.output_rate // RATE * 4 * p.demod.channels for p in plans)
+    return dict(compulsory=samples * 4 + audio_out, coarse=coarse, fine=fine, demod=demod, audio=audio_out)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_gb300(args):
+    import torch
+    import revenant_gb300 as rg
+    from revenant_gb300 import abi
+    from revenant_gb300.chain import Chain
+    from revenant_gb300.device import Device
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    rg.build()
+    torch.cuda.set_device(local)
+    dev = Device(local)
+    n = 1 << args.log2n
+    codes = capture(n)
+    reqs = receivers(args.receivers)
+
+    def make_chain(mode, run_samples, profile=True):
+        ch = Chain(dev, grid=GRID, rate=RATE, fmt=abi.FORMAT_CS16, mode=mode, max_run_samples=run_samples,
+                   keep_audio=False, profile=profile)
+        for r in reqs:
+            ch.add_receiver(r)
+        return ch
+
+    # replicas: every rank processes its own copy of the workload (the path
+    # shards only by time or receiver, with no exchange step)
+    d_codes = dev.array(codes)
+    pinned = dev.buffer(codes.nbytes, abi.MEMORY_UPLOAD)
+    pinned.upload(codes)
+    chain = make_chain(abi.CHAIN_BATCHED, RUN_SAMPLES)
+    plans = [chain.info(i)[0] for i in range(len(reqs))]
+    stream = torch.cuda.ExternalStream(dev.stream)
+
+    def step(ch, source):
+        at = 0
+        while at < n:
+            m = min(RUN_SAMPLES, n - at)
+            if source == "device":
+                ch.run(_Offset(d_codes, at * 4), m)
+            else:
+                ch.run(_Offset(pinned, at * 4), m, host=True)
+            at += m
+
+    def timed(source):
+        for _ in range(args.warmup):
+            step(chain, source)
+        base = chain.stats()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        dev.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        wall = time.perf_counter()
+        for _ in range(args.steps):
+            step(chain, source)
+        t1.record(stream)
+        t1.synchronize()
+        wall = time.perf_counter() - wall
+        ms = t0.elapsed_time(t1)
+        torch.cuda.synchronize()
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, wall, chain.stats(), base
+
+    with Clocks(local) as clocks:
+        ms, wall, st, base = timed("device")
+    ms_e2e, _, st_e2e, base_e2e = timed("host")
+    per_step_ms = ms / args.steps
+    samples_step = n
+    value = samples_step * world * args.steps / (ms / 1e3) / 1e6
+    e2e = samples_step * world * args.steps / (ms_e2e / 1e3) / 1e6
+    d = {k: getattr(st, k) - getattr(base, k) for k in ("launches", "coarse_ms", "fine_ms", "demod_ms",
+                                                          "input_ms", "readback_ms", "audio_bytes", "runs")}
+    stage_ms = {"coarse": d["coarse_ms"], "fine": d["fine_ms"], "demod": d["demod_ms"]}
+    dominant = max(stage_ms, key=stage_ms.get)
+    ab = algorithmic_bytes(plans, samples_step * args.steps)
+    pk, pk_kind = peaks()
+    achieved = ab[dominant] / (stage_ms[dominant] / 1e3) / 1e9
+    hbm_frac = ab["compulsory"] / (ms / 1e3) / 1e9 / pk["hbm_gbs"]
+
+    plain = None
+    if not args.no_plain:
+        # the reference's recording, one launch per stage per receiver, on
+        # a shorter capture (it is ~two orders of magnitude slower)
+        pn = 1 << 22
+        pch = make_chain(abi.CHAIN_PLAIN, 1 << 20)
+        for at in range(0, 1 << 20, 1 << 20):
+            pch.run(_Offset(d_codes, at * 4), 1 << 20)  # warm-up
+        dev.synchronize()
+        t = time.perf_counter()
+        at = 1 << 20
+        while at < (1 << 20) + pn:
+            pch.run(_Offset(d_codes, at * 4), 1 << 20)
+            at += 1 << 20
+        dt = time.perf_counter() - t
+        pst = pch.stats()
+        plain = {"value": pn / dt / 1e6, "unit": "MS/s", "sample": "2^22 samples after a 2^20 warm-up, same 256 receivers",
+                 "launches_per_run": pst.launches / max(pst.runs, 1)}
+        pch.close()
+
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "MS/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(per_step_ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched uneven receivers: 2^%d cs16 samples at 20 MS/s, M=64 D=32 T=17, %d receivers "
+                               "NFM/AM/USB/LSB/WFM 12.5-200 kHz (seed %d)" % (args.log2n, args.receivers, SEED),
+                   "grid": list(GRID), "rate": RATE, "receivers": args.receivers, "run_samples": RUN_SAMPLES,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (512 MiB capture per step)"},
+        "e2e": {"value": round(e2e, 2), "unit": "MS/s", "h2d_bytes_per_step": samples_step * 4,
+                "d2h_bytes_per_step": int(d["audio_bytes"] / args.steps)},
+        "gpu_launches": int(d["launches"]),
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": None,
+                     "peak_kind": pk_kind, "algorithmic_bytes_per_step": int(ab[dominant] / args.steps),
+                     "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()},
+                     "compulsory_hbm_frac": round(hbm_frac, 5)},
+        "realtime_factor": round(value * 1e6 / RATE / max(world, 1), 1),
+        "plain_path": plain,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_plain and plain:
+        line["vs_plain_path"] = round(value / plain["value"], 2)
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(reqs, threads=os.cpu_count())
+    if rank == 0:
+        print(json.dumps(line))
+    chain.close()
+    dev.close()
+
+
+class _Offset:
+    """A device or pinned buffer address plus a byte offset, for Chain.run."""
+
+    def __init__(self, buf, offset):
+        self.address = buf.address + offset
+
+
+def cpu_baseline(reqs, threads=None, sample_log2=18):
+    """The oracle (the reference's twins restated in C) on the host cores over
+    a bounded sample of the same workload: the coarse chain over all host
+    threads, then every receiver's fine stage and demodulator with the
+    receivers spread over the threads."""
+    import ctypes as C
+    from concurrent.futures import ThreadPoolExecutor
+
+    from bindings import cf32, oracle
+    from oracle_chain import OracleChain
+    from revenant_gb300 import abi
+
+    threads = threads or os.cpu_count() or 1
+    n = 1 << sample_log2
+    codes = capture(n, seed=SEED + 100)
+    M, T, D = GRID
+    ora = oracle()
+    proto = OracleChain(GRID, RATE, abi.FORMAT_CS16, [], ring_log2=4, chan_log2=4)
+    blocks = n // D
+    chan_blocks = 1 << int(np.ceil(np.log2(blocks + 300)))
+    chan = cf32(M * chan_blocks)
+    g = abi.GridParams(*GRID)
+    t = time.perf_counter()
+    st = ora.lib.or_coarse_cs16(C.byref(g), proto.taps.ctypes.data, proto.tw.ctypes.data, codes.ctypes.data, n, 0,
+                                blocks, chan_blocks, chan.ctypes.data, threads)
+    assert st == 0
+    coarse_s = time.perf_counter() - t
+    groups = [g_ for g_ in (reqs[i::threads] for i in range(threads)) if g_]
+    workers = []
+    for group in groups:
+        c = OracleChain(GRID, RATE, abi.FORMAT_CS16, group, ring_log2=4, chan_log2=int(np.log2(chan_blocks)))
+        c.chan = chan
+        workers.append(c)
+    t = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        list(pool.map(lambda c: c.receivers(0, blocks - 1), workers))
+    rx_s = time.perf_counter() - t
+    total = coarse_s + rx_s
+    return {"value": round(n / total / 1e6, 4), "unit": "MS/s", "cores": threads, "kind": "port",
+            "sample": "2^%d samples (%.1f ms of signal), all %d receivers: coarse %.2f s + receivers %.2f s on %d "
+                      "threads" % (sample_log2, n / RATE * 1e3, len(reqs), coarse_s, rx_s, threads)}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import revenant_gb300 as rg
+    rg.build()
+    reqs = receivers(args.receivers)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(reqs, threads=os.cpu_count()))
+    v = float(np.median([x["value"] for x in vals]))
+    line = {"metric": METRIC, "value": round(v, 4), "unit": "MS/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "batched uneven receivers: 2^%d cs16 samples at 20 MS/s, M=64 D=32 T=17, %d receivers "
+                                   "NFM/AM/USB/LSB/WFM 12.5-200 kHz (seed %d)" % (args.log2n, args.receivers, SEED)},
+            "cpu_baseline": dict(vals[-1], value=round(v, 4)),
+            "e2e": {"value": round(v, 4), "unit": "MS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

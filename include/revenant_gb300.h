@@ -315,6 +315,9 @@ uint64_t rv_buffer_size(const rv_buffer* buffer);
 int32_t rv_buffer_upload(rv_buffer* buffer, uint64_t offset, const void* src, uint64_t bytes);
 int32_t rv_buffer_download(const rv_buffer* buffer, uint64_t offset, void* dst, uint64_t bytes);
 int32_t rv_buffer_clear(rv_buffer* buffer);
+/* Synchronous copy between any two addresses (host or device) on the
+ * context stream (core/gpu/kernel.h CommandRunner::copy). */
+int32_t rv_copy(rv_context* context, void* dst, const void* src, uint64_t bytes);
 
 /* ===================================================================== *
  * Plain kernels: one launch per reference dispatch, bit-identical to the  *
@@ -387,6 +390,12 @@ typedef struct rv_coarse_params {
     uint32_t block_base;      /* absolute output block index of block 0 */
     uint32_t out_ring_blocks; /* channel ring blocks per channel, power of two */
     uint32_t out_ring_mask;
+    /* Samples at the start of block 0's filter support (the M*T samples
+     * ending at x[base_offset]) that precede the stream and read as 0.0, as
+     * a freshly zeroed cf32 ring does in the plain path; at most M*T - 1,
+     * zero once the stream has M*T - 1 samples of history. A native ring
+     * cannot hold that zero itself: no cu8 code converts to 0.0. */
+    uint32_t lead_zero;
 } rv_coarse_params;
 
 /* convert -> pfb_branch -> pfb_fft in one launch, reading the staging ring
@@ -401,6 +410,70 @@ int32_t rv_coarse_fused(void* stream, const rv_grid_params* grid, int32_t format
                         uint64_t raw_ring_bytes, const float* taps_dev, uint64_t taps_len,
                         const rv_cf32* twiddles_dev, uint64_t twiddles_len,
                         rv_cf32* channel_ring_dev, uint64_t channel_ring_len);
+
+/* ===================================================================== *
+ * The chain: raw IQ -> channel ring -> N receivers -> audio               *
+ * (core/engine/graph.h Graph::on_block + core/engine/vrx_stage.cpp       *
+ * DemodStage::record, with the same cursor arithmetic)                   *
+ * ===================================================================== */
+
+#define RV_CHAIN_BATCHED 0 /* fused coarse kernel + one launch per receiver stage */
+#define RV_CHAIN_PLAIN 1   /* one launch per stage per receiver, as the reference records */
+
+typedef struct rv_chain rv_chain;
+
+typedef struct rv_chain_config {
+    rv_grid_params grid;
+    uint32_t reserved;
+    int64_t rate;             /* input samples per second; a multiple of D */
+    int32_t format;           /* RV_FORMAT_CS16 or RV_FORMAT_CU8 */
+    int32_t mode;             /* RV_CHAIN_BATCHED or RV_CHAIN_PLAIN */
+    uint32_t max_run_samples; /* largest count one rv_chain_run may carry */
+    uint32_t keep_audio;      /* 1: accumulate audio for rv_chain_read_audio */
+    double attenuation_db;    /* prototype stopband target, 0 = 120 dB */
+    uint32_t profile;         /* 1: time each stage with CUDA events into rv_chain_stats */
+    uint32_t reserved2;
+} rv_chain_config;
+
+typedef struct rv_chain_stats {
+    uint64_t runs;
+    uint64_t blocks;      /* channel blocks produced */
+    uint64_t launches;    /* kernel launches issued */
+    uint64_t work_items;  /* batched work items */
+    uint64_t audio_bytes; /* bytes read back to the host */
+    /* device time per stage, summed over runs, when profiling is on
+     * (CUDA events on the chain's stream; core/engine/graph.h GraphStats) */
+    double input_ms;      /* host/device copy of the run's samples */
+    double coarse_ms;     /* convert + branch + FFT */
+    double fine_ms;       /* fine stage (+ carrier) */
+    double demod_ms;      /* detector + audio */
+    double readback_ms;   /* audio to the host */
+} rv_chain_stats;
+
+/* Allocates the chain's rings (the only allocating calls of the chain API
+ * are create and add_receiver). */
+int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_chain** out);
+int32_t rv_chain_destroy(rv_chain* chain);
+/* engine::place + dsp::plan_vrx, tables uploaded; the receiver starts at the
+ * first channel block of the next run (DemodStage::anchor_to). */
+int32_t rv_chain_add_receiver(rv_chain* chain, const rv_vrx_request* request, uint32_t* id);
+/* Consumes `count` input samples in the chain's format. where = 0: host
+ * memory, 1: device memory. Produces every channel block, fine sample and
+ * audio frame whose inputs now exist; audio is read back before it returns. */
+int32_t rv_chain_run(rv_chain* chain, const void* samples, uint64_t count, int32_t where);
+int32_t rv_chain_receiver_info(const rv_chain* chain, uint32_t id, rv_vrx_plan_info* info,
+                               uint64_t* audio_frames, uint64_t* first_audio);
+/* Drains up to `capacity` floats of accumulated audio (frames x channels). */
+int32_t rv_chain_read_audio(rv_chain* chain, uint32_t id, float* dst, uint64_t capacity,
+                            uint64_t* written);
+int32_t rv_chain_get_stats(const rv_chain* chain, rv_chain_stats* stats);
+/* A receiver's device rings: fine samples (cf32) and detector values (f32),
+ * both indexed by fine sample index modulo (mask + 1). Detector values exist
+ * only in the batched mode. */
+int32_t rv_chain_receiver_rings(const rv_chain* chain, uint32_t id, const rv_cf32** fine,
+                                const float** detector, uint32_t* mask);
+/* The device channel ring [M][ring_blocks] (block m at slot m mod ring_blocks). */
+int32_t rv_chain_channel_ring(const rv_chain* chain, const rv_cf32** ring, uint32_t* ring_blocks);
 
 /* ===================================================================== *
  * Host planning (core/dsp/pfb_design.cpp, vrx_reference.cpp,             *

@@ -100,7 +100,7 @@ class VrxCarrierParams(_S):
 
 class CoarseParams(_S):
     _fields_ = [("ring_mask", U32), ("base_offset", U32), ("block_count", U32), ("block_base", U32),
-                ("out_ring_blocks", U32), ("out_ring_mask", U32)]
+                ("out_ring_blocks", U32), ("out_ring_mask", U32), ("lead_zero", U32)]
 
 
 class VrxRequest(_S):
@@ -144,7 +144,22 @@ class DeviceInfo(_S):
                 ("max_shared_per_block", U64), ("l2_bytes", U64)]
 
 
-EXTRA_STRUCTS = {"rv_coarse_params": CoarseParams}
+CHAIN_BATCHED, CHAIN_PLAIN = 0, 1
+
+
+class ChainConfig(_S):
+    _fields_ = [("grid", GridParams), ("reserved", U32), ("rate", I64), ("format", I32), ("mode", I32),
+                ("max_run_samples", U32), ("keep_audio", U32), ("attenuation_db", C.c_double),
+                ("profile", U32), ("reserved2", U32)]
+
+
+class ChainStats(_S):
+    _fields_ = [("runs", U64), ("blocks", U64), ("launches", U64), ("work_items", U64), ("audio_bytes", U64),
+                ("input_ms", C.c_double), ("coarse_ms", C.c_double), ("fine_ms", C.c_double),
+                ("demod_ms", C.c_double), ("readback_ms", C.c_double)]
+
+
+EXTRA_STRUCTS = {"rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
 
 
 def request(center=0, bandwidth=0, demod="nfm", deemphasis=0, stereo=True, audio_rate=0,

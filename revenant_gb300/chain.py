@@ -1,0 +1,97 @@
+"""Host mirror of the chain API (rv_chain_*): the engine-level entry point.
+
+A ``Chain`` owns one rv_chain on a ``Device``: add receivers with
+``add_receiver(center=..., bandwidth=..., demod=...)``, feed raw IQ with
+``run(samples)`` (numpy uint8 / int16 on the host, or a device ``Buffer``),
+and read each receiver's audio with ``audio(id)``. All the work happens in
+librevenant_gb300.so.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .library import check, lib
+
+
+class Chain:
+    def __init__(self, device, grid=(64, 17, 32), rate=20_000_000, fmt=abi.FORMAT_CS16, mode=abi.CHAIN_BATCHED,
+                 max_run_samples=1 << 20, keep_audio=True, attenuation_db=120.0, profile=False):
+        self.device = device
+        cfg = abi.ChainConfig()
+        cfg.grid = abi.GridParams(*grid)
+        cfg.rate = rate
+        cfg.format = fmt
+        cfg.mode = mode
+        cfg.max_run_samples = max_run_samples
+        cfg.keep_audio = 1 if keep_audio else 0
+        cfg.attenuation_db = attenuation_db
+        cfg.profile = 1 if profile else 0
+        self.config = cfg
+        self.bytes_per_sample = 4 if fmt == abi.FORMAT_CS16 else 2
+        handle = C.c_void_p()
+        check(lib().rv_chain_create(device.handle, C.byref(cfg), C.byref(handle)))
+        self.handle = handle
+        self.ids = []
+
+    def add_receiver(self, request=None, **kw):
+        req = request if request is not None else abi.request(**kw)
+        rid = C.c_uint32()
+        check(lib().rv_chain_add_receiver(self.handle, C.byref(req), C.byref(rid)))
+        self.ids.append(rid.value)
+        return rid.value
+
+    def run(self, samples, count=None, host=False):
+        """Feed samples: a host numpy array of raw bytes / int16 codes, or any
+        object with an ``address`` (a Buffer): device memory, or host memory
+        (pinned) when ``host`` is true; then ``count`` samples from there."""
+        if hasattr(samples, "address"):
+            check(lib().rv_chain_run(self.handle, C.c_void_p(samples.address), count, 0 if host else 1))
+            return
+        a = np.ascontiguousarray(samples)
+        n = a.nbytes // self.bytes_per_sample
+        check(lib().rv_chain_run(self.handle, a.ctypes.data_as(C.c_void_p), n, 0))
+
+    def info(self, rid):
+        info = abi.VrxPlanInfo()
+        frames, first = C.c_uint64(), C.c_uint64()
+        check(lib().rv_chain_receiver_info(self.handle, rid, C.byref(info), C.byref(frames), C.byref(first)))
+        return info, frames.value, first.value
+
+    def audio(self, rid):
+        info, frames, _ = self.info(rid)
+        cap = max(frames * info.demod.channels, 1)
+        out = np.empty(cap, np.float32)
+        n = C.c_uint64()
+        check(lib().rv_chain_read_audio(self.handle, rid, out.ctypes.data_as(C.c_void_p), cap, C.byref(n)))
+        return out[:n.value]
+
+    def rings(self, rid):
+        """(fine ring (n, 2) float32, detector ring float32 or None) copied
+        from the device."""
+        fine, det, mask = C.c_void_p(), C.c_void_p(), C.c_uint32()
+        check(lib().rv_chain_receiver_rings(self.handle, rid, C.byref(fine), C.byref(det), C.byref(mask)))
+        n = mask.value + 1
+        f = np.empty((n, 2), np.float32)
+        self.device.copy_to_host(f, fine.value)
+        d = None
+        if det.value:
+            d = np.empty(n, np.float32)
+            self.device.copy_to_host(d, det.value)
+        return f, d
+
+    def stats(self):
+        s = abi.ChainStats()
+        check(lib().rv_chain_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def close(self):
+        if self.handle:
+            lib().rv_chain_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,698 @@
+// The receive chain: raw IQ in, channel ring, N virtual receivers, audio out.
+//
+// Host-side equivalent of Graph::on_block + DemodStage::record
+// (core/engine/graph.cpp:4770-5485, core/engine/vrx_stage.cpp:1119-1430): per
+// run of input samples it converts and channelizes the new blocks, then
+// advances every receiver's fine stage, carrier loop and demodulator by
+// exactly the outputs whose inputs now exist, with the reference's cursor
+// arithmetic (highest_output_for / lowest_output_for, anchor_to).
+//
+// Two execution modes share that bookkeeping and produce identical bits:
+//  * RV_CHAIN_PLAIN: the reference's recording, one launch per stage per
+//    receiver (convert, branch, FFT, then fine [+ carrier] + demod for each
+//    receiver) through the plain kernels. This is the baseline.
+//  * RV_CHAIN_BATCHED: the fused coarse kernel, then one launch per receiver
+//    stage covering every receiver (fine, carrier, detector, audio), driven by
+//    work lists built on the host and uploaded once per run.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+#include "receivers.cuh"
+#include "revenant_gb300.h"
+
+namespace rv {
+int32_t plan_receiver(const rv_grid_params& g, int64_t rate, const rv_vrx_request& r, rv_vrx_plan_info& info,
+                      std::vector<rv_cf32>& taps, std::vector<float>& weights);
+int32_t design_prototype_table(const rv_grid_params& g, double atten, std::vector<float>& taps);
+int32_t build_twiddle_table(uint32_t M, std::vector<rv_cf32>& out);
+int32_t build_nco(uint32_t log2, std::vector<rv_cf32>& out);
+int32_t validate_grid(const rv_grid_params* g);
+uint32_t demod_fine_history(const rv_vrx_demod_config* c);
+int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
+                            const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring);
+}  // namespace rv
+
+using namespace rv;
+
+namespace {
+
+constexpr uint32_t kFineWindow = 6144;   // float2 per fine work item (48 KB)
+constexpr uint32_t kDetWindow = 8192;    // floats per detector / audio item (32 KB)
+constexpr uint32_t kMaxItem = kRxThreads;
+constexpr uint64_t kMaxLerpEntries = 1u << 20;
+
+uint64_t bit_ceil64(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// core/engine/vrx_stage.cpp:173-197
+uint64_t highest_output_for(uint64_t newest, uint64_t fc, uint64_t fd) {
+    const uint64_t bound = newest + 1u, whole = bound / fc, part = bound % fc;
+    if (part == 0) return whole * fd - 1u;
+    return whole * fd + (part * fd - 1u) / fc;
+}
+uint64_t lowest_output_for(uint64_t needed, uint64_t fc, uint64_t fd) {
+    const uint64_t whole = needed / fc, part = needed % fc;
+    return whole * fd + (part * fd + fc - 1u) / fc;
+}
+
+template <class T>
+struct DeviceArray {
+    T* ptr = nullptr;
+    size_t count = 0;
+    int32_t alloc(size_t n) {
+        release();
+        if (n == 0) n = 1;
+        if (int32_t st = cuda_status(cudaMalloc(&ptr, n * sizeof(T)), "chain allocation")) return st;
+        count = n;
+        return RV_OK;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+};
+
+template <class T>
+struct PinnedArray {
+    T* ptr = nullptr;
+    size_t count = 0;
+    int32_t reserve(size_t n) {
+        if (n <= count) return RV_OK;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        count = 0;
+        if (int32_t st = cuda_status(cudaHostAlloc(&ptr, n * sizeof(T), cudaHostAllocDefault), "chain pinned"))
+            return st;
+        count = n;
+        return RV_OK;
+    }
+    void release() {
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+};
+
+struct Receiver {
+    rv_vrx_request request{};
+    rv_vrx_plan_info plan{};
+    std::vector<rv_cf32> taps;
+    std::vector<float> weights;
+    uint32_t period = 0;
+    uint32_t fine_history = 0, det_history = 0, reach = 0;
+    uint32_t fine_mask = 0;
+    uint32_t max_fine_item = 0, max_det_item = 0, max_audio_item = 0;
+    bool started = false;
+    bool carrier_reset = true;
+    uint64_t first_output = 0, next_output = 0, next_audio = 0;
+    uint64_t audio_frames_total = 0;
+    DeviceArray<rv_cf32> d_taps;
+    DeviceArray<float2> d_lerped;
+    DeviceArray<rv_cf32> d_fine;
+    DeviceArray<float> d_det;
+    DeviceArray<float> d_weights;
+    DeviceArray<uint32_t> d_state;
+    std::vector<float> audio;  // accumulated on the host when keep_audio
+    uint64_t run_audio_offset = 0, run_audio_frames = 0;
+};
+
+}  // namespace
+
+struct rv_chain {
+    rv_context* context = nullptr;
+    cudaStream_t stream = nullptr;
+    rv_chain_config config{};
+    uint32_t stages = 0;
+    uint32_t bytes_per_sample = 0;
+    // rings
+    uint32_t raw_mask = 0;         // raw ring capacity (samples) - 1
+    uint32_t chan_blocks = 0;      // channel ring blocks per channel
+    DeviceArray<uint8_t> raw;      // batched: native-format ring; plain: staging for one run
+    DeviceArray<rv_cf32> cf32_ring;  // plain only
+    DeviceArray<rv_cf32> branch;     // plain only
+    DeviceArray<rv_cf32> channel;
+    DeviceArray<float> proto;
+    DeviceArray<rv_cf32> twiddles;
+    DeviceArray<rv_cf32> nco;
+    std::vector<float> proto_host;
+    std::vector<Receiver> rx;
+    DeviceArray<RxDev> rx_table;
+    bool table_dirty = true;
+    // per-run work lists and audio
+    PinnedArray<WorkItem> items_host;
+    DeviceArray<WorkItem> items_dev;
+    DeviceArray<float> audio_dev;
+    PinnedArray<float> audio_host;
+    uint64_t samples_in = 0;
+    uint64_t next_block = 0;
+    rv_chain_stats stats{};
+    // stage boundaries for profiling: input, coarse, fine, demod, readback
+    cudaEvent_t marks[6] = {};
+};
+
+namespace {
+void mark(rv_chain* c, int i) {
+    if (c->config.profile && c->marks[i]) cudaEventRecord(c->marks[i], c->stream);
+}
+void collect_marks(rv_chain* c) {
+    if (!c->config.profile) return;
+    float ms[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&ms[i], c->marks[i], c->marks[i + 1]);
+    c->stats.input_ms += ms[0];
+    c->stats.coarse_ms += ms[1];
+    c->stats.fine_ms += ms[2];
+    c->stats.demod_ms += ms[3];
+    c->stats.readback_ms += ms[4];
+}
+}  // namespace
+
+namespace {
+
+int32_t upload_table(rv_chain* c) {
+    std::vector<RxDev> table(c->rx.size());
+    for (size_t i = 0; i < c->rx.size(); ++i) {
+        Receiver& r = c->rx[i];
+        RxDev& d = table[i];
+        memset(&d, 0, sizeof d);
+        const rv_vrx_plan_info& p = r.plan;
+        d.chan_base = p.placement.channel * c->chan_blocks;
+        d.chan_mask = c->chan_blocks - 1u;
+        d.taps = p.fine.taps;
+        d.period = r.period;
+        d.step_whole = (uint32_t)(p.channel_rate / p.demod_rate);
+        d.step_rem = (uint32_t)(p.channel_rate % p.demod_rate);
+        d.out_rate = (uint32_t)p.demod_rate;
+        d.nco_log2 = p.fine.nco_log2;
+        d.nco_delta = p.fine_nco_delta;
+        d.lerped = r.d_lerped.ptr;
+        d.taps_raw = reinterpret_cast<const float2*>(r.d_taps.ptr);
+        d.phases = p.fine.phases;
+        d.inv_out_rate = 1.0f / (float)p.demod_rate;
+        d.nco = reinterpret_cast<const float2*>(c->nco.ptr);
+        d.fine = reinterpret_cast<float2*>(r.d_fine.ptr);
+        d.fine_mask = r.fine_mask;
+        d.mode = p.demod.mode;
+        d.decimation = p.demod.decimation;
+        d.audio_taps = p.demod.audio_taps;
+        d.dc_taps = p.demod.dc_taps;
+        d.channels = p.demod.channels;
+        d.pilot_taps = p.demod.pilot_taps;
+        d.gain = p.demod_gain;
+        d.reach = r.reach;
+        d.weights = r.d_weights.ptr;
+        d.det = r.d_det.ptr;
+        d.carrier_state = r.d_state.ptr;
+        d.carrier = p.carrier_loop;
+        d.carrier_power = p.carrier.power;
+    }
+    if (c->rx_table.count < table.size())
+        if (int32_t st = c->rx_table.alloc(table.size())) return st;
+    if (!table.empty())
+        if (int32_t st = cuda_status(cudaMemcpyAsync(c->rx_table.ptr, table.data(), table.size() * sizeof(RxDev),
+                                                     cudaMemcpyHostToDevice, c->stream),
+                                     "receiver table upload"))
+            return st;
+    c->table_dirty = false;
+    return RV_OK;
+}
+
+// Copy `count` samples of native-format input into ring positions starting
+// at `pos` (wrapping). `where` 0 = host memory, 1 = device memory.
+int32_t copy_into_ring(rv_chain* c, uint8_t* ring, uint64_t ring_samples, uint64_t pos, const uint8_t* src,
+                       uint64_t count, int32_t where) {
+    const uint64_t bps = c->bytes_per_sample;
+    const cudaMemcpyKind kind = where ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    uint64_t done = 0;
+    while (done < count) {
+        const uint64_t at = (pos + done) % ring_samples;
+        const uint64_t n = std::min<uint64_t>(count - done, ring_samples - at);
+        if (int32_t st = cuda_status(cudaMemcpyAsync(ring + at * bps, src + done * bps, n * bps, kind, c->stream),
+                                     "input copy"))
+            return st;
+        done += n;
+    }
+    return RV_OK;
+}
+
+int32_t coarse_plain(rv_chain* c, uint64_t first_sample, const uint8_t* src, uint64_t count, int32_t where,
+                     uint64_t first_block, uint32_t blocks) {
+    const rv_grid_params& g = c->config.grid;
+    // staging copy of this run's raw bytes, then convert into the cf32 ring
+    if (int32_t st = copy_into_ring(c, c->raw.ptr, count + 1, 0, src, count, where)) return st;
+    mark(c, 1);
+    rv_convert_params cp{c->raw_mask, (uint32_t)first_sample, 0u, (uint32_t)count};
+    if (int32_t st = rv_convert(c->stream, c->config.format, &cp, c->raw.ptr, c->raw.count, c->cf32_ring.ptr,
+                                c->cf32_ring.count))
+        return st;
+    c->stats.launches += 1;
+    if (blocks == 0) return RV_OK;
+    rv_pfb_branch_params bp{c->raw_mask, (uint32_t)(first_block * g.decimation), blocks};
+    if (int32_t st = rv_pfb_branch(c->stream, &g, &bp, c->proto.ptr, c->proto.count, c->cf32_ring.ptr,
+                                   c->cf32_ring.count, c->branch.ptr, c->branch.count))
+        return st;
+    rv_pfb_fft_params fp{g.channels, g.decimation, ilog2(g.channels), (uint32_t)first_block, blocks, c->chan_blocks,
+                         c->chan_blocks - 1u};
+    if (int32_t st = rv_pfb_fft(c->stream, &fp, c->branch.ptr, c->branch.count, c->twiddles.ptr, c->twiddles.count,
+                                c->channel.ptr, c->channel.count))
+        return st;
+    c->stats.launches += 2;
+    return RV_OK;
+}
+
+int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, uint64_t count, int32_t where,
+                       uint64_t first_block, uint32_t blocks) {
+    const rv_grid_params& g = c->config.grid;
+    if (int32_t st = copy_into_ring(c, c->raw.ptr, (uint64_t)c->raw_mask + 1u, first_sample, src, count, where))
+        return st;
+    mark(c, 1);
+    if (blocks == 0) return RV_OK;
+    // stream-start history reads as zero, as the plain path's zeroed ring does
+    const uint64_t support = (uint64_t)g.channels * g.taps_per_branch - 1u;
+    const uint64_t centre = first_block * g.decimation;
+    const uint32_t lead_zero = centre >= support ? 0u : (uint32_t)(support - centre);
+    rv_coarse_params p{c->raw_mask, (uint32_t)(first_block * g.decimation) & c->raw_mask, blocks, (uint32_t)first_block,
+                       c->chan_blocks, c->chan_blocks - 1u, lead_zero};
+    if (int32_t st = launch_coarse_fused(c->stream, g, c->config.format, p, c->raw.ptr, c->proto.ptr,
+                                         c->twiddles.ptr, c->channel.ptr))
+        return st;
+    c->stats.launches += 1;
+    return RV_OK;
+}
+
+void push_items(std::vector<WorkItem>& list, uint32_t rx, uint64_t first, uint64_t count, uint32_t per_item,
+                uint64_t out, uint32_t out_stride) {
+    uint64_t done = 0;
+    while (done < count) {
+        const uint32_t n = (uint32_t)std::min<uint64_t>(count - done, per_item);
+        list.push_back(WorkItem{rx, n, first + done, out + done * out_stride});
+        done += n;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_chain** out) {
+    if (context == nullptr || config == nullptr || out == nullptr)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: NULL argument");
+    *out = nullptr;
+    if (int32_t st = validate_grid(&config->grid)) return st;
+    const rv_grid_params& g = config->grid;
+    if (config->format != RV_FORMAT_CS16 && config->format != RV_FORMAT_CU8)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_chain_create: input format %d (cs16 and cu8 are supported)",
+                             config->format);
+    if (config->mode != RV_CHAIN_BATCHED && config->mode != RV_CHAIN_PLAIN)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: mode %d", config->mode);
+    if (config->rate <= 0 || config->rate % g.decimation != 0)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: rate %lld must be a positive multiple of D=%u",
+                             (long long)config->rate, g.decimation);
+    if (config->max_run_samples == 0 || config->max_run_samples > (1u << 30))
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: max_run_samples must be in [1, 2^30]");
+    rv_chain* c = new (std::nothrow) rv_chain;
+    if (c == nullptr) return set_error_fmt(RV_ERR_NO_MEMORY, "rv_chain_create: out of host memory");
+    c->context = context;
+    c->stream = reinterpret_cast<cudaStream_t>(rv_context_stream(context));
+    c->config = *config;
+    if (c->config.attenuation_db <= 0.0) c->config.attenuation_db = 120.0;
+    c->bytes_per_sample = config->format == RV_FORMAT_CS16 ? 4u : 2u;
+    const uint64_t history = (uint64_t)g.channels * g.taps_per_branch + g.decimation;
+    const uint64_t raw_cap = bit_ceil64((uint64_t)config->max_run_samples + history + 1u);
+    if (raw_cap > (1ull << 31)) {
+        delete c;
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: ring of %llu samples is too large", (unsigned long long)raw_cap);
+    }
+    c->raw_mask = (uint32_t)(raw_cap - 1u);
+    const uint64_t blocks_per_run = config->max_run_samples / g.decimation + 2u;
+    c->chan_blocks = (uint32_t)bit_ceil64(blocks_per_run + 256u + 8u);
+    int32_t st = RV_OK;
+    if (config->mode == RV_CHAIN_BATCHED) {
+        st = c->raw.alloc(raw_cap * c->bytes_per_sample);
+        if (!st) st = cuda_status(cudaMemsetAsync(c->raw.ptr, 0, raw_cap * c->bytes_per_sample, c->stream), "ring clear");
+    } else {
+        st = c->raw.alloc(((uint64_t)config->max_run_samples + 1u) * c->bytes_per_sample);
+        if (!st) st = c->cf32_ring.alloc(raw_cap);
+        if (!st) st = cuda_status(cudaMemsetAsync(c->cf32_ring.ptr, 0, raw_cap * sizeof(rv_cf32), c->stream), "ring clear");
+        if (!st) st = c->branch.alloc(blocks_per_run * g.channels);
+    }
+    if (!st) st = c->channel.alloc((uint64_t)g.channels * c->chan_blocks);
+    if (!st) st = cuda_status(cudaMemsetAsync(c->channel.ptr, 0, (uint64_t)g.channels * c->chan_blocks * sizeof(rv_cf32), c->stream),
+                              "channel clear");
+    std::vector<rv_cf32> tw, nco;
+    if (!st) st = design_prototype_table(g, c->config.attenuation_db, c->proto_host);
+    if (!st) st = build_twiddle_table(g.channels, tw);
+    if (!st) st = build_nco(16, nco);
+    if (!st) st = c->proto.alloc(c->proto_host.size());
+    if (!st) st = c->twiddles.alloc(tw.size());
+    if (!st) st = c->nco.alloc(nco.size());
+    if (!st) st = cuda_status(cudaMemcpyAsync(c->proto.ptr, c->proto_host.data(), c->proto_host.size() * 4, cudaMemcpyHostToDevice, c->stream), "prototype upload");
+    if (!st) st = cuda_status(cudaMemcpyAsync(c->twiddles.ptr, tw.data(), tw.size() * 8, cudaMemcpyHostToDevice, c->stream), "twiddle upload");
+    if (!st) st = cuda_status(cudaMemcpyAsync(c->nco.ptr, nco.data(), nco.size() * 8, cudaMemcpyHostToDevice, c->stream), "nco upload");
+    if (!st && c->config.profile)
+        for (int i = 0; i < 6 && !st; ++i) st = cuda_status(cudaEventCreate(&c->marks[i]), "chain events");
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "chain create");
+    if (st) {
+        rv_chain_destroy(c);
+        return st;
+    }
+    *out = c;
+    return clear_error();
+}
+
+int32_t rv_chain_destroy(rv_chain* c) {
+    if (c == nullptr) return RV_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (Receiver& r : c->rx) {
+        r.d_taps.release();
+        r.d_lerped.release();
+        r.d_fine.release();
+        r.d_det.release();
+        r.d_weights.release();
+        r.d_state.release();
+    }
+    c->raw.release();
+    c->cf32_ring.release();
+    c->branch.release();
+    c->channel.release();
+    c->proto.release();
+    c->twiddles.release();
+    c->nco.release();
+    c->rx_table.release();
+    c->items_dev.release();
+    c->items_host.release();
+    c->audio_dev.release();
+    c->audio_host.release();
+    for (cudaEvent_t e : c->marks)
+        if (e) cudaEventDestroy(e);
+    delete c;
+    return clear_error();
+}
+
+int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32_t* id) {
+    if (c == nullptr || request == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_add_receiver: NULL");
+    Receiver r;
+    r.request = *request;
+    if (int32_t st = plan_receiver(c->config.grid, c->config.rate, *request, r.plan, r.taps, r.weights)) return st;
+    const rv_vrx_plan_info& p = r.plan;
+    const uint64_t fc = (uint64_t)p.channel_rate, fd = (uint64_t)p.demod_rate;
+    const uint64_t rem = fc % fd;
+    r.period = (uint32_t)(fd / std::gcd(rem == 0 ? fd : rem, fd));
+    r.fine_history = demod_fine_history(&p.demod);
+    r.det_history = (p.demod.mode == RV_DEMOD_AM || p.demod.mode == RV_DEMOD_SAM) ? p.demod.dc_taps - 1u
+                    : (p.demod.mode == RV_DEMOD_NFM || p.demod.mode == RV_DEMOD_WFM)   ? 1u
+                                                                                        : 0u;
+    r.reach = r.fine_history - r.det_history;
+    // fine outputs one run can produce, plus history, plus a carry of one run
+    const uint64_t blocks = c->config.max_run_samples / c->config.grid.decimation + 2u;
+    const uint64_t max_fine = blocks * fd / fc + 2u;
+    const uint64_t cap = bit_ceil64(2u * max_fine + r.fine_history + 1024u);
+    if (cap > (1ull << 31)) return set_error_fmt(RV_ERR_INVALID, "rv_chain_add_receiver: fine ring too large");
+    r.fine_mask = (uint32_t)(cap - 1u);
+    // item sizes that keep every staged window inside shared memory
+    const uint64_t step_max = fc / fd + 1u;
+    r.max_fine_item = (uint32_t)std::min<uint64_t>(kMaxItem, (kFineWindow - p.fine.taps) / step_max + 1u);
+    r.max_det_item = (uint32_t)std::min<uint64_t>(kMaxItem, kDetWindow - (p.demod.dc_taps - 1u));
+    const uint64_t dec = p.demod.decimation;
+    if (r.reach + 1u > kDetWindow)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_chain_add_receiver: audio history %u exceeds the %u-sample window",
+                             r.reach, kDetWindow);
+    r.max_audio_item = (uint32_t)std::min<uint64_t>(kMaxItem, (kDetWindow - r.reach - 1u) / dec + 1u);
+    int32_t st = r.d_taps.alloc(r.taps.size());
+    if (!st) st = cuda_status(cudaMemcpyAsync(r.d_taps.ptr, r.taps.data(), r.taps.size() * 8, cudaMemcpyHostToDevice, c->stream), "taps upload");
+    if (!st && c->config.mode == RV_CHAIN_BATCHED && (uint64_t)r.period * p.fine.taps <= kMaxLerpEntries) {
+        st = r.d_lerped.alloc((uint64_t)r.period * p.fine.taps);
+        if (!st)
+            st = launch_lerp_table(c->stream, r.d_taps.ptr, r.d_lerped.ptr, p.fine.taps, p.fine.phases, r.period,
+                                   (uint32_t)rem, (uint32_t)fd, 1.0f / (float)fd);
+    }
+    if (!st) st = r.d_fine.alloc(cap);
+    if (!st) st = cuda_status(cudaMemsetAsync(r.d_fine.ptr, 0, cap * sizeof(rv_cf32), c->stream), "fine clear");
+    if (!st) st = r.d_det.alloc(cap);
+    if (!st) st = cuda_status(cudaMemsetAsync(r.d_det.ptr, 0, cap * sizeof(float), c->stream), "det clear");
+    if (!st) st = r.d_weights.alloc(r.weights.size());
+    if (!st) st = cuda_status(cudaMemcpyAsync(r.d_weights.ptr, r.weights.data(), r.weights.size() * 4, cudaMemcpyHostToDevice, c->stream), "weights upload");
+    if (!st) st = r.d_state.alloc(RV_CARRIER_STATE_WORDS);
+    if (!st) st = cuda_status(cudaMemsetAsync(r.d_state.ptr, 0, RV_CARRIER_STATE_WORDS * 4, c->stream), "state clear");
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "receiver setup");
+    if (st) {
+        r.d_taps.release();
+        r.d_lerped.release();
+        r.d_fine.release();
+        r.d_det.release();
+        r.d_weights.release();
+        r.d_state.release();
+        return st;
+    }
+    c->rx.push_back(std::move(r));
+    c->table_dirty = true;
+    if (id) *id = (uint32_t)(c->rx.size() - 1u);
+    return clear_error();
+}
+
+int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t where) {
+    if (c == nullptr || (samples == nullptr && count > 0)) return set_error_fmt(RV_ERR_INVALID, "rv_chain_run: NULL");
+    if (count > c->config.max_run_samples)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_run: %llu samples exceed max_run_samples %u",
+                             (unsigned long long)count, c->config.max_run_samples);
+    if (count == 0) return clear_error();
+    const rv_grid_params& g = c->config.grid;
+    const bool plain = c->config.mode == RV_CHAIN_PLAIN;
+    const uint8_t* src = static_cast<const uint8_t*>(samples);
+    const uint64_t first_sample = c->samples_in;
+    const uint64_t newest_sample = first_sample + count - 1u;
+    const uint64_t last_block = newest_sample / g.decimation;
+    const uint64_t first_block = c->next_block;
+    const uint32_t blocks = last_block >= first_block ? (uint32_t)(last_block - first_block + 1u) : 0u;
+    mark(c, 0);
+    int32_t st = plain ? coarse_plain(c, first_sample, src, count, where, first_block, blocks)
+                       : coarse_batched(c, first_sample, src, count, where, first_block, blocks);
+    if (st) return st;
+    mark(c, 2);
+    c->samples_in += count;
+    c->next_block += blocks;
+    c->stats.blocks += blocks;
+    if (blocks == 0 || c->rx.empty()) {
+        mark(c, 3);
+        mark(c, 4);
+        mark(c, 5);
+        if ((st = cuda_status(cudaStreamSynchronize(c->stream), "run sync"))) return st;
+        collect_marks(c);
+        return clear_error();
+    }
+    if (!plain && c->table_dirty)
+        if ((st = upload_table(c))) return st;
+
+    // ---- per-receiver cursors (DemodStage::record) and work lists
+    std::vector<WorkItem> fine_items, carrier_items, det_items, audio_items;
+    uint64_t audio_floats = 0;
+    struct Span { uint64_t fine_first, fine_count, det_first, det_count, audio_first, audio_count; };
+    std::vector<Span> spans(c->rx.size());
+    for (size_t ri = 0; ri < c->rx.size(); ++ri) {
+        Receiver& r = c->rx[ri];
+        const rv_vrx_plan_info& p = r.plan;
+        const uint64_t fc = (uint64_t)p.channel_rate, fd = (uint64_t)p.demod_rate, dec = p.demod.decimation;
+        if (!r.started) {
+            const uint64_t needed = first_block + p.fine.taps - 1u;
+            r.first_output = lowest_output_for(needed, fc, fd);
+            r.next_output = r.first_output;
+            r.next_audio = (r.first_output + r.fine_history + dec - 1u) / dec;
+            r.started = true;
+        }
+        Span& s = spans[ri];
+        memset(&s, 0, sizeof s);
+        const uint64_t limit = highest_output_for(last_block, fc, fd);
+        if (limit + 1u > r.next_output) {
+            s.fine_first = r.next_output;
+            s.fine_count = limit + 1u - r.next_output;
+        }
+        const uint64_t fine_end = s.fine_first + s.fine_count;
+        if (s.fine_count) {
+            const uint64_t det_from = std::max<uint64_t>(s.fine_first, r.first_output + r.det_history);
+            if (fine_end > det_from) {
+                s.det_first = det_from;
+                s.det_count = fine_end - det_from;
+            }
+            r.next_output = fine_end;
+        }
+        if (r.next_output > r.first_output) {
+            const uint64_t audio_limit = (r.next_output - 1u) / dec;
+            if (audio_limit + 1u > r.next_audio) {
+                s.audio_first = r.next_audio;
+                s.audio_count = audio_limit + 1u - r.next_audio;
+                r.next_audio += s.audio_count;
+            }
+        }
+        r.run_audio_offset = audio_floats;
+        r.run_audio_frames = s.audio_count;
+        audio_floats += s.audio_count * p.demod.channels;
+        if (!plain) {
+            push_items(fine_items, (uint32_t)ri, s.fine_first, s.fine_count, r.max_fine_item, 0, 0);
+            if (s.fine_count && p.carrier.power != 0) {
+                carrier_items.push_back(WorkItem{(uint32_t)ri, (uint32_t)s.fine_count, s.fine_first, r.carrier_reset ? 1u : 0u});
+                r.carrier_reset = false;
+            }
+            if (!is_complex_demod(p.demod.mode))
+                push_items(det_items, (uint32_t)ri, s.det_first, s.det_count, r.max_det_item, 0, 0);
+            push_items(audio_items, (uint32_t)ri, s.audio_first, s.audio_count, r.max_audio_item, r.run_audio_offset,
+                       p.demod.channels);
+        }
+    }
+    if (c->audio_dev.count < audio_floats + 1)
+        if ((st = c->audio_dev.alloc(audio_floats + 1 + audio_floats / 4))) return st;
+
+    if (plain) {
+        // the reference's recording: fine [+ carrier] + demod per receiver
+        // (profiling books the whole receiver loop as fine_ms)
+        for (size_t ri = 0; ri < c->rx.size(); ++ri) {
+            Receiver& r = c->rx[ri];
+            const Span& s = spans[ri];
+            const rv_vrx_plan_info& p = r.plan;
+            const uint32_t chan_base = p.placement.channel * c->chan_blocks;
+            // fine dispatches small enough for the kernel's 32-bit recurrence
+            const uint64_t rem = (uint64_t)(p.channel_rate % p.demod_rate);
+            const uint64_t per = rem == 0 ? s.fine_count : std::max<uint64_t>(1, (0xFFFFFFFFull - (uint64_t)p.demod_rate) / rem);
+            for (uint64_t done = 0; done < s.fine_count;) {
+                const uint32_t n = (uint32_t)std::min<uint64_t>({s.fine_count - done, per, (uint64_t)r.fine_mask + 1u});
+                rv_vrx_fine_block fb;
+                if ((st = rv_fine_block(&p, chan_base, c->chan_blocks - 1u, r.fine_mask, s.fine_first + done, n, &fb))) return st;
+                if ((st = rv_vrx_fine(c->stream, &p.fine, &fb.params, c->channel.ptr, c->channel.count, r.d_taps.ptr,
+                                      r.d_taps.count, c->nco.ptr, c->nco.count, r.d_fine.ptr, r.d_fine.count)))
+                    return st;
+                c->stats.launches += 1;
+                done += n;
+            }
+            if (s.fine_count && p.carrier.power != 0) {
+                rv_vrx_carrier_params cp;
+                if ((st = rv_carrier_block(&p, r.fine_mask, s.fine_first, (uint32_t)s.fine_count, r.carrier_reset, 0.0f, &cp)))
+                    return st;
+                if ((st = rv_vrx_carrier(c->stream, &p.carrier, &cp, c->nco.ptr, c->nco.count, r.d_fine.ptr,
+                                         r.d_fine.count, r.d_state.ptr)))
+                    return st;
+                r.carrier_reset = false;
+                c->stats.launches += 1;
+            }
+            if (s.audio_count) {
+                rv_vrx_demod_block db;
+                if ((st = rv_demod_block(&p, r.fine_mask, s.audio_first, (uint32_t)s.audio_count, &db))) return st;
+                if ((st = rv_vrx_demod(c->stream, &p.demod, &db.params, r.d_fine.ptr, r.d_fine.count, r.d_weights.ptr,
+                                       r.d_weights.count, c->audio_dev.ptr + r.run_audio_offset,
+                                       s.audio_count * p.demod.channels)))
+                    return st;
+                c->stats.launches += 1;
+            }
+        }
+        mark(c, 3);
+        mark(c, 4);
+    } else {
+        const size_t total = fine_items.size() + carrier_items.size() + det_items.size() + audio_items.size();
+        if ((st = c->items_host.reserve(total + 1))) return st;
+        if (c->items_dev.count < total + 1)
+            if ((st = c->items_dev.alloc(total + 1 + total / 4))) return st;
+        WorkItem* h = c->items_host.ptr;
+        size_t at = 0;
+        for (auto* list : {&fine_items, &carrier_items, &det_items, &audio_items}) {
+            if (!list->empty()) memcpy(h + at, list->data(), list->size() * sizeof(WorkItem));
+            at += list->size();
+        }
+        if ((st = cuda_status(cudaMemcpyAsync(c->items_dev.ptr, h, total * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                                              c->stream),
+                              "work list upload")))
+            return st;
+        const WorkItem* d = c->items_dev.ptr;
+        const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
+        if ((st = launch_fine_batched(c->stream, c->rx_table.ptr, d, (uint32_t)fine_items.size(), chan, kFineWindow)))
+            return st;
+        d += fine_items.size();
+        if ((st = launch_carrier_batched(c->stream, c->rx_table.ptr, d, (uint32_t)carrier_items.size()))) return st;
+        d += carrier_items.size();
+        mark(c, 3);
+        if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, d, (uint32_t)det_items.size(), kDetWindow)))
+            return st;
+        d += det_items.size();
+        if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, d, (uint32_t)audio_items.size(), c->audio_dev.ptr,
+                                       kDetWindow)))
+            return st;
+        mark(c, 4);
+        c->stats.launches += 3 + (carrier_items.empty() ? 0 : 1);
+        c->stats.work_items += total;
+    }
+
+    // ---- audio back to the host (the reference's readback copies)
+    if (audio_floats > 0) {
+        if ((st = c->audio_host.reserve(audio_floats))) return st;
+        if ((st = cuda_status(cudaMemcpyAsync(c->audio_host.ptr, c->audio_dev.ptr, audio_floats * sizeof(float),
+                                              cudaMemcpyDeviceToHost, c->stream),
+                              "audio readback")))
+            return st;
+        if ((st = cuda_status(cudaStreamSynchronize(c->stream), "audio readback sync"))) return st;
+        for (Receiver& r : c->rx) {
+            const uint64_t n = r.run_audio_frames * r.plan.demod.channels;
+            if (c->config.keep_audio && n)
+                r.audio.insert(r.audio.end(), c->audio_host.ptr + r.run_audio_offset,
+                               c->audio_host.ptr + r.run_audio_offset + n);
+            r.audio_frames_total += r.run_audio_frames;
+        }
+        c->stats.audio_bytes += audio_floats * sizeof(float);
+    }
+    mark(c, 5);
+    // the pinned work-list buffer is rewritten by the next run
+    if ((st = cuda_status(cudaStreamSynchronize(c->stream), "run sync"))) return st;
+    collect_marks(c);
+    c->stats.runs += 1;
+    return clear_error();
+}
+
+int32_t rv_chain_receiver_info(const rv_chain* c, uint32_t id, rv_vrx_plan_info* info, uint64_t* audio_frames,
+                               uint64_t* first_audio) {
+    if (c == nullptr || id >= c->rx.size()) return set_error_fmt(RV_ERR_INVALID, "rv_chain_receiver_info: no receiver %u", id);
+    const Receiver& r = c->rx[id];
+    if (info) *info = r.plan;
+    if (audio_frames) *audio_frames = r.audio_frames_total;
+    if (first_audio) *first_audio = r.next_audio - r.audio_frames_total;
+    return clear_error();
+}
+
+int32_t rv_chain_read_audio(rv_chain* c, uint32_t id, float* dst, uint64_t capacity, uint64_t* written) {
+    if (c == nullptr || id >= c->rx.size()) return set_error_fmt(RV_ERR_INVALID, "rv_chain_read_audio: no receiver %u", id);
+    Receiver& r = c->rx[id];
+    const uint64_t n = std::min<uint64_t>(capacity, r.audio.size());
+    if (dst && n) memcpy(dst, r.audio.data(), n * sizeof(float));
+    r.audio.erase(r.audio.begin(), r.audio.begin() + n);
+    if (written) *written = n;
+    return clear_error();
+}
+
+int32_t rv_chain_get_stats(const rv_chain* c, rv_chain_stats* stats) {
+    if (c == nullptr || stats == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_get_stats: NULL");
+    *stats = c->stats;
+    return clear_error();
+}
+
+int32_t rv_chain_receiver_rings(const rv_chain* c, uint32_t id, const rv_cf32** fine, const float** det, uint32_t* mask) {
+    if (c == nullptr || id >= c->rx.size()) return set_error_fmt(RV_ERR_INVALID, "rv_chain_receiver_rings: no receiver %u", id);
+    const Receiver& r = c->rx[id];
+    if (fine) *fine = r.d_fine.ptr;
+    if (det) *det = c->config.mode == RV_CHAIN_BATCHED ? r.d_det.ptr : nullptr;
+    if (mask) *mask = r.fine_mask;
+    return clear_error();
+}
+
+int32_t rv_chain_channel_ring(const rv_chain* c, const rv_cf32** ring, uint32_t* ring_blocks) {
+    if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_channel_ring: NULL");
+    if (ring) *ring = c->channel.ptr;
+    if (ring_blocks) *ring_blocks = c->chan_blocks;
+    return clear_error();
+}
+
+}  // extern "C"

@@ -42,10 +42,14 @@ constexpr int kChunksPerTile = 8;
 
 __device__ __forceinline__ int32_t sext16(uint32_t raw) { return ((int32_t)(raw << 16)) >> 16; }
 
-// One raw sample at ring position pos (already masked), converted exactly as
-// the plain convert kernel converts it.
+// One raw sample at unmasked ring position n, converted exactly as the plain
+// convert kernel converts it; positions in the first lead_zero samples of
+// block 0's support (before the stream began) read as 0.0.
 template <int FMT>
-__device__ __forceinline__ float2 load_sample(const uint32_t* __restrict__ raw, uint32_t pos) {
+__device__ __forceinline__ float2 load_sample(const uint32_t* __restrict__ raw, uint32_t n, const rv_coarse_params& p,
+                                              uint32_t window_start) {
+    if (n - window_start < p.lead_zero) return make_float2(0.0F, 0.0F);
+    const uint32_t pos = n & p.ring_mask;
     if (FMT == RV_FORMAT_CS16) {
         const uint32_t w = __ldg(&raw[pos]);
         return make_float2((float)sext16(w & 0xFFFFu) * 0.000030517578125F,
@@ -111,6 +115,7 @@ k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const
     float2* B = A + S * CB * M;       // [M][S*CB] channel-major staging
 
     const uint32_t tid = threadIdx.x;
+    const uint32_t window_start = p.base_offset - (uint32_t)(M * T - 1);
     for (uint32_t i = tid; i < (uint32_t)M; i += NT) twd[i] = ld_cf32(&tw_g[i]);
 
     const uint32_t r = tid % M;
@@ -127,14 +132,14 @@ k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const
         const uint32_t n0 = p.base_offset + (tile0 + s * NB + par) * (uint32_t)D - r;
         float2 win[T];
 #pragma unroll
-        for (int q = 1; q < T; ++q) win[T - q] = load_sample<FMT>(raw, (n0 - (uint32_t)(q * M)) & p.ring_mask);
+        for (int q = 1; q < T; ++q) win[T - q] = load_sample<FMT>(raw, n0 - (uint32_t)(q * M), p, window_start);
 
         for (int c = 0; c < kChunksPerTile; ++c) {
             // ---- branch FIR: T steps, window slot of sample q at step i is (i - q) mod T
 #pragma unroll
             for (int i = 0; i < T; ++i) {
                 const uint32_t g = (uint32_t)(c * T + i);
-                win[i] = load_sample<FMT>(raw, (n0 + g * (uint32_t)M) & p.ring_mask);
+                win[i] = load_sample<FMT>(raw, n0 + g * (uint32_t)M, p, window_start);
                 float2 acc = make_float2(0.0F, 0.0F);
 #pragma unroll
                 for (int q = 0; q < T; ++q) mac(acc, win[(i - q + T) % T], h[q]);
@@ -281,6 +286,8 @@ int32_t validate_coarse(const rv_grid_params* g, int32_t format, const rv_coarse
     if (span > cap)
         return set_error_fmt(RV_ERR_INVALID, "coarse_fused: needs %llu samples of history, ring capacity is %llu",
                              (unsigned long long)span, (unsigned long long)cap);
+    if (p->lead_zero > M * T - 1u)
+        return set_error_fmt(RV_ERR_INVALID, "coarse_fused: lead_zero %u exceeds M*T - 1 = %u", p->lead_zero, M * T - 1u);
     if (!is_pow2(p->out_ring_blocks) || p->out_ring_mask != p->out_ring_blocks - 1u)
         return set_error_fmt(RV_ERR_INVALID, "coarse_fused: out_ring_blocks must be a power of two and out_ring_mask one less");
     if (p->block_count > p->out_ring_blocks)

@@ -134,6 +134,12 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// engine::is_complex_tap (core/engine/vrx.h): modes that hand out baseband.
+__host__ __device__ __forceinline__ bool is_complex_demod(uint32_t m) {
+    return m == RV_DEMOD_RAW || m == RV_DEMOD_P25P1 || m == RV_DEMOD_DSTAR || m == RV_DEMOD_TETRA ||
+           m == RV_DEMOD_DMR;
+}
+
 __device__ __forceinline__ uint32_t brev(uint32_t v, uint32_t stages) {
     return stages == 0 ? 0u : (__brev(v) >> (32u - stages));
 }

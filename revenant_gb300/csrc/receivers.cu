@@ -1,0 +1,350 @@
+// Batched receivers: every virtual receiver of the chain in one launch per
+// stage, over a work list of (receiver, output run) items.
+//
+// The arithmetic per output is the reference's (vrx_fine.comp:270-369,
+// vrx_demod.comp:445-659; twins core/dsp/vrx_reference.cpp:489-917), so every
+// fine sample and audio frame is bit-identical to the plain per-receiver
+// kernels. Three redundancies of the per-receiver dispatch are removed without
+// changing a rounding:
+//
+//  * Pre-blended polyphase taps. A receiver's (phase, blend) pair depends only
+//    on frac(j) = j * (Fc mod Fd) mod Fd for fine output j, which repeats with
+//    period Fd / gcd(Fc mod Fd, Fd) (48 outputs for a 625 kS/s channel
+//    resampled to 48 kS/s, 336 for 336 kS/s). The blended taps
+//    g0 * (1 - b) + g1 * b are computed once per pattern phase, with the same
+//    two multiplies and one add, and the per-output FIR reads them: half the
+//    tap-table reads and six fewer flops per tap.
+//  * The detector once per fine sample. The reference evaluates the FM
+//    discriminator, the AM magnitude and its DC-removal FIR inside the audio
+//    FIR's tap loop, i.e. audio_taps (x dc_taps for AM) times per audio frame.
+//    Here the detector runs once per fine sample into a ring and the audio FIR
+//    reads it: identical values, since the detector is a pure function of the
+//    fine samples.
+//  * One launch per stage for all receivers, each CTA staging the input window
+//    of its run in shared memory.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "carrier.cuh"
+#include "common.cuh"
+#include "receivers.cuh"
+
+namespace rv {
+namespace {
+
+__global__ void k_lerp_table(const rv_cf32* __restrict__ taps, float2* __restrict__ out, uint32_t T, uint32_t P,
+                             uint32_t period, uint32_t step_rem, uint32_t fd, float inv_fd) {
+    const uint32_t total = period * T;
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const uint32_t pp = idx / T, k = idx % T;
+        // frac of any fine output j with j mod period == pp
+        const uint32_t frac = (uint32_t)(((uint64_t)pp * step_rem) % fd);
+        const uint32_t scaled = frac * P;
+        const uint32_t phase = scaled / fd;
+        const uint32_t blend_num = scaled - phase * fd;
+        const float blend = (float)blend_num * inv_fd;
+        const float blend_c = 1.0F - blend;
+        const uint32_t slot = phase + k * P;
+        const float2 g0 = ld_cf32(&taps[slot]);
+        const float2 g1 = ld_cf32(&taps[slot + 1u]);
+        out[(uint64_t)pp * T + k] = make_float2(g0.x * blend_c + g1.x * blend, g0.y * blend_c + g1.y * blend);
+    }
+}
+
+// ---- fine stage ---------------------------------------------------------
+
+__global__ void __launch_bounds__(kRxThreads)
+k_fine_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
+               const float2* __restrict__ chan, uint32_t window_cap) {
+    extern __shared__ float2 xs[];
+    __shared__ RxDev rx;
+    __shared__ uint64_t s_n0;
+    __shared__ uint32_t s_frac0, s_len, s_p0;
+    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const WorkItem item = items[it];
+        if (threadIdx.x == 0) {
+            rx = rxs[item.rx];
+            // exact input index of the first output (resample_block,
+            // core/dsp/vrx_reference.cpp:2786-2810), split to stay in 64 bits
+            const uint64_t fd = rx.out_rate, j0 = item.first;
+            const uint64_t whole = j0 / fd, part = j0 % fd;
+            const uint64_t cp = part * rx.step_rem;
+            s_n0 = j0 * rx.step_whole + whole * rx.step_rem + cp / fd;
+            s_frac0 = (uint32_t)(cp % fd);
+            const uint64_t last_acc = (uint64_t)s_frac0 + (uint64_t)(item.count - 1u) * rx.step_rem;
+            const uint64_t n_last = s_n0 + (uint64_t)(item.count - 1u) * rx.step_whole + last_acc / fd;
+            s_len = (uint32_t)(n_last - s_n0) + rx.taps;
+            s_p0 = (uint32_t)(j0 % rx.period);
+        }
+        __syncthreads();
+        const uint32_t T = rx.taps;
+        const uint64_t base = s_n0 - (T - 1u);
+        const uint32_t len = s_len < window_cap ? s_len : window_cap;
+        for (uint32_t e = threadIdx.x; e < len; e += blockDim.x)
+            xs[e] = chan[(uint64_t)rx.chan_base + (uint32_t)((base + e) & rx.chan_mask)];
+        __syncthreads();
+        const uint32_t i = threadIdx.x;
+        const uint32_t fd = rx.out_rate;
+        const uint32_t acc = s_frac0 + i * rx.step_rem;
+        const uint32_t carry = acc / fd;
+        const uint32_t n_rel = i * rx.step_whole + carry;
+        // n_rel + T - 1 < len always holds for items the chain builds; the
+        // guard keeps every shared-memory read inside the staged window
+        if (i < item.count && n_rel + T - 1u < len) {
+            const float2* w = xs + n_rel + T - 1u;  // w[-k] = x[n(j) - k]
+            float ar = 0.0F, ai = 0.0F;
+            if (rx.lerped != nullptr) {
+                const uint32_t pp = (s_p0 + i) % rx.period;
+                const float2* __restrict__ tp = rx.lerped + (uint64_t)pp * T;
+                for (uint32_t k = 0; k < T; ++k) {
+                    const float2 s = w[-(int)k];
+                    const float2 t = tp[k];
+                    ar = ar + (s.x * t.x - s.y * t.y);
+                    ai = ai + (s.x * t.y + s.y * t.x);
+                }
+            } else {
+                // blend on the fly, exactly as the plain kernel does
+                const uint32_t frac = acc - carry * fd;
+                const uint32_t scaled = frac * rx.phases;
+                const uint32_t phase = scaled / fd;
+                const uint32_t blend_num = scaled - phase * fd;
+                const float blend = (float)blend_num * rx.inv_out_rate;
+                const float blend_c = 1.0F - blend;
+                for (uint32_t k = 0; k < T; ++k) {
+                    const uint32_t slot = phase + k * rx.phases;
+                    const float2 g0 = rx.taps_raw[slot];
+                    const float2 g1 = rx.taps_raw[slot + 1u];
+                    const float tr = g0.x * blend_c + g1.x * blend;
+                    const float ti = g0.y * blend_c + g1.y * blend;
+                    const float2 s = w[-(int)k];
+                    ar = ar + (s.x * tr - s.y * ti);
+                    ai = ai + (s.x * ti + s.y * tr);
+                }
+            }
+            const uint64_t j = item.first + i;
+            const uint64_t phi = rx.nco_delta * j;
+            const uint32_t idx = (rx.nco_log2 == 0) ? 0u : ((uint32_t)(phi >> 32) >> (32u - rx.nco_log2));
+            const float2 rot = rx.nco[idx];
+            rx.fine[(uint32_t)j & rx.fine_mask] = make_float2(ar * rot.x - ai * rot.y, ar * rot.y + ai * rot.x);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- carrier loop (SAM / DSB): serial per receiver ----------------------
+
+__global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems) {
+    const uint32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nitems) return;
+    const WorkItem item = items[it];
+    const RxDev& rx = rxs[item.rx];
+    rv_vrx_carrier_params p = rx.carrier;
+    p.in_mask = rx.fine_mask;
+    p.in_offset = (uint32_t)item.first & rx.fine_mask;
+    p.count = item.count;
+    p.flags = (uint32_t)item.out;  // the reset flag travels in `out`
+    p.shift = 0.0F;
+    carrier_loop(reinterpret_cast<const rv_cf32*>(rx.nco), reinterpret_cast<rv_cf32*>(rx.fine), rx.carrier_state,
+                 rx.carrier_power, rx.nco_log2, p);
+}
+
+// ---- detector, once per fine sample ---------------------------------------
+
+__global__ void __launch_bounds__(kRxThreads)
+k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
+                 uint32_t window_cap) {
+    extern __shared__ float sd[];
+    __shared__ RxDev rx;
+    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const WorkItem item = items[it];
+        if (threadIdx.x == 0) rx = rxs[item.rx];
+        __syncthreads();
+        const uint32_t mode = rx.mode;
+        const uint32_t i = threadIdx.x;
+        const uint32_t first = (uint32_t)item.first;  // ring arithmetic is modulo the mask
+        if (mode == RV_DEMOD_AM || mode == RV_DEMOD_SAM) {
+            // window of detector inputs: |z| (AM) or Re z (SAM) for
+            // fine samples [first - dc + 1, first + count)
+            const uint32_t dc = rx.dc_taps;
+            const uint32_t len = item.count + dc - 1u;
+            const uint32_t start = first - (dc - 1u);
+            for (uint32_t e = threadIdx.x; e < len && e < window_cap; e += blockDim.x) {
+                const float2 z = rx.fine[(start + e) & rx.fine_mask];
+                sd[e] = (mode == RV_DEMOD_AM) ? det_sqrt(z.x * z.x + z.y * z.y) : z.x;
+            }
+            __syncthreads();
+            if (i < item.count && i + dc - 1u < (len < window_cap ? len : window_cap)) {
+                const float* v = sd + i + dc - 1u;  // v[-w] = input at fine (first + i - w)
+                const float* __restrict__ dw = rx.weights + rx.audio_taps;
+                float acc = 0.0F;
+                for (uint32_t w = 0; w < dc; ++w) {
+                    const float term = v[-(int)w] * dw[w];
+                    acc = acc + term;
+                }
+                rx.det[(first + i) & rx.fine_mask] = v[0] - acc;
+            }
+        } else if (i < item.count) {
+            const uint32_t f = first + i;
+            const float2 z = rx.fine[f & rx.fine_mask];
+            float d;
+            if (mode == RV_DEMOD_NFM || mode == RV_DEMOD_WFM) {
+                const float2 q = rx.fine[(f - 1u) & rx.fine_mask];
+                const float pr = z.x * q.x + z.y * q.y;
+                const float pi = z.y * q.x - z.x * q.y;
+                d = det_atan2(pi, pr);
+            } else {
+                d = z.x;
+            }
+            rx.det[f & rx.fine_mask] = d;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- audio FIR with decimation, mono or stereo ----------------------------
+
+__global__ void __launch_bounds__(kRxThreads)
+k_audio_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
+                float* __restrict__ audio, uint32_t window_cap) {
+    extern __shared__ float sd[];
+    __shared__ RxDev rx;
+    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const WorkItem item = items[it];
+        if (threadIdx.x == 0) rx = rxs[item.rx];
+        __syncthreads();
+        const uint32_t i = threadIdx.x;
+        const uint32_t dec = rx.decimation;
+        const uint32_t first_index = (uint32_t)(item.first * dec);  // fine index of the first frame, mod 2^32
+        float* out = audio + item.out;
+        if (is_complex_demod(rx.mode)) {
+            if (i < item.count) {
+                const float2 z = rx.fine[(first_index + i * dec) & rx.fine_mask];
+                out[2u * i] = z.x * rx.gain;
+                out[2u * i + 1u] = z.y * rx.gain;
+            }
+            __syncthreads();
+            continue;
+        }
+        // detector window [first_index - reach, last index]
+        const uint32_t len = (item.count - 1u) * dec + rx.reach + 1u;
+        const uint32_t start = first_index - rx.reach;
+        for (uint32_t e = threadIdx.x; e < len && e < window_cap; e += blockDim.x)
+            sd[e] = rx.det[(start + e) & rx.fine_mask];
+        __syncthreads();
+        if (i < item.count && rx.reach + i * dec < (len < window_cap ? len : window_cap)) {
+            const float* v = sd + rx.reach + i * dec;  // v[-t] = detector at (index - t)
+            const float* __restrict__ w = rx.weights;
+            if (rx.channels == 2u) {
+                const uint32_t pilot_base = rx.audio_taps + rx.dc_taps;
+                const uint32_t rotation_base = pilot_base + 2u * rx.pilot_taps;
+                const float* pv = v - (int)(rx.audio_taps / 2u);
+                float pr = 0.0F, pi = 0.0F;
+                for (uint32_t k = 0; k < rx.pilot_taps; ++k) {
+                    const float comp = pv[-(int)k];
+                    const float tr = comp * w[pilot_base + 2u * k];
+                    const float ti = comp * w[pilot_base + 2u * k + 1u];
+                    pr = pr + tr;
+                    pi = pi + ti;
+                }
+                const float sr = pr * rx.gain, si = pi * rx.gain;
+                const float rr = sr * sr, ii = si * si;
+                const float power = rr + ii;
+                const float inverse = det_recip((power < 2.0e-5F) ? 2.0e-5F : power);
+                const float cross = sr * si;
+                const float cos_two = (ii - rr) * inverse;
+                const float sin_two = (-2.0F * cross) * inverse;
+                const float locked = (power >= 2.0e-5F) ? 1.0F : 0.0F;
+                float sum = 0.0F, diff = 0.0F;
+                for (uint32_t t = 0; t < rx.audio_taps; ++t) {
+                    const float weighted = v[-(int)t] * w[t];
+                    sum = sum + weighted;
+                    const float ref = sin_two * w[rotation_base + 2u * t] - cos_two * w[rotation_base + 2u * t + 1u];
+                    const float term = weighted * ref;
+                    diff = diff + term;
+                }
+                const float gated = diff * locked;
+                out[2u * i] = (sum + gated) * rx.gain;
+                out[2u * i + 1u] = (sum - gated) * rx.gain;
+            } else {
+                float acc = 0.0F;
+                for (uint32_t t = 0; t < rx.audio_taps; ++t) {
+                    const float term = v[-(int)t] * w[t];
+                    acc = acc + term;
+                }
+                out[i] = acc * rx.gain;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+unsigned persistent_grid(const void* kern, int threads, size_t shared, uint32_t nitems) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, shared);
+    const uint32_t cap = (uint32_t)((per_sm > 0 ? per_sm : 1) * sms);
+    return nitems < cap ? (nitems == 0 ? 1u : nitems) : cap;
+}
+
+// Dynamic plus static shared memory above 48 KB needs the opt-in attribute;
+// it is set whenever a launch asks for more than it was last set to.
+int32_t set_shared(const void* kern, size_t shared) {
+    cudaFuncAttributes attr;
+    if (int32_t st = cuda_status(cudaFuncGetAttributes(&attr, kern), "receiver kernel attributes")) return st;
+    if ((size_t)attr.maxDynamicSharedSizeBytes >= shared) return RV_OK;
+    return cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared),
+                       "receiver kernel shared memory");
+}
+
+}  // namespace
+
+int32_t launch_lerp_table(cudaStream_t s, const rv_cf32* taps, float2* lerped, uint32_t T, uint32_t P,
+                          uint32_t period, uint32_t step_rem, uint32_t fd, float inv_fd) {
+    const uint32_t total = period * T;
+    const unsigned grid = (total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096;
+    k_lerp_table<<<grid, 256, 0, s>>>(taps, lerped, T, P, period, step_rem, fd, inv_fd);
+    return cuda_status(cudaGetLastError(), "lerp table");
+}
+
+int32_t launch_fine_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
+                            const float2* chan, uint32_t window_cap) {
+    if (nitems == 0) return RV_OK;
+    const size_t shared = (size_t)window_cap * sizeof(float2);
+    if (int32_t st = set_shared((const void*)k_fine_batched, shared)) return st;
+    const unsigned grid = persistent_grid((const void*)k_fine_batched, kRxThreads, shared, nitems);
+    k_fine_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, chan, window_cap);
+    return cuda_status(cudaGetLastError(), "fine batched");
+}
+
+int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems) {
+    if (nitems == 0) return RV_OK;
+    k_carrier_batched<<<(nitems + 31) / 32, 32, 0, s>>>(rxs, items, nitems);
+    return cuda_status(cudaGetLastError(), "carrier batched");
+}
+
+int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
+                              uint32_t window_cap) {
+    if (nitems == 0) return RV_OK;
+    const size_t shared = (size_t)window_cap * sizeof(float);
+    if (int32_t st = set_shared((const void*)k_detect_batched, shared)) return st;
+    const unsigned grid = persistent_grid((const void*)k_detect_batched, kRxThreads, shared, nitems);
+    k_detect_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap);
+    return cuda_status(cudaGetLastError(), "detect batched");
+}
+
+int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems, float* audio,
+                             uint32_t window_cap) {
+    if (nitems == 0) return RV_OK;
+    const size_t shared = (size_t)window_cap * sizeof(float);
+    if (int32_t st = set_shared((const void*)k_audio_batched, shared)) return st;
+    const unsigned grid = persistent_grid((const void*)k_audio_batched, kRxThreads, shared, nitems);
+    k_audio_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap);
+    return cuda_status(cudaGetLastError(), "audio batched");
+}
+
+}  // namespace rv

@@ -260,4 +260,13 @@ int32_t rv_buffer_clear(rv_buffer* b) {
     return rv::clear_error();
 }
 
+int32_t rv_copy(rv_context* ctx, void* dst, const void* src, uint64_t bytes) {
+    if (ctx == nullptr || dst == nullptr || src == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_copy: NULL");
+    if (ctx->destroyed) return set_error_fmt(RV_ERR_INVALID, "rv_copy: context was destroyed");
+    if (bytes == 0) return rv::clear_error();
+    if (int32_t st = cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, ctx->stream), "rv_copy")) return st;
+    if (int32_t st = cuda_status(cudaStreamSynchronize(ctx->stream), "rv_copy sync")) return st;
+    return rv::clear_error();
+}
+
 }  // extern "C"

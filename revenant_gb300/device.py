@@ -80,6 +80,11 @@ class Device:
         b.clear()
         return b
 
+    def copy_to_host(self, out, device_address):
+        """Copy out.nbytes from a device address into numpy array `out`."""
+        check(lib().rv_copy(self.handle, out.ctypes.data_as(C.c_void_p), C.c_void_p(device_address), out.nbytes))
+        return out
+
     def synchronize(self):
         check(lib().rv_context_synchronize(self.handle))
 

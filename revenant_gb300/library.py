@@ -135,6 +135,7 @@ SIGNATURES = {
     "rv_buffer_upload": (I32, [P, U64, P, U64]),
     "rv_buffer_download": (I32, [P, U64, P, U64]),
     "rv_buffer_clear": (I32, [P]),
+    "rv_copy": (I32, [P, P, P, U64]),
     "rv_convert": (I32, [P, I32, ptr(abi.ConvertParams), P, U64, P, U64]),
     "rv_pfb_branch": (I32, [P, ptr(abi.GridParams), ptr(abi.PfbBranchParams), P, U64, P, U64, P, U64]),
     "rv_pfb_fft": (I32, [P, ptr(abi.PfbFftParams), P, U64, P, U64, P, U64]),
@@ -144,6 +145,15 @@ SIGNATURES = {
     "rv_vrx_demod": (I32, [P, ptr(abi.VrxDemodConfig), ptr(abi.VrxDemodParams), P, U64, P, U64, P, U64]),
     "rv_vrx_carrier": (I32, [P, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P]),
     "rv_coarse_fused": (I32, [P, ptr(abi.GridParams), I32, ptr(abi.CoarseParams), P, U64, P, U64, P, U64, P, U64]),
+    "rv_chain_create": (I32, [P, ptr(abi.ChainConfig), ptr(P)]),
+    "rv_chain_destroy": (I32, [P]),
+    "rv_chain_add_receiver": (I32, [P, ptr(abi.VrxRequest), ptr(U32)]),
+    "rv_chain_run": (I32, [P, P, U64, I32]),
+    "rv_chain_receiver_info": (I32, [P, U32, ptr(abi.VrxPlanInfo), ptr(U64), ptr(U64)]),
+    "rv_chain_read_audio": (I32, [P, U32, P, U64, ptr(U64)]),
+    "rv_chain_get_stats": (I32, [P, ptr(abi.ChainStats)]),
+    "rv_chain_channel_ring": (I32, [P, ptr(P), ptr(U32)]),
+    "rv_chain_receiver_rings": (I32, [P, U32, ptr(P), ptr(P), ptr(U32)]),
     "rv_validate_grid": (I32, [ptr(abi.GridParams)]),
     "rv_design_prototype": (I32, [ptr(abi.GridParams), F64, P, U64, ptr(F64), ptr(U64)]),
     "rv_build_twiddles": (I32, [U32, P, U64]),

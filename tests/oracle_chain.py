@@ -1,0 +1,136 @@
+"""The receive chain driven through the oracle, run by run.
+
+Mirrors what the reference's Graph::on_block and DemodStage::record do per
+source block (core/engine/graph.cpp:5118-5330, core/engine/vrx_stage.cpp:
+1119-1430): convert the new samples into the ring, branch-filter and FFT the
+new channel blocks, then for every receiver run the fine stage over the
+outputs whose inputs now exist, the carrier loop if the mode has one, and the
+demodulator over the audio frames whose fine history is complete. Block
+parameters come from the library's planner (rv_fine_block / rv_demod_block),
+which tests/test_planner.py pins to the reference's planner. Test
+infrastructure only.
+"""
+import ctypes as C
+
+import numpy as np
+
+from bindings import cf32, oracle
+from revenant_gb300 import abi
+from revenant_gb300.library import lib
+
+
+def _check(st):
+    assert st == 0, lib().rv_last_error().decode()
+
+
+def highest_output_for(newest, fc, fd):
+    bound = newest + 1
+    whole, part = divmod(bound, fc)
+    return whole * fd - 1 if part == 0 else whole * fd + (part * fd - 1) // fc
+
+
+def lowest_output_for(needed, fc, fd):
+    whole, part = divmod(needed, fc)
+    return whole * fd + (part * fd + fc - 1) // fc
+
+
+class OracleChain:
+    def __init__(self, grid, rate, fmt, requests, ring_log2=20, chan_log2=17, fine_log2=17):
+        self.ora = oracle()
+        self.g = abi.GridParams(*grid)
+        self.rate, self.fmt = rate, fmt
+        M, T, D = grid
+        self.taps = np.zeros(M * T, np.float32)
+        _check(lib().rv_design_prototype(C.byref(self.g), 120.0, self.taps.ctypes.data, self.taps.size, None, None))
+        self.tw = np.zeros((M, 2), np.float32)
+        _check(lib().rv_build_twiddles(M, self.tw.ctypes.data, M))
+        self.nco = np.zeros((1 << 16, 2), np.float32)
+        _check(lib().rv_build_nco_table(16, self.nco.ctypes.data, 1 << 16))
+        self.ring = cf32(1 << ring_log2)
+        self.ring_mask = (1 << ring_log2) - 1
+        self.chan_blocks = 1 << chan_log2
+        self.chan = cf32(M * self.chan_blocks)
+        self.fine_mask = (1 << fine_log2) - 1
+        self.samples_in = 0
+        self.next_block = 0
+        self.rx = []
+        for req in requests:
+            pl = abi.VrxPlacement()
+            _check(lib().rv_place(C.byref(self.g), rate, C.byref(req), C.byref(pl)))
+            info = abi.VrxPlanInfo()
+            _check(lib().rv_plan_vrx(C.byref(self.g), rate, C.byref(req), C.byref(pl), C.byref(info), None, 0, None, 0))
+            taps = np.zeros((info.fine_tap_count, 2), np.float32)
+            w = np.zeros(info.demod_weight_count, np.float32)
+            _check(lib().rv_plan_vrx(C.byref(self.g), rate, C.byref(req), C.byref(pl), C.byref(info), taps.ctypes.data,
+                                     taps.shape[0], w.ctypes.data, w.size))
+            self.rx.append(dict(info=info, taps=taps, w=w, fine=cf32(self.fine_mask + 1), state=np.zeros(8, np.uint32),
+                                started=False, reset=True, audio=[],
+                                history=lib().rv_demod_fine_history(C.byref(info.demod))))
+
+    def run(self, packed, count):
+        M, D = self.g.channels, self.g.decimation
+        o = self.ora
+        cp = abi.ConvertParams(self.ring_mask, self.samples_in & 0xFFFFFFFF, 0, count)
+        assert o.convert(self.fmt, cp, packed, self.ring) == 0, o.error()
+        first_block = self.next_block
+        last_block = (self.samples_in + count - 1) // D
+        self.samples_in += count
+        if last_block < first_block:
+            return
+        blocks = last_block - first_block + 1
+        self.next_block = last_block + 1
+        branch = cf32(blocks * M)
+        bp = abi.PfbBranchParams(self.ring_mask, (first_block * D) & 0xFFFFFFFF, blocks)
+        assert o.pfb_branch(self.g, bp, self.taps, self.ring, branch) == 0, o.error()
+        fp = abi.PfbFftParams(M, D, int(np.log2(M)), first_block & 0xFFFFFFFF, blocks, self.chan_blocks,
+                              self.chan_blocks - 1)
+        assert o.pfb_fft(fp, branch, self.tw, self.chan) == 0, o.error()
+        self.receivers(first_block, last_block)
+
+    def receivers(self, first_block, last_block):
+        """Advance every receiver over channel blocks [first_block, last_block]
+        already in the channel ring (DemodStage::record)."""
+        o = self.ora
+        for r in self.rx:
+            info = r["info"]
+            fc, fd, dec = info.channel_rate, info.demod_rate, info.demod.decimation
+            if not r["started"]:
+                r["first"] = lowest_output_for(first_block + info.fine.taps - 1, fc, fd)
+                r["next_out"] = r["first"]
+                r["next_audio"] = (r["first"] + r["history"] + dec - 1) // dec
+                r["started"] = True
+            limit = highest_output_for(last_block, fc, fd)
+            if limit + 1 > r["next_out"]:
+                n_total = limit + 1 - r["next_out"]
+                rem = fc % fd
+                per = n_total if rem == 0 else max(1, (0xFFFFFFFF - fd) // rem)
+                done = 0
+                while done < n_total:
+                    n = min(n_total - done, per)
+                    fb = abi.VrxFineBlock()
+                    _check(lib().rv_fine_block(C.byref(info), info.placement.channel * self.chan_blocks,
+                                               self.chan_blocks - 1, self.fine_mask, r["next_out"] + done, n,
+                                               C.byref(fb)))
+                    assert o.vrx_fine(info.fine, fb.params, self.chan, r["taps"], self.nco, r["fine"]) == 0, o.error()
+                    done += n
+                if info.carrier.power:
+                    cpar = abi.VrxCarrierParams()
+                    _check(lib().rv_carrier_block(C.byref(info), self.fine_mask, r["next_out"], n_total,
+                                                  1 if r["reset"] else 0, 0.0, C.byref(cpar)))
+                    assert o.vrx_carrier(info.carrier, cpar, self.nco, r["fine"], r["state"]) == 0, o.error()
+                    r["reset"] = False
+                r["next_out"] += n_total
+            if r["next_out"] > r["first"]:
+                audio_limit = (r["next_out"] - 1) // dec
+                if audio_limit + 1 > r["next_audio"]:
+                    n = audio_limit + 1 - r["next_audio"]
+                    db = abi.VrxDemodBlock()
+                    _check(lib().rv_demod_block(C.byref(info), self.fine_mask, r["next_audio"], n, C.byref(db)))
+                    out = np.zeros(n * info.demod.channels, np.float32)
+                    assert o.vrx_demod(info.demod, db.params, r["fine"], r["w"], out) == 0, o.error()
+                    r["audio"].append(out)
+                    r["next_audio"] += n
+
+    def audio(self, i):
+        a = self.rx[i]["audio"]
+        return np.concatenate(a) if a else np.zeros(0, np.float32)

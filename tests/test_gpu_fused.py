@@ -49,6 +49,10 @@ def oracle_chain(ora, g, fmt, ring_log2, raw, p, taps, tw):
     ring = cf32(n)
     cp = abi.ConvertParams(n - 1, 0, 0, n)
     assert ora.convert(fmt, cp, raw, ring) == 0
+    # the first lead_zero samples of block 0's support read as zero
+    start = (p.base_offset - (g.channels * g.taps_per_branch - 1)) & (n - 1)
+    for k in range(p.lead_zero):
+        ring[(start + k) & (n - 1)] = 0.0
     M = g.channels
     branch = cf32(max(p.block_count, 1) * M)
     bp = abi.PfbBranchParams(n - 1, p.base_offset, p.block_count)
@@ -61,8 +65,10 @@ def oracle_chain(ora, g, fmt, ring_log2, raw, p, taps, tw):
 
 
 CASES = [
-    # (M, T, D, fmt, ring_log2, blocks, base_offset, block_base)
+    # (M, T, D, fmt, ring_log2, blocks, base_offset, block_base[, lead_zero])
     (64, 17, 32, abi.FORMAT_CS16, 16, 1, 5000, 0),
+    (64, 17, 32, abi.FORMAT_CU8, 16, 300, 0, 0, 1087),
+    (8, 17, 4, abi.FORMAT_CU8, 14, 500, 40, 10, 95),
     (64, 17, 32, abi.FORMAT_CS16, 16, 33, (1 << 16) - 40, 7),
     (64, 17, 32, abi.FORMAT_CS16, 18, 5000, 123456, 0xFFFFFF00),
     (64, 17, 32, abi.FORMAT_CU8, 18, 7000, 99, 3),
@@ -81,12 +87,14 @@ def describe_mismatch(got, want):
         bad.size, g.size, bad[:4], g[bad[:4]], w[bad[:4]], ulp.max(), np.median(ulp), rel.max())
 
 
-@pytest.mark.parametrize("M,T,D,fmt,ring_log2,blocks,base,block_base", CASES)
-def test_coarse_fused_matches_oracle(gpu, ora, M, T, D, fmt, ring_log2, blocks, base, block_base):
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "-".join(map(str, c)))
+def test_coarse_fused_matches_oracle(gpu, ora, case):
+    M, T, D, fmt, ring_log2, blocks, base, block_base = case[:8]
+    lead_zero = case[8] if len(case) > 8 else 0
     g, taps, tw = prototype(M, T, D)
     raw = raw_ring(blocks + M, fmt, 1 << ring_log2)
     ring_blocks = 1 << int(np.ceil(np.log2(blocks)))
-    p = abi.CoarseParams((1 << ring_log2) - 1, base, blocks, block_base, ring_blocks, ring_blocks - 1)
+    p = abi.CoarseParams((1 << ring_log2) - 1, base, blocks, block_base, ring_blocks, ring_blocks - 1, lead_zero)
     want = oracle_chain(ora, g, fmt, ring_log2, raw, p, taps, tw)
     d_raw, d_taps, d_tw = gpu.array(raw), gpu.array(taps), gpu.array(tw)
     d_out = gpu.zeros(M * ring_blocks * 8)
