@@ -113,6 +113,8 @@ struct Receiver {
     uint32_t fine_history = 0, det_history = 0, reach = 0;
     uint32_t fine_mask = 0;
     uint32_t max_fine_item = 0, max_det_item = 0, max_audio_item = 0;
+    uint32_t table_rows = 0;      // tap rows of the blended table staged at a time by the unit kernel
+    uint32_t max_unit_item = 0;   // outputs per item on the unit path
     bool started = false;
     bool carrier_reset = true;
     uint64_t first_output = 0, next_output = 0, next_audio = 0;
@@ -152,6 +154,11 @@ struct rv_chain {
     // per-run work lists and audio
     PinnedArray<WorkItem> items_host;
     DeviceArray<WorkItem> items_dev;
+    DeviceArray<Queues> queues;
+    DeviceArray<FineUnit> units_dev;
+    PinnedArray<FineUnit> units_host;
+    uint32_t unit_budget = 0;
+    uint32_t weights_cap = 32;  // largest staged demodulator weight table (floats)
     DeviceArray<float> audio_dev;
     PinnedArray<float> audio_host;
     uint64_t samples_in = 0;
@@ -295,9 +302,47 @@ void push_items(std::vector<WorkItem>& list, uint32_t rx, uint64_t first, uint64
     uint64_t done = 0;
     while (done < count) {
         const uint32_t n = (uint32_t)std::min<uint64_t>(count - done, per_item);
-        list.push_back(WorkItem{rx, n, first + done, out + done * out_stride});
+        WorkItem w{};
+        w.rx = rx;
+        w.count = n;
+        w.first = first + done;
+        w.out = out + done * out_stride;
+        list.push_back(w);
         done += n;
     }
+}
+
+// Fine items carry the exact input index of their first output and its
+// resampler fraction (resample_block, core/dsp/vrx_reference.cpp:2786-2810)
+// so the device does no 64-bit division. Returns the largest window.
+uint32_t push_fine_items(std::vector<WorkItem>& list, uint32_t rx, const Receiver& r, uint64_t first, uint64_t count,
+                         uint32_t per_item) {
+    const uint64_t fc = (uint64_t)r.plan.channel_rate, fd = (uint64_t)r.plan.demod_rate;
+    const uint64_t step_whole = fc / fd, step_rem = fc % fd;
+    auto input_of = [&](uint64_t j, uint64_t* frac) {
+        const uint64_t whole = j / fd, part = j % fd, cp = part * step_rem;
+        if (frac) *frac = cp % fd;
+        return j * step_whole + whole * step_rem + cp / fd;
+    };
+    uint32_t widest = 0;
+    uint64_t done = 0;
+    while (done < count) {
+        const uint32_t n = (uint32_t)std::min<uint64_t>(count - done, per_item);
+        WorkItem w{};
+        w.rx = rx;
+        w.count = n;
+        w.first = first + done;
+        uint64_t frac0 = 0;
+        w.n0 = input_of(w.first, &frac0);
+        w.frac0 = (uint32_t)frac0;
+        w.p0 = (uint32_t)(w.first % r.period);
+        const uint64_t n_last = input_of(w.first + n - 1u, nullptr);
+        w.window = (uint32_t)(n_last - w.n0) + r.plan.fine.taps;
+        widest = std::max(widest, w.window);
+        list.push_back(w);
+        done += n;
+    }
+    return widest;
 }
 
 }  // namespace
@@ -391,6 +436,9 @@ int32_t rv_chain_destroy(rv_chain* c) {
     c->rx_table.release();
     c->items_dev.release();
     c->items_host.release();
+    c->queues.release();
+    c->units_dev.release();
+    c->units_host.release();
     c->audio_dev.release();
     c->audio_host.release();
     for (cudaEvent_t e : c->marks)
@@ -422,7 +470,11 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
     // item sizes that keep every staged window inside shared memory
     const uint64_t step_max = fc / fd + 1u;
     r.max_fine_item = (uint32_t)std::min<uint64_t>(kMaxItem, (kFineWindow - p.fine.taps) / step_max + 1u);
-    r.max_det_item = (uint32_t)std::min<uint64_t>(kMaxItem, kDetWindow - (p.demod.dc_taps - 1u));
+    // AM / SAM run four DC-removal outputs per thread (window count + dc + 2)
+    if (p.demod.mode == RV_DEMOD_AM || p.demod.mode == RV_DEMOD_SAM)
+        r.max_det_item = (uint32_t)std::min<uint64_t>(4u * kMaxItem, kDetWindow - p.demod.dc_taps - 2u - 8u);
+    else
+        r.max_det_item = kMaxItem;
     const uint64_t dec = p.demod.decimation;
     if (r.reach + 1u > kDetWindow)
         return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_chain_add_receiver: audio history %u exceeds the %u-sample window",
@@ -435,6 +487,28 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
         if (!st)
             st = launch_lerp_table(c->stream, r.d_taps.ptr, r.d_lerped.ptr, p.fine.taps, p.fine.phases, r.period,
                                    (uint32_t)rem, (uint32_t)fd, 1.0f / (float)fd);
+    }
+    if (!st && r.d_lerped.ptr) {
+        // the unit kernel keeps the whole blended table in shared memory when
+        // it leaves room for a window of 256 outputs; otherwise half of shared
+        // memory holds the window and the other half row chunks of the table
+        if (c->unit_budget == 0) c->unit_budget = fine_unit_shared_budget();
+        const uint64_t T = p.fine.taps;
+        const uint64_t table = (uint64_t)r.period * T;
+        const uint64_t min_window = 256u * step_max + T;
+        uint64_t avail;
+        if (table + min_window <= c->unit_budget) {
+            r.table_rows = (uint32_t)T;
+            avail = c->unit_budget - table;
+        } else {
+            avail = c->unit_budget / 2;
+            r.table_rows = (uint32_t)std::min<uint64_t>(T, (c->unit_budget - avail) / r.period);
+        }
+        if (r.table_rows == 0 || avail < T + step_max) {
+            r.max_unit_item = 0;  // the per-item kernel with taps from L2
+        } else {
+            r.max_unit_item = (uint32_t)std::min<uint64_t>(kUnitThreads, (avail - T) / step_max + 1u);
+        }
     }
     if (!st) st = r.d_fine.alloc(cap);
     if (!st) st = cuda_status(cudaMemsetAsync(r.d_fine.ptr, 0, cap * sizeof(rv_cf32), c->stream), "fine clear");
@@ -453,6 +527,11 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
         r.d_weights.release();
         r.d_state.release();
         return st;
+    }
+    {
+        const uint32_t nw = (p.demod.channels == 2u && p.demod.pilot_taps != 0u) ? (uint32_t)r.weights.size()
+                                                                                : p.demod.audio_taps;
+        c->weights_cap = std::max<uint32_t>(c->weights_cap, (nw + 31u) & ~31u);
     }
     c->rx.push_back(std::move(r));
     c->table_dirty = true;
@@ -494,7 +573,12 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         if ((st = upload_table(c))) return st;
 
     // ---- per-receiver cursors (DemodStage::record) and work lists
-    std::vector<WorkItem> fine_items, carrier_items, det_items, audio_items;
+    std::vector<WorkItem> fine_items, carrier_items, det_items, audio_items, unit_items;
+    std::vector<FineUnit> units;
+    uint32_t fine_window = 0;
+    uint64_t unit_cost_total = 0;
+    struct UnitSpan { uint32_t rx, first, count; uint64_t cost_per_item; };
+    std::vector<UnitSpan> unit_spans;
     uint64_t audio_floats = 0;
     struct Span { uint64_t fine_first, fine_count, det_first, det_count, audio_first, audio_count; };
     std::vector<Span> spans(c->rx.size());
@@ -537,7 +621,18 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         r.run_audio_frames = s.audio_count;
         audio_floats += s.audio_count * p.demod.channels;
         if (!plain) {
-            push_items(fine_items, (uint32_t)ri, s.fine_first, s.fine_count, r.max_fine_item, 0, 0);
+            if (r.max_unit_item != 0) {
+                const uint32_t before = (uint32_t)unit_items.size();
+                push_fine_items(unit_items, (uint32_t)ri, r, s.fine_first, s.fine_count, r.max_unit_item);
+                const uint32_t added = (uint32_t)unit_items.size() - before;
+                if (added) {
+                    unit_spans.push_back(UnitSpan{(uint32_t)ri, before, added, (uint64_t)r.max_unit_item * p.fine.taps});
+                    unit_cost_total += s.fine_count * p.fine.taps;
+                }
+            } else {
+                fine_window = std::max(fine_window, push_fine_items(fine_items, (uint32_t)ri, r, s.fine_first,
+                                                                    s.fine_count, r.max_fine_item));
+            }
             if (s.fine_count && p.carrier.power != 0) {
                 carrier_items.push_back(WorkItem{(uint32_t)ri, (uint32_t)s.fine_count, s.fine_first, r.carrier_reset ? 1u : 0u});
                 r.carrier_reset = false;
@@ -595,13 +690,31 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         mark(c, 3);
         mark(c, 4);
     } else {
-        const size_t total = fine_items.size() + carrier_items.size() + det_items.size() + audio_items.size();
-        if ((st = c->items_host.reserve(total + 1))) return st;
+        // cost-balanced units: about four per SM, each one receiver's items
+        {
+            int sms = 0, dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            const uint64_t target = std::max<uint64_t>(1, unit_cost_total / (uint64_t)(4 * std::max(sms, 1)));
+            for (const UnitSpan& us : unit_spans) {
+                const uint32_t per = (uint32_t)std::max<uint64_t>(1, target / std::max<uint64_t>(1, us.cost_per_item));
+                for (uint32_t k = 0; k < us.count; k += per)
+                    units.push_back(FineUnit{us.rx, us.first + k, std::min(per, us.count - k), c->rx[us.rx].table_rows});
+            }
+        }
+        // unit items sit after the per-item lists; units index into that tail
+        const size_t unit_base = fine_items.size() + carrier_items.size() + det_items.size() + audio_items.size();
+        for (FineUnit& u : units) u.first_item += (uint32_t)unit_base;
+        const size_t total = unit_base + unit_items.size();
+        if ((st = c->items_host.reserve(total + 1 + total / 2))) return st;  // headroom: no re-pinning per run
+        if (c->queues.count == 0)
+            if ((st = c->queues.alloc(1))) return st;
+        if ((st = cuda_status(cudaMemsetAsync(c->queues.ptr, 0, sizeof(Queues), c->stream), "queue reset"))) return st;
         if (c->items_dev.count < total + 1)
             if ((st = c->items_dev.alloc(total + 1 + total / 4))) return st;
         WorkItem* h = c->items_host.ptr;
         size_t at = 0;
-        for (auto* list : {&fine_items, &carrier_items, &det_items, &audio_items}) {
+        for (auto* list : {&fine_items, &carrier_items, &det_items, &audio_items, &unit_items}) {
             if (!list->empty()) memcpy(h + at, list->data(), list->size() * sizeof(WorkItem));
             at += list->size();
         }
@@ -609,28 +722,44 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
                                               c->stream),
                               "work list upload")))
             return st;
+        if (!units.empty()) {
+            if ((st = c->units_host.reserve(units.size() + units.size() / 2 + 1))) return st;
+            if (c->units_dev.count < units.size())
+                if ((st = c->units_dev.alloc(units.size() + units.size() / 2 + 1))) return st;
+            memcpy(c->units_host.ptr, units.data(), units.size() * sizeof(FineUnit));
+            if ((st = cuda_status(cudaMemcpyAsync(c->units_dev.ptr, c->units_host.ptr, units.size() * sizeof(FineUnit),
+                                                  cudaMemcpyHostToDevice, c->stream),
+                                  "unit upload")))
+                return st;
+        }
         const WorkItem* d = c->items_dev.ptr;
         const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
-        if ((st = launch_fine_batched(c->stream, c->rx_table.ptr, d, (uint32_t)fine_items.size(), chan, kFineWindow)))
+        if ((st = launch_fine_units(c->stream, c->rx_table.ptr, c->items_dev.ptr, c->units_dev.ptr,
+                                    (uint32_t)units.size(), chan, c->unit_budget, &c->queues.ptr->pad)))
+            return st;
+        const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
+        if ((st = launch_fine_batched(c->stream, c->rx_table.ptr, d, (uint32_t)fine_items.size(), chan, window,
+                                      &c->queues.ptr->fine)))
             return st;
         d += fine_items.size();
         if ((st = launch_carrier_batched(c->stream, c->rx_table.ptr, d, (uint32_t)carrier_items.size()))) return st;
         d += carrier_items.size();
         mark(c, 3);
-        if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, d, (uint32_t)det_items.size(), kDetWindow)))
+        if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, d, (uint32_t)det_items.size(), kDetWindow,
+                                        &c->queues.ptr->detect)))
             return st;
         d += det_items.size();
         if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, d, (uint32_t)audio_items.size(), c->audio_dev.ptr,
-                                       kDetWindow)))
+                                       kDetWindow, c->weights_cap, &c->queues.ptr->audio)))
             return st;
         mark(c, 4);
-        c->stats.launches += 3 + (carrier_items.empty() ? 0 : 1);
+        c->stats.launches += 2 + (fine_items.empty() ? 0 : 1) + (units.empty() ? 0 : 1) + (carrier_items.empty() ? 0 : 1);
         c->stats.work_items += total;
     }
 
     // ---- audio back to the host (the reference's readback copies)
     if (audio_floats > 0) {
-        if ((st = c->audio_host.reserve(audio_floats))) return st;
+        if ((st = c->audio_host.reserve(audio_floats + audio_floats / 4))) return st;
         if ((st = cuda_status(cudaMemcpyAsync(c->audio_host.ptr, c->audio_dev.ptr, audio_floats * sizeof(float),
                                               cudaMemcpyDeviceToHost, c->stream),
                               "audio readback")))

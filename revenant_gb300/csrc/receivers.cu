@@ -47,42 +47,39 @@ __global__ void k_lerp_table(const rv_cf32* __restrict__ taps, float2* __restric
         const uint32_t slot = phase + k * P;
         const float2 g0 = ld_cf32(&taps[slot]);
         const float2 g1 = ld_cf32(&taps[slot + 1u]);
-        out[(uint64_t)pp * T + k] = make_float2(g0.x * blend_c + g1.x * blend, g0.y * blend_c + g1.y * blend);
+        // tap-major: the 32 lanes of a warp hold 32 consecutive outputs, i.e.
+        // consecutive pattern phases, so tap k of all of them is contiguous
+        out[(uint64_t)k * period + pp] = make_float2(g0.x * blend_c + g1.x * blend, g0.y * blend_c + g1.y * blend);
     }
 }
 
 // ---- fine stage ---------------------------------------------------------
 
+// Next item index from the launch's queue (one atomic per CTA per item).
+__device__ __forceinline__ uint32_t next_item(uint32_t* queue, uint32_t* slot) {
+    __syncthreads();
+    if (threadIdx.x == 0) *slot = atomicAdd(queue, 1u);
+    __syncthreads();
+    return *slot;
+}
+
 __global__ void __launch_bounds__(kRxThreads)
 k_fine_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-               const float2* __restrict__ chan, uint32_t window_cap) {
+               const float2* __restrict__ chan, uint32_t window_cap, uint32_t* queue) {
     extern __shared__ float2 xs[];
+    __shared__ uint32_t s_it;
     __shared__ RxDev rx;
-    __shared__ uint64_t s_n0;
-    __shared__ uint32_t s_frac0, s_len, s_p0;
-    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
         const WorkItem item = items[it];
-        if (threadIdx.x == 0) {
-            rx = rxs[item.rx];
-            // exact input index of the first output (resample_block,
-            // core/dsp/vrx_reference.cpp:2786-2810), split to stay in 64 bits
-            const uint64_t fd = rx.out_rate, j0 = item.first;
-            const uint64_t whole = j0 / fd, part = j0 % fd;
-            const uint64_t cp = part * rx.step_rem;
-            s_n0 = j0 * rx.step_whole + whole * rx.step_rem + cp / fd;
-            s_frac0 = (uint32_t)(cp % fd);
-            const uint64_t last_acc = (uint64_t)s_frac0 + (uint64_t)(item.count - 1u) * rx.step_rem;
-            const uint64_t n_last = s_n0 + (uint64_t)(item.count - 1u) * rx.step_whole + last_acc / fd;
-            s_len = (uint32_t)(n_last - s_n0) + rx.taps;
-            s_p0 = (uint32_t)(j0 % rx.period);
-        }
+        if (threadIdx.x == 0) rx = rxs[item.rx];
         __syncthreads();
         const uint32_t T = rx.taps;
-        const uint64_t base = s_n0 - (T - 1u);
-        const uint32_t len = s_len < window_cap ? s_len : window_cap;
+        const uint64_t base = item.n0 - (T - 1u);
+        const uint32_t len = item.window < window_cap ? item.window : window_cap;
         for (uint32_t e = threadIdx.x; e < len; e += blockDim.x)
             xs[e] = chan[(uint64_t)rx.chan_base + (uint32_t)((base + e) & rx.chan_mask)];
         __syncthreads();
+        const uint32_t s_frac0 = item.frac0, s_p0 = item.p0;
         const uint32_t i = threadIdx.x;
         const uint32_t fd = rx.out_rate;
         const uint32_t acc = s_frac0 + i * rx.step_rem;
@@ -95,10 +92,12 @@ k_fine_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items
             float ar = 0.0F, ai = 0.0F;
             if (rx.lerped != nullptr) {
                 const uint32_t pp = (s_p0 + i) % rx.period;
-                const float2* __restrict__ tp = rx.lerped + (uint64_t)pp * T;
+                const uint32_t stride = rx.period;
+                const float2* __restrict__ tp = rx.lerped + pp;
+#pragma unroll 4
                 for (uint32_t k = 0; k < T; ++k) {
                     const float2 s = w[-(int)k];
-                    const float2 t = tp[k];
+                    const float2 t = __ldg(&tp[(uint64_t)k * stride]);
                     ar = ar + (s.x * t.x - s.y * t.y);
                     ai = ai + (s.x * t.y + s.y * t.x);
                 }
@@ -131,6 +130,79 @@ k_fine_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items
     }
 }
 
+// ---- fine stage, tap table resident in shared memory ----------------------
+//
+// One CTA per unit: the receiver's blended taps ([T][period], tap-major) are
+// copied into shared memory once, then each item of the unit stages its input
+// window after the table and every thread computes one fine output with both
+// operands in shared memory (consecutive lanes read consecutive pattern phases
+// of one tap row: no bank conflicts on the taps).
+
+__global__ void __launch_bounds__(kUnitThreads)
+k_fine_units(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, const FineUnit* __restrict__ units,
+             uint32_t nunits, const float2* __restrict__ chan, uint32_t shared_float2s, uint32_t* queue) {
+    extern __shared__ float2 sm[];
+    __shared__ uint32_t s_it;
+    __shared__ RxDev rx;
+    for (uint32_t u = next_item(queue, &s_it); u < nunits; u = next_item(queue, &s_it)) {
+        const FineUnit unit = units[u];
+        if (threadIdx.x == 0) rx = rxs[unit.rx];
+        __syncthreads();
+        const uint32_t T = rx.taps, period = rx.period;
+        const uint32_t rows = unit.rows < T ? unit.rows : T;
+        const bool resident = rows == T;
+        const uint32_t chunk = rows * period;  // float2 of table in shared memory
+        if (resident)
+            for (uint32_t e = threadIdx.x; e < chunk; e += blockDim.x) sm[e] = __ldg(&rx.lerped[e]);
+        float2* xs = sm + chunk;
+        const uint32_t cap = shared_float2s - chunk;
+        for (uint32_t k = 0; k < unit.items; ++k) {
+            const WorkItem item = items[unit.first_item + k];
+            const uint64_t base = item.n0 - (T - 1u);
+            const uint32_t len = item.window < cap ? item.window : cap;
+            __syncthreads();  // the previous item's readers are done with xs
+            for (uint32_t e = threadIdx.x; e < len; e += blockDim.x)
+                xs[e] = chan[(uint64_t)rx.chan_base + (uint32_t)((base + e) & rx.chan_mask)];
+            const uint32_t i = threadIdx.x;
+            const uint32_t fd = rx.out_rate;
+            const uint32_t acc = item.frac0 + i * rx.step_rem;
+            const uint32_t carry = acc / fd;
+            const uint32_t n_rel = i * rx.step_whole + carry;
+            const bool active = i < item.count && n_rel + T - 1u < len;
+            const float2* w = xs + n_rel + T - 1u;  // w[-q] = x[n(j) - q]
+            const uint32_t pp = active ? (item.p0 + i) % period : 0u;
+            float ar = 0.0F, ai = 0.0F;
+            for (uint32_t q0 = 0; q0 < T; q0 += rows) {
+                const uint32_t q1 = (q0 + rows < T) ? q0 + rows : T;
+                if (!resident) {
+                    __syncthreads();  // everyone is done with the previous chunk
+                    const float2* src = rx.lerped + (uint64_t)q0 * period;
+                    const uint32_t n = (q1 - q0) * period;
+                    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) sm[e] = __ldg(&src[e]);
+                }
+                __syncthreads();  // window (and chunk) staged
+                if (active) {
+                    const float2* tp = sm + pp;
+#pragma unroll 4
+                    for (uint32_t q = q0; q < q1; ++q) {
+                        const float2 sv = w[-(int)q];
+                        const float2 t = tp[(q - q0) * period];
+                        ar = ar + (sv.x * t.x - sv.y * t.y);
+                        ai = ai + (sv.x * t.y + sv.y * t.x);
+                    }
+                }
+            }
+            if (active) {
+                const uint64_t j = item.first + i;
+                const uint64_t phi = rx.nco_delta * j;
+                const uint32_t idx = (rx.nco_log2 == 0) ? 0u : ((uint32_t)(phi >> 32) >> (32u - rx.nco_log2));
+                const float2 rot = rx.nco[idx];
+                rx.fine[(uint32_t)j & rx.fine_mask] = make_float2(ar * rot.x - ai * rot.y, ar * rot.y + ai * rot.x);
+            }
+        }
+    }
+}
+
 // ---- carrier loop (SAM / DSB): serial per receiver ----------------------
 
 __global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems) {
@@ -152,10 +224,11 @@ __global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem*
 
 __global__ void __launch_bounds__(kRxThreads)
 k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-                 uint32_t window_cap) {
-    extern __shared__ float sd[];
+                 uint32_t window_cap, uint32_t* queue) {
+    extern __shared__ __align__(16) float sd[];
+    __shared__ uint32_t s_it;
     __shared__ RxDev rx;
-    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
         const WorkItem item = items[it];
         if (threadIdx.x == 0) rx = rxs[item.rx];
         __syncthreads();
@@ -163,25 +236,64 @@ k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ ite
         const uint32_t i = threadIdx.x;
         const uint32_t first = (uint32_t)item.first;  // ring arithmetic is modulo the mask
         if (mode == RV_DEMOD_AM || mode == RV_DEMOD_SAM) {
-            // window of detector inputs: |z| (AM) or Re z (SAM) for
-            // fine samples [first - dc + 1, first + count)
+            // DC removal FIR over |z| (AM) or Re z (SAM), four consecutive
+            // outputs per thread: each staged input and each weight is read
+            // once per four multiply-adds; every output still sums its terms
+            // in ascending weight order, one rounded multiply and one rounded
+            // add each, as the reference's detect() does.
             const uint32_t dc = rx.dc_taps;
-            const uint32_t len = item.count + dc - 1u;
+            float* dws = sd + window_cap;  // weights, after the window (16-byte aligned)
+            // Stage the inputs at an offset o in [4, 8) chosen so that the
+            // window base v of every thread is 16-byte aligned and the last
+            // group's look-ahead read stays inside the allocation.
+            const uint32_t o = 4u + ((4u - ((dc - 1u) & 3u)) & 3u);
+            const uint32_t len = item.count + dc - 1u + 3u;  // +3: the last thread's tail
             const uint32_t start = first - (dc - 1u);
-            for (uint32_t e = threadIdx.x; e < len && e < window_cap; e += blockDim.x) {
+            for (uint32_t e = threadIdx.x; e < len && o + e < window_cap; e += blockDim.x) {
                 const float2 z = rx.fine[(start + e) & rx.fine_mask];
-                sd[e] = (mode == RV_DEMOD_AM) ? det_sqrt(z.x * z.x + z.y * z.y) : z.x;
+                sd[o + e] = (mode == RV_DEMOD_AM) ? det_sqrt(z.x * z.x + z.y * z.y) : z.x;
             }
+            for (uint32_t e = threadIdx.x; e < dc; e += blockDim.x) dws[e] = rx.weights[rx.audio_taps + e];
             __syncthreads();
-            if (i < item.count && i + dc - 1u < (len < window_cap ? len : window_cap)) {
-                const float* v = sd + i + dc - 1u;  // v[-w] = input at fine (first + i - w)
-                const float* __restrict__ dw = rx.weights + rx.audio_taps;
-                float acc = 0.0F;
-                for (uint32_t w = 0; w < dc; ++w) {
-                    const float term = v[-(int)w] * dw[w];
-                    acc = acc + term;
+            const uint32_t i0 = 4u * i;
+            if (i0 < item.count && o + i0 + 3u + dc - 1u < (o + len < window_cap ? o + len : window_cap)) {
+                const float* v = sd + o + i0 + dc - 1u;  // v[r - w] = input at fine (first + i0 + r - w)
+                // x_r holds v[r - w] at the top of each group of four steps:
+                //   step w  : a_r += v[r-w]   * wt[w]    -> x0 x1 x2 x3
+                //   step w+1: a_r += v[r-w-1] * wt[w+1]  -> y  x0 x1 x2
+                //   step w+2: a_r += v[r-w-2] * wt[w+2]  -> z  y  x0 x1
+                //   step w+3: a_r += v[r-w-3] * wt[w+3]  -> u  z  y  x0
+                // with (n, u, z, y) = v[-w-4 .. -w-1], one aligned 16-byte load,
+                // and the next group's x0..x3 = n, u, z, y.
+                float a0 = 0.0F, a1 = 0.0F, a2 = 0.0F, a3 = 0.0F;
+                const float4 first4 = *reinterpret_cast<const float4*>(v);
+                float x0 = first4.x, x1 = first4.y, x2 = first4.z, x3 = first4.w;
+                uint32_t w = 0;
+                for (; w + 4u <= dc; w += 4u) {
+                    const float4 nz = *reinterpret_cast<const float4*>(v - (int)w - 4);
+                    const float4 wt = *reinterpret_cast<const float4*>(dws + w);
+                    const float y = nz.w, z = nz.z, u = nz.y;
+                    a0 = a0 + x0 * wt.x; a1 = a1 + x1 * wt.x; a2 = a2 + x2 * wt.x; a3 = a3 + x3 * wt.x;
+                    a0 = a0 + y * wt.y; a1 = a1 + x0 * wt.y; a2 = a2 + x1 * wt.y; a3 = a3 + x2 * wt.y;
+                    a0 = a0 + z * wt.z; a1 = a1 + y * wt.z; a2 = a2 + x0 * wt.z; a3 = a3 + x1 * wt.z;
+                    a0 = a0 + u * wt.w; a1 = a1 + z * wt.w; a2 = a2 + y * wt.w; a3 = a3 + x0 * wt.w;
+                    x3 = y;
+                    x2 = z;
+                    x1 = u;
+                    x0 = nz.x;
                 }
-                rx.det[(first + i) & rx.fine_mask] = v[0] - acc;
+                for (; w < dc; ++w) {
+                    const float wt = dws[w];
+                    a0 = a0 + x0 * wt; a1 = a1 + x1 * wt; a2 = a2 + x2 * wt; a3 = a3 + x3 * wt;
+                    x3 = x2;
+                    x2 = x1;
+                    x1 = x0;
+                    x0 = v[-(int)w - 1];
+                }
+                const float acc[4] = {a0, a1, a2, a3};
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (i0 + (uint32_t)r < item.count) rx.det[(first + i0 + (uint32_t)r) & rx.fine_mask] = v[r] - acc[r];
             }
         } else if (i < item.count) {
             const uint32_t f = first + i;
@@ -205,10 +317,11 @@ k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ ite
 
 __global__ void __launch_bounds__(kRxThreads)
 k_audio_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-                float* __restrict__ audio, uint32_t window_cap) {
+                float* __restrict__ audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue) {
     extern __shared__ float sd[];
+    __shared__ uint32_t s_it;
     __shared__ RxDev rx;
-    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
         const WorkItem item = items[it];
         if (threadIdx.x == 0) rx = rxs[item.rx];
         __syncthreads();
@@ -225,15 +338,19 @@ k_audio_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ item
             __syncthreads();
             continue;
         }
-        // detector window [first_index - reach, last index]
+        // detector window [first_index - reach, last index], then the weights
         const uint32_t len = (item.count - 1u) * dec + rx.reach + 1u;
         const uint32_t start = first_index - rx.reach;
         for (uint32_t e = threadIdx.x; e < len && e < window_cap; e += blockDim.x)
             sd[e] = rx.det[(start + e) & rx.fine_mask];
+        float* ws = sd + window_cap;
+        const uint32_t nw = rx.channels == 2u ? rx.audio_taps + rx.dc_taps + 2u * rx.pilot_taps + 2u * rx.audio_taps
+                                              : rx.audio_taps;
+        for (uint32_t e = threadIdx.x; e < nw && e < weights_cap; e += blockDim.x) ws[e] = rx.weights[e];
         __syncthreads();
         if (i < item.count && rx.reach + i * dec < (len < window_cap ? len : window_cap)) {
             const float* v = sd + rx.reach + i * dec;  // v[-t] = detector at (index - t)
-            const float* __restrict__ w = rx.weights;
+            const float* w = ws;
             if (rx.channels == 2u) {
                 const uint32_t pilot_base = rx.audio_taps + rx.dc_taps;
                 const uint32_t rotation_base = pilot_base + 2u * rx.pilot_taps;
@@ -312,13 +429,35 @@ int32_t launch_lerp_table(cudaStream_t s, const rv_cf32* taps, float2* lerped, u
 }
 
 int32_t launch_fine_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                            const float2* chan, uint32_t window_cap) {
+                            const float2* chan, uint32_t window_cap, uint32_t* queue) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)window_cap * sizeof(float2);
     if (int32_t st = set_shared((const void*)k_fine_batched, shared)) return st;
     const unsigned grid = persistent_grid((const void*)k_fine_batched, kRxThreads, shared, nitems);
-    k_fine_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, chan, window_cap);
+    k_fine_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, chan, window_cap, queue);
     return cuda_status(cudaGetLastError(), "fine batched");
+}
+
+uint32_t fine_unit_shared_budget() {
+    static uint32_t budget = 0;
+    if (budget == 0) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        // leave room for the kernel's static shared memory
+        budget = (uint32_t)((optin > 2048 ? optin - 2048 : optin) / sizeof(float2));
+    }
+    return budget;
+}
+
+int32_t launch_fine_units(cudaStream_t s, const RxDev* rxs, const WorkItem* items, const FineUnit* units,
+                          uint32_t nunits, const float2* chan, uint32_t shared_float2s, uint32_t* queue) {
+    if (nunits == 0) return RV_OK;
+    const size_t shared = (size_t)shared_float2s * sizeof(float2);
+    if (int32_t st = set_shared((const void*)k_fine_units, shared)) return st;
+    const unsigned grid = persistent_grid((const void*)k_fine_units, kUnitThreads, shared, nunits);
+    k_fine_units<<<grid, kUnitThreads, shared, s>>>(rxs, items, units, nunits, chan, shared_float2s, queue);
+    return cuda_status(cudaGetLastError(), "fine units");
 }
 
 int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems) {
@@ -328,22 +467,22 @@ int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem*
 }
 
 int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                              uint32_t window_cap) {
+                              uint32_t window_cap, uint32_t* queue) {
     if (nitems == 0) return RV_OK;
-    const size_t shared = (size_t)window_cap * sizeof(float);
+    const size_t shared = (size_t)(window_cap + 4096u) * sizeof(float);  // window + DC weights
     if (int32_t st = set_shared((const void*)k_detect_batched, shared)) return st;
     const unsigned grid = persistent_grid((const void*)k_detect_batched, kRxThreads, shared, nitems);
-    k_detect_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap);
+    k_detect_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap, queue);
     return cuda_status(cudaGetLastError(), "detect batched");
 }
 
 int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems, float* audio,
-                             uint32_t window_cap) {
+                             uint32_t window_cap, uint32_t weights_cap, uint32_t* queue) {
     if (nitems == 0) return RV_OK;
-    const size_t shared = (size_t)window_cap * sizeof(float);
+    const size_t shared = (size_t)(window_cap + weights_cap) * sizeof(float);  // window, then the weights
     if (int32_t st = set_shared((const void*)k_audio_batched, shared)) return st;
     const unsigned grid = persistent_grid((const void*)k_audio_batched, kRxThreads, shared, nitems);
-    k_audio_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap);
+    k_audio_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap, weights_cap, queue);
     return cuda_status(cudaGetLastError(), "audio batched");
 }
 

@@ -43,12 +43,41 @@ struct RxDev {
 
 // A contiguous run of outputs of one receiver: fine outputs (fine stage),
 // fine samples (detector stage) or audio frames (audio stage). `out` is where
-// audio frames go in the run's audio buffer (in floats).
+// audio frames go in the run's audio buffer (in floats), or the carrier's
+// reset flag. Fine items carry the exact input index of their first output,
+// its resampler fraction and pattern phase, computed on the host in 64 bits
+// (resample_block, core/dsp/vrx_reference.cpp:2786-2810), and the length of
+// the input window they stage.
 struct WorkItem {
     uint32_t rx;
     uint32_t count;
     uint64_t first;
     uint64_t out;
+    uint64_t n0;      // fine: input index of output `first`
+    uint32_t frac0;   // fine: (first * (Fc mod Fd)) mod Fd
+    uint32_t p0;      // fine: first mod period
+    uint32_t window;  // fine: input samples staged (last input - n0 + T)
+    uint32_t pad;
+};
+
+// A run of consecutive fine items of one receiver, processed by one CTA with
+// the receiver's blended tap table in shared memory: `rows` tap rows
+// ([rows][period] float2) at a time. rows == T keeps the whole table resident
+// for the unit; rows < T passes the table through in row chunks for every
+// item, each thread carrying its output's accumulator across chunks, so the
+// per-output summation order (ascending tap) is unchanged.
+struct FineUnit {
+    uint32_t rx;
+    uint32_t first_item;
+    uint32_t items;
+    uint32_t rows;
+};
+
+// Per-launch queue heads: items are handed out in list order, so the CTAs on
+// an SM at any moment work on the same receiver (its tables stay in L1), and
+// a slow item never holds up a fixed share of the list.
+struct Queues {
+    uint32_t fine, detect, audio, pad;
 };
 
 constexpr int kRxThreads = 256;
@@ -56,11 +85,19 @@ constexpr int kRxThreads = 256;
 int32_t launch_lerp_table(cudaStream_t s, const rv_cf32* taps, float2* lerped, uint32_t T, uint32_t P,
                           uint32_t period, uint32_t step_rem, uint32_t fd, float inv_fd);
 int32_t launch_fine_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                            const float2* chan, uint32_t window_cap);
+                            const float2* chan, uint32_t window_cap, uint32_t* queue);
+// Units of fine items with shared-memory tap tables; `shared_floats2` is the
+// dynamic shared memory per CTA (largest table + window), 1024 threads a CTA.
+constexpr int kUnitThreads = 1024;
+int32_t launch_fine_units(cudaStream_t s, const RxDev* rxs, const WorkItem* items, const FineUnit* units,
+                          uint32_t nunits, const float2* chan, uint32_t shared_float2s, uint32_t* queue);
+uint32_t fine_unit_shared_budget();  // float2 entries of dynamic shared memory a CTA may use
 int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems);
 int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                              uint32_t window_cap);
+                              uint32_t window_cap, uint32_t* queue);
+// weights_cap: floats of demodulator weights staged per CTA (the largest
+// table among the receivers: audio taps, or the whole stereo table)
 int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                             float* audio, uint32_t window_cap);
+                             float* audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue);
 
 }  // namespace rv
