@@ -377,6 +377,25 @@ int32_t rv_vrx_carrier(void* stream, const rv_vrx_carrier_config* config,
                        uint64_t nco_len, rv_cf32* fine_ring_dev, uint64_t fine_ring_len,
                        uint32_t* state_dev);
 
+/* Branch filter then FFT (rv_pfb_branch + rv_pfb_fft, same outputs bit for
+ * bit) with the branch values between them kept in a fixed array inside the
+ * library, for callers that may not allocate device memory on their path:
+ * per-block processing callbacks, where cudaMalloc can stall the device while
+ * samples keep arriving, and plugins or hosts that work inside a device-memory
+ * budget they do not own. No counterpart in the reference. The array holds
+ * RV_NOALLOC_BRANCH_VALUES complex values (block_count * M at most), stays
+ * allocated on every GPU that loads the library, and is shared by all calls on
+ * a device: calls whose work overlaps on the GPU race on it. The first call on
+ * a device looks the array's address up (cudaGetSymbolAddress) and should come
+ * before any stream capture. Calls no cudaMalloc / cudaFree. */
+#define RV_NOALLOC_BRANCH_VALUES (1u << 20)
+int32_t rv_pfb_channelize_noalloc(void* stream, const rv_grid_params* grid,
+                                  const rv_pfb_branch_params* branch_params,
+                                  const rv_pfb_fft_params* fft_params, const float* taps_dev,
+                                  uint64_t taps_len, const rv_cf32* ring_dev, uint64_t ring_len,
+                                  const rv_cf32* twiddles_dev, uint64_t twiddles_len,
+                                  rv_cf32* channel_ring_dev, uint64_t channel_ring_len);
+
 /* ===================================================================== *
  * Fused kernels (same outputs as the plain chain, bit for bit)           *
  * ===================================================================== */

@@ -144,6 +144,8 @@ SIGNATURES = {
     "rv_vrx_fine": (I32, [P, ptr(abi.VrxFineConfig), ptr(abi.VrxFineParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_vrx_demod": (I32, [P, ptr(abi.VrxDemodConfig), ptr(abi.VrxDemodParams), P, U64, P, U64, P, U64]),
     "rv_vrx_carrier": (I32, [P, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P]),
+    "rv_pfb_channelize_noalloc": (I32, [P, ptr(abi.GridParams), ptr(abi.PfbBranchParams), ptr(abi.PfbFftParams),
+                                        P, U64, P, U64, P, U64, P, U64]),
     "rv_coarse_fused": (I32, [P, ptr(abi.GridParams), I32, ptr(abi.CoarseParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_chain_create": (I32, [P, ptr(abi.ChainConfig), ptr(P)]),
     "rv_chain_destroy": (I32, [P]),
