@@ -38,7 +38,7 @@ GRID = (64, 17, 32)
 LOG2N = 27
 RECEIVERS = 256
 SEED = 3
-RUN_SAMPLES = 1 << 24
+RUN_SAMPLES = 1 << 24  # default samples per rv_chain_run (--run-log2)
 METRIC = "input MS/s through channelizer+N VRX on 1 GB300, % HBM roofline, vs plain path"
 
 
@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--receivers", type=int, default=RECEIVERS)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--run-log2", type=int, default=24, help="log2 samples per rv_chain_run")
     return ap.parse_args()
 
 
@@ -195,14 +196,16 @@ def run_gb300(args):
     d_codes = dev.array(codes)
     pinned = dev.buffer(codes.nbytes, abi.MEMORY_UPLOAD)
     pinned.upload(codes)
-    chain = make_chain(abi.CHAIN_BATCHED, RUN_SAMPLES)
+    chain = make_chain(abi.CHAIN_BATCHED, min(1 << args.run_log2, n))
     plans = [chain.info(i)[0] for i in range(len(reqs))]
     stream = torch.cuda.ExternalStream(dev.stream)
+
+    run_samples = min(1 << args.run_log2, n)
 
     def step(ch, source):
         at = 0
         while at < n:
-            m = min(RUN_SAMPLES, n - at)
+            m = min(run_samples, n - at)
             if source == "device":
                 ch.run(_Offset(d_codes, at * 4), m)
             else:
@@ -276,7 +279,7 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "batched uneven receivers: 2^%d cs16 samples at 20 MS/s, M=64 D=32 T=17, %d receivers "
                                "NFM/AM/USB/LSB/WFM 12.5-200 kHz (seed %d)" % (args.log2n, args.receivers, SEED),
-                   "grid": list(GRID), "rate": RATE, "receivers": args.receivers, "run_samples": RUN_SAMPLES,
+                   "grid": list(GRID), "rate": RATE, "receivers": args.receivers, "run_samples": min(1 << args.run_log2, n),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (512 MiB capture per step)"},
         "e2e": {"value": round(e2e, 2), "unit": "MS/s", "h2d_bytes_per_step": samples_step * 4,
