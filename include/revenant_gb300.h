@@ -352,6 +352,38 @@ int32_t rv_spectrum(void* stream, const rv_spectrum_params* params,
                     const rv_cf32* twiddles_dev, uint64_t twiddles_len, const float* window_dev,
                     uint64_t window_len, float* frame_dev, uint64_t frame_len);
 
+/* Averaged power spectrum, lw-radio-dsp's Spectrum::compute
+ * (third_party/lw-radio-dsp/src/spectrum.cpp:32-44, src/fft.cpp:31-50): frames
+ * of `size` samples, window, FFT, |X|^2 * norm (norm = 1/(sum w)^2), fftshift,
+ * averaged, 10 log10(max(p, 1e-30)) dB. MEAN: one output spectrum per
+ * `average` consecutive frames; EXPONENTIAL: avg = alpha*avg + (1-alpha)*p
+ * over all frames, one output. avg_dev (optional, N floats per output)
+ * receives the linear average; with `resume` it also seeds the exponential
+ * average, as lwdsp keeps it between calls. Tolerance-level agreement with an
+ * FP64 restatement (the reference transforms with pocketfft). */
+#define RV_AVERAGE_MEAN 0
+#define RV_AVERAGE_EXPONENTIAL 1
+#define RV_WINDOW_RECTANGULAR 0
+#define RV_WINDOW_HANN 1
+#define RV_WINDOW_BLACKMAN_HARRIS 2
+typedef struct rv_spectrum_average_params {
+    uint32_t size;    /* N, a power of two in [16, 8192] */
+    uint32_t frames;  /* consecutive N-sample frames in the input */
+    uint32_t average; /* frames per output spectrum (MEAN) */
+    uint32_t mode;    /* RV_AVERAGE_* */
+    float alpha;      /* exponential weight (EXPONENTIAL), lwdsp's `averaging` */
+    float norm;       /* 1 / (sum of the window)^2 */
+    uint32_t resume;  /* EXPONENTIAL: 1 = continue from the average in avg_dev */
+    uint32_t reserved;
+} rv_spectrum_average_params;
+int32_t rv_spectrum_average(void* stream, const rv_spectrum_average_params* params,
+                            const rv_cf32* iq_dev, uint64_t iq_len, const float* window_dev,
+                            uint64_t window_len, const rv_cf32* twiddles_dev, uint64_t twiddles_len,
+                            float* out_dev, uint64_t out_len, float* avg_dev, uint64_t avg_len);
+/* make_window (third_party/lw-radio-dsp/src/primitives.cpp:124): n floats of
+ * the symmetric window; *norm = 1 / (sum of the floats, in double)^2. */
+int32_t rv_build_lwdsp_window(uint32_t kind, uint32_t n, float* window, double* norm);
+
 /* core/shaders/spectrum_levels.comp; twin
  * core/dsp/spectrum_levels_reference.cpp:75. levels_dev receives 2 floats. */
 int32_t rv_spectrum_levels(void* stream, const rv_spectrum_levels_params* params,

@@ -25,6 +25,8 @@
 #include "core/dsp/vrx_reference.h"
 #include "core/engine/vrx.h"
 #include "include/revenant_gb300.h"
+#include "lwdsp/primitives.h"
+#include "lwdsp/spectrum.h"
 
 namespace dsp = revenant::dsp;
 namespace engine = revenant::engine;
@@ -364,6 +366,29 @@ int32_t ref_demod_block(const rv_grid_params* g, int64_t rate, const rv_vrx_requ
     std::memcpy(&out->params, &block->params, sizeof(out->params));
     out->first_fine = block->first_fine;
     out->oldest_fine = block->oldest_fine;
+    return 0;
+}
+
+// lw-radio-dsp make_window (src/primitives.cpp:124); kind is lwdsp::Window's
+// value (0 rectangular, 1 Hann, 2 Blackman-Harris).
+int32_t ref_lwdsp_window(uint32_t kind, uint32_t n, float* out) {
+    const auto w = lwdsp::make_window(static_cast<lwdsp::Window>(kind), static_cast<int>(n));
+    std::memcpy(out, w.data(), w.size() * sizeof(float));
+    return 0;
+}
+
+// lw-radio-dsp Spectrum::compute (src/spectrum.cpp:32-44) called once per
+// frame of `size` samples on one Spectrum object, so the exponential average
+// carries across frames as it does across the reference's calls; every call's
+// dB row is written to db_out[frame * size ...].
+int32_t ref_lwdsp_spectrum(uint32_t size, uint32_t kind, float averaging, const rv_cf32* iq,
+                           uint64_t frames, float* db_out) {
+    lwdsp::Spectrum spec({.size = static_cast<int>(size), .window = static_cast<lwdsp::Window>(kind),
+                          .averaging = averaging});
+    const auto* z = reinterpret_cast<const std::complex<float>*>(iq);
+    for (uint64_t f = 0; f < frames; ++f)
+        spec.compute(std::span<const std::complex<float>>(z + f * size, size),
+                     std::span<float>(db_out + f * size, size));
     return 0;
 }
 

@@ -103,6 +103,15 @@ class CoarseParams(_S):
                 ("out_ring_blocks", U32), ("out_ring_mask", U32), ("lead_zero", U32)]
 
 
+class SpectrumAverageParams(_S):
+    _fields_ = [("size", U32), ("frames", U32), ("average", U32), ("mode", U32), ("alpha", F32), ("norm", F32),
+                ("resume", U32), ("reserved", U32)]
+
+
+AVERAGE_MEAN, AVERAGE_EXPONENTIAL = 0, 1
+WINDOW_RECTANGULAR, WINDOW_HANN, WINDOW_BLACKMAN_HARRIS = 0, 1, 2
+
+
 class VrxRequest(_S):
     _fields_ = [("center", I64), ("bandwidth", I64), ("passband_low", I64), ("passband_high", I64),
                 ("demod", U32), ("deemphasis", U32), ("stereo", U32), ("reserved", U32),
@@ -159,7 +168,7 @@ class ChainStats(_S):
                 ("demod_ms", C.c_double), ("readback_ms", C.c_double)]
 
 
-EXTRA_STRUCTS = {"rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
+EXTRA_STRUCTS = {"rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
 
 
 def request(center=0, bandwidth=0, demod="nfm", deemphasis=0, stereo=True, audio_rate=0,

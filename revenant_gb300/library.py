@@ -141,6 +141,8 @@ SIGNATURES = {
     "rv_pfb_fft": (I32, [P, ptr(abi.PfbFftParams), P, U64, P, U64, P, U64]),
     "rv_spectrum": (I32, [P, ptr(abi.SpectrumParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_spectrum_levels": (I32, [P, ptr(abi.SpectrumLevelsParams), P, U64, P]),
+    "rv_spectrum_average": (I32, [P, ptr(abi.SpectrumAverageParams), P, U64, P, U64, P, U64, P, U64, P, U64]),
+    "rv_build_lwdsp_window": (I32, [U32, U32, P, ptr(F64)]),
     "rv_vrx_fine": (I32, [P, ptr(abi.VrxFineConfig), ptr(abi.VrxFineParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_vrx_demod": (I32, [P, ptr(abi.VrxDemodConfig), ptr(abi.VrxDemodParams), P, U64, P, U64, P, U64]),
     "rv_vrx_carrier": (I32, [P, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P]),

@@ -100,6 +100,10 @@ def reference():
         lib.ref_demod_block.restype = I32
         lib.ref_demod_block.argtypes = [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), U32, U64, U32,
                                         ptr(abi.VrxDemodBlock)]
+        lib.ref_lwdsp_window.restype = I32
+        lib.ref_lwdsp_window.argtypes = [U32, U32, P]
+        lib.ref_lwdsp_spectrum.restype = I32
+        lib.ref_lwdsp_spectrum.argtypes = [U32, U32, F32, P, U64, P]
         _reference = Lib(lib, "ref_")
     return _reference
 
