@@ -499,6 +499,9 @@ typedef struct rv_chain_stats {
     double fine_ms;       /* fine stage (+ carrier) */
     double demod_ms;      /* detector + audio */
     double readback_ms;   /* audio to the host */
+    uint64_t graph_launches; /* runs replayed from the captured graph */
+    uint64_t graph_captures; /* times the graph was (re)captured */
+    double graph_ms;      /* captured runs: work-list upload + the whole graph */
 } rv_chain_stats;
 
 /* Allocates the chain's rings (the only allocating calls of the chain API
@@ -518,6 +521,18 @@ int32_t rv_chain_receiver_info(const rv_chain* chain, uint32_t id, rv_vrx_plan_i
 int32_t rv_chain_read_audio(rv_chain* chain, uint32_t id, float* dst, uint64_t capacity,
                             uint64_t* written);
 int32_t rv_chain_get_stats(const rv_chain* chain, rv_chain_stats* stats);
+/* Batched chains only (RV_ERR_UNSUPPORTED for a plain one). From the next run
+ * on, the coarse kernel and every batched receiver kernel run from one
+ * captured CUDA graph: each run uploads its work lists and a small count
+ * header (the kernels read their item counts and the coarse parameters from
+ * it) and replays the graph with a single cudaGraphLaunch. The graph is
+ * captured again only when a run's work lists outgrow its capacities or a
+ * buffer it names moved (a receiver was added). Outputs are bit-identical to
+ * the direct batched run. */
+int32_t rv_chain_capture_graph(rv_chain* chain);
+/* Waits for all of the chain's device work (a run returns with its audio
+ * read back already; this is the engine's drain at stop). */
+int32_t rv_chain_drain(rv_chain* chain);
 /* A receiver's device rings: fine samples (cf32) and detector values (f32),
  * both indexed by fine sample index modulo (mask + 1). Detector values exist
  * only in the batched mode. */
@@ -537,6 +552,10 @@ int32_t rv_design_prototype(const rv_grid_params* grid, double attenuation_db, f
                             uint64_t taps_len, double* stopband_db, uint64_t* group_delay);
 /* build_twiddles (core/dsp/pfb_design.cpp:515); M entries. */
 int32_t rv_build_twiddles(uint32_t channels, rv_cf32* table, uint64_t table_len);
+/* build_twiddles' first-octant construction for any power of two up to 65536
+ * (the reference caps its channel grid at 2048; the averaged spectrum and
+ * wider transforms use this). Equal to rv_build_twiddles where both apply. */
+int32_t rv_build_fft_twiddles(uint32_t n, rv_cf32* table, uint64_t len);
 /* build_nco_table (core/dsp/vrx_reference.cpp:364); 2^log2 entries. */
 int32_t rv_build_nco_table(uint32_t log2_size, rv_cf32* table, uint64_t table_len);
 /* build_spectrum_window (core/dsp/spectrum_reference.cpp:195); 3N/2 floats. */

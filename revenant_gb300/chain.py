@@ -80,6 +80,13 @@ class Chain:
             self.device.copy_to_host(d, det.value)
         return f, d
 
+    def capture_graph(self):
+        """Run the batched kernels from one captured CUDA graph from now on."""
+        check(lib().rv_chain_capture_graph(self.handle))
+
+    def drain(self):
+        check(lib().rv_chain_drain(self.handle))
+
     def stats(self):
         s = abi.ChainStats()
         check(lib().rv_chain_get_stats(self.handle, C.byref(s)))

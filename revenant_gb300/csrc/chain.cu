@@ -36,7 +36,8 @@ int32_t build_nco(uint32_t log2, std::vector<rv_cf32>& out);
 int32_t validate_grid(const rv_grid_params* g);
 uint32_t demod_fine_history(const rv_vrx_demod_config* c);
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
-                            const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring);
+                            const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
+                            const rv_coarse_params* dyn = nullptr);
 }  // namespace rv
 
 using namespace rv;
@@ -129,6 +130,19 @@ struct Receiver {
     uint64_t run_audio_offset = 0, run_audio_frames = 0;
 };
 
+// What a captured graph was built for: the capacity of each work list (its
+// section of the device item array), the launch shapes and the buffers baked
+// into its kernel arguments. A run that needs more, or different buffers,
+// captures again.
+struct GraphShape {
+    uint32_t fine = 0, carrier = 0, det = 0, audio = 0, unit_items = 0, units = 0;
+    uint32_t fine_window = 0, weights_cap = 0, unit_budget = 0;
+    const void* audio_ptr = nullptr;
+    const void* table_ptr = nullptr;
+    const void* items_ptr = nullptr;
+    const void* units_ptr = nullptr;
+};
+
 }  // namespace
 
 struct rv_chain {
@@ -166,6 +180,13 @@ struct rv_chain {
     rv_chain_stats stats{};
     // stage boundaries for profiling: input, coarse, fine, demod, readback
     cudaEvent_t marks[6] = {};
+    // captured runs (rv_chain_capture_graph)
+    bool graph = false;
+    bool captured_run = false;  // this run replayed the graph
+    cudaGraphExec_t exec = nullptr;
+    GraphShape shape{};
+    DeviceArray<RunCounts> counts_dev;
+    PinnedArray<RunCounts> counts_host;
 };
 
 namespace {
@@ -177,9 +198,14 @@ void collect_marks(rv_chain* c) {
     float ms[5] = {0, 0, 0, 0, 0};
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&ms[i], c->marks[i], c->marks[i + 1]);
     c->stats.input_ms += ms[0];
-    c->stats.coarse_ms += ms[1];
-    c->stats.fine_ms += ms[2];
-    c->stats.demod_ms += ms[3];
+    if (c->captured_run) {
+        // the graph's stages are not separable: work-list upload + graph
+        c->stats.graph_ms += ms[1] + ms[2] + ms[3];
+    } else {
+        c->stats.coarse_ms += ms[1];
+        c->stats.fine_ms += ms[2];
+        c->stats.demod_ms += ms[3];
+    }
     c->stats.readback_ms += ms[4];
 }
 }  // namespace
@@ -277,8 +303,10 @@ int32_t coarse_plain(rv_chain* c, uint64_t first_sample, const uint8_t* src, uin
     return RV_OK;
 }
 
+// With `deferred`, the coarse parameters are returned for a captured run to
+// hand to its graph instead of being launched here.
 int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, uint64_t count, int32_t where,
-                       uint64_t first_block, uint32_t blocks) {
+                       uint64_t first_block, uint32_t blocks, rv_coarse_params* deferred) {
     const rv_grid_params& g = c->config.grid;
     if (int32_t st = copy_into_ring(c, c->raw.ptr, (uint64_t)c->raw_mask + 1u, first_sample, src, count, where))
         return st;
@@ -290,6 +318,10 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
     const uint32_t lead_zero = centre >= support ? 0u : (uint32_t)(support - centre);
     rv_coarse_params p{c->raw_mask, (uint32_t)(first_block * g.decimation) & c->raw_mask, blocks, (uint32_t)first_block,
                        c->chan_blocks, c->chan_blocks - 1u, lead_zero};
+    if (deferred != nullptr) {
+        *deferred = p;
+        return RV_OK;
+    }
     if (int32_t st = launch_coarse_fused(c->stream, g, c->config.format, p, c->raw.ptr, c->proto.ptr,
                                          c->twiddles.ptr, c->channel.ptr))
         return st;
@@ -343,6 +375,149 @@ uint32_t push_fine_items(std::vector<WorkItem>& list, uint32_t rx, const Receive
         done += n;
     }
     return widest;
+}
+
+// Section offsets of the work lists in the device item array of a captured
+// run: fine, carrier, detector, audio, then the unit items.
+struct Sections {
+    size_t fine, carrier, det, audio, unit, total;
+    explicit Sections(const GraphShape& sh)
+        : fine(0), carrier(sh.fine), det(carrier + sh.carrier), audio(det + sh.det), unit(audio + sh.audio),
+          total(unit + sh.unit_items) {}
+};
+
+// Records the coarse kernel and every batched receiver kernel, reading their
+// counts and the coarse parameters from c->counts_dev, into one graph.
+int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
+    const GraphShape& sh = c->shape;
+    const Sections o(sh);
+    RunCounts* rc = c->counts_dev.ptr;
+    const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
+    WorkItem* items = c->items_dev.ptr;
+    cudaGraph_t graph = nullptr;
+    if (int32_t st = cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "graph capture begin"))
+        return st;
+    int32_t st = launch_coarse_fused(c->stream, c->config.grid, c->config.format, coarse, c->raw.ptr, c->proto.ptr,
+                                     c->twiddles.ptr, c->channel.ptr, &rc->coarse);
+    if (!st)
+        st = launch_fine_units(c->stream, c->rx_table.ptr, items, c->units_dev.ptr, sh.units, chan, c->unit_budget,
+                               &rc->queues.pad, &rc->units);
+    if (!st)
+        st = launch_fine_batched(c->stream, c->rx_table.ptr, items + o.fine, sh.fine, chan, sh.fine_window,
+                                 &rc->queues.fine, &rc->fine);
+    if (!st) st = launch_carrier_batched(c->stream, c->rx_table.ptr, items + o.carrier, sh.carrier, &rc->carrier);
+    if (!st)
+        st = launch_detect_batched(c->stream, c->rx_table.ptr, items + o.det, sh.det, kDetWindow, &rc->queues.detect,
+                                   &rc->detect);
+    if (!st)
+        st = launch_audio_batched(c->stream, c->rx_table.ptr, items + o.audio, sh.audio, c->audio_dev.ptr, kDetWindow,
+                                  sh.weights_cap, &rc->queues.audio, &rc->audio);
+    const int32_t end = cuda_status(cudaStreamEndCapture(c->stream, &graph), "graph capture end");
+    if (st || end) {
+        if (graph) cudaGraphDestroy(graph);
+        return st ? st : end;
+    }
+    st = cuda_status(cudaGraphInstantiate(&c->exec, graph, 0), "graph instantiate");
+    cudaGraphDestroy(graph);
+    if (st) {
+        c->exec = nullptr;
+        return st;
+    }
+    c->stats.graph_captures += 1;
+    return RV_OK;
+}
+
+// A captured run: upload this run's counts and work lists into the sections
+// the graph reads, capture first when the graph is missing or too small, then
+// replay it with one launch.
+int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vector<WorkItem>& fine,
+                     const std::vector<WorkItem>& carrier, const std::vector<WorkItem>& det,
+                     const std::vector<WorkItem>& audio, const std::vector<WorkItem>& unit_items,
+                     const std::vector<FineUnit>& units, uint32_t fine_window) {
+    const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
+    GraphShape& sh = c->shape;
+    const bool fits = c->exec != nullptr && fine.size() <= sh.fine && carrier.size() <= sh.carrier &&
+                      det.size() <= sh.det && audio.size() <= sh.audio && unit_items.size() <= sh.unit_items &&
+                      units.size() <= sh.units && window <= sh.fine_window && sh.weights_cap == c->weights_cap &&
+                      sh.unit_budget == c->unit_budget && sh.audio_ptr == c->audio_dev.ptr &&
+                      sh.table_ptr == c->rx_table.ptr && sh.items_ptr == c->items_dev.ptr &&
+                      sh.units_ptr == c->units_dev.ptr;
+    if (!fits) {
+        if (c->exec) cudaGraphExecDestroy(c->exec);
+        c->exec = nullptr;
+        auto grow = [](size_t need, uint32_t old) {
+            return (uint32_t)std::max<size_t>(old, need == 0 ? 0 : need + need / 2 + 16);
+        };
+        GraphShape n;
+        n.fine = grow(fine.size(), sh.fine);
+        n.carrier = grow(carrier.size(), sh.carrier);
+        n.det = grow(det.size(), sh.det);
+        n.audio = grow(audio.size(), sh.audio);
+        n.unit_items = grow(unit_items.size(), sh.unit_items);
+        n.units = grow(units.size(), sh.units);
+        n.fine_window = std::max(window, sh.fine_window);
+        n.weights_cap = c->weights_cap;
+        n.unit_budget = c->unit_budget;
+        const size_t total = Sections(n).total;
+        if (c->items_dev.count < total + 1)
+            if (int32_t st = c->items_dev.alloc(total + 1)) return st;
+        if (c->units_dev.count < (size_t)n.units + 1)
+            if (int32_t st = c->units_dev.alloc(n.units + 1)) return st;
+        if (c->counts_dev.count == 0)
+            if (int32_t st = c->counts_dev.alloc(1)) return st;
+        n.audio_ptr = c->audio_dev.ptr;
+        n.table_ptr = c->rx_table.ptr;
+        n.items_ptr = c->items_dev.ptr;
+        n.units_ptr = c->units_dev.ptr;
+        sh = n;
+    }
+    const Sections o(sh);
+    if (int32_t st = c->items_host.reserve(o.total + 1)) return st;
+    if (int32_t st = c->units_host.reserve((size_t)sh.units + 1)) return st;
+    if (int32_t st = c->counts_host.reserve(1)) return st;
+    RunCounts* rc = c->counts_host.ptr;
+    memset(rc, 0, sizeof *rc);
+    rc->units = (uint32_t)units.size();
+    rc->fine = (uint32_t)fine.size();
+    rc->carrier = (uint32_t)carrier.size();
+    rc->detect = (uint32_t)det.size();
+    rc->audio = (uint32_t)audio.size();
+    rc->coarse = coarse;
+    if (int32_t st = cuda_status(cudaMemcpyAsync(c->counts_dev.ptr, rc, sizeof *rc, cudaMemcpyHostToDevice, c->stream),
+                                 "run counts upload"))
+        return st;
+    const std::pair<const std::vector<WorkItem>*, size_t> lists[] = {
+        {&fine, o.fine}, {&carrier, o.carrier}, {&det, o.det}, {&audio, o.audio}, {&unit_items, o.unit}};
+    for (const auto& l : lists) {
+        if (l.first->empty()) continue;
+        WorkItem* h = c->items_host.ptr + l.second;
+        memcpy(h, l.first->data(), l.first->size() * sizeof(WorkItem));
+        if (int32_t st = cuda_status(cudaMemcpyAsync(c->items_dev.ptr + l.second, h, l.first->size() * sizeof(WorkItem),
+                                                     cudaMemcpyHostToDevice, c->stream),
+                                     "work list upload"))
+            return st;
+    }
+    if (!units.empty()) {
+        for (size_t i = 0; i < units.size(); ++i) {
+            c->units_host.ptr[i] = units[i];
+            c->units_host.ptr[i].first_item += (uint32_t)o.unit;
+        }
+        if (int32_t st = cuda_status(cudaMemcpyAsync(c->units_dev.ptr, c->units_host.ptr, units.size() * sizeof(FineUnit),
+                                                     cudaMemcpyHostToDevice, c->stream),
+                                     "unit upload"))
+            return st;
+    }
+    if (c->exec == nullptr)
+        if (int32_t st = capture(c, coarse)) return st;
+    mark(c, 2);
+    mark(c, 3);
+    if (int32_t st = cuda_status(cudaGraphLaunch(c->exec, c->stream), "graph launch")) return st;
+    mark(c, 4);
+    c->stats.graph_launches += 1;
+    c->stats.launches += 1 + (sh.units ? 1 : 0) + (sh.fine ? 1 : 0) + (sh.carrier ? 1 : 0) + (sh.det ? 1 : 0) +
+                         (sh.audio ? 1 : 0);
+    c->stats.work_items += fine.size() + carrier.size() + det.size() + audio.size() + unit_items.size();
+    return RV_OK;
 }
 
 }  // namespace
@@ -441,6 +616,9 @@ int32_t rv_chain_destroy(rv_chain* c) {
     c->units_host.release();
     c->audio_dev.release();
     c->audio_host.release();
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    c->counts_dev.release();
+    c->counts_host.release();
     for (cudaEvent_t e : c->marks)
         if (e) cudaEventDestroy(e);
     delete c;
@@ -554,10 +732,14 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
     const uint64_t first_block = c->next_block;
     const uint32_t blocks = last_block >= first_block ? (uint32_t)(last_block - first_block + 1u) : 0u;
     mark(c, 0);
+    // a captured run launches the coarse kernel inside its graph
+    c->captured_run = !plain && c->graph && blocks > 0 && !c->rx.empty();
+    rv_coarse_params coarse{};
     int32_t st = plain ? coarse_plain(c, first_sample, src, count, where, first_block, blocks)
-                       : coarse_batched(c, first_sample, src, count, where, first_block, blocks);
+                       : coarse_batched(c, first_sample, src, count, where, first_block, blocks,
+                                        c->captured_run ? &coarse : nullptr);
     if (st) return st;
-    mark(c, 2);
+    if (!c->captured_run) mark(c, 2);
     c->samples_in += count;
     c->next_block += blocks;
     c->stats.blocks += blocks;
@@ -570,7 +752,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         return clear_error();
     }
     if (!plain && c->table_dirty)
-        if ((st = upload_table(c))) return st;
+        if ((st = upload_table(c))) return st;  // (a captured run whose table moved captures again)
 
     // ---- per-receiver cursors (DemodStage::record) and work lists
     std::vector<WorkItem> fine_items, carrier_items, det_items, audio_items, unit_items;
@@ -702,6 +884,11 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
                     units.push_back(FineUnit{us.rx, us.first + k, std::min(per, us.count - k), c->rx[us.rx].table_rows});
             }
         }
+        if (c->graph) {
+            if ((st = run_captured(c, coarse, fine_items, carrier_items, det_items, audio_items, unit_items, units,
+                                   fine_window)))
+                return st;
+        } else {
         // unit items sit after the per-item lists; units index into that tail
         const size_t unit_base = fine_items.size() + carrier_items.size() + det_items.size() + audio_items.size();
         for (FineUnit& u : units) u.first_item += (uint32_t)unit_base;
@@ -755,6 +942,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         mark(c, 4);
         c->stats.launches += 2 + (fine_items.empty() ? 0 : 1) + (units.empty() ? 0 : 1) + (carrier_items.empty() ? 0 : 1);
         c->stats.work_items += total;
+        }
     }
 
     // ---- audio back to the host (the reference's readback copies)
@@ -779,6 +967,22 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
     if ((st = cuda_status(cudaStreamSynchronize(c->stream), "run sync"))) return st;
     collect_marks(c);
     c->stats.runs += 1;
+    return clear_error();
+}
+
+int32_t rv_chain_capture_graph(rv_chain* c) {
+    if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_capture_graph: NULL");
+    if (c->config.mode != RV_CHAIN_BATCHED)
+        return set_error_fmt(RV_ERR_UNSUPPORTED,
+                             "rv_chain_capture_graph: a plain chain records one launch per stage per receiver; only "
+                             "the batched chain runs from a graph");
+    c->graph = true;
+    return clear_error();
+}
+
+int32_t rv_chain_drain(rv_chain* c) {
+    if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_drain: NULL");
+    if (int32_t st = cuda_status(cudaStreamSynchronize(c->stream), "rv_chain_drain")) return st;
     return clear_error();
 }
 

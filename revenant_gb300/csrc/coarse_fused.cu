@@ -96,7 +96,7 @@ __device__ __forceinline__ uint32_t group_pos(uint32_t t, uint32_t u, int g) {
 template <int M, int T, int D, int FMT, int S>
 __global__ void __launch_bounds__(M*(M / D) * S)
 k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const rv_cf32* __restrict__ tw_g,
-         rv_cf32* __restrict__ ring, rv_coarse_params p, uint32_t tiles) {
+         rv_cf32* __restrict__ ring, rv_coarse_params p_arg, uint32_t tiles_arg, const rv_coarse_params* dyn) {
     constexpr int P = M / D;          // block phases sharing no samples
     constexpr int NT = M * P * S;     // threads
     constexpr int CB = T * P;         // blocks per chunk per sub-stream
@@ -108,6 +108,10 @@ k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const
     constexpr int FT = M / 8;         // FFT threads per block
     constexpr int TASKS = S * CB * FT;
     constexpr int ROUNDS = (TASKS + NT - 1) / NT;
+    // a launch captured in a CUDA graph reads this run's parameters from
+    // device memory; a direct launch has them as arguments
+    const rv_coarse_params p = dyn != nullptr ? *dyn : p_arg;
+    const uint32_t tiles = dyn != nullptr ? (p.block_count + (uint32_t)TILE - 1u) / (uint32_t)TILE : tiles_arg;
 
     extern __shared__ float2 smem[];
     float2* twd = smem;               // [M]
@@ -219,7 +223,7 @@ k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const
 
 template <int M, int T, int D, int FMT, int S>
 int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
-               const rv_coarse_params& p) {
+               const rv_coarse_params& p, const rv_coarse_params* dyn) {
     constexpr int P = M / D, NT = M * P * S, CB = T * P;
     constexpr int TILE = S * CB * kChunksPerTile;
     const size_t shared = sizeof(float2) * (M + 2 * S * CB * M);
@@ -240,8 +244,9 @@ int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, cons
         max_grid = (per_sm > 0 ? per_sm : 1) * sms;
     }
     const uint32_t tiles = (p.block_count + TILE - 1) / TILE;
-    const uint32_t grid = tiles < (uint32_t)max_grid ? tiles : (uint32_t)max_grid;
-    kern<<<grid, NT, shared, stream>>>(raw, taps, tw, ring, p, tiles);
+    // captured: the full resident grid, for whatever block count the run has
+    const uint32_t grid = dyn != nullptr ? (uint32_t)max_grid : (tiles < (uint32_t)max_grid ? tiles : (uint32_t)max_grid);
+    kern<<<grid, NT, shared, stream>>>(raw, taps, tw, ring, p, tiles, dyn);
     return cuda_status(cudaGetLastError(), "coarse_fused launch");
 }
 
@@ -250,12 +255,13 @@ int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, cons
 // Dispatch over the instantiated grids. Returns RV_ERR_UNSUPPORTED for a
 // grid this build has no fused kernel for (the plain kernels cover it).
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
-                            const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring) {
+                            const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
+                            const rv_coarse_params* dyn) {
     const uint32_t* w = static_cast<const uint32_t*>(raw);
 #define RV_COARSE_CASE(MM, TT, DD, SS)                                                                    \
     if (g.channels == MM && g.taps_per_branch == TT && g.decimation == DD) {                             \
-        if (format == RV_FORMAT_CS16) return launch<MM, TT, DD, RV_FORMAT_CS16, SS>(stream, w, taps, tw, ring, p); \
-        if (format == RV_FORMAT_CU8) return launch<MM, TT, DD, RV_FORMAT_CU8, SS>(stream, w, taps, tw, ring, p);   \
+        if (format == RV_FORMAT_CS16) return launch<MM, TT, DD, RV_FORMAT_CS16, SS>(stream, w, taps, tw, ring, p, dyn); \
+        if (format == RV_FORMAT_CU8) return launch<MM, TT, DD, RV_FORMAT_CU8, SS>(stream, w, taps, tw, ring, p, dyn);   \
     }
     RV_COARSE_CASE(64, 17, 32, 1)
     RV_COARSE_CASE(8, 17, 4, 8)
@@ -313,7 +319,7 @@ extern "C" int32_t rv_coarse_fused(void* stream, const rv_grid_params* grid, int
     if (((uintptr_t)raw_ring_dev & 3u) != 0)
         return rv::set_error_fmt(RV_ERR_INVALID, "rv_coarse_fused: raw ring is not 4-byte aligned");
     if (int32_t st = rv::launch_coarse_fused(reinterpret_cast<cudaStream_t>(stream), *grid, format, *params,
-                                             raw_ring_dev, taps_dev, twiddles_dev, channel_ring_dev))
+                                             raw_ring_dev, taps_dev, twiddles_dev, channel_ring_dev, nullptr))
         return st;
     return rv::clear_error();
 }

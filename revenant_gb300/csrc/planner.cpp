@@ -206,9 +206,9 @@ int32_t design_prototype(const rv_grid_params& g, double attenuation_db, std::ve
     return RV_OK;
 }
 
-int32_t build_twiddles(uint32_t M, std::vector<rv_cf32>& out) {
+int32_t build_twiddles(uint32_t M, std::vector<rv_cf32>& out, uint32_t cap = 2048) {
     if (M == 0 || (M & (M - 1)) != 0) return set_error_fmt(RV_ERR_INVALID, "build_twiddles: %u is not a power of two", M);
-    if (M > 2048) return set_error_fmt(RV_ERR_INVALID, "build_twiddles: %u exceeds 2048", M);
+    if (M > cap) return set_error_fmt(RV_ERR_INVALID, "build_twiddles: %u exceeds %u", M, cap);
     const uint32_t half = M / 2, quarter = M / 4, octant = M / 8;
     std::vector<double> oc(octant + 1, 0.0), os(octant + 1, 0.0);
     for (uint32_t i = 0; i <= octant; ++i) {
@@ -988,6 +988,17 @@ int32_t rv_build_twiddles(uint32_t channels, rv_cf32* table, uint64_t len) {
     std::vector<rv_cf32> t;
     if (int32_t st = build_twiddles(channels, t)) return st;
     if (len != t.size()) return set_error_fmt(RV_ERR_INVALID, "rv_build_twiddles: wants %zu entries", t.size());
+    memcpy(table, t.data(), t.size() * sizeof(rv_cf32));
+    return rv::clear_error();
+}
+
+// The same first-octant construction for transforms beyond the channel
+// grid's 2048 (the averaged spectrum, up to 8192 points, and wider DFTs).
+int32_t rv_build_fft_twiddles(uint32_t n, rv_cf32* table, uint64_t len) {
+    if (table == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_build_fft_twiddles: NULL");
+    std::vector<rv_cf32> t;
+    if (int32_t st = build_twiddles(n, t, 1u << 16)) return st;
+    if (len != t.size()) return set_error_fmt(RV_ERR_INVALID, "rv_build_fft_twiddles: wants %zu entries", t.size());
     memcpy(table, t.data(), t.size() * sizeof(rv_cf32));
     return rv::clear_error();
 }

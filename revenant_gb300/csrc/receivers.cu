@@ -65,10 +65,11 @@ __device__ __forceinline__ uint32_t next_item(uint32_t* queue, uint32_t* slot) {
 
 __global__ void __launch_bounds__(kRxThreads)
 k_fine_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-               const float2* __restrict__ chan, uint32_t window_cap, uint32_t* queue) {
+               const float2* __restrict__ chan, uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
     extern __shared__ float2 xs[];
     __shared__ uint32_t s_it;
     __shared__ RxDev rx;
+    if (dyn != nullptr) nitems = *dyn;
     for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
         const WorkItem item = items[it];
         if (threadIdx.x == 0) rx = rxs[item.rx];
@@ -140,10 +141,12 @@ k_fine_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items
 
 __global__ void __launch_bounds__(kUnitThreads)
 k_fine_units(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, const FineUnit* __restrict__ units,
-             uint32_t nunits, const float2* __restrict__ chan, uint32_t shared_float2s, uint32_t* queue) {
+             uint32_t nunits, const float2* __restrict__ chan, uint32_t shared_float2s, uint32_t* queue,
+             const uint32_t* dyn) {
     extern __shared__ float2 sm[];
     __shared__ uint32_t s_it;
     __shared__ RxDev rx;
+    if (dyn != nullptr) nunits = *dyn;
     for (uint32_t u = next_item(queue, &s_it); u < nunits; u = next_item(queue, &s_it)) {
         const FineUnit unit = units[u];
         if (threadIdx.x == 0) rx = rxs[unit.rx];
@@ -205,8 +208,10 @@ k_fine_units(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, 
 
 // ---- carrier loop (SAM / DSB): serial per receiver ----------------------
 
-__global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems) {
+__global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
+                                  const uint32_t* dyn) {
     const uint32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dyn != nullptr) nitems = *dyn;
     if (it >= nitems) return;
     const WorkItem item = items[it];
     const RxDev& rx = rxs[item.rx];
@@ -224,10 +229,11 @@ __global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem*
 
 __global__ void __launch_bounds__(kRxThreads)
 k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-                 uint32_t window_cap, uint32_t* queue) {
+                 uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
     extern __shared__ __align__(16) float sd[];
     __shared__ uint32_t s_it;
     __shared__ RxDev rx;
+    if (dyn != nullptr) nitems = *dyn;
     for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
         const WorkItem item = items[it];
         if (threadIdx.x == 0) rx = rxs[item.rx];
@@ -317,10 +323,12 @@ k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ ite
 
 __global__ void __launch_bounds__(kRxThreads)
 k_audio_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-                float* __restrict__ audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue) {
+                float* __restrict__ audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue,
+                const uint32_t* dyn) {
     extern __shared__ float sd[];
     __shared__ uint32_t s_it;
     __shared__ RxDev rx;
+    if (dyn != nullptr) nitems = *dyn;
     for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
         const WorkItem item = items[it];
         if (threadIdx.x == 0) rx = rxs[item.rx];
@@ -429,12 +437,12 @@ int32_t launch_lerp_table(cudaStream_t s, const rv_cf32* taps, float2* lerped, u
 }
 
 int32_t launch_fine_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                            const float2* chan, uint32_t window_cap, uint32_t* queue) {
+                            const float2* chan, uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)window_cap * sizeof(float2);
     if (int32_t st = set_shared((const void*)k_fine_batched, shared)) return st;
-    const unsigned grid = persistent_grid((const void*)k_fine_batched, kRxThreads, shared, nitems);
-    k_fine_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, chan, window_cap, queue);
+    const unsigned grid = persistent_grid((const void*)k_fine_batched, kRxThreads, shared, dyn ? ~0u : nitems);
+    k_fine_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, chan, window_cap, queue, dyn);
     return cuda_status(cudaGetLastError(), "fine batched");
 }
 
@@ -451,38 +459,40 @@ uint32_t fine_unit_shared_budget() {
 }
 
 int32_t launch_fine_units(cudaStream_t s, const RxDev* rxs, const WorkItem* items, const FineUnit* units,
-                          uint32_t nunits, const float2* chan, uint32_t shared_float2s, uint32_t* queue) {
+                          uint32_t nunits, const float2* chan, uint32_t shared_float2s, uint32_t* queue,
+                          const uint32_t* dyn) {
     if (nunits == 0) return RV_OK;
     const size_t shared = (size_t)shared_float2s * sizeof(float2);
     if (int32_t st = set_shared((const void*)k_fine_units, shared)) return st;
-    const unsigned grid = persistent_grid((const void*)k_fine_units, kUnitThreads, shared, nunits);
-    k_fine_units<<<grid, kUnitThreads, shared, s>>>(rxs, items, units, nunits, chan, shared_float2s, queue);
+    const unsigned grid = persistent_grid((const void*)k_fine_units, kUnitThreads, shared, dyn ? ~0u : nunits);
+    k_fine_units<<<grid, kUnitThreads, shared, s>>>(rxs, items, units, nunits, chan, shared_float2s, queue, dyn);
     return cuda_status(cudaGetLastError(), "fine units");
 }
 
-int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems) {
+int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
+                               const uint32_t* dyn) {
     if (nitems == 0) return RV_OK;
-    k_carrier_batched<<<(nitems + 31) / 32, 32, 0, s>>>(rxs, items, nitems);
+    k_carrier_batched<<<(nitems + 31) / 32, 32, 0, s>>>(rxs, items, nitems, dyn);
     return cuda_status(cudaGetLastError(), "carrier batched");
 }
 
 int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                              uint32_t window_cap, uint32_t* queue) {
+                              uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)(window_cap + 4096u) * sizeof(float);  // window + DC weights
     if (int32_t st = set_shared((const void*)k_detect_batched, shared)) return st;
-    const unsigned grid = persistent_grid((const void*)k_detect_batched, kRxThreads, shared, nitems);
-    k_detect_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap, queue);
+    const unsigned grid = persistent_grid((const void*)k_detect_batched, kRxThreads, shared, dyn ? ~0u : nitems);
+    k_detect_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap, queue, dyn);
     return cuda_status(cudaGetLastError(), "detect batched");
 }
 
 int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems, float* audio,
-                             uint32_t window_cap, uint32_t weights_cap, uint32_t* queue) {
+                             uint32_t window_cap, uint32_t weights_cap, uint32_t* queue, const uint32_t* dyn) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)(window_cap + weights_cap) * sizeof(float);  // window, then the weights
     if (int32_t st = set_shared((const void*)k_audio_batched, shared)) return st;
-    const unsigned grid = persistent_grid((const void*)k_audio_batched, kRxThreads, shared, nitems);
-    k_audio_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap, weights_cap, queue);
+    const unsigned grid = persistent_grid((const void*)k_audio_batched, kRxThreads, shared, dyn ? ~0u : nitems);
+    k_audio_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap, weights_cap, queue, dyn);
     return cuda_status(cudaGetLastError(), "audio batched");
 }
 

@@ -82,22 +82,40 @@ struct Queues {
 
 constexpr int kRxThreads = 256;
 
+// The per-run values a captured run's kernels read from device memory
+// instead of their launch arguments: the queue heads (zeroed by every
+// upload), the item count of each list and the coarse kernel's parameters.
+struct RunCounts {
+    Queues queues;
+    uint32_t units, fine, carrier, detect, audio, pad0, pad1, pad2;
+    rv_coarse_params coarse;
+    uint32_t pad3;
+};
+
+// Every batched launcher takes `dyn`: nullptr for a direct launch, where
+// `nitems` is the item count; or a device pointer to the count inside a
+// RunCounts, for a launch captured in a CUDA graph, where `nitems` is the
+// capacity of the list and the grid is the kernel's full resident grid.
+
 int32_t launch_lerp_table(cudaStream_t s, const rv_cf32* taps, float2* lerped, uint32_t T, uint32_t P,
                           uint32_t period, uint32_t step_rem, uint32_t fd, float inv_fd);
 int32_t launch_fine_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                            const float2* chan, uint32_t window_cap, uint32_t* queue);
+                            const float2* chan, uint32_t window_cap, uint32_t* queue, const uint32_t* dyn = nullptr);
 // Units of fine items with shared-memory tap tables; `shared_floats2` is the
 // dynamic shared memory per CTA (largest table + window), 1024 threads a CTA.
 constexpr int kUnitThreads = 1024;
 int32_t launch_fine_units(cudaStream_t s, const RxDev* rxs, const WorkItem* items, const FineUnit* units,
-                          uint32_t nunits, const float2* chan, uint32_t shared_float2s, uint32_t* queue);
+                          uint32_t nunits, const float2* chan, uint32_t shared_float2s, uint32_t* queue,
+                          const uint32_t* dyn = nullptr);
 uint32_t fine_unit_shared_budget();  // float2 entries of dynamic shared memory a CTA may use
-int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems);
+int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
+                               const uint32_t* dyn = nullptr);
 int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                              uint32_t window_cap, uint32_t* queue);
+                              uint32_t window_cap, uint32_t* queue, const uint32_t* dyn = nullptr);
 // weights_cap: floats of demodulator weights staged per CTA (the largest
 // table among the receivers: audio taps, or the whole stereo table)
 int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
-                             float* audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue);
+                             float* audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue,
+                             const uint32_t* dyn = nullptr);
 
 }  // namespace rv

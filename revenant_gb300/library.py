@@ -156,11 +156,14 @@ SIGNATURES = {
     "rv_chain_receiver_info": (I32, [P, U32, ptr(abi.VrxPlanInfo), ptr(U64), ptr(U64)]),
     "rv_chain_read_audio": (I32, [P, U32, P, U64, ptr(U64)]),
     "rv_chain_get_stats": (I32, [P, ptr(abi.ChainStats)]),
+    "rv_chain_capture_graph": (I32, [P]),
+    "rv_chain_drain": (I32, [P]),
     "rv_chain_channel_ring": (I32, [P, ptr(P), ptr(U32)]),
     "rv_chain_receiver_rings": (I32, [P, U32, ptr(P), ptr(P), ptr(U32)]),
     "rv_validate_grid": (I32, [ptr(abi.GridParams)]),
     "rv_design_prototype": (I32, [ptr(abi.GridParams), F64, P, U64, ptr(F64), ptr(U64)]),
     "rv_build_twiddles": (I32, [U32, P, U64]),
+    "rv_build_fft_twiddles": (I32, [U32, P, U64]),
     "rv_build_nco_table": (I32, [U32, P, U64]),
     "rv_build_spectrum_window": (I32, [U32, U32, F64, P, U64]),
     "rv_place": (I32, [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), ptr(abi.VrxPlacement)]),

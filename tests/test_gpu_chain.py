@@ -136,3 +136,70 @@ def test_wfm_stereo_recovers_the_tone(gpu, c1_capture):
     f = np.fft.rfftfreq(a.shape[0], 1 / 48000)
     k1 = np.argmin(np.abs(f - 1000))
     assert spec_l[k1 - 2:k1 + 3].max() > 20 * np.median(spec_l)
+
+
+def _run_pair(gpu, grid, rate, fmt, reqs, codes, runs, bps_values, late=None, late_at=None):
+    """The same feed through a direct batched chain and a captured one."""
+    out = []
+    for captured in (False, True):
+        ch = Chain(gpu, grid=grid, rate=rate, fmt=fmt, mode=abi.CHAIN_BATCHED, max_run_samples=max(runs))
+        if captured:
+            ch.capture_graph()
+        ids = [ch.add_receiver(r) for r in reqs]
+        at = 0
+        for k, n in enumerate(runs):
+            if late is not None and k == late_at:
+                ids.append(ch.add_receiver(late))
+            ch.run(codes[at * bps_values:(at + n) * bps_values])
+            at += n
+        ch.drain()
+        out.append(([ch.audio(i) for i in ids], ch.stats()))
+        ch.close()
+    return out
+
+
+def test_captured_chain_matches_direct_batched(gpu, c1_capture):
+    """One CUDA graph per chain, replayed every run: the same bits as direct launches."""
+    (direct, _), (graph, st) = _run_pair(gpu, (8, 17, 4), 2_400_000, abi.FORMAT_CU8, c1_requests(), c1_capture,
+                                         RUNS_A, 2)
+    for i, (a, b) in enumerate(zip(direct, graph)):
+        assert a.size == b.size and a.size > 0, "receiver %d" % i
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d differs when captured" % i
+    assert st.graph_launches == len(RUNS_A)
+    assert 1 <= st.graph_captures < len(RUNS_A)
+
+
+def test_captured_chain_replays_without_recapture(gpu, c1_capture):
+    (direct, _), (graph, st) = _run_pair(gpu, (8, 17, 4), 2_400_000, abi.FORMAT_CU8, c1_requests()[:4], c1_capture,
+                                         RUNS_B, 2)
+    for a, b in zip(direct, graph):
+        assert a.size > 0 and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert st.graph_launches == len(RUNS_B)
+    assert st.graph_captures <= 2  # equal runs: the first capture's capacities hold
+
+
+def test_captured_chain_with_a_receiver_added_mid_stream(gpu, c1_capture):
+    reqs = c1_requests()
+    (direct, _), (graph, st) = _run_pair(gpu, (8, 17, 4), 2_400_000, abi.FORMAT_CU8, reqs[:3], c1_capture, RUNS_B, 2,
+                                         late=reqs[6], late_at=5)
+    assert len(graph) == 4
+    for i, (a, b) in enumerate(zip(direct, graph)):
+        assert a.size > 0 and np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d" % i
+
+
+def test_captured_wideband_chain_matches_direct(gpu):
+    rate, n = 20_000_000, 1 << 19
+    reqs = signals.random_receivers(24, rate, seed=4)
+    z = signals.scene(n, rate, [("am", r.center, 0.2) for r in reqs[:6]], snr_db=30.0, seed=4)
+    codes = signals.quantise(z, "cs16")
+    runs = [1 << 17, 100_000, 1 << 17, (1 << 19) - 2 * (1 << 17) - 100_000]
+    (direct, _), (graph, _) = _run_pair(gpu, (64, 17, 32), rate, abi.FORMAT_CS16, reqs, codes, runs, 2)
+    for i, (a, b) in enumerate(zip(direct, graph)):
+        assert a.size > 0 and np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d" % i
+
+
+def test_plain_chain_refuses_capture(gpu):
+    from revenant_gb300.library import lib
+    ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=abi.CHAIN_PLAIN, max_run_samples=4096)
+    assert lib().rv_chain_capture_graph(ch.handle) == abi.RV_ERR_UNSUPPORTED
+    ch.close()

@@ -114,8 +114,16 @@ def test_oracle_vs_reference_live(ref, kind, n, frames, alpha):
 
 def _twiddles(n):
     tw = np.zeros((n, 2), np.float32)
-    assert lib().rv_build_twiddles(n, tw.ctypes.data, n) == 0
+    assert lib().rv_build_fft_twiddles(n, tw.ctypes.data, n) == 0
     return tw
+
+
+@pytest.mark.parametrize("n", [16, 256, 2048])
+def test_fft_twiddles_equal_the_grid_twiddles(rv, n):
+    a, b = np.zeros((n, 2), np.float32), np.zeros((n, 2), np.float32)
+    assert lib().rv_build_twiddles(n, a.ctypes.data, n) == 0
+    assert lib().rv_build_fft_twiddles(n, b.ctypes.data, n) == 0
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
 def gpu_spectrum(gpu, iq, n, kind, mode, average=1, alpha=0.0, avg_in=None, resume=False):
