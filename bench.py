@@ -248,7 +248,7 @@ def run_gb300(args):
     value = samples_step * world * args.steps / (ms / 1e3) / 1e6
     e2e = samples_step * world * args.steps / (ms_e2e / 1e3) / 1e6
     d = {k: getattr(st, k) - getattr(base, k) for k in ("launches", "audio_bytes", "runs", "graph_launches",
-                                                          "graph_captures")}
+                                                          "graph_captures", "host_ms")}
     # per-stage device time from the direct batched chain, CUDA events between
     # stages on the chain's stream, over the same number of steps
     sch = make_chain(abi.CHAIN_BATCHED, run_samples, profile=True)
@@ -304,6 +304,7 @@ def run_gb300(args):
                      "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": None,
                      "peak_kind": pk_kind, "algorithmic_bytes_per_step": int(ab[dominant] / args.steps),
                      "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()},
+                     "host_ms_per_step": round(d["host_ms"] / args.steps, 3),
                      "compulsory_hbm_frac": round(hbm_frac, 5)},
         "realtime_factor": round(value * 1e6 / RATE / max(world, 1), 1),
         "plain_path": plain,

@@ -502,6 +502,8 @@ typedef struct rv_chain_stats {
     uint64_t graph_launches; /* runs replayed from the captured graph */
     uint64_t graph_captures; /* times the graph was (re)captured */
     double graph_ms;      /* captured runs: work-list upload + the whole graph */
+    double host_ms;       /* host time from a run's start until its launches are queued
+                           * (cursor and work-list building, uploads and launch calls) */
 } rv_chain_stats;
 
 /* Allocates the chain's rings (the only allocating calls of the chain API

@@ -166,7 +166,7 @@ class ChainStats(_S):
     _fields_ = [("runs", U64), ("blocks", U64), ("launches", U64), ("work_items", U64), ("audio_bytes", U64),
                 ("input_ms", C.c_double), ("coarse_ms", C.c_double), ("fine_ms", C.c_double),
                 ("demod_ms", C.c_double), ("readback_ms", C.c_double), ("graph_launches", U64),
-                ("graph_captures", U64), ("graph_ms", C.c_double)]
+                ("graph_captures", U64), ("graph_ms", C.c_double), ("host_ms", C.c_double)]
 
 
 EXTRA_STRUCTS = {"rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}

@@ -19,6 +19,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <new>
 #include <numeric>
 #include <vector>
@@ -116,6 +117,11 @@ struct Receiver {
     uint32_t max_fine_item = 0, max_det_item = 0, max_audio_item = 0;
     uint32_t table_rows = 0;      // tap rows of the blended table staged at a time by the unit kernel
     uint32_t max_unit_item = 0;   // outputs per item on the unit path
+    // 2D tiles (fine_tiles.cu); tile_cols == 0: the unit or per-item path
+    uint32_t tile_cols = 0, tile_block = 0, tile_rows = 0, tile_buffers = 0, tile_seg = 0, tile_stride = 0;
+    uint32_t tile_period = 0;
+    uint64_t row_step = 0;
+    uint32_t tile_shared = 0;     // float2 of shared memory a tile of this receiver needs
     bool started = false;
     bool carrier_reset = true;
     uint64_t first_output = 0, next_output = 0, next_audio = 0;
@@ -135,8 +141,10 @@ struct Receiver {
 // into its kernel arguments. A run that needs more, or different buffers,
 // captures again.
 struct GraphShape {
-    uint32_t fine = 0, carrier = 0, det = 0, audio = 0, unit_items = 0, units = 0;
-    uint32_t fine_window = 0, weights_cap = 0, unit_budget = 0;
+    uint32_t fine = 0, carrier = 0, unit_items = 0, units = 0, tiles = 0, nrx = 0;
+    uint32_t fine_window = 0, weights_cap = 0, unit_budget = 0, tile_shared = 0;
+    const void* tiles_ptr = nullptr;
+    const void* spans_ptr = nullptr;
     const void* audio_ptr = nullptr;
     const void* table_ptr = nullptr;
     const void* items_ptr = nullptr;
@@ -171,7 +179,12 @@ struct rv_chain {
     DeviceArray<Queues> queues;
     DeviceArray<FineUnit> units_dev;
     PinnedArray<FineUnit> units_host;
+    DeviceArray<FineTile> tiles_dev;
+    PinnedArray<FineTile> tiles_host;
+    DeviceArray<uint8_t> spans_dev;   // RxRun[nrx], detector prefix [nrx + 1], audio prefix [nrx + 1]
+    PinnedArray<uint8_t> spans_host;
     uint32_t unit_budget = 0;
+    uint32_t tile_shared = 0;   // float2 of shared memory per tile CTA (largest tiled receiver)
     uint32_t weights_cap = 32;  // largest staged demodulator weight table (floats)
     DeviceArray<float> audio_dev;
     PinnedArray<float> audio_host;
@@ -248,6 +261,16 @@ int32_t upload_table(rv_chain* c) {
         d.carrier_state = r.d_state.ptr;
         d.carrier = p.carrier_loop;
         d.carrier_power = p.carrier.power;
+        d.tile_cols = r.tile_cols;
+        d.tile_block = r.tile_block;
+        d.tile_rows = r.tile_rows;
+        d.tile_buffers = r.tile_buffers;
+        d.tile_seg = r.tile_seg;
+        d.tile_stride = r.tile_stride;
+        d.tile_period = r.tile_period;
+        d.det_item = r.max_det_item;
+        d.audio_item = r.max_audio_item;
+        d.row_step = r.row_step;
     }
     if (c->rx_table.count < table.size())
         if (int32_t st = c->rx_table.alloc(table.size())) return st;
@@ -329,6 +352,79 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
     return RV_OK;
 }
 
+// The 2D tile shape of a receiver's fine stage (fine_tiles.cu): rows of P'
+// outputs (the pattern period times the smallest k making it 48 or more), cut
+// into column blocks of at most 16 R columns (16 slots of R adjacent columns),
+// chunks of 16 rows. Among R = 4..1 and one or two staged chunks whose table
+// slice and row segments fit in `budget` float2 of shared memory, the shape
+// that leaves the fewest column slots idle wins (then the larger R, then two
+// buffers). Leaves tile_cols at 0 (not tiled) when nothing fits.
+void plan_tiles(Receiver& r, uint64_t fc, uint64_t fd, uint32_t budget) {
+    const uint64_t T = r.plan.fine.taps;
+    r.tile_cols = 0;
+    if (r.period == 0) return;
+    const uint64_t P = (uint64_t)r.period * ((48u + r.period - 1u) / r.period);
+    if (P > 65535u || (P * fc) % fd != 0) return;
+    double best = 0.0;
+    for (uint32_t R = 4; R >= 1; --R) {
+        const uint64_t cap = (uint64_t)kTileSlots * R;
+        const uint64_t nblk = (P + cap - 1u) / cap;
+        const uint64_t A = (P + nblk - 1u) / nblk;
+        uint64_t L = 0;
+        for (uint64_t a0 = 0; a0 < P; a0 += A) {
+            const uint64_t w = std::min<uint64_t>(A, P - a0);
+            L = std::max<uint64_t>(L, (a0 + w - 1u) * fc / fd - a0 * fc / fd + T);
+        }
+        const uint64_t Ap = A, Lp = L | 1u;
+        // every block runs all 16 slots of R columns
+        const double fill = (double)P / (double)(nblk * kTileSlots * R);
+        for (uint32_t nb = 2; nb >= 1; --nb) {
+            const uint64_t need = (T + 1u) / 2u * 2u * Ap + (uint64_t)nb * kTileRows * Lp;  // tap pairs + rows
+            if (need > budget) continue;
+            const double score = fill * (1.0 + 0.01 * R) * (nb == 2 ? 1.0 : 0.97);
+            if (score > best) {
+                best = score;
+                r.tile_cols = (uint32_t)Ap;
+                r.tile_block = (uint32_t)A;
+                r.tile_rows = R;
+                r.tile_buffers = nb;
+                r.tile_seg = (uint32_t)L;
+                r.tile_stride = (uint32_t)Lp;
+                r.row_step = P * fc / fd;
+                r.tile_period = (uint32_t)P;
+                r.tile_shared = (uint32_t)need;
+            }
+        }
+    }
+}
+
+// Tiles covering fine outputs [first, first + count) of receiver `rx`: every
+// column block over the rows those outputs touch, rows split so a tile costs
+// about `target` complex MACs (at least two row chunks).
+void push_tiles(std::vector<FineTile>& list, uint32_t rx, const Receiver& r, uint64_t first, uint64_t count,
+                uint64_t target) {
+    if (count == 0) return;
+    const uint64_t P = r.tile_period, T = r.plan.fine.taps, end = first + count;
+    const uint64_t row_lo = first / P, row_hi = (end - 1u) / P + 1u;
+    const uint64_t chunk = kTileRows;
+    for (uint64_t a0 = 0; a0 < P; a0 += r.tile_block) {
+        const uint64_t w = std::min<uint64_t>(r.tile_block, P - a0);
+        uint64_t rows = std::max<uint64_t>(2u * chunk, target / std::max<uint64_t>(1u, w * T));
+        rows = (rows + chunk - 1u) / chunk * chunk;
+        for (uint64_t b = row_lo; b < row_hi; b += rows) {
+            FineTile t{};
+            t.rx = rx;
+            t.a0 = (uint32_t)a0;
+            t.width = (uint32_t)w;
+            t.rows = (uint32_t)std::min<uint64_t>(rows, row_hi - b);
+            t.row0 = b;
+            t.first = first;
+            t.end = end;
+            list.push_back(t);
+        }
+    }
+}
+
 void push_items(std::vector<WorkItem>& list, uint32_t rx, uint64_t first, uint64_t count, uint32_t per_item,
                 uint64_t out, uint32_t out_stride) {
     uint64_t done = 0;
@@ -380,11 +476,42 @@ uint32_t push_fine_items(std::vector<WorkItem>& list, uint32_t rx, const Receive
 // Section offsets of the work lists in the device item array of a captured
 // run: fine, carrier, detector, audio, then the unit items.
 struct Sections {
-    size_t fine, carrier, det, audio, unit, total;
+    size_t fine, carrier, unit, total;
     explicit Sections(const GraphShape& sh)
-        : fine(0), carrier(sh.fine), det(carrier + sh.carrier), audio(det + sh.det), unit(audio + sh.audio),
-          total(unit + sh.unit_items) {}
+        : fine(0), carrier(sh.fine), unit(carrier + sh.carrier), total(unit + sh.unit_items) {}
 };
+
+// This run's detector and audio spans per receiver (the batched detector and
+// audio kernels cut them into items on the device).
+struct SpanTable {
+    std::vector<RxRun> runs;
+    std::vector<uint32_t> det_prefix, audio_prefix;
+    uint32_t det_total = 0, audio_total = 0;
+};
+
+size_t span_bytes(size_t nrx) { return nrx * sizeof(RxRun) + 2u * (nrx + 1u) * sizeof(uint32_t); }
+
+// Device addresses of the span table's parts for `nrx` receivers.
+void span_lists(rv_chain* c, uint32_t nrx, SpanList* det, SpanList* audio) {
+    const uint8_t* base = c->spans_dev.ptr;
+    const RxRun* runs = reinterpret_cast<const RxRun*>(base);
+    const uint32_t* dp = reinterpret_cast<const uint32_t*>(base + nrx * sizeof(RxRun));
+    *det = SpanList{runs, dp, nrx, 0u};
+    *audio = SpanList{runs, dp + nrx + 1u, nrx, 1u};
+}
+
+// Copies the span table to the device (capacity kept from earlier runs).
+int32_t upload_spans(rv_chain* c, const SpanTable& t) {
+    const size_t nrx = t.runs.size(), bytes = span_bytes(nrx);
+    if (c->spans_dev.count < bytes)
+        if (int32_t st = c->spans_dev.alloc(bytes + bytes / 2)) return st;
+    if (int32_t st = c->spans_host.reserve(bytes + bytes / 2)) return st;
+    uint8_t* h = c->spans_host.ptr;
+    memcpy(h, t.runs.data(), nrx * sizeof(RxRun));
+    memcpy(h + nrx * sizeof(RxRun), t.det_prefix.data(), (nrx + 1u) * sizeof(uint32_t));
+    memcpy(h + nrx * sizeof(RxRun) + (nrx + 1u) * sizeof(uint32_t), t.audio_prefix.data(), (nrx + 1u) * sizeof(uint32_t));
+    return cuda_status(cudaMemcpyAsync(c->spans_dev.ptr, h, bytes, cudaMemcpyHostToDevice, c->stream), "span upload");
+}
 
 // Records the coarse kernel and every batched receiver kernel, reading their
 // counts and the coarse parameters from c->counts_dev, into one graph.
@@ -400,17 +527,22 @@ int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
     int32_t st = launch_coarse_fused(c->stream, c->config.grid, c->config.format, coarse, c->raw.ptr, c->proto.ptr,
                                      c->twiddles.ptr, c->channel.ptr, &rc->coarse);
     if (!st)
+        st = launch_fine_tiles(c->stream, c->rx_table.ptr, c->tiles_dev.ptr, sh.tiles, chan, sh.tile_shared,
+                               &rc->queues.tiles, &rc->tiles);
+    if (!st)
         st = launch_fine_units(c->stream, c->rx_table.ptr, items, c->units_dev.ptr, sh.units, chan, c->unit_budget,
-                               &rc->queues.pad, &rc->units);
+                               &rc->queues.units, &rc->units);
     if (!st)
         st = launch_fine_batched(c->stream, c->rx_table.ptr, items + o.fine, sh.fine, chan, sh.fine_window,
                                  &rc->queues.fine, &rc->fine);
     if (!st) st = launch_carrier_batched(c->stream, c->rx_table.ptr, items + o.carrier, sh.carrier, &rc->carrier);
+    SpanList det, audio;
+    span_lists(c, sh.nrx, &det, &audio);
     if (!st)
-        st = launch_detect_batched(c->stream, c->rx_table.ptr, items + o.det, sh.det, kDetWindow, &rc->queues.detect,
+        st = launch_detect_batched(c->stream, c->rx_table.ptr, det, sh.nrx, kDetWindow, &rc->queues.detect,
                                    &rc->detect);
     if (!st)
-        st = launch_audio_batched(c->stream, c->rx_table.ptr, items + o.audio, sh.audio, c->audio_dev.ptr, kDetWindow,
+        st = launch_audio_batched(c->stream, c->rx_table.ptr, audio, sh.nrx, c->audio_dev.ptr, kDetWindow,
                                   sh.weights_cap, &rc->queues.audio, &rc->audio);
     const int32_t end = cuda_status(cudaStreamEndCapture(c->stream, &graph), "graph capture end");
     if (st || end) {
@@ -431,14 +563,17 @@ int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
 // the graph reads, capture first when the graph is missing or too small, then
 // replay it with one launch.
 int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vector<WorkItem>& fine,
-                     const std::vector<WorkItem>& carrier, const std::vector<WorkItem>& det,
-                     const std::vector<WorkItem>& audio, const std::vector<WorkItem>& unit_items,
-                     const std::vector<FineUnit>& units, uint32_t fine_window) {
+                     const std::vector<WorkItem>& carrier, const SpanTable& spans,
+                     const std::vector<WorkItem>& unit_items, const std::vector<FineUnit>& units,
+                     const std::vector<FineTile>& tiles, uint32_t fine_window) {
     const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
     GraphShape& sh = c->shape;
+    const uint32_t nrx = (uint32_t)spans.runs.size();
+    if (int32_t st = upload_spans(c, spans)) return st;
     const bool fits = c->exec != nullptr && fine.size() <= sh.fine && carrier.size() <= sh.carrier &&
-                      det.size() <= sh.det && audio.size() <= sh.audio && unit_items.size() <= sh.unit_items &&
-                      units.size() <= sh.units && window <= sh.fine_window && sh.weights_cap == c->weights_cap &&
+                      sh.nrx == nrx && sh.spans_ptr == c->spans_dev.ptr && unit_items.size() <= sh.unit_items &&
+                      units.size() <= sh.units && tiles.size() <= sh.tiles && sh.tile_shared == c->tile_shared &&
+                      sh.tiles_ptr == c->tiles_dev.ptr && window <= sh.fine_window && sh.weights_cap == c->weights_cap &&
                       sh.unit_budget == c->unit_budget && sh.audio_ptr == c->audio_dev.ptr &&
                       sh.table_ptr == c->rx_table.ptr && sh.items_ptr == c->items_dev.ptr &&
                       sh.units_ptr == c->units_dev.ptr;
@@ -451,10 +586,12 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
         GraphShape n;
         n.fine = grow(fine.size(), sh.fine);
         n.carrier = grow(carrier.size(), sh.carrier);
-        n.det = grow(det.size(), sh.det);
-        n.audio = grow(audio.size(), sh.audio);
+        n.nrx = nrx;
+        n.spans_ptr = c->spans_dev.ptr;
         n.unit_items = grow(unit_items.size(), sh.unit_items);
         n.units = grow(units.size(), sh.units);
+        n.tiles = grow(tiles.size(), sh.tiles);
+        n.tile_shared = c->tile_shared;
         n.fine_window = std::max(window, sh.fine_window);
         n.weights_cap = c->weights_cap;
         n.unit_budget = c->unit_budget;
@@ -463,31 +600,36 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
             if (int32_t st = c->items_dev.alloc(total + 1)) return st;
         if (c->units_dev.count < (size_t)n.units + 1)
             if (int32_t st = c->units_dev.alloc(n.units + 1)) return st;
+        if (c->tiles_dev.count < (size_t)n.tiles + 1)
+            if (int32_t st = c->tiles_dev.alloc(n.tiles + 1)) return st;
         if (c->counts_dev.count == 0)
             if (int32_t st = c->counts_dev.alloc(1)) return st;
         n.audio_ptr = c->audio_dev.ptr;
         n.table_ptr = c->rx_table.ptr;
         n.items_ptr = c->items_dev.ptr;
         n.units_ptr = c->units_dev.ptr;
+        n.tiles_ptr = c->tiles_dev.ptr;
         sh = n;
     }
     const Sections o(sh);
     if (int32_t st = c->items_host.reserve(o.total + 1)) return st;
     if (int32_t st = c->units_host.reserve((size_t)sh.units + 1)) return st;
+    if (int32_t st = c->tiles_host.reserve((size_t)sh.tiles + 1)) return st;
     if (int32_t st = c->counts_host.reserve(1)) return st;
     RunCounts* rc = c->counts_host.ptr;
     memset(rc, 0, sizeof *rc);
     rc->units = (uint32_t)units.size();
     rc->fine = (uint32_t)fine.size();
     rc->carrier = (uint32_t)carrier.size();
-    rc->detect = (uint32_t)det.size();
-    rc->audio = (uint32_t)audio.size();
+    rc->detect = spans.det_total;
+    rc->audio = spans.audio_total;
+    rc->tiles = (uint32_t)tiles.size();
     rc->coarse = coarse;
     if (int32_t st = cuda_status(cudaMemcpyAsync(c->counts_dev.ptr, rc, sizeof *rc, cudaMemcpyHostToDevice, c->stream),
                                  "run counts upload"))
         return st;
     const std::pair<const std::vector<WorkItem>*, size_t> lists[] = {
-        {&fine, o.fine}, {&carrier, o.carrier}, {&det, o.det}, {&audio, o.audio}, {&unit_items, o.unit}};
+        {&fine, o.fine}, {&carrier, o.carrier}, {&unit_items, o.unit}};
     for (const auto& l : lists) {
         if (l.first->empty()) continue;
         WorkItem* h = c->items_host.ptr + l.second;
@@ -507,6 +649,13 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
                                      "unit upload"))
             return st;
     }
+    if (!tiles.empty()) {
+        memcpy(c->tiles_host.ptr, tiles.data(), tiles.size() * sizeof(FineTile));
+        if (int32_t st = cuda_status(cudaMemcpyAsync(c->tiles_dev.ptr, c->tiles_host.ptr, tiles.size() * sizeof(FineTile),
+                                                     cudaMemcpyHostToDevice, c->stream),
+                                     "tile upload"))
+            return st;
+    }
     if (c->exec == nullptr)
         if (int32_t st = capture(c, coarse)) return st;
     mark(c, 2);
@@ -514,9 +663,10 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
     if (int32_t st = cuda_status(cudaGraphLaunch(c->exec, c->stream), "graph launch")) return st;
     mark(c, 4);
     c->stats.graph_launches += 1;
-    c->stats.launches += 1 + (sh.units ? 1 : 0) + (sh.fine ? 1 : 0) + (sh.carrier ? 1 : 0) + (sh.det ? 1 : 0) +
-                         (sh.audio ? 1 : 0);
-    c->stats.work_items += fine.size() + carrier.size() + det.size() + audio.size() + unit_items.size();
+    c->stats.launches += 1 + (sh.units ? 1 : 0) + (sh.fine ? 1 : 0) + (sh.carrier ? 1 : 0) + (sh.nrx ? 2 : 0) +
+                         (sh.tiles ? 1 : 0);
+    c->stats.work_items += fine.size() + carrier.size() + spans.det_total + spans.audio_total + unit_items.size() +
+                           tiles.size();
     return RV_OK;
 }
 
@@ -614,6 +764,10 @@ int32_t rv_chain_destroy(rv_chain* c) {
     c->queues.release();
     c->units_dev.release();
     c->units_host.release();
+    c->tiles_dev.release();
+    c->tiles_host.release();
+    c->spans_dev.release();
+    c->spans_host.release();
     c->audio_dev.release();
     c->audio_host.release();
     if (c->exec) cudaGraphExecDestroy(c->exec);
@@ -687,6 +841,9 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
         } else {
             r.max_unit_item = (uint32_t)std::min<uint64_t>(kUnitThreads, (avail - T) / step_max + 1u);
         }
+        // the 2D tiles take over where a table slice and a chunk of rows fit
+        plan_tiles(r, fc, fd, c->unit_budget);
+        if (r.tile_cols != 0) c->tile_shared = std::max(c->tile_shared, r.tile_shared);
     }
     if (!st) st = r.d_fine.alloc(cap);
     if (!st) st = cuda_status(cudaMemsetAsync(r.d_fine.ptr, 0, cap * sizeof(rv_cf32), c->stream), "fine clear");
@@ -723,6 +880,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_run: %llu samples exceed max_run_samples %u",
                              (unsigned long long)count, c->config.max_run_samples);
     if (count == 0) return clear_error();
+    const auto host_start = std::chrono::steady_clock::now();
     const rv_grid_params& g = c->config.grid;
     const bool plain = c->config.mode == RV_CHAIN_PLAIN;
     const uint8_t* src = static_cast<const uint8_t*>(samples);
@@ -755,8 +913,18 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         if ((st = upload_table(c))) return st;  // (a captured run whose table moved captures again)
 
     // ---- per-receiver cursors (DemodStage::record) and work lists
-    std::vector<WorkItem> fine_items, carrier_items, det_items, audio_items, unit_items;
+    std::vector<WorkItem> fine_items, carrier_items, unit_items;
+    SpanTable rx_spans;
+    if (!plain) {
+        rx_spans.runs.assign(c->rx.size(), RxRun{});
+        rx_spans.det_prefix.assign(c->rx.size() + 1u, 0u);
+        rx_spans.audio_prefix.assign(c->rx.size() + 1u, 0u);
+    }
     std::vector<FineUnit> units;
+    std::vector<FineTile> tiles;
+    struct TileSpan { uint32_t rx; uint64_t first, count; };
+    std::vector<TileSpan> tile_spans;
+    uint64_t tile_cost_total = 0;
     uint32_t fine_window = 0;
     uint64_t unit_cost_total = 0;
     struct UnitSpan { uint32_t rx, first, count; uint64_t cost_per_item; };
@@ -803,7 +971,12 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         r.run_audio_frames = s.audio_count;
         audio_floats += s.audio_count * p.demod.channels;
         if (!plain) {
-            if (r.max_unit_item != 0) {
+            if (r.tile_cols != 0) {
+                if (s.fine_count) {
+                    tile_spans.push_back(TileSpan{(uint32_t)ri, s.fine_first, s.fine_count});
+                    tile_cost_total += s.fine_count * p.fine.taps;
+                }
+            } else if (r.max_unit_item != 0) {
                 const uint32_t before = (uint32_t)unit_items.size();
                 push_fine_items(unit_items, (uint32_t)ri, r, s.fine_first, s.fine_count, r.max_unit_item);
                 const uint32_t added = (uint32_t)unit_items.size() - before;
@@ -819,10 +992,17 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
                 carrier_items.push_back(WorkItem{(uint32_t)ri, (uint32_t)s.fine_count, s.fine_first, r.carrier_reset ? 1u : 0u});
                 r.carrier_reset = false;
             }
-            if (!is_complex_demod(p.demod.mode))
-                push_items(det_items, (uint32_t)ri, s.det_first, s.det_count, r.max_det_item, 0, 0);
-            push_items(audio_items, (uint32_t)ri, s.audio_first, s.audio_count, r.max_audio_item, r.run_audio_offset,
-                       p.demod.channels);
+            RxRun& run = rx_spans.runs[ri];
+            if (!is_complex_demod(p.demod.mode)) {
+                run.det_first = s.det_first;
+                run.det_count = (uint32_t)s.det_count;
+            }
+            run.audio_first = s.audio_first;
+            run.audio_count = (uint32_t)s.audio_count;
+            run.audio_out = r.run_audio_offset;
+            rx_spans.det_prefix[ri + 1u] = rx_spans.det_prefix[ri] + (run.det_count + r.max_det_item - 1u) / r.max_det_item;
+            rx_spans.audio_prefix[ri + 1u] =
+                rx_spans.audio_prefix[ri] + (run.audio_count + r.max_audio_item - 1u) / r.max_audio_item;
         }
     }
     if (c->audio_dev.count < audio_floats + 1)
@@ -872,11 +1052,18 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         mark(c, 3);
         mark(c, 4);
     } else {
-        // cost-balanced units: about four per SM, each one receiver's items
+        // cost-balanced units and tiles: about four per SM
         {
             int sms = 0, dev = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            const uint64_t tile_target = std::max<uint64_t>(1, tile_cost_total / (uint64_t)(4 * std::max(sms, 1)));
+            for (const TileSpan& ts : tile_spans) push_tiles(tiles, ts.rx, c->rx[ts.rx], ts.first, ts.count, tile_target);
+            // largest first, so the last tiles to start are the short ones
+            std::stable_sort(tiles.begin(), tiles.end(), [&](const FineTile& x, const FineTile& y) {
+                return (uint64_t)x.rows * x.width * c->rx[x.rx].plan.fine.taps >
+                       (uint64_t)y.rows * y.width * c->rx[y.rx].plan.fine.taps;
+            });
             const uint64_t target = std::max<uint64_t>(1, unit_cost_total / (uint64_t)(4 * std::max(sms, 1)));
             for (const UnitSpan& us : unit_spans) {
                 const uint32_t per = (uint32_t)std::max<uint64_t>(1, target / std::max<uint64_t>(1, us.cost_per_item));
@@ -885,12 +1072,16 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
             }
         }
         if (c->graph) {
-            if ((st = run_captured(c, coarse, fine_items, carrier_items, det_items, audio_items, unit_items, units,
-                                   fine_window)))
+            rx_spans.det_total = rx_spans.det_prefix.back();
+            rx_spans.audio_total = rx_spans.audio_prefix.back();
+            if ((st = run_captured(c, coarse, fine_items, carrier_items, rx_spans, unit_items, units, tiles, fine_window)))
                 return st;
         } else {
         // unit items sit after the per-item lists; units index into that tail
-        const size_t unit_base = fine_items.size() + carrier_items.size() + det_items.size() + audio_items.size();
+        rx_spans.det_total = rx_spans.det_prefix.back();
+        rx_spans.audio_total = rx_spans.audio_prefix.back();
+        if ((st = upload_spans(c, rx_spans))) return st;
+        const size_t unit_base = fine_items.size() + carrier_items.size();
         for (FineUnit& u : units) u.first_item += (uint32_t)unit_base;
         const size_t total = unit_base + unit_items.size();
         if ((st = c->items_host.reserve(total + 1 + total / 2))) return st;  // headroom: no re-pinning per run
@@ -901,7 +1092,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
             if ((st = c->items_dev.alloc(total + 1 + total / 4))) return st;
         WorkItem* h = c->items_host.ptr;
         size_t at = 0;
-        for (auto* list : {&fine_items, &carrier_items, &det_items, &audio_items, &unit_items}) {
+        for (auto* list : {&fine_items, &carrier_items, &unit_items}) {
             if (!list->empty()) memcpy(h + at, list->data(), list->size() * sizeof(WorkItem));
             at += list->size();
         }
@@ -919,10 +1110,23 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
                                   "unit upload")))
                 return st;
         }
+        if (!tiles.empty()) {
+            if ((st = c->tiles_host.reserve(tiles.size() + tiles.size() / 2 + 1))) return st;
+            if (c->tiles_dev.count < tiles.size())
+                if ((st = c->tiles_dev.alloc(tiles.size() + tiles.size() / 2 + 1))) return st;
+            memcpy(c->tiles_host.ptr, tiles.data(), tiles.size() * sizeof(FineTile));
+            if ((st = cuda_status(cudaMemcpyAsync(c->tiles_dev.ptr, c->tiles_host.ptr, tiles.size() * sizeof(FineTile),
+                                                  cudaMemcpyHostToDevice, c->stream),
+                                  "tile upload")))
+                return st;
+        }
         const WorkItem* d = c->items_dev.ptr;
         const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
+        if ((st = launch_fine_tiles(c->stream, c->rx_table.ptr, c->tiles_dev.ptr, (uint32_t)tiles.size(), chan,
+                                    c->tile_shared, &c->queues.ptr->tiles)))
+            return st;
         if ((st = launch_fine_units(c->stream, c->rx_table.ptr, c->items_dev.ptr, c->units_dev.ptr,
-                                    (uint32_t)units.size(), chan, c->unit_budget, &c->queues.ptr->pad)))
+                                    (uint32_t)units.size(), chan, c->unit_budget, &c->queues.ptr->units)))
             return st;
         const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
         if ((st = launch_fine_batched(c->stream, c->rx_table.ptr, d, (uint32_t)fine_items.size(), chan, window,
@@ -932,19 +1136,23 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         if ((st = launch_carrier_batched(c->stream, c->rx_table.ptr, d, (uint32_t)carrier_items.size()))) return st;
         d += carrier_items.size();
         mark(c, 3);
-        if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, d, (uint32_t)det_items.size(), kDetWindow,
+        SpanList det_list, audio_list;
+        span_lists(c, (uint32_t)c->rx.size(), &det_list, &audio_list);
+        if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, det_list, rx_spans.det_total, kDetWindow,
                                         &c->queues.ptr->detect)))
             return st;
-        d += det_items.size();
-        if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, d, (uint32_t)audio_items.size(), c->audio_dev.ptr,
+        if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, audio_list, rx_spans.audio_total, c->audio_dev.ptr,
                                        kDetWindow, c->weights_cap, &c->queues.ptr->audio)))
             return st;
         mark(c, 4);
-        c->stats.launches += 2 + (fine_items.empty() ? 0 : 1) + (units.empty() ? 0 : 1) + (carrier_items.empty() ? 0 : 1);
-        c->stats.work_items += total;
+        c->stats.launches += (rx_spans.det_total ? 1 : 0) + (rx_spans.audio_total ? 1 : 0) + (fine_items.empty() ? 0 : 1) +
+                             (units.empty() ? 0 : 1) + (carrier_items.empty() ? 0 : 1) + (tiles.empty() ? 0 : 1);
+        c->stats.work_items += total + rx_spans.det_total + rx_spans.audio_total + tiles.size();
         }
     }
 
+    c->stats.host_ms +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_start).count();
     // ---- audio back to the host (the reference's readback copies)
     if (audio_floats > 0) {
         if ((st = c->audio_host.reserve(audio_floats + audio_floats / 4))) return st;

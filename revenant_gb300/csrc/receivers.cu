@@ -63,6 +63,33 @@ __device__ __forceinline__ uint32_t next_item(uint32_t* queue, uint32_t* slot) {
     return *slot;
 }
 
+// Item `it` of a span list: the receiver by binary search over the prefix
+// sums (the largest r with prefix[r] <= it is the one that owns it; empty
+// receivers share their prefix with the next), then the item's range.
+__device__ __forceinline__ WorkItem span_item(const SpanList& sl, const RxDev* __restrict__ rxs, uint32_t it) {
+    uint32_t lo = 0, hi = sl.nrx;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (sl.prefix[mid] <= it) lo = mid;
+        else hi = mid;
+    }
+    const RxRun run = sl.runs[lo];
+    const uint32_t k = it - sl.prefix[lo];
+    WorkItem w{};
+    w.rx = lo;
+    if (sl.audio == 0) {
+        const uint32_t size = rxs[lo].det_item;
+        w.first = run.det_first + (uint64_t)k * size;
+        w.count = min(size, run.det_count - k * size);
+    } else {
+        const uint32_t size = rxs[lo].audio_item;
+        w.first = run.audio_first + (uint64_t)k * size;
+        w.count = min(size, run.audio_count - k * size);
+        w.out = run.audio_out + (uint64_t)k * size * rxs[lo].channels;
+    }
+    return w;
+}
+
 __global__ void __launch_bounds__(kRxThreads)
 k_fine_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
                const float2* __restrict__ chan, uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
@@ -228,16 +255,20 @@ __global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem*
 // ---- detector, once per fine sample ---------------------------------------
 
 __global__ void __launch_bounds__(kRxThreads)
-k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-                 uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
+k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, uint32_t window_cap, uint32_t* queue,
+                 const uint32_t* dyn) {
     extern __shared__ __align__(16) float sd[];
     __shared__ uint32_t s_it;
     __shared__ RxDev rx;
+    __shared__ WorkItem s_item;
     if (dyn != nullptr) nitems = *dyn;
     for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
-        const WorkItem item = items[it];
-        if (threadIdx.x == 0) rx = rxs[item.rx];
+        if (threadIdx.x == 0) {
+            s_item = span_item(spans, rxs, it);
+            rx = rxs[s_item.rx];
+        }
         __syncthreads();
+        const WorkItem item = s_item;
         const uint32_t mode = rx.mode;
         const uint32_t i = threadIdx.x;
         const uint32_t first = (uint32_t)item.first;  // ring arithmetic is modulo the mask
@@ -322,17 +353,20 @@ k_detect_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ ite
 // ---- audio FIR with decimation, mono or stereo ----------------------------
 
 __global__ void __launch_bounds__(kRxThreads)
-k_audio_batched(const RxDev* __restrict__ rxs, const WorkItem* __restrict__ items, uint32_t nitems,
-                float* __restrict__ audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue,
-                const uint32_t* dyn) {
+k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, float* __restrict__ audio,
+                uint32_t window_cap, uint32_t weights_cap, uint32_t* queue, const uint32_t* dyn) {
     extern __shared__ float sd[];
     __shared__ uint32_t s_it;
     __shared__ RxDev rx;
+    __shared__ WorkItem s_item;
     if (dyn != nullptr) nitems = *dyn;
     for (uint32_t it = next_item(queue, &s_it); it < nitems; it = next_item(queue, &s_it)) {
-        const WorkItem item = items[it];
-        if (threadIdx.x == 0) rx = rxs[item.rx];
+        if (threadIdx.x == 0) {
+            s_item = span_item(spans, rxs, it);
+            rx = rxs[s_item.rx];
+        }
         __syncthreads();
+        const WorkItem item = s_item;
         const uint32_t i = threadIdx.x;
         const uint32_t dec = rx.decimation;
         const uint32_t first_index = (uint32_t)(item.first * dec);  // fine index of the first frame, mod 2^32
@@ -476,7 +510,7 @@ int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem*
     return cuda_status(cudaGetLastError(), "carrier batched");
 }
 
-int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
+int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, SpanList items, uint32_t nitems,
                               uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)(window_cap + 4096u) * sizeof(float);  // window + DC weights
@@ -486,7 +520,7 @@ int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* 
     return cuda_status(cudaGetLastError(), "detect batched");
 }
 
-int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems, float* audio,
+int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, SpanList items, uint32_t nitems, float* audio,
                              uint32_t window_cap, uint32_t weights_cap, uint32_t* queue, const uint32_t* dyn) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)(window_cap + weights_cap) * sizeof(float);  // window, then the weights

@@ -38,7 +38,37 @@ struct RxDev {
     uint32_t* carrier_state;  // 8 words, SAM / DSB only
     rv_vrx_carrier_params carrier;  // per-receiver loop constants
     uint32_t carrier_power;
+    // fine stage as 2D tiles (fine_tiles.cu); tile_cols == 0: not tiled
+    uint32_t tile_cols;     // columns of the table slice in shared memory (the block width)
+    uint32_t tile_block;    // A: columns (pattern phases) per block
+    uint32_t tile_rows;     // R: adjacent columns per thread (1 to 4)
+    uint32_t tile_buffers;  // row chunks staged at once (2: the next chunk overlaps compute)
+    uint32_t tile_seg;      // L: input samples of one row segment
+    uint32_t tile_stride;   // float2 between row segments in shared memory (odd)
+    uint32_t tile_period;   // P': outputs per row, a multiple of the pattern period
+    uint32_t det_item;      // detector item: fine samples (batched detector)
+    uint32_t audio_item;    // audio item: frames (batched audio)
     uint32_t pad;
+    uint64_t row_step;      // Dp = P' Fc / Fd: input samples between rows
+};
+
+// One receiver's detector and audio work of a run. The device splits it into
+// items of det_item fine samples / audio_item frames: item k covers
+// [first + k size, first + min(count, (k + 1) size)).
+struct RxRun {
+    uint64_t det_first;
+    uint64_t audio_first;
+    uint64_t audio_out;  // where the run's first frame goes in the audio buffer (floats)
+    uint32_t det_count, audio_count;
+};
+
+// A run's item list of one stage: receiver r owns items [prefix[r],
+// prefix[r + 1]); the host writes O(receivers) values, not one per item.
+struct SpanList {
+    const RxRun* runs;
+    const uint32_t* prefix;  // [nrx + 1], exclusive prefix sums of item counts
+    uint32_t nrx;
+    uint32_t audio;          // 0: detector items, 1: audio items
 };
 
 // A contiguous run of outputs of one receiver: fine outputs (fine stage),
@@ -77,8 +107,25 @@ struct FineUnit {
 // an SM at any moment work on the same receiver (its tables stay in L1), and
 // a slow item never holds up a fixed share of the list.
 struct Queues {
-    uint32_t fine, detect, audio, pad;
+    uint32_t fine, detect, audio, units, tiles, pad0, pad1, pad2;
 };
+
+// One tile of the 2D fine stage: columns [a0, a0 + width) of rows
+// [row0, row0 + rows) of one receiver, where output j = row * P' + column;
+// only outputs in [first, end), this run's, are written.
+struct FineTile {
+    uint32_t rx;
+    uint32_t a0;
+    uint32_t width;
+    uint32_t rows;
+    uint64_t row0;
+    uint64_t first;
+    uint64_t end;
+};
+
+constexpr int kTileThreads = 256;
+constexpr uint32_t kTileRows = 16;  // rows per staged chunk: one half-warp
+constexpr uint32_t kTileSlots = kTileThreads / kTileRows;  // column slots of R columns each
 
 constexpr int kRxThreads = 256;
 
@@ -87,9 +134,9 @@ constexpr int kRxThreads = 256;
 // upload), the item count of each list and the coarse kernel's parameters.
 struct RunCounts {
     Queues queues;
-    uint32_t units, fine, carrier, detect, audio, pad0, pad1, pad2;
+    uint32_t units, fine, carrier, detect, audio, tiles, pad0, pad1;
     rv_coarse_params coarse;
-    uint32_t pad3;
+    uint32_t pad2;
 };
 
 // Every batched launcher takes `dyn`: nullptr for a direct launch, where
@@ -108,13 +155,17 @@ int32_t launch_fine_units(cudaStream_t s, const RxDev* rxs, const WorkItem* item
                           uint32_t nunits, const float2* chan, uint32_t shared_float2s, uint32_t* queue,
                           const uint32_t* dyn = nullptr);
 uint32_t fine_unit_shared_budget();  // float2 entries of dynamic shared memory a CTA may use
+// 2D tiles of the fine stage; `shared_float2s` of dynamic shared memory per
+// CTA (the largest tiled receiver's table slice plus row buffers).
+int32_t launch_fine_tiles(cudaStream_t s, const RxDev* rxs, const FineTile* tiles, uint32_t ntiles,
+                          const float2* chan, uint32_t shared_float2s, uint32_t* queue, const uint32_t* dyn = nullptr);
 int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
                                const uint32_t* dyn = nullptr);
-int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
+int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, SpanList spans, uint32_t nitems,
                               uint32_t window_cap, uint32_t* queue, const uint32_t* dyn = nullptr);
 // weights_cap: floats of demodulator weights staged per CTA (the largest
 // table among the receivers: audio taps, or the whole stereo table)
-int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
+int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, SpanList spans, uint32_t nitems,
                              float* audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue,
                              const uint32_t* dyn = nullptr);
 
