@@ -803,10 +803,12 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
     const uint64_t step_max = fc / fd + 1u;
     r.max_fine_item = (uint32_t)std::min<uint64_t>(kMaxItem, (kFineWindow - p.fine.taps) / step_max + 1u);
     // AM / SAM run four DC-removal outputs per thread (window count + dc + 2)
+    // (the other detectors also take four outputs per thread: bigger items,
+    // fewer per-item queue and barrier steps)
     if (p.demod.mode == RV_DEMOD_AM || p.demod.mode == RV_DEMOD_SAM)
         r.max_det_item = (uint32_t)std::min<uint64_t>(4u * kMaxItem, kDetWindow - p.demod.dc_taps - 2u - 8u);
     else
-        r.max_det_item = kMaxItem;
+        r.max_det_item = 4u * kMaxItem;
     const uint64_t dec = p.demod.decimation;
     if (r.reach + 1u > kDetWindow)
         return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_chain_add_receiver: audio history %u exceeds the %u-sample window",
@@ -865,7 +867,7 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
     }
     {
         const uint32_t nw = (p.demod.channels == 2u && p.demod.pilot_taps != 0u) ? (uint32_t)r.weights.size()
-                                                                                : p.demod.audio_taps;
+                                                                                : mono_weight_floats(p.demod.audio_taps);
         c->weights_cap = std::max<uint32_t>(c->weights_cap, (nw + 31u) & ~31u);
     }
     c->rx.push_back(std::move(r));

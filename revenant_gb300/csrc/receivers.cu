@@ -332,19 +332,22 @@ k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems,
                 for (int r = 0; r < 4; ++r)
                     if (i0 + (uint32_t)r < item.count) rx.det[(first + i0 + (uint32_t)r) & rx.fine_mask] = v[r] - acc[r];
             }
-        } else if (i < item.count) {
-            const uint32_t f = first + i;
-            const float2 z = rx.fine[f & rx.fine_mask];
-            float d;
-            if (mode == RV_DEMOD_NFM || mode == RV_DEMOD_WFM) {
-                const float2 q = rx.fine[(f - 1u) & rx.fine_mask];
-                const float pr = z.x * q.x + z.y * q.y;
-                const float pi = z.y * q.x - z.x * q.y;
-                d = det_atan2(pi, pr);
-            } else {
-                d = z.x;
+        } else {
+            // one detector value per fine sample, items of up to four per thread
+            for (uint32_t k = i; k < item.count; k += blockDim.x) {
+                const uint32_t f = first + k;
+                const float2 z = rx.fine[f & rx.fine_mask];
+                float d;
+                if (mode == RV_DEMOD_NFM || mode == RV_DEMOD_WFM) {
+                    const float2 q = rx.fine[(f - 1u) & rx.fine_mask];
+                    const float pr = z.x * q.x + z.y * q.y;
+                    const float pi = z.y * q.x - z.x * q.y;
+                    d = det_atan2(pi, pr);
+                } else {
+                    d = z.x;
+                }
+                rx.det[f & rx.fine_mask] = d;
             }
-            rx.det[f & rx.fine_mask] = d;
         }
         __syncthreads();
     }
@@ -355,7 +358,7 @@ k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems,
 __global__ void __launch_bounds__(kRxThreads)
 k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, float* __restrict__ audio,
                 uint32_t window_cap, uint32_t weights_cap, uint32_t* queue, const uint32_t* dyn) {
-    extern __shared__ float sd[];
+    extern __shared__ __align__(16) float sd[];
     __shared__ uint32_t s_it;
     __shared__ RxDev rx;
     __shared__ WorkItem s_item;
@@ -386,9 +389,24 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
         for (uint32_t e = threadIdx.x; e < len && e < window_cap; e += blockDim.x)
             sd[e] = rx.det[(start + e) & rx.fine_mask];
         float* ws = sd + window_cap;
-        const uint32_t nw = rx.channels == 2u ? rx.audio_taps + rx.dc_taps + 2u * rx.pilot_taps + 2u * rx.audio_taps
-                                              : rx.audio_taps;
-        for (uint32_t e = threadIdx.x; e < nw && e < weights_cap; e += blockDim.x) ws[e] = rx.weights[e];
+        if (rx.channels == 2u) {
+            const uint32_t nw = rx.audio_taps + rx.dc_taps + 2u * rx.pilot_taps + 2u * rx.audio_taps;
+            for (uint32_t e = threadIdx.x; e < nw && e < weights_cap; e += blockDim.x) ws[e] = rx.weights[e];
+        } else {
+            // the taps, then the four shifted copies (mono_weight_floats)
+            const uint32_t Ta = rx.audio_taps, C0 = mono_copy_base(Ta), S = mono_copy_stride(Ta);
+            const uint32_t nw = mono_weight_floats(Ta);
+            for (uint32_t e = threadIdx.x; e < nw && e < weights_cap; e += blockDim.x) {
+                float v = 0.0F;
+                if (e < Ta) {
+                    v = rx.weights[e];
+                } else if (e >= C0) {
+                    const uint32_t h = (e - C0) / S + 1u, jj = (e - C0) % S;
+                    if (jj + h < Ta) v = rx.weights[jj + h];
+                }
+                ws[e] = v;
+            }
+        }
         __syncthreads();
         if (i < item.count && rx.reach + i * dec < (len < window_cap ? len : window_cap)) {
             const float* v = sd + rx.reach + i * dec;  // v[-t] = detector at (index - t)
@@ -425,8 +443,33 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
                 out[2u * i] = (sum + gated) * rx.gain;
                 out[2u * i + 1u] = (sum - gated) * rx.gain;
             } else {
+                // taps 0..h-1 from the frame's first quad of samples, then
+                // aligned four-tap steps (samples as 16-byte vectors read
+                // backwards, weights from the copy shifted by h), then the
+                // rest; every product is rounded and added in tap order
+                const uint32_t Ta = rx.audio_taps;
+                const uint32_t base = rx.reach + i * dec;  // v = sd + base
+                const uint32_t q0 = base & ~3u;
+                const uint32_t h = base - q0 + 1u;
+                const uint32_t hp = h < Ta ? h : Ta;
                 float acc = 0.0F;
-                for (uint32_t t = 0; t < rx.audio_taps; ++t) {
+                for (uint32_t t = 0; t < hp; ++t) {
+                    const float term = v[-(int)t] * w[t];
+                    acc = acc + term;
+                }
+                const uint32_t nq = (Ta - hp) / 4u;
+                const float* sq = sd + q0 - 4u;
+                const float* wq = ws + mono_copy_base(Ta) + (h - 1u) * mono_copy_stride(Ta);
+#pragma unroll 4
+                for (uint32_t k = 0; k < nq; ++k) {
+                    const float4 s4 = *reinterpret_cast<const float4*>(sq - 4u * k);
+                    const float4 w4 = *reinterpret_cast<const float4*>(wq + 4u * k);
+                    acc = acc + s4.w * w4.x;
+                    acc = acc + s4.z * w4.y;
+                    acc = acc + s4.y * w4.z;
+                    acc = acc + s4.x * w4.w;
+                }
+                for (uint32_t t = hp + 4u * nq; t < Ta; ++t) {
                     const float term = v[-(int)t] * w[t];
                     acc = acc + term;
                 }

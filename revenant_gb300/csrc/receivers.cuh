@@ -129,6 +129,16 @@ constexpr uint32_t kTileSlots = kTileThreads / kTileRows;  // column slots of R 
 
 constexpr int kRxThreads = 256;
 
+// Shared-memory layout of a mono audio FIR's weights: the taps, then four
+// copies shifted by 1, 2, 3 and 4 taps, each 16-byte aligned and starting in a
+// different bank quad, so that after a frame's first (partial) quad of
+// samples every lane reads its weights as aligned four-tap vectors.
+__host__ __device__ inline uint32_t mono_copy_base(uint32_t taps) { return (taps + 31u) & ~31u; }
+__host__ __device__ inline uint32_t mono_copy_stride(uint32_t taps) { return ((taps + 3u + 31u) & ~31u) + 4u; }
+__host__ __device__ inline uint32_t mono_weight_floats(uint32_t taps) {
+    return mono_copy_base(taps) + 4u * mono_copy_stride(taps);
+}
+
 // The per-run values a captured run's kernels read from device memory
 // instead of their launch arguments: the queue heads (zeroed by every
 // upload), the item count of each list and the coarse kernel's parameters.
