@@ -544,6 +544,97 @@ int32_t rv_chain_receiver_rings(const rv_chain* chain, uint32_t id, const rv_cf3
 int32_t rv_chain_channel_ring(const rv_chain* chain, const rv_cf32** ring, uint32_t* ring_blocks);
 
 /* ===================================================================== *
+ * Wideband detector (core/detect/detector.h:1316-1460, detector.cpp:186-1586):
+ * the exponential average of the spectrum frames, and at every decision the
+ * noise floor, the summed-bin width ladder and the candidate bands, then the
+ * residual rejection. The per-bin average, the noise-floor percentiles and
+ * interpolation, the prefix sums and the ladder's deflections and peaks run
+ * on the GPU; the greedy band growth and candidate emission run on the host.
+ * Tracking (Detector::update_tracks) is not part of this interface.
+ * ===================================================================== */
+typedef struct rv_detector_config {
+    int64_t source_rate;          /* source samples per second */
+    int64_t source_center;        /* Hz */
+    uint32_t bins;                /* SpectrumGeometry::bins */
+    uint32_t noise_knots;         /* DetectorConfig defaults in brackets: 32 */
+    int64_t bin_width_numerator;  /* SpectrumGeometry's exact bin width and bin-0 frequency */
+    int64_t bin_width_denominator;
+    int64_t bin_zero_numerator;
+    int64_t bin_zero_denominator;
+    double detection_threshold_db;    /* 6 */
+    double average_seconds;           /* 1 */
+    double decision_interval_seconds; /* 0.1 */
+    uint32_t noise_window_knots;      /* 8 */
+    uint32_t max_sum_bins;            /* 0: bit_floor(bins / 8) */
+    double noise_percentile;          /* 0.10 */
+    double noise_percentile_high;     /* 0.40 */
+    double noise_excision_sigma;      /* 4 */
+    uint32_t max_peaks;               /* 0: bins */
+    uint32_t split_gap_bins;          /* 8 */
+    double edge_floor_fraction;       /* 0 */
+    double edge_floor_sigma;          /* 3 */
+    double occupied_power_fraction;   /* 0.99 */
+    double split_gap_db;              /* 1 */
+    double residual_rate_tolerance;   /* 0.25 */
+    uint32_t residual_decisions;      /* 4 */
+    uint32_t reserved;
+} rv_detector_config;
+
+/* Candidate + BandShape (core/detect/detector.h:299-359, shape.h:53-75). */
+typedef struct rv_detector_candidate {
+    int64_t center;               /* Hz */
+    int64_t bandwidth;            /* Hz */
+    double snr_2500_db;
+    double margin_confidence;
+    double noise_floor_dbfs;
+    double peak_dbfs;
+    uint32_t first_bin;
+    uint32_t last_bin;
+    double peak_to_mean;
+    double concentration;
+    double lower_fraction;
+    double skirt_fraction;
+    uint64_t skirt_bins_available;
+    uint32_t measured;
+    uint32_t reserved;
+} rv_detector_candidate;
+
+typedef struct rv_detector_stats {
+    uint64_t frames;
+    uint64_t decisions;
+    uint64_t frames_rejected;
+    uint64_t candidates;             /* summed over decisions, after residual rejection */
+    uint64_t peaks_overflowed;
+    uint64_t candidates_residual;
+    uint64_t residual_parts_degenerate;
+    double device_ms;                /* stream time of the consume calls (CUDA events): kernels,
+                                      * read-backs and the waits for the decisions' host part */
+    double host_ms;                  /* host part of the decisions */
+} rv_detector_stats;
+
+typedef struct rv_detector rv_detector;
+/* Detector::create: the same validation and derived constants. */
+int32_t rv_detector_create(rv_context* context, const rv_detector_config* config, rv_detector** out);
+int32_t rv_detector_destroy(rv_detector* detector);
+/* Detector::consume of one frame of `bins` dB values (where = 0: host memory,
+ * 1: device memory) covering source samples [start, start + count); *decided
+ * is 1 when the frame completed a decision. */
+int32_t rv_detector_consume(rv_detector* detector, const float* power_db, uint64_t start, uint64_t count,
+                            int32_t where, int32_t* decided);
+/* `frames` consecutive frames at power_db + f * bins, frame f covering
+ * [start + f * hop, start + f * hop + count): consume() for each, with the
+ * averaging of all the frames up to each decision in one launch. Returns the
+ * number of decisions in *decisions; candidates() then holds the last one's. */
+int32_t rv_detector_consume_frames(rv_detector* detector, const float* power_db, uint32_t frames, uint64_t start,
+                                   uint64_t hop, uint64_t count, int32_t where, uint32_t* decisions);
+/* Detector::candidates after the latest decision. */
+int32_t rv_detector_candidates(const rv_detector* detector, rv_detector_candidate* out, uint32_t capacity,
+                               uint32_t* count);
+/* Detector::averaged_power / noise_floor (bins doubles each; either may be NULL). */
+int32_t rv_detector_state(rv_detector* detector, double* average, double* floor, uint64_t bins);
+int32_t rv_detector_get_stats(const rv_detector* detector, rv_detector_stats* stats);
+
+/* ===================================================================== *
  * Host planning (core/dsp/pfb_design.cpp, vrx_reference.cpp,             *
  * core/engine/vrx_place.cpp), restated; results equal the reference's.   *
  * ===================================================================== */

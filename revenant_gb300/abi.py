@@ -5,7 +5,7 @@ sizes and that the shared library exports every declared entry point.
 """
 import ctypes as C
 
-U32, U64, I32, I64, F32 = C.c_uint32, C.c_uint64, C.c_int32, C.c_int64, C.c_float
+U32, U64, I32, I64, F32, F64 = C.c_uint32, C.c_uint64, C.c_int32, C.c_int64, C.c_float, C.c_double
 
 RV_OK = 0
 RV_ERR_INVALID = -1
@@ -112,6 +112,30 @@ AVERAGE_MEAN, AVERAGE_EXPONENTIAL = 0, 1
 WINDOW_RECTANGULAR, WINDOW_HANN, WINDOW_BLACKMAN_HARRIS = 0, 1, 2
 
 
+class DetectorConfig(_S):
+    _fields_ = [("source_rate", I64), ("source_center", I64), ("bins", U32), ("noise_knots", U32),
+                ("bin_width_numerator", I64), ("bin_width_denominator", I64), ("bin_zero_numerator", I64),
+                ("bin_zero_denominator", I64), ("detection_threshold_db", F64), ("average_seconds", F64),
+                ("decision_interval_seconds", F64), ("noise_window_knots", U32), ("max_sum_bins", U32),
+                ("noise_percentile", F64), ("noise_percentile_high", F64), ("noise_excision_sigma", F64),
+                ("max_peaks", U32), ("split_gap_bins", U32), ("edge_floor_fraction", F64),
+                ("edge_floor_sigma", F64), ("occupied_power_fraction", F64), ("split_gap_db", F64),
+                ("residual_rate_tolerance", F64), ("residual_decisions", U32), ("reserved", U32)]
+
+
+class DetectorCandidate(_S):
+    _fields_ = [("center", I64), ("bandwidth", I64), ("snr_2500_db", F64), ("margin_confidence", F64),
+                ("noise_floor_dbfs", F64), ("peak_dbfs", F64), ("first_bin", U32), ("last_bin", U32),
+                ("peak_to_mean", F64), ("concentration", F64), ("lower_fraction", F64), ("skirt_fraction", F64),
+                ("skirt_bins_available", U64), ("measured", U32), ("reserved", U32)]
+
+
+class DetectorStats(_S):
+    _fields_ = [("frames", U64), ("decisions", U64), ("frames_rejected", U64), ("candidates", U64),
+                ("peaks_overflowed", U64), ("candidates_residual", U64), ("residual_parts_degenerate", U64),
+                ("device_ms", F64), ("host_ms", F64)]
+
+
 class VrxRequest(_S):
     _fields_ = [("center", I64), ("bandwidth", I64), ("passband_low", I64), ("passband_high", I64),
                 ("demod", U32), ("deemphasis", U32), ("stereo", U32), ("reserved", U32),
@@ -169,7 +193,8 @@ class ChainStats(_S):
                 ("graph_captures", U64), ("graph_ms", C.c_double), ("host_ms", C.c_double)]
 
 
-EXTRA_STRUCTS = {"rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
+EXTRA_STRUCTS = {"rv_detector_config": DetectorConfig, "rv_detector_candidate": DetectorCandidate,
+                 "rv_detector_stats": DetectorStats, "rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
 
 
 def request(center=0, bandwidth=0, demod="nfm", deemphasis=0, stereo=True, audio_rate=0,

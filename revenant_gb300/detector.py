@@ -1,0 +1,79 @@
+"""Host mirror of the wideband detector API (rv_detector_*).
+
+``Detector(device, config)`` wraps one rv_detector: feed spectrum frames with
+``consume(frame_db, start, count)`` or many at once with ``consume_frames``,
+read the latest decision's ``candidates()`` and the ``state()`` arrays. All the
+work happens in librevenant_gb300.so.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .library import check, lib
+
+CANDIDATE_DTYPE = np.dtype([(name, np.int64 if t is C.c_int64 else np.uint64 if t is C.c_uint64 else
+                             np.uint32 if t is C.c_uint32 else np.float64)
+                            for name, t in abi.DetectorCandidate._fields_])
+
+
+class Detector:
+    def __init__(self, device, config):
+        self.device = device
+        self.config = config
+        self.bins = config.bins
+        handle = C.c_void_p()
+        check(lib().rv_detector_create(device.handle, C.byref(config), C.byref(handle)))
+        self.handle = handle
+
+    def consume(self, frame_db, start, count):
+        """One frame (numpy float32 of `bins` values on the host); True when it decided."""
+        frame = np.ascontiguousarray(frame_db, np.float32)
+        decided = C.c_int32()
+        check(lib().rv_detector_consume(self.handle, frame.ctypes.data, start, count, 0, C.byref(decided)))
+        return bool(decided.value)
+
+    def consume_frames(self, frames, start, hop, count, device=False):
+        """frames: numpy [n][bins] float32 on the host, or a device address (device=True, n = frames)."""
+        made = C.c_uint32()
+        if device:
+            address, n = frames
+            check(lib().rv_detector_consume_frames(self.handle, address, n, start, hop, count, 1, C.byref(made)))
+        else:
+            f = np.ascontiguousarray(frames, np.float32)
+            check(lib().rv_detector_consume_frames(self.handle, f.ctypes.data, f.shape[0], start, hop, count, 0,
+                                                   C.byref(made)))
+        return made.value
+
+    def candidates(self):
+        n = C.c_uint32()
+        check(lib().rv_detector_candidates(self.handle, None, 0, C.byref(n)))
+        buf = (abi.DetectorCandidate * max(n.value, 1))()
+        check(lib().rv_detector_candidates(self.handle, buf, n.value, C.byref(n)))
+        out = np.zeros(n.value, CANDIDATE_DTYPE)
+        for i in range(n.value):
+            for name, _ in abi.DetectorCandidate._fields_:
+                out[i][name] = getattr(buf[i], name)
+        return out
+
+    def state(self):
+        avg = np.zeros(self.bins, np.float64)
+        flo = np.zeros(self.bins, np.float64)
+        check(lib().rv_detector_state(self.handle, avg.ctypes.data, flo.ctypes.data, self.bins))
+        return avg, flo
+
+    def stats(self):
+        s = abi.DetectorStats()
+        check(lib().rv_detector_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def close(self):
+        if self.handle:
+            lib().rv_detector_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

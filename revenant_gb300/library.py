@@ -157,6 +157,13 @@ SIGNATURES = {
     "rv_chain_read_audio": (I32, [P, U32, P, U64, ptr(U64)]),
     "rv_chain_get_stats": (I32, [P, ptr(abi.ChainStats)]),
     "rv_chain_capture_graph": (I32, [P]),
+    "rv_detector_create": (I32, [P, ptr(abi.DetectorConfig), ptr(P)]),
+    "rv_detector_destroy": (I32, [P]),
+    "rv_detector_consume": (I32, [P, P, U64, U64, I32, ptr(I32)]),
+    "rv_detector_consume_frames": (I32, [P, P, U32, U64, U64, U64, I32, ptr(U32)]),
+    "rv_detector_candidates": (I32, [P, P, U32, ptr(U32)]),
+    "rv_detector_state": (I32, [P, P, P, U64]),
+    "rv_detector_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
     "rv_chain_drain": (I32, [P]),
     "rv_chain_channel_ring": (I32, [P, ptr(P), ptr(U32)]),
     "rv_chain_receiver_rings": (I32, [P, U32, ptr(P), ptr(P), ptr(U32)]),

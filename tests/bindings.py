@@ -170,3 +170,42 @@ def cf32(n):
 
 def same_bits(a, b):
     return np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
+
+
+_detref = None
+
+
+def detector_reference():
+    """The reference's own wideband detector (oracle/_ref/libdetref.so), or None."""
+    global _detref
+    if _detref is None:
+        path = os.path.join(ROOT, "oracle", "_ref", "libdetref.so")
+        if not os.path.exists(path):
+            return None
+        lib = C.CDLL(path)
+        lib.refdet_last_error.restype = C.c_char_p
+        lib.refdet_create.restype = I32
+        lib.refdet_create.argtypes = [ptr(abi.DetectorConfig), ptr(P)]
+        lib.refdet_destroy.restype = None
+        lib.refdet_destroy.argtypes = [P]
+        lib.refdet_consume.restype = I32
+        lib.refdet_consume.argtypes = [P, P, U64, U64, ptr(I32)]
+        lib.refdet_candidates.restype = I32
+        lib.refdet_candidates.argtypes = [P, P, U32, ptr(U32)]
+        lib.refdet_state.restype = I32
+        lib.refdet_state.argtypes = [P, P, P, U64]
+        lib.refdet_stats.restype = I32
+        lib.refdet_stats.argtypes = [P, ptr(abi.DetectorStats)]
+        _detref = lib
+    return _detref
+
+
+def candidates_array(cands):
+    """ctypes candidates -> numpy structured array (one row each)."""
+    dt = np.dtype([(name, np.int64 if t in (C.c_int64,) else np.uint64 if t is C.c_uint64 else
+                    np.uint32 if t is C.c_uint32 else np.float64) for name, t in abi.DetectorCandidate._fields_])
+    out = np.zeros(len(cands), dt)
+    for i, c in enumerate(cands):
+        for name, _ in abi.DetectorCandidate._fields_:
+            out[i][name] = getattr(c, name)
+    return out
