@@ -49,6 +49,7 @@ constexpr uint32_t kFineWindow = 6144;   // float2 per fine work item (48 KB)
 constexpr uint32_t kDetWindow = 8192;    // floats per detector / audio item (32 KB)
 constexpr uint32_t kMaxItem = kRxThreads;
 constexpr uint64_t kMaxLerpEntries = 1u << 20;
+constexpr uint32_t kTileShare = 2;  // fine tiles aim at this many CTAs per SM
 
 uint64_t bit_ceil64(uint64_t v) {
     uint64_t p = 1;
@@ -843,8 +844,11 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
         } else {
             r.max_unit_item = (uint32_t)std::min<uint64_t>(kUnitThreads, (avail - T) / step_max + 1u);
         }
-        // the 2D tiles take over where a table slice and a chunk of rows fit
-        plan_tiles(r, fc, fd, c->unit_budget);
+        // the 2D tiles take over where a table slice and a chunk of rows fit;
+        // a shape within `tile_share` of shared memory leaves room for more
+        // CTAs per SM (measured: two per SM beat one with twice the rows)
+        plan_tiles(r, fc, fd, c->unit_budget / kTileShare - 128u);
+        if (r.tile_cols == 0) plan_tiles(r, fc, fd, c->unit_budget);
         if (r.tile_cols != 0) c->tile_shared = std::max(c->tile_shared, r.tile_shared);
     }
     if (!st) st = r.d_fine.alloc(cap);
