@@ -482,8 +482,15 @@ typedef struct rv_chain_config {
     uint32_t max_run_samples; /* largest count one rv_chain_run may carry */
     uint32_t keep_audio;      /* 1: accumulate audio for rv_chain_read_audio */
     double attenuation_db;    /* prototype stopband target, 0 = 120 dB */
-    uint32_t profile;         /* 1: time each stage with CUDA events into rv_chain_stats */
-    uint32_t reserved2;
+    uint32_t profile;         /* 1: time each stage with CUDA events into rv_chain_stats
+                               * (not with pipelined runs) */
+    uint32_t pipelined;       /* batched only. 1: rv_chain_run returns once the run is queued;
+                               * the next run is prepared, and its input copied on a second
+                               * stream, while this one executes. A run's audio reaches
+                               * rv_chain_read_audio when the run after next begins or at
+                               * rv_chain_drain (read_audio, receiver_info and get_stats
+                               * drain first). Host input must stay valid and unchanged
+                               * until the next rv_chain_run or rv_chain_drain returns. */
 } rv_chain_config;
 
 typedef struct rv_chain_stats {

@@ -183,7 +183,7 @@ CHAIN_BATCHED, CHAIN_PLAIN = 0, 1
 class ChainConfig(_S):
     _fields_ = [("grid", GridParams), ("reserved", U32), ("rate", I64), ("format", I32), ("mode", I32),
                 ("max_run_samples", U32), ("keep_audio", U32), ("attenuation_db", C.c_double),
-                ("profile", U32), ("reserved2", U32)]
+                ("profile", U32), ("pipelined", U32)]
 
 
 class ChainStats(_S):

@@ -16,7 +16,7 @@ from .library import check, lib
 
 class Chain:
     def __init__(self, device, grid=(64, 17, 32), rate=20_000_000, fmt=abi.FORMAT_CS16, mode=abi.CHAIN_BATCHED,
-                 max_run_samples=1 << 20, keep_audio=True, attenuation_db=120.0, profile=False):
+                 max_run_samples=1 << 20, keep_audio=True, attenuation_db=120.0, profile=False, pipelined=False):
         self.device = device
         cfg = abi.ChainConfig()
         cfg.grid = abi.GridParams(*grid)
@@ -27,6 +27,7 @@ class Chain:
         cfg.keep_audio = 1 if keep_audio else 0
         cfg.attenuation_db = attenuation_db
         cfg.profile = 1 if profile else 0
+        cfg.pipelined = 1 if pipelined else 0
         self.config = cfg
         self.bytes_per_sample = 4 if fmt == abi.FORMAT_CS16 else 2
         handle = C.c_void_p()

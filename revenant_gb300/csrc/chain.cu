@@ -152,6 +152,50 @@ struct GraphShape {
     const void* units_ptr = nullptr;
 };
 
+// The buffers one run's launches read and write, its captured graph and its
+// audio on the way to the host. A pipelined chain alternates two, so that one
+// run is prepared and its input copied while the previous one executes.
+struct RunSlot {
+    PinnedArray<WorkItem> items_host;
+    DeviceArray<WorkItem> items_dev;
+    DeviceArray<Queues> queues;
+    DeviceArray<FineUnit> units_dev;
+    PinnedArray<FineUnit> units_host;
+    DeviceArray<FineTile> tiles_dev;
+    PinnedArray<FineTile> tiles_host;
+    DeviceArray<uint8_t> spans_dev;   // RxRun[nrx], detector prefix [nrx + 1], audio prefix [nrx + 1]
+    PinnedArray<uint8_t> spans_host;
+    DeviceArray<float> audio_dev;
+    PinnedArray<float> audio_host;
+    cudaGraphExec_t exec = nullptr;
+    GraphShape shape{};
+    DeviceArray<RunCounts> counts_dev;
+    PinnedArray<RunCounts> counts_host;
+    cudaEvent_t done = nullptr;  // recorded after the run's audio read-back
+    bool pending = false;        // audio not yet handed to the receivers
+    uint64_t audio_floats = 0;
+    std::vector<std::pair<uint64_t, uint64_t>> parts;  // per receiver: audio offset (floats), frames
+    void release() {
+        items_host.release();
+        items_dev.release();
+        queues.release();
+        units_dev.release();
+        units_host.release();
+        tiles_dev.release();
+        tiles_host.release();
+        spans_dev.release();
+        spans_host.release();
+        audio_dev.release();
+        audio_host.release();
+        counts_dev.release();
+        counts_host.release();
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        if (done) cudaEventDestroy(done);
+        done = nullptr;
+    }
+};
+
 }  // namespace
 
 struct rv_chain {
@@ -174,21 +218,14 @@ struct rv_chain {
     std::vector<Receiver> rx;
     DeviceArray<RxDev> rx_table;
     bool table_dirty = true;
-    // per-run work lists and audio
-    PinnedArray<WorkItem> items_host;
-    DeviceArray<WorkItem> items_dev;
-    DeviceArray<Queues> queues;
-    DeviceArray<FineUnit> units_dev;
-    PinnedArray<FineUnit> units_host;
-    DeviceArray<FineTile> tiles_dev;
-    PinnedArray<FineTile> tiles_host;
-    DeviceArray<uint8_t> spans_dev;   // RxRun[nrx], detector prefix [nrx + 1], audio prefix [nrx + 1]
-    PinnedArray<uint8_t> spans_host;
+    // per-run buffers: slot 0 only, or both alternately when pipelined
+    RunSlot slots[2];
+    uint32_t cur = 0;
+    cudaStream_t copy_stream = nullptr;  // pipelined: input copies
+    cudaEvent_t input_ready = nullptr;
     uint32_t unit_budget = 0;
     uint32_t tile_shared = 0;   // float2 of shared memory per tile CTA (largest tiled receiver)
     uint32_t weights_cap = 32;  // largest staged demodulator weight table (floats)
-    DeviceArray<float> audio_dev;
-    PinnedArray<float> audio_host;
     uint64_t samples_in = 0;
     uint64_t next_block = 0;
     rv_chain_stats stats{};
@@ -197,18 +234,19 @@ struct rv_chain {
     // captured runs (rv_chain_capture_graph)
     bool graph = false;
     bool captured_run = false;  // this run replayed the graph
-    cudaGraphExec_t exec = nullptr;
-    GraphShape shape{};
-    DeviceArray<RunCounts> counts_dev;
-    PinnedArray<RunCounts> counts_host;
 };
 
 namespace {
+RunSlot& S(rv_chain* c) { return c->slots[c->cur]; }
+bool pipelined(const rv_chain* c) { return c->config.pipelined != 0; }
+}  // namespace
+
+namespace {
 void mark(rv_chain* c, int i) {
-    if (c->config.profile && c->marks[i]) cudaEventRecord(c->marks[i], c->stream);
+    if (c->config.profile && !pipelined(c) && c->marks[i]) cudaEventRecord(c->marks[i], c->stream);
 }
 void collect_marks(rv_chain* c) {
-    if (!c->config.profile) return;
+    if (!c->config.profile || pipelined(c)) return;
     float ms[5] = {0, 0, 0, 0, 0};
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&ms[i], c->marks[i], c->marks[i + 1]);
     c->stats.input_ms += ms[0];
@@ -225,6 +263,29 @@ void collect_marks(rv_chain* c) {
 }  // namespace
 
 namespace {
+
+// Hands a finished run's audio to its receivers (waits for the run first).
+int32_t collect_slot(rv_chain* c, RunSlot& sl) {
+    if (!sl.pending) return RV_OK;
+    if (int32_t st = cuda_status(cudaEventSynchronize(sl.done), "run completion")) return st;
+    sl.pending = false;
+    for (size_t i = 0; i < sl.parts.size() && i < c->rx.size(); ++i) {
+        Receiver& r = c->rx[i];
+        const uint64_t frames = sl.parts[i].second, n = frames * r.plan.demod.channels;
+        if (c->config.keep_audio && n)
+            r.audio.insert(r.audio.end(), sl.audio_host.ptr + sl.parts[i].first, sl.audio_host.ptr + sl.parts[i].first + n);
+        r.audio_frames_total += frames;
+    }
+    c->stats.audio_bytes += sl.audio_floats * sizeof(float);
+    return RV_OK;
+}
+
+// Every run still in flight, oldest first (the current slot holds the older
+// one after a pipelined run flipped it).
+int32_t collect_all(rv_chain* c) {
+    if (int32_t st = collect_slot(c, c->slots[c->cur])) return st;
+    return collect_slot(c, c->slots[c->cur ^ 1u]);
+}
 
 int32_t upload_table(rv_chain* c) {
     std::vector<RxDev> table(c->rx.size());
@@ -290,14 +351,21 @@ int32_t copy_into_ring(rv_chain* c, uint8_t* ring, uint64_t ring_samples, uint64
                        uint64_t count, int32_t where) {
     const uint64_t bps = c->bytes_per_sample;
     const cudaMemcpyKind kind = where ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    // pipelined: on the copy stream, overlapping the previous run's kernels
+    // (the ring holds two runs beyond the filter history, so this run's
+    // samples never land where a run still in flight reads)
+    cudaStream_t s = pipelined(c) ? c->copy_stream : c->stream;
     uint64_t done = 0;
     while (done < count) {
         const uint64_t at = (pos + done) % ring_samples;
         const uint64_t n = std::min<uint64_t>(count - done, ring_samples - at);
-        if (int32_t st = cuda_status(cudaMemcpyAsync(ring + at * bps, src + done * bps, n * bps, kind, c->stream),
-                                     "input copy"))
+        if (int32_t st = cuda_status(cudaMemcpyAsync(ring + at * bps, src + done * bps, n * bps, kind, s), "input copy"))
             return st;
         done += n;
+    }
+    if (pipelined(c)) {
+        if (int32_t st = cuda_status(cudaEventRecord(c->input_ready, s), "input event")) return st;
+        if (int32_t st = cuda_status(cudaStreamWaitEvent(c->stream, c->input_ready, 0), "input wait")) return st;
     }
     return RV_OK;
 }
@@ -494,7 +562,7 @@ size_t span_bytes(size_t nrx) { return nrx * sizeof(RxRun) + 2u * (nrx + 1u) * s
 
 // Device addresses of the span table's parts for `nrx` receivers.
 void span_lists(rv_chain* c, uint32_t nrx, SpanList* det, SpanList* audio) {
-    const uint8_t* base = c->spans_dev.ptr;
+    const uint8_t* base = S(c).spans_dev.ptr;
     const RxRun* runs = reinterpret_cast<const RxRun*>(base);
     const uint32_t* dp = reinterpret_cast<const uint32_t*>(base + nrx * sizeof(RxRun));
     *det = SpanList{runs, dp, nrx, 0u};
@@ -504,34 +572,34 @@ void span_lists(rv_chain* c, uint32_t nrx, SpanList* det, SpanList* audio) {
 // Copies the span table to the device (capacity kept from earlier runs).
 int32_t upload_spans(rv_chain* c, const SpanTable& t) {
     const size_t nrx = t.runs.size(), bytes = span_bytes(nrx);
-    if (c->spans_dev.count < bytes)
-        if (int32_t st = c->spans_dev.alloc(bytes + bytes / 2)) return st;
-    if (int32_t st = c->spans_host.reserve(bytes + bytes / 2)) return st;
-    uint8_t* h = c->spans_host.ptr;
+    if (S(c).spans_dev.count < bytes)
+        if (int32_t st = S(c).spans_dev.alloc(bytes + bytes / 2)) return st;
+    if (int32_t st = S(c).spans_host.reserve(bytes + bytes / 2)) return st;
+    uint8_t* h = S(c).spans_host.ptr;
     memcpy(h, t.runs.data(), nrx * sizeof(RxRun));
     memcpy(h + nrx * sizeof(RxRun), t.det_prefix.data(), (nrx + 1u) * sizeof(uint32_t));
     memcpy(h + nrx * sizeof(RxRun) + (nrx + 1u) * sizeof(uint32_t), t.audio_prefix.data(), (nrx + 1u) * sizeof(uint32_t));
-    return cuda_status(cudaMemcpyAsync(c->spans_dev.ptr, h, bytes, cudaMemcpyHostToDevice, c->stream), "span upload");
+    return cuda_status(cudaMemcpyAsync(S(c).spans_dev.ptr, h, bytes, cudaMemcpyHostToDevice, c->stream), "span upload");
 }
 
 // Records the coarse kernel and every batched receiver kernel, reading their
-// counts and the coarse parameters from c->counts_dev, into one graph.
+// counts and the coarse parameters from S(c).counts_dev, into one graph.
 int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
-    const GraphShape& sh = c->shape;
+    const GraphShape& sh = S(c).shape;
     const Sections o(sh);
-    RunCounts* rc = c->counts_dev.ptr;
+    RunCounts* rc = S(c).counts_dev.ptr;
     const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
-    WorkItem* items = c->items_dev.ptr;
+    WorkItem* items = S(c).items_dev.ptr;
     cudaGraph_t graph = nullptr;
     if (int32_t st = cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "graph capture begin"))
         return st;
     int32_t st = launch_coarse_fused(c->stream, c->config.grid, c->config.format, coarse, c->raw.ptr, c->proto.ptr,
                                      c->twiddles.ptr, c->channel.ptr, &rc->coarse);
     if (!st)
-        st = launch_fine_tiles(c->stream, c->rx_table.ptr, c->tiles_dev.ptr, sh.tiles, chan, sh.tile_shared,
+        st = launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, sh.tiles, chan, sh.tile_shared,
                                &rc->queues.tiles, &rc->tiles);
     if (!st)
-        st = launch_fine_units(c->stream, c->rx_table.ptr, items, c->units_dev.ptr, sh.units, chan, c->unit_budget,
+        st = launch_fine_units(c->stream, c->rx_table.ptr, items, S(c).units_dev.ptr, sh.units, chan, c->unit_budget,
                                &rc->queues.units, &rc->units);
     if (!st)
         st = launch_fine_batched(c->stream, c->rx_table.ptr, items + o.fine, sh.fine, chan, sh.fine_window,
@@ -543,17 +611,17 @@ int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
         st = launch_detect_batched(c->stream, c->rx_table.ptr, det, sh.nrx, kDetWindow, &rc->queues.detect,
                                    &rc->detect);
     if (!st)
-        st = launch_audio_batched(c->stream, c->rx_table.ptr, audio, sh.nrx, c->audio_dev.ptr, kDetWindow,
+        st = launch_audio_batched(c->stream, c->rx_table.ptr, audio, sh.nrx, S(c).audio_dev.ptr, kDetWindow,
                                   sh.weights_cap, &rc->queues.audio, &rc->audio);
     const int32_t end = cuda_status(cudaStreamEndCapture(c->stream, &graph), "graph capture end");
     if (st || end) {
         if (graph) cudaGraphDestroy(graph);
         return st ? st : end;
     }
-    st = cuda_status(cudaGraphInstantiate(&c->exec, graph, 0), "graph instantiate");
+    st = cuda_status(cudaGraphInstantiate(&S(c).exec, graph, 0), "graph instantiate");
     cudaGraphDestroy(graph);
     if (st) {
-        c->exec = nullptr;
+        S(c).exec = nullptr;
         return st;
     }
     c->stats.graph_captures += 1;
@@ -568,19 +636,19 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
                      const std::vector<WorkItem>& unit_items, const std::vector<FineUnit>& units,
                      const std::vector<FineTile>& tiles, uint32_t fine_window) {
     const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
-    GraphShape& sh = c->shape;
+    GraphShape& sh = S(c).shape;
     const uint32_t nrx = (uint32_t)spans.runs.size();
     if (int32_t st = upload_spans(c, spans)) return st;
-    const bool fits = c->exec != nullptr && fine.size() <= sh.fine && carrier.size() <= sh.carrier &&
-                      sh.nrx == nrx && sh.spans_ptr == c->spans_dev.ptr && unit_items.size() <= sh.unit_items &&
+    const bool fits = S(c).exec != nullptr && fine.size() <= sh.fine && carrier.size() <= sh.carrier &&
+                      sh.nrx == nrx && sh.spans_ptr == S(c).spans_dev.ptr && unit_items.size() <= sh.unit_items &&
                       units.size() <= sh.units && tiles.size() <= sh.tiles && sh.tile_shared == c->tile_shared &&
-                      sh.tiles_ptr == c->tiles_dev.ptr && window <= sh.fine_window && sh.weights_cap == c->weights_cap &&
-                      sh.unit_budget == c->unit_budget && sh.audio_ptr == c->audio_dev.ptr &&
-                      sh.table_ptr == c->rx_table.ptr && sh.items_ptr == c->items_dev.ptr &&
-                      sh.units_ptr == c->units_dev.ptr;
+                      sh.tiles_ptr == S(c).tiles_dev.ptr && window <= sh.fine_window && sh.weights_cap == c->weights_cap &&
+                      sh.unit_budget == c->unit_budget && sh.audio_ptr == S(c).audio_dev.ptr &&
+                      sh.table_ptr == c->rx_table.ptr && sh.items_ptr == S(c).items_dev.ptr &&
+                      sh.units_ptr == S(c).units_dev.ptr;
     if (!fits) {
-        if (c->exec) cudaGraphExecDestroy(c->exec);
-        c->exec = nullptr;
+        if (S(c).exec) cudaGraphExecDestroy(S(c).exec);
+        S(c).exec = nullptr;
         auto grow = [](size_t need, uint32_t old) {
             return (uint32_t)std::max<size_t>(old, need == 0 ? 0 : need + need / 2 + 16);
         };
@@ -588,7 +656,7 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
         n.fine = grow(fine.size(), sh.fine);
         n.carrier = grow(carrier.size(), sh.carrier);
         n.nrx = nrx;
-        n.spans_ptr = c->spans_dev.ptr;
+        n.spans_ptr = S(c).spans_dev.ptr;
         n.unit_items = grow(unit_items.size(), sh.unit_items);
         n.units = grow(units.size(), sh.units);
         n.tiles = grow(tiles.size(), sh.tiles);
@@ -597,27 +665,27 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
         n.weights_cap = c->weights_cap;
         n.unit_budget = c->unit_budget;
         const size_t total = Sections(n).total;
-        if (c->items_dev.count < total + 1)
-            if (int32_t st = c->items_dev.alloc(total + 1)) return st;
-        if (c->units_dev.count < (size_t)n.units + 1)
-            if (int32_t st = c->units_dev.alloc(n.units + 1)) return st;
-        if (c->tiles_dev.count < (size_t)n.tiles + 1)
-            if (int32_t st = c->tiles_dev.alloc(n.tiles + 1)) return st;
-        if (c->counts_dev.count == 0)
-            if (int32_t st = c->counts_dev.alloc(1)) return st;
-        n.audio_ptr = c->audio_dev.ptr;
+        if (S(c).items_dev.count < total + 1)
+            if (int32_t st = S(c).items_dev.alloc(total + 1)) return st;
+        if (S(c).units_dev.count < (size_t)n.units + 1)
+            if (int32_t st = S(c).units_dev.alloc(n.units + 1)) return st;
+        if (S(c).tiles_dev.count < (size_t)n.tiles + 1)
+            if (int32_t st = S(c).tiles_dev.alloc(n.tiles + 1)) return st;
+        if (S(c).counts_dev.count == 0)
+            if (int32_t st = S(c).counts_dev.alloc(1)) return st;
+        n.audio_ptr = S(c).audio_dev.ptr;
         n.table_ptr = c->rx_table.ptr;
-        n.items_ptr = c->items_dev.ptr;
-        n.units_ptr = c->units_dev.ptr;
-        n.tiles_ptr = c->tiles_dev.ptr;
+        n.items_ptr = S(c).items_dev.ptr;
+        n.units_ptr = S(c).units_dev.ptr;
+        n.tiles_ptr = S(c).tiles_dev.ptr;
         sh = n;
     }
     const Sections o(sh);
-    if (int32_t st = c->items_host.reserve(o.total + 1)) return st;
-    if (int32_t st = c->units_host.reserve((size_t)sh.units + 1)) return st;
-    if (int32_t st = c->tiles_host.reserve((size_t)sh.tiles + 1)) return st;
-    if (int32_t st = c->counts_host.reserve(1)) return st;
-    RunCounts* rc = c->counts_host.ptr;
+    if (int32_t st = S(c).items_host.reserve(o.total + 1)) return st;
+    if (int32_t st = S(c).units_host.reserve((size_t)sh.units + 1)) return st;
+    if (int32_t st = S(c).tiles_host.reserve((size_t)sh.tiles + 1)) return st;
+    if (int32_t st = S(c).counts_host.reserve(1)) return st;
+    RunCounts* rc = S(c).counts_host.ptr;
     memset(rc, 0, sizeof *rc);
     rc->units = (uint32_t)units.size();
     rc->fine = (uint32_t)fine.size();
@@ -626,42 +694,42 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
     rc->audio = spans.audio_total;
     rc->tiles = (uint32_t)tiles.size();
     rc->coarse = coarse;
-    if (int32_t st = cuda_status(cudaMemcpyAsync(c->counts_dev.ptr, rc, sizeof *rc, cudaMemcpyHostToDevice, c->stream),
+    if (int32_t st = cuda_status(cudaMemcpyAsync(S(c).counts_dev.ptr, rc, sizeof *rc, cudaMemcpyHostToDevice, c->stream),
                                  "run counts upload"))
         return st;
     const std::pair<const std::vector<WorkItem>*, size_t> lists[] = {
         {&fine, o.fine}, {&carrier, o.carrier}, {&unit_items, o.unit}};
     for (const auto& l : lists) {
         if (l.first->empty()) continue;
-        WorkItem* h = c->items_host.ptr + l.second;
+        WorkItem* h = S(c).items_host.ptr + l.second;
         memcpy(h, l.first->data(), l.first->size() * sizeof(WorkItem));
-        if (int32_t st = cuda_status(cudaMemcpyAsync(c->items_dev.ptr + l.second, h, l.first->size() * sizeof(WorkItem),
+        if (int32_t st = cuda_status(cudaMemcpyAsync(S(c).items_dev.ptr + l.second, h, l.first->size() * sizeof(WorkItem),
                                                      cudaMemcpyHostToDevice, c->stream),
                                      "work list upload"))
             return st;
     }
     if (!units.empty()) {
         for (size_t i = 0; i < units.size(); ++i) {
-            c->units_host.ptr[i] = units[i];
-            c->units_host.ptr[i].first_item += (uint32_t)o.unit;
+            S(c).units_host.ptr[i] = units[i];
+            S(c).units_host.ptr[i].first_item += (uint32_t)o.unit;
         }
-        if (int32_t st = cuda_status(cudaMemcpyAsync(c->units_dev.ptr, c->units_host.ptr, units.size() * sizeof(FineUnit),
+        if (int32_t st = cuda_status(cudaMemcpyAsync(S(c).units_dev.ptr, S(c).units_host.ptr, units.size() * sizeof(FineUnit),
                                                      cudaMemcpyHostToDevice, c->stream),
                                      "unit upload"))
             return st;
     }
     if (!tiles.empty()) {
-        memcpy(c->tiles_host.ptr, tiles.data(), tiles.size() * sizeof(FineTile));
-        if (int32_t st = cuda_status(cudaMemcpyAsync(c->tiles_dev.ptr, c->tiles_host.ptr, tiles.size() * sizeof(FineTile),
+        memcpy(S(c).tiles_host.ptr, tiles.data(), tiles.size() * sizeof(FineTile));
+        if (int32_t st = cuda_status(cudaMemcpyAsync(S(c).tiles_dev.ptr, S(c).tiles_host.ptr, tiles.size() * sizeof(FineTile),
                                                      cudaMemcpyHostToDevice, c->stream),
                                      "tile upload"))
             return st;
     }
-    if (c->exec == nullptr)
+    if (S(c).exec == nullptr)
         if (int32_t st = capture(c, coarse)) return st;
     mark(c, 2);
     mark(c, 3);
-    if (int32_t st = cuda_status(cudaGraphLaunch(c->exec, c->stream), "graph launch")) return st;
+    if (int32_t st = cuda_status(cudaGraphLaunch(S(c).exec, c->stream), "graph launch")) return st;
     mark(c, 4);
     c->stats.graph_launches += 1;
     c->stats.launches += 1 + (sh.units ? 1 : 0) + (sh.fine ? 1 : 0) + (sh.carrier ? 1 : 0) + (sh.nrx ? 2 : 0) +
@@ -691,6 +759,8 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
                              (long long)config->rate, g.decimation);
     if (config->max_run_samples == 0 || config->max_run_samples > (1u << 30))
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: max_run_samples must be in [1, 2^30]");
+    if (config->pipelined > 1u || (config->pipelined && config->mode != RV_CHAIN_BATCHED))
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: pipelined runs are a batched-chain mode (pipelined = 1)");
     rv_chain* c = new (std::nothrow) rv_chain;
     if (c == nullptr) return set_error_fmt(RV_ERR_NO_MEMORY, "rv_chain_create: out of host memory");
     c->context = context;
@@ -699,7 +769,10 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     if (c->config.attenuation_db <= 0.0) c->config.attenuation_db = 120.0;
     c->bytes_per_sample = config->format == RV_FORMAT_CS16 ? 4u : 2u;
     const uint64_t history = (uint64_t)g.channels * g.taps_per_branch + g.decimation;
-    const uint64_t raw_cap = bit_ceil64((uint64_t)config->max_run_samples + history + 1u);
+    // pipelined: two runs in the ring beyond the history, so that a run's input
+    // copy never overwrites samples the run before it still reads
+    const uint64_t runs_held = config->pipelined ? 2u : 1u;
+    const uint64_t raw_cap = bit_ceil64(runs_held * config->max_run_samples + history + 1u);
     if (raw_cap > (1ull << 31)) {
         delete c;
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: ring of %llu samples is too large", (unsigned long long)raw_cap);
@@ -732,6 +805,12 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     if (!st) st = cuda_status(cudaMemcpyAsync(c->nco.ptr, nco.data(), nco.size() * 8, cudaMemcpyHostToDevice, c->stream), "nco upload");
     if (!st && c->config.profile)
         for (int i = 0; i < 6 && !st; ++i) st = cuda_status(cudaEventCreate(&c->marks[i]), "chain events");
+    for (RunSlot& sl : c->slots)
+        if (!st) st = cuda_status(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming), "chain events");
+    if (!st && c->config.pipelined) {
+        st = cuda_status(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "copy stream");
+        if (!st) st = cuda_status(cudaEventCreateWithFlags(&c->input_ready, cudaEventDisableTiming), "chain events");
+    }
     if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "chain create");
     if (st) {
         rv_chain_destroy(c);
@@ -760,20 +839,9 @@ int32_t rv_chain_destroy(rv_chain* c) {
     c->twiddles.release();
     c->nco.release();
     c->rx_table.release();
-    c->items_dev.release();
-    c->items_host.release();
-    c->queues.release();
-    c->units_dev.release();
-    c->units_host.release();
-    c->tiles_dev.release();
-    c->tiles_host.release();
-    c->spans_dev.release();
-    c->spans_host.release();
-    c->audio_dev.release();
-    c->audio_host.release();
-    if (c->exec) cudaGraphExecDestroy(c->exec);
-    c->counts_dev.release();
-    c->counts_host.release();
+    for (RunSlot& sl : c->slots) sl.release();
+    if (c->input_ready) cudaEventDestroy(c->input_ready);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (cudaEvent_t e : c->marks)
         if (e) cudaEventDestroy(e);
     delete c;
@@ -886,6 +954,8 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_run: %llu samples exceed max_run_samples %u",
                              (unsigned long long)count, c->config.max_run_samples);
     if (count == 0) return clear_error();
+    // this run's slot was last used two runs ago: hand that run's audio over
+    if (int32_t st = collect_slot(c, S(c))) return st;
     const auto host_start = std::chrono::steady_clock::now();
     const rv_grid_params& g = c->config.grid;
     const bool plain = c->config.mode == RV_CHAIN_PLAIN;
@@ -911,8 +981,10 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         mark(c, 3);
         mark(c, 4);
         mark(c, 5);
-        if ((st = cuda_status(cudaStreamSynchronize(c->stream), "run sync"))) return st;
-        collect_marks(c);
+        if (!pipelined(c)) {
+            if ((st = cuda_status(cudaStreamSynchronize(c->stream), "run sync"))) return st;
+            collect_marks(c);
+        }
         return clear_error();
     }
     if (!plain && c->table_dirty)
@@ -1011,8 +1083,8 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
                 rx_spans.audio_prefix[ri] + (run.audio_count + r.max_audio_item - 1u) / r.max_audio_item;
         }
     }
-    if (c->audio_dev.count < audio_floats + 1)
-        if ((st = c->audio_dev.alloc(audio_floats + 1 + audio_floats / 4))) return st;
+    if (S(c).audio_dev.count < audio_floats + 1)
+        if ((st = S(c).audio_dev.alloc(audio_floats + 1 + audio_floats / 4))) return st;
 
     if (plain) {
         // the reference's recording: fine [+ carrier] + demod per receiver
@@ -1049,7 +1121,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
                 rv_vrx_demod_block db;
                 if ((st = rv_demod_block(&p, r.fine_mask, s.audio_first, (uint32_t)s.audio_count, &db))) return st;
                 if ((st = rv_vrx_demod(c->stream, &p.demod, &db.params, r.d_fine.ptr, r.d_fine.count, r.d_weights.ptr,
-                                       r.d_weights.count, c->audio_dev.ptr + r.run_audio_offset,
+                                       r.d_weights.count, S(c).audio_dev.ptr + r.run_audio_offset,
                                        s.audio_count * p.demod.channels)))
                     return st;
                 c->stats.launches += 1;
@@ -1090,53 +1162,53 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         const size_t unit_base = fine_items.size() + carrier_items.size();
         for (FineUnit& u : units) u.first_item += (uint32_t)unit_base;
         const size_t total = unit_base + unit_items.size();
-        if ((st = c->items_host.reserve(total + 1 + total / 2))) return st;  // headroom: no re-pinning per run
-        if (c->queues.count == 0)
-            if ((st = c->queues.alloc(1))) return st;
-        if ((st = cuda_status(cudaMemsetAsync(c->queues.ptr, 0, sizeof(Queues), c->stream), "queue reset"))) return st;
-        if (c->items_dev.count < total + 1)
-            if ((st = c->items_dev.alloc(total + 1 + total / 4))) return st;
-        WorkItem* h = c->items_host.ptr;
+        if ((st = S(c).items_host.reserve(total + 1 + total / 2))) return st;  // headroom: no re-pinning per run
+        if (S(c).queues.count == 0)
+            if ((st = S(c).queues.alloc(1))) return st;
+        if ((st = cuda_status(cudaMemsetAsync(S(c).queues.ptr, 0, sizeof(Queues), c->stream), "queue reset"))) return st;
+        if (S(c).items_dev.count < total + 1)
+            if ((st = S(c).items_dev.alloc(total + 1 + total / 4))) return st;
+        WorkItem* h = S(c).items_host.ptr;
         size_t at = 0;
         for (auto* list : {&fine_items, &carrier_items, &unit_items}) {
             if (!list->empty()) memcpy(h + at, list->data(), list->size() * sizeof(WorkItem));
             at += list->size();
         }
-        if ((st = cuda_status(cudaMemcpyAsync(c->items_dev.ptr, h, total * sizeof(WorkItem), cudaMemcpyHostToDevice,
+        if ((st = cuda_status(cudaMemcpyAsync(S(c).items_dev.ptr, h, total * sizeof(WorkItem), cudaMemcpyHostToDevice,
                                               c->stream),
                               "work list upload")))
             return st;
         if (!units.empty()) {
-            if ((st = c->units_host.reserve(units.size() + units.size() / 2 + 1))) return st;
-            if (c->units_dev.count < units.size())
-                if ((st = c->units_dev.alloc(units.size() + units.size() / 2 + 1))) return st;
-            memcpy(c->units_host.ptr, units.data(), units.size() * sizeof(FineUnit));
-            if ((st = cuda_status(cudaMemcpyAsync(c->units_dev.ptr, c->units_host.ptr, units.size() * sizeof(FineUnit),
+            if ((st = S(c).units_host.reserve(units.size() + units.size() / 2 + 1))) return st;
+            if (S(c).units_dev.count < units.size())
+                if ((st = S(c).units_dev.alloc(units.size() + units.size() / 2 + 1))) return st;
+            memcpy(S(c).units_host.ptr, units.data(), units.size() * sizeof(FineUnit));
+            if ((st = cuda_status(cudaMemcpyAsync(S(c).units_dev.ptr, S(c).units_host.ptr, units.size() * sizeof(FineUnit),
                                                   cudaMemcpyHostToDevice, c->stream),
                                   "unit upload")))
                 return st;
         }
         if (!tiles.empty()) {
-            if ((st = c->tiles_host.reserve(tiles.size() + tiles.size() / 2 + 1))) return st;
-            if (c->tiles_dev.count < tiles.size())
-                if ((st = c->tiles_dev.alloc(tiles.size() + tiles.size() / 2 + 1))) return st;
-            memcpy(c->tiles_host.ptr, tiles.data(), tiles.size() * sizeof(FineTile));
-            if ((st = cuda_status(cudaMemcpyAsync(c->tiles_dev.ptr, c->tiles_host.ptr, tiles.size() * sizeof(FineTile),
+            if ((st = S(c).tiles_host.reserve(tiles.size() + tiles.size() / 2 + 1))) return st;
+            if (S(c).tiles_dev.count < tiles.size())
+                if ((st = S(c).tiles_dev.alloc(tiles.size() + tiles.size() / 2 + 1))) return st;
+            memcpy(S(c).tiles_host.ptr, tiles.data(), tiles.size() * sizeof(FineTile));
+            if ((st = cuda_status(cudaMemcpyAsync(S(c).tiles_dev.ptr, S(c).tiles_host.ptr, tiles.size() * sizeof(FineTile),
                                                   cudaMemcpyHostToDevice, c->stream),
                                   "tile upload")))
                 return st;
         }
-        const WorkItem* d = c->items_dev.ptr;
+        const WorkItem* d = S(c).items_dev.ptr;
         const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
-        if ((st = launch_fine_tiles(c->stream, c->rx_table.ptr, c->tiles_dev.ptr, (uint32_t)tiles.size(), chan,
-                                    c->tile_shared, &c->queues.ptr->tiles)))
+        if ((st = launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
+                                    c->tile_shared, &S(c).queues.ptr->tiles)))
             return st;
-        if ((st = launch_fine_units(c->stream, c->rx_table.ptr, c->items_dev.ptr, c->units_dev.ptr,
-                                    (uint32_t)units.size(), chan, c->unit_budget, &c->queues.ptr->units)))
+        if ((st = launch_fine_units(c->stream, c->rx_table.ptr, S(c).items_dev.ptr, S(c).units_dev.ptr,
+                                    (uint32_t)units.size(), chan, c->unit_budget, &S(c).queues.ptr->units)))
             return st;
         const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
         if ((st = launch_fine_batched(c->stream, c->rx_table.ptr, d, (uint32_t)fine_items.size(), chan, window,
-                                      &c->queues.ptr->fine)))
+                                      &S(c).queues.ptr->fine)))
             return st;
         d += fine_items.size();
         if ((st = launch_carrier_batched(c->stream, c->rx_table.ptr, d, (uint32_t)carrier_items.size()))) return st;
@@ -1145,10 +1217,10 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         SpanList det_list, audio_list;
         span_lists(c, (uint32_t)c->rx.size(), &det_list, &audio_list);
         if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, det_list, rx_spans.det_total, kDetWindow,
-                                        &c->queues.ptr->detect)))
+                                        &S(c).queues.ptr->detect)))
             return st;
-        if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, audio_list, rx_spans.audio_total, c->audio_dev.ptr,
-                                       kDetWindow, c->weights_cap, &c->queues.ptr->audio)))
+        if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, audio_list, rx_spans.audio_total, S(c).audio_dev.ptr,
+                                       kDetWindow, c->weights_cap, &S(c).queues.ptr->audio)))
             return st;
         mark(c, 4);
         c->stats.launches += (rx_spans.det_total ? 1 : 0) + (rx_spans.audio_total ? 1 : 0) + (fine_items.empty() ? 0 : 1) +
@@ -1159,28 +1231,29 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
 
     c->stats.host_ms +=
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_start).count();
-    // ---- audio back to the host (the reference's readback copies)
+    // ---- audio back to the host (the reference's readback copies), into the
+    // slot; handed to the receivers now, or when the slot comes round again
+    RunSlot& sl = S(c);
+    sl.audio_floats = audio_floats;
+    sl.parts.resize(c->rx.size());
+    for (size_t i = 0; i < c->rx.size(); ++i) sl.parts[i] = {c->rx[i].run_audio_offset, c->rx[i].run_audio_frames};
     if (audio_floats > 0) {
-        if ((st = c->audio_host.reserve(audio_floats + audio_floats / 4))) return st;
-        if ((st = cuda_status(cudaMemcpyAsync(c->audio_host.ptr, c->audio_dev.ptr, audio_floats * sizeof(float),
+        if ((st = sl.audio_host.reserve(audio_floats + audio_floats / 4))) return st;
+        if ((st = cuda_status(cudaMemcpyAsync(sl.audio_host.ptr, sl.audio_dev.ptr, audio_floats * sizeof(float),
                                               cudaMemcpyDeviceToHost, c->stream),
                               "audio readback")))
             return st;
-        if ((st = cuda_status(cudaStreamSynchronize(c->stream), "audio readback sync"))) return st;
-        for (Receiver& r : c->rx) {
-            const uint64_t n = r.run_audio_frames * r.plan.demod.channels;
-            if (c->config.keep_audio && n)
-                r.audio.insert(r.audio.end(), c->audio_host.ptr + r.run_audio_offset,
-                               c->audio_host.ptr + r.run_audio_offset + n);
-            r.audio_frames_total += r.run_audio_frames;
-        }
-        c->stats.audio_bytes += audio_floats * sizeof(float);
     }
     mark(c, 5);
-    // the pinned work-list buffer is rewritten by the next run
-    if ((st = cuda_status(cudaStreamSynchronize(c->stream), "run sync"))) return st;
-    collect_marks(c);
+    if ((st = cuda_status(cudaEventRecord(sl.done, c->stream), "run event"))) return st;
+    sl.pending = true;
     c->stats.runs += 1;
+    if (pipelined(c)) {
+        c->cur ^= 1u;  // the next run prepares the other slot while this one executes
+        return clear_error();
+    }
+    if ((st = collect_slot(c, sl))) return st;
+    collect_marks(c);
     return clear_error();
 }
 
@@ -1196,13 +1269,17 @@ int32_t rv_chain_capture_graph(rv_chain* c) {
 
 int32_t rv_chain_drain(rv_chain* c) {
     if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_drain: NULL");
+    if (int32_t st = collect_all(c)) return st;
     if (int32_t st = cuda_status(cudaStreamSynchronize(c->stream), "rv_chain_drain")) return st;
+    if (c->copy_stream)
+        if (int32_t st = cuda_status(cudaStreamSynchronize(c->copy_stream), "rv_chain_drain")) return st;
     return clear_error();
 }
 
 int32_t rv_chain_receiver_info(const rv_chain* c, uint32_t id, rv_vrx_plan_info* info, uint64_t* audio_frames,
                                uint64_t* first_audio) {
     if (c == nullptr || id >= c->rx.size()) return set_error_fmt(RV_ERR_INVALID, "rv_chain_receiver_info: no receiver %u", id);
+    if (int32_t st = collect_all(const_cast<rv_chain*>(c))) return st;  // runs in flight first
     const Receiver& r = c->rx[id];
     if (info) *info = r.plan;
     if (audio_frames) *audio_frames = r.audio_frames_total;
@@ -1212,6 +1289,7 @@ int32_t rv_chain_receiver_info(const rv_chain* c, uint32_t id, rv_vrx_plan_info*
 
 int32_t rv_chain_read_audio(rv_chain* c, uint32_t id, float* dst, uint64_t capacity, uint64_t* written) {
     if (c == nullptr || id >= c->rx.size()) return set_error_fmt(RV_ERR_INVALID, "rv_chain_read_audio: no receiver %u", id);
+    if (int32_t st = collect_all(c)) return st;  // runs in flight first
     Receiver& r = c->rx[id];
     const uint64_t n = std::min<uint64_t>(capacity, r.audio.size());
     if (dst && n) memcpy(dst, r.audio.data(), n * sizeof(float));
@@ -1222,6 +1300,7 @@ int32_t rv_chain_read_audio(rv_chain* c, uint32_t id, float* dst, uint64_t capac
 
 int32_t rv_chain_get_stats(const rv_chain* c, rv_chain_stats* stats) {
     if (c == nullptr || stats == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_get_stats: NULL");
+    if (int32_t st = collect_all(const_cast<rv_chain*>(c))) return st;  // runs in flight first
     *stats = c->stats;
     return clear_error();
 }

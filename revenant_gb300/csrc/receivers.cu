@@ -306,6 +306,9 @@ k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems,
                 const float4 first4 = *reinterpret_cast<const float4*>(v);
                 float x0 = first4.x, x1 = first4.y, x2 = first4.z, x3 = first4.w;
                 uint32_t w = 0;
+                // unrolled four groups deep: the window's rotation is then a
+                // renaming of registers rather than moves
+#pragma unroll 4
                 for (; w + 4u <= dc; w += 4u) {
                     const float4 nz = *reinterpret_cast<const float4*>(v - (int)w - 4);
                     const float4 wt = *reinterpret_cast<const float4*>(dws + w);

@@ -138,11 +138,13 @@ def test_wfm_stereo_recovers_the_tone(gpu, c1_capture):
     assert spec_l[k1 - 2:k1 + 3].max() > 20 * np.median(spec_l)
 
 
-def _run_pair(gpu, grid, rate, fmt, reqs, codes, runs, bps_values, late=None, late_at=None):
-    """The same feed through a direct batched chain and a captured one."""
+def _run_pair(gpu, grid, rate, fmt, reqs, codes, runs, bps_values, late=None, late_at=None,
+              variants=((False, False), (True, False))):
+    """The same feed through batched chains: (captured, pipelined) per variant."""
     out = []
-    for captured in (False, True):
-        ch = Chain(gpu, grid=grid, rate=rate, fmt=fmt, mode=abi.CHAIN_BATCHED, max_run_samples=max(runs))
+    for captured, pipelined in variants:
+        ch = Chain(gpu, grid=grid, rate=rate, fmt=fmt, mode=abi.CHAIN_BATCHED, max_run_samples=max(runs),
+                   pipelined=pipelined)
         if captured:
             ch.capture_graph()
         ids = [ch.add_receiver(r) for r in reqs]
@@ -203,3 +205,57 @@ def test_plain_chain_refuses_capture(gpu):
     ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=abi.CHAIN_PLAIN, max_run_samples=4096)
     assert lib().rv_chain_capture_graph(ch.handle) == abi.RV_ERR_UNSUPPORTED
     ch.close()
+
+
+@pytest.mark.parametrize("captured", [False, True])
+def test_pipelined_chain_matches_synchronous(gpu, c1_capture, captured):
+    """Runs queued while the previous one executes (two slots, input copies on
+    a second stream): the audio is the synchronous chain's, bit for bit."""
+    (sync, _), (piped, st) = _run_pair(gpu, (8, 17, 4), 2_400_000, abi.FORMAT_CU8, c1_requests(), c1_capture, RUNS_A,
+                                       2, variants=((False, False), (captured, True)))
+    for i, (a, b) in enumerate(zip(sync, piped)):
+        assert a.size == b.size and a.size > 0, "receiver %d" % i
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d differs when pipelined" % i
+    assert st.runs == len(RUNS_A)
+
+
+def test_pipelined_chain_with_a_receiver_added_mid_stream(gpu, c1_capture):
+    reqs = c1_requests()
+    (sync, _), (piped, _) = _run_pair(gpu, (8, 17, 4), 2_400_000, abi.FORMAT_CU8, reqs[:3], c1_capture, RUNS_B, 2,
+                                      late=reqs[6], late_at=5, variants=((False, False), (True, True)))
+    for i, (a, b) in enumerate(zip(sync, piped)):
+        assert a.size > 0 and np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d" % i
+
+
+def test_pipelined_wideband_chain_from_device_memory(gpu):
+    from revenant_gb300.chain import Chain as _Chain
+    rate, n, run = 20_000_000, 1 << 19, 1 << 17
+    reqs = signals.random_receivers(16, rate, seed=6)
+    z = signals.scene(n, rate, [("am", r.center, 0.2) for r in reqs[:4]], snr_db=30.0, seed=6)
+    codes = signals.quantise(z, "cs16")
+    dev = gpu.array(codes)
+    out = []
+    for pipelined in (False, True):
+        ch = _Chain(gpu, grid=(64, 17, 32), rate=rate, fmt=abi.FORMAT_CS16, mode=abi.CHAIN_BATCHED,
+                    max_run_samples=run, pipelined=pipelined)
+        ids = [ch.add_receiver(r) for r in reqs]
+        for k in range(n // run):
+            ch.run(_At(dev, k * run * 4), run)
+        ch.drain()
+        out.append([ch.audio(i) for i in ids])
+        ch.close()
+    for i, (a, b) in enumerate(zip(*out)):
+        assert a.size > 0 and np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d" % i
+
+
+def test_plain_chain_refuses_pipelining(gpu):
+    with pytest.raises(Exception):
+        Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=abi.CHAIN_PLAIN, max_run_samples=4096,
+              pipelined=True)
+
+
+class _At:
+    """A device buffer address plus a byte offset, for Chain.run."""
+
+    def __init__(self, buf, offset):
+        self.address = buf.address + offset
