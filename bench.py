@@ -40,6 +40,11 @@ RECEIVERS = 256
 SEED = 3
 RUN_SAMPLES = 1 << 24  # default samples per rv_chain_run (--run-log2)
 METRIC = "input MS/s through channelizer+N VRX on 1 GB300, % HBM roofline, vs plain path"
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each stage's
+# kernels for one 2^22-sample run of this workload, from one ncu capture
+# (ncu --set full on bench.py --log2n 24 --run-log2 22); a launch of another
+# run size is scaled by its samples, the traffic growing with the work
+MEASURED_TRAFFIC_2P22 = {"coarse": 28.71e6, "fine": 203.71e6, "demod": 157.39e6}
 
 
 def parse():
@@ -303,7 +308,10 @@ def run_gb300(args):
                 "d2h_bytes_per_step": int(d["audio_bytes"] / args.steps)},
         "gpu_launches": int(d["launches"]),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
-                     "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
+                     "traffic": int(MEASURED_TRAFFIC_2P22[dominant] * run_samples / (1 << 22)),
+                     "traffic_note": "DRAM bytes per launch (one run of %d samples), ncu on a 2^22-sample run scaled "
+                                     "by samples" % run_samples,
                      "peak_kind": pk_kind, "algorithmic_bytes_per_step": int(ab[dominant] / args.steps),
                      "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()},
                      "host_ms_per_step": round(d["host_ms"] / args.steps, 3),
