@@ -352,6 +352,53 @@ int32_t rv_spectrum(void* stream, const rv_spectrum_params* params,
                     const rv_cf32* twiddles_dev, uint64_t twiddles_len, const float* window_dev,
                     uint64_t window_len, float* frame_dev, uint64_t frame_len);
 
+/* Front-end DC and IQ-imbalance correction (core/dsp/front_end_correction.h,
+ * front_end_correction_reference.cpp; shaders iq_moments.comp, iq_correct.comp):
+ * per 64-sample chunk the five sums (I, Q, I^2, Q^2, IQ) in float, in order;
+ * the host totals them in double and updates the running estimate; the
+ * correction i' = I - dc_i, q' = cross * i' + scale * (Q - dc_q) in place. */
+#define RV_IQ_MOMENTS_CHUNK 64u
+#define RV_IQ_MOMENTS_PER_CHUNK 5u
+typedef struct rv_iq_moments_params { /* IqMomentsParams, 12 B */
+    uint32_t ring_mask;
+    uint32_t src_offset;
+    uint32_t count;
+} rv_iq_moments_params;
+typedef struct rv_iq_correct_params { /* IqCorrectParams, 28 B */
+    uint32_t ring_mask;
+    uint32_t offset;
+    uint32_t count;
+    float dc_i;
+    float dc_q;
+    float cross;
+    float scale;
+} rv_iq_correct_params;
+int32_t rv_iq_moments(void* stream, const rv_iq_moments_params* params, const rv_cf32* ring_dev,
+                      uint64_t ring_len, float* sums_dev, uint64_t sums_len);
+int32_t rv_iq_correct(void* stream, const rv_iq_correct_params* params, const rv_cf32* in_dev,
+                      uint64_t in_len, rv_cf32* out_dev, uint64_t out_len);
+/* FrontEndCorrector (core/dsp/front_end_correction.cpp) as a plain struct:
+ * the configuration, the estimate and the running second moments. */
+typedef struct rv_front_end {
+    double dc_time_constant_s;    /* 0.1 */
+    double iq_time_constant_s;    /* 1.0 */
+    double max_gain_error_db;     /* 6 */
+    double max_phase_error_deg;   /* 30 */
+    uint32_t measured;
+    uint32_t iq_plausible;
+    uint64_t samples_seen;
+    double dc_i, dc_q, gain, sin_phase;
+    double m_ii, m_qq, m_iq;
+} rv_front_end;
+/* FrontEndCorrector() with the reference's defaults, then reset(). */
+int32_t rv_front_end_init(rv_front_end* state);
+int32_t rv_front_end_reset(rv_front_end* state);
+/* total_moments over chunk sums of a `count`-sample block, then update(). */
+int32_t rv_front_end_update(rv_front_end* state, const float* chunk_sums, uint64_t sums_len, uint32_t count,
+                            int64_t rate);
+/* correction(dc, iq): the parameters' dc/cross/scale fields (ring fields untouched). */
+int32_t rv_front_end_correction(const rv_front_end* state, int32_t dc, int32_t iq, rv_iq_correct_params* out);
+
 /* Averaged power spectrum, lw-radio-dsp's Spectrum::compute
  * (third_party/lw-radio-dsp/src/spectrum.cpp:32-44, src/fft.cpp:31-50): frames
  * of `size` samples, window, FFT, |X|^2 * norm (norm = 1/(sum w)^2), fftshift,
@@ -539,6 +586,14 @@ int32_t rv_chain_get_stats(const rv_chain* chain, rv_chain_stats* stats);
  * buffer it names moved (a receiver was added). Outputs are bit-identical to
  * the direct batched run. */
 int32_t rv_chain_capture_graph(rv_chain* chain);
+/* Graph::set_front_end_correction: from the next run on, each run's samples
+ * get their moments measured and are corrected with the estimate built from
+ * the runs `lag` or more before it (the engine's estimate lags by its frames
+ * in flight; a pipelined chain needs lag >= 2). Switching on resets the
+ * estimate. Off by default. */
+int32_t rv_chain_set_front_end(rv_chain* chain, int32_t dc_removal, int32_t iq_correction, uint32_t lag);
+/* The current estimate (Graph::front_end_correction); drains first. */
+int32_t rv_chain_front_end_estimate(rv_chain* chain, rv_front_end* out);
 /* Waits for all of the chain's device work (a run returns with its audio
  * read back already; this is the engine's drain at stop). */
 int32_t rv_chain_drain(rv_chain* chain);

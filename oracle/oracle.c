@@ -980,3 +980,118 @@ int32_t or_vrx_carrier(const rv_vrx_carrier_config* c, const rv_vrx_carrier_para
     flush_end(&s);
     return ok();
 }
+
+/* ---- front-end correction (core/dsp/front_end_correction_reference.cpp:46-111,
+ * core/dsp/front_end_correction.cpp:36-114) ------------------------------- */
+
+int32_t or_iq_moments(const rv_iq_moments_params* p, const rv_cf32* ring, uint64_t ring_len, float* sums,
+                      uint64_t sums_len) {
+    const uint64_t cap = (uint64_t)p->ring_mask + 1u;
+    if ((cap & (uint64_t)p->ring_mask) != 0 || ring_len < cap || p->count > cap) return fail("iq_moments: bad ring");
+    const uint32_t chunks = (p->count + 63u) / 64u;
+    if (sums_len < (uint64_t)chunks * 5u) return fail("iq_moments: sums too short");
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t chunk = 0; chunk < chunks; ++chunk) {
+        const uint32_t first = chunk * 64u, last = first + 64u < p->count ? first + 64u : p->count;
+        float si = 0.0F, sq = 0.0F, sii = 0.0F, sqq = 0.0F, siq = 0.0F;
+        for (uint32_t k = first; k < last; ++k) {
+            const rv_cf32 v = ring[(p->src_offset + k) & p->ring_mask];
+            si = si + v.re;
+            sq = sq + v.im;
+            sii = sii + v.re * v.re;
+            sqq = sqq + v.im * v.im;
+            siq = siq + v.re * v.im;
+        }
+        float* out = sums + (uint64_t)chunk * 5u;
+        out[0] = si;
+        out[1] = sq;
+        out[2] = sii;
+        out[3] = sqq;
+        out[4] = siq;
+    }
+    flush_end(&s);
+    return 0;
+}
+
+int32_t or_iq_correct(const rv_iq_correct_params* p, const rv_cf32* in, uint64_t in_len, rv_cf32* out,
+                      uint64_t out_len) {
+    const uint64_t cap = (uint64_t)p->ring_mask + 1u;
+    if ((cap & (uint64_t)p->ring_mask) != 0 || in_len < cap || p->count > cap || out_len < in_len)
+        return fail("iq_correct: bad ring");
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t index = 0; index < p->count; ++index) {
+        const uint32_t slot = (p->offset + index) & p->ring_mask;
+        const rv_cf32 v = in[slot];
+        const float i = v.re - p->dc_i;
+        const float q_dc = v.im - p->dc_q;
+        const float a = p->cross * i, b = p->scale * q_dc;
+        out[slot].re = i;
+        out[slot].im = a + b;
+    }
+    flush_end(&s);
+    return 0;
+}
+
+/* FrontEndCorrector::update over total_moments of a block's chunk sums. */
+int32_t or_front_end_update(rv_front_end* st, const float* sums, uint64_t sums_len, uint32_t count, int64_t rate) {
+    if (count == 0) return 0;
+    uint64_t chunks = (count + 63u) / 64u;
+    if (chunks > sums_len / 5u) chunks = sums_len / 5u;
+    double t[5] = {0, 0, 0, 0, 0};
+    for (uint64_t c = 0; c < chunks; ++c)
+        for (int k = 0; k < 5; ++k) t[k] += (double)sums[c * 5u + k];
+    const double n = (double)count;
+    const double mean_i = t[0] / n, mean_q = t[1] / n;
+    const double c_ii = t[2] / n - mean_i * mean_i;
+    const double c_qq = t[3] / n - mean_q * mean_q;
+    const double c_iq = t[4] / n - mean_i * mean_q;
+    const int first = !st->measured;
+    double a_dc = 1.0, a_iq = 1.0;
+    if (!first) {
+        if (st->dc_time_constant_s > 0.0 && rate > 0)
+            a_dc = 1.0 - exp(-(double)count / (st->dc_time_constant_s * (double)rate));
+        if (st->iq_time_constant_s > 0.0 && rate > 0)
+            a_iq = 1.0 - exp(-(double)count / (st->iq_time_constant_s * (double)rate));
+    }
+    st->dc_i += a_dc * (mean_i - st->dc_i);
+    st->dc_q += a_dc * (mean_q - st->dc_q);
+    st->m_ii += a_iq * (c_ii - st->m_ii);
+    st->m_qq += a_iq * (c_qq - st->m_qq);
+    st->m_iq += a_iq * (c_iq - st->m_iq);
+    st->measured = 1;
+    st->samples_seen += count;
+    if (st->m_ii > 0.0 && st->m_qq > 0.0) {
+        st->gain = sqrt(st->m_qq / st->m_ii);
+        st->sin_phase = st->m_iq / sqrt(st->m_ii * st->m_qq);
+        const double gain_db = fabs(20.0 * log10(st->gain));
+        const double sp = st->sin_phase < -1.0 ? -1.0 : (st->sin_phase > 1.0 ? 1.0 : st->sin_phase);
+        const double phase_deg = fabs(asin(sp) * 180.0 / 3.141592653589793238462643383279502884);
+        st->iq_plausible = isfinite(st->gain) && isfinite(st->sin_phase) && gain_db <= st->max_gain_error_db &&
+                           phase_deg <= st->max_phase_error_deg;
+    } else {
+        st->gain = 1.0;
+        st->sin_phase = 0.0;
+        st->iq_plausible = 0;
+    }
+    return 0;
+}
+
+int32_t or_front_end_correction(const rv_front_end* st, int32_t dc, int32_t iq, rv_iq_correct_params* out) {
+    out->dc_i = 0.0F;
+    out->dc_q = 0.0F;
+    out->cross = 0.0F;
+    out->scale = 1.0F;
+    if (!st->measured) return 0;
+    if (dc) {
+        out->dc_i = (float)st->dc_i;
+        out->dc_q = (float)st->dc_q;
+    }
+    if (iq && st->iq_plausible) {
+        const double cos_phase = sqrt(1.0 - st->sin_phase * st->sin_phase);
+        out->cross = (float)(-st->sin_phase / cos_phase);
+        out->scale = (float)(1.0 / (st->gain * cos_phase));
+    }
+    return 0;
+}

@@ -84,4 +84,13 @@ int32_t or_pfb_f64(const rv_grid_params* g, const float* taps, const rv_cf32* ri
 }
 #endif
 
+
+/* front-end correction: twins of core/dsp/front_end_correction_reference.cpp
+ * and the host FrontEndCorrector (core/dsp/front_end_correction.cpp) */
+int32_t or_iq_moments(const rv_iq_moments_params* p, const rv_cf32* ring, uint64_t ring_len, float* sums,
+                      uint64_t sums_len);
+int32_t or_iq_correct(const rv_iq_correct_params* p, const rv_cf32* in, uint64_t in_len, rv_cf32* out,
+                      uint64_t out_len);
+int32_t or_front_end_update(rv_front_end* st, const float* sums, uint64_t sums_len, uint32_t count, int64_t rate);
+int32_t or_front_end_correction(const rv_front_end* st, int32_t dc, int32_t iq, rv_iq_correct_params* out);
 #endif

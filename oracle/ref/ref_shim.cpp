@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "core/dsp/convert.h"
+#include "core/dsp/front_end_correction.h"
 #include "core/dsp/pfb.h"
 #include "core/dsp/pfb_branch_reference.h"
 #include "core/dsp/pfb_fft_reference.h"
@@ -389,6 +390,61 @@ int32_t ref_lwdsp_spectrum(uint32_t size, uint32_t kind, float averaging, const 
     for (uint64_t f = 0; f < frames; ++f)
         spec.compute(std::span<const std::complex<float>>(z + f * size, size),
                      std::span<float>(db_out + f * size, size));
+    return 0;
+}
+
+// core/dsp/front_end_correction_reference.cpp reference_iq_moments
+int32_t ref_iq_moments(const rv_iq_moments_params* p, const rv_cf32* ring, uint64_t ring_len, float* sums,
+                       uint64_t sums_len) {
+    dsp::IqMomentsParams params{p->ring_mask, p->src_offset, p->count};
+    auto st = dsp::reference_iq_moments(
+        std::span<const std::complex<float>>(reinterpret_cast<const std::complex<float>*>(ring), ring_len), params,
+        std::span<float>(sums, sums_len));
+    return st ? 0 : report(st);
+}
+
+// reference_iq_correct
+int32_t ref_iq_correct(const rv_iq_correct_params* p, const rv_cf32* in, uint64_t in_len, rv_cf32* out,
+                       uint64_t out_len) {
+    dsp::IqCorrectParams params;
+    params.ring_mask = p->ring_mask;
+    params.offset = p->offset;
+    params.count = p->count;
+    params.dc_i = p->dc_i;
+    params.dc_q = p->dc_q;
+    params.cross = p->cross;
+    params.scale = p->scale;
+    auto st = dsp::reference_iq_correct(
+        std::span<const std::complex<float>>(reinterpret_cast<const std::complex<float>*>(in), in_len), params,
+        std::span<std::complex<float>>(reinterpret_cast<std::complex<float>*>(out), out_len));
+    return st ? 0 : report(st);
+}
+
+// A FrontEndCorrector (core/dsp/front_end_correction.cpp) with its default
+// configuration over `blocks` blocks: block b's chunk sums at
+// sums + b * stride, `counts[b]` samples; after each update the estimate's
+// fields go to estimates[b] and correction(dc, iq) to corrections[b].
+int32_t ref_front_end_sequence(const float* sums, uint64_t stride, const uint32_t* counts, uint32_t blocks,
+                               int64_t rate, int32_t dc, int32_t iq, rv_front_end* estimates,
+                               rv_iq_correct_params* corrections) {
+    dsp::FrontEndCorrector corrector;
+    for (uint32_t b = 0; b < blocks; ++b) {
+        const uint32_t count = counts[b];
+        const std::size_t floats = (std::size_t)dsp::iq_moments_chunks(count) * dsp::kIqMomentsPerChunk;
+        corrector.update(dsp::total_moments(std::span<const float>(sums + b * stride, floats), count), rate);
+        const dsp::FrontEndEstimate& e = corrector.estimate();
+        rv_front_end& o = estimates[b];
+        std::memset(&o, 0, sizeof o);
+        o.measured = e.measured ? 1u : 0u;
+        o.iq_plausible = e.iq_plausible ? 1u : 0u;
+        o.samples_seen = e.samples_seen;
+        o.dc_i = e.dc_i;
+        o.dc_q = e.dc_q;
+        o.gain = e.gain;
+        o.sin_phase = e.sin_phase;
+        const dsp::IqCorrectParams c = corrector.correction(dc != 0, iq != 0);
+        corrections[b] = rv_iq_correct_params{0u, 0u, 0u, c.dc_i, c.dc_q, c.cross, c.scale};
+    }
     return 0;
 }
 

@@ -112,6 +112,22 @@ AVERAGE_MEAN, AVERAGE_EXPONENTIAL = 0, 1
 WINDOW_RECTANGULAR, WINDOW_HANN, WINDOW_BLACKMAN_HARRIS = 0, 1, 2
 
 
+class IqMomentsParams(_S):
+    _fields_ = [("ring_mask", U32), ("src_offset", U32), ("count", U32)]
+
+
+class IqCorrectParams(_S):
+    _fields_ = [("ring_mask", U32), ("offset", U32), ("count", U32), ("dc_i", F32), ("dc_q", F32), ("cross", F32),
+                ("scale", F32)]
+
+
+class FrontEnd(_S):
+    _fields_ = [("dc_time_constant_s", F64), ("iq_time_constant_s", F64), ("max_gain_error_db", F64),
+                ("max_phase_error_deg", F64), ("measured", U32), ("iq_plausible", U32), ("samples_seen", U64),
+                ("dc_i", F64), ("dc_q", F64), ("gain", F64), ("sin_phase", F64), ("m_ii", F64), ("m_qq", F64),
+                ("m_iq", F64)]
+
+
 class DetectorConfig(_S):
     _fields_ = [("source_rate", I64), ("source_center", I64), ("bins", U32), ("noise_knots", U32),
                 ("bin_width_numerator", I64), ("bin_width_denominator", I64), ("bin_zero_numerator", I64),
@@ -193,7 +209,8 @@ class ChainStats(_S):
                 ("graph_captures", U64), ("graph_ms", C.c_double), ("host_ms", C.c_double)]
 
 
-EXTRA_STRUCTS = {"rv_detector_config": DetectorConfig, "rv_detector_candidate": DetectorCandidate,
+EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params": IqCorrectParams,
+                 "rv_front_end": FrontEnd, "rv_detector_config": DetectorConfig, "rv_detector_candidate": DetectorCandidate,
                  "rv_detector_stats": DetectorStats, "rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
 
 

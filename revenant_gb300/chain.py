@@ -85,6 +85,15 @@ class Chain:
         """Run the batched kernels from one captured CUDA graph from now on."""
         check(lib().rv_chain_capture_graph(self.handle))
 
+    def set_front_end(self, dc=True, iq=True, lag=1):
+        """Front-end DC / IQ-imbalance correction from the next run on."""
+        check(lib().rv_chain_set_front_end(self.handle, 1 if dc else 0, 1 if iq else 0, lag))
+
+    def front_end_estimate(self):
+        st = abi.FrontEnd()
+        check(lib().rv_chain_front_end_estimate(self.handle, C.byref(st)))
+        return st
+
     def drain(self):
         check(lib().rv_chain_drain(self.handle))
 

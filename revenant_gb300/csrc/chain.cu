@@ -36,9 +36,14 @@ int32_t build_twiddle_table(uint32_t M, std::vector<rv_cf32>& out);
 int32_t build_nco(uint32_t log2, std::vector<rv_cf32>& out);
 int32_t validate_grid(const rv_grid_params* g);
 uint32_t demod_fine_history(const rv_vrx_demod_config* c);
+int32_t launch_iq_moments(cudaStream_t s, const rv_iq_moments_params& p, const rv_cf32* ring, float* sums);
+int32_t launch_iq_moments_raw(cudaStream_t s, int32_t format, const rv_iq_moments_params& p, const void* raw,
+                              float* sums);
+void front_end_update(rv_front_end* st, const double totals[5], uint64_t samples, int64_t rate);
+void total_moments(const float* sums, uint64_t chunks, double totals[5]);
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
                             const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
-                            const rv_coarse_params* dyn = nullptr);
+                            const rv_coarse_params* dyn = nullptr, const FrontEndTable* fe = nullptr);
 }  // namespace rv
 
 using namespace rv;
@@ -143,7 +148,7 @@ struct Receiver {
 // captures again.
 struct GraphShape {
     uint32_t fine = 0, carrier = 0, unit_items = 0, units = 0, tiles = 0, nrx = 0;
-    uint32_t fine_window = 0, weights_cap = 0, unit_budget = 0, tile_shared = 0;
+    uint32_t fine_window = 0, weights_cap = 0, unit_budget = 0, tile_shared = 0, front_end = 0;
     const void* tiles_ptr = nullptr;
     const void* spans_ptr = nullptr;
     const void* audio_ptr = nullptr;
@@ -173,6 +178,14 @@ struct RunSlot {
     PinnedArray<RunCounts> counts_host;
     cudaEvent_t done = nullptr;  // recorded after the run's audio read-back
     bool pending = false;        // audio not yet handed to the receivers
+    // front-end moments of the run, read back with its audio
+    DeviceArray<float> sums_dev;
+    PinnedArray<float> sums_host;
+    DeviceArray<FrontEndTable> fe_dev;
+    PinnedArray<FrontEndTable> fe_host;
+    uint32_t sums_count = 0;
+    uint64_t sums_run = 0;
+    bool sums_pending = false;
     uint64_t audio_floats = 0;
     std::vector<std::pair<uint64_t, uint64_t>> parts;  // per receiver: audio offset (floats), frames
     void release() {
@@ -189,6 +202,10 @@ struct RunSlot {
         audio_host.release();
         counts_dev.release();
         counts_host.release();
+        sums_dev.release();
+        sums_host.release();
+        fe_dev.release();
+        fe_host.release();
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
         if (done) cudaEventDestroy(done);
@@ -234,6 +251,23 @@ struct rv_chain {
     // captured runs (rv_chain_capture_graph)
     bool graph = false;
     bool captured_run = false;  // this run replayed the graph
+    // front-end correction (Graph::set_front_end_correction)
+    bool fe_dc = false, fe_iq = false, fe_was_on = false;
+    uint32_t fe_lag = 1;
+    rv_front_end fe{};
+    uint64_t run_index = 0;
+    struct FePending {
+        uint64_t run;
+        uint32_t count;
+        double totals[5];
+    };
+    std::vector<FePending> fe_pending;  // moments not yet in the estimate
+    struct FeRun {
+        uint64_t start, end;  // the run's source samples
+        FrontEndEntry entry;  // the correction applied to them
+    };
+    std::vector<FeRun> fe_runs;  // the runs a coarse window can still reach
+    const FrontEndTable* fe_table = nullptr;  // this run's table on the device, or none
 };
 
 namespace {
@@ -265,10 +299,21 @@ void collect_marks(rv_chain* c) {
 namespace {
 
 // Hands a finished run's audio to its receivers (waits for the run first).
+// A finished run's front-end moments, totalled in chunk order, into the
+// estimator's queue (core/dsp/front_end_correction.cpp total_moments).
+void fe_collect(rv_chain* c, RunSlot& sl) {
+    if (!sl.sums_pending) return;
+    sl.sums_pending = false;
+    rv_chain::FePending p{sl.sums_run, sl.sums_count, {0, 0, 0, 0, 0}};
+    total_moments(sl.sums_host.ptr, (sl.sums_count + RV_IQ_MOMENTS_CHUNK - 1u) / RV_IQ_MOMENTS_CHUNK, p.totals);
+    c->fe_pending.push_back(p);
+}
+
 int32_t collect_slot(rv_chain* c, RunSlot& sl) {
     if (!sl.pending) return RV_OK;
     if (int32_t st = cuda_status(cudaEventSynchronize(sl.done), "run completion")) return st;
     sl.pending = false;
+    fe_collect(c, sl);
     for (size_t i = 0; i < sl.parts.size() && i < c->rx.size(); ++i) {
         Receiver& r = c->rx[i];
         const uint64_t frames = sl.parts[i].second, n = frames * r.plan.demod.channels;
@@ -285,6 +330,99 @@ int32_t collect_slot(rv_chain* c, RunSlot& sl) {
 int32_t collect_all(rv_chain* c) {
     if (int32_t st = collect_slot(c, c->slots[c->cur])) return st;
     return collect_slot(c, c->slots[c->cur ^ 1u]);
+}
+
+// Graph::record_front_end_correction's bookkeeping (core/engine/graph.cpp:
+// 1382-1436) for the run of `count` samples from `first_sample`: reset when
+// switched on, the estimate brought up to the runs `fe_lag` or more before
+// this one (the engine's estimate lags by its frames in flight), and the
+// correction this run's samples get, remembered for later coarse windows.
+FrontEndEntry fe_prepare(rv_chain* c, uint64_t first_sample, uint64_t count, bool* on) {
+    *on = c->fe_dc || c->fe_iq;
+    if (*on && !c->fe_was_on) {
+        rv_front_end_reset(&c->fe);
+        c->fe_pending.clear();
+    }
+    c->fe_was_on = *on;
+    size_t used = 0;
+    for (; used < c->fe_pending.size() && c->fe_pending[used].run + c->fe_lag <= c->run_index; ++used)
+        front_end_update(&c->fe, c->fe_pending[used].totals, c->fe_pending[used].count, c->config.rate);
+    c->fe_pending.erase(c->fe_pending.begin(), c->fe_pending.begin() + (ptrdiff_t)used);
+    FrontEndEntry e{0u, 0u, 0.0F, 0.0F, 0.0F, 1.0F};
+    if (*on && count > 0 && c->fe.measured) {
+        rv_iq_correct_params cp;
+        rv_front_end_correction(&c->fe, c->fe_dc ? 1 : 0, c->fe_iq ? 1 : 0, &cp);
+        e = FrontEndEntry{0u, 1u, cp.dc_i, cp.dc_q, cp.cross, cp.scale};
+    }
+    c->fe_runs.push_back(rv_chain::FeRun{first_sample, first_sample + count, e});
+    if (c->fe_runs.size() > 4u * kFrontEndEntries)  // a plain chain never reads them back
+        c->fe_runs.erase(c->fe_runs.begin(), c->fe_runs.end() - kFrontEndEntries);
+    return e;
+}
+
+// The run's moments into its slot (read back with its audio).
+int32_t fe_moments(rv_chain* c, uint64_t first_sample, uint32_t count) {
+    RunSlot& sl = S(c);
+    const uint64_t floats = (uint64_t)((count + RV_IQ_MOMENTS_CHUNK - 1u) / RV_IQ_MOMENTS_CHUNK) * RV_IQ_MOMENTS_PER_CHUNK;
+    if (floats == 0) return RV_OK;
+    const uint64_t cap = (uint64_t)((c->config.max_run_samples + RV_IQ_MOMENTS_CHUNK - 1u) / RV_IQ_MOMENTS_CHUNK) *
+                         RV_IQ_MOMENTS_PER_CHUNK;
+    if (sl.sums_dev.count < cap)
+        if (int32_t st = sl.sums_dev.alloc(cap)) return st;
+    if (int32_t st = sl.sums_host.reserve(cap)) return st;
+    const rv_iq_moments_params mp{c->raw_mask, (uint32_t)(first_sample & c->raw_mask), count};
+    int32_t st = c->config.mode == RV_CHAIN_PLAIN
+                     ? launch_iq_moments(c->stream, mp, c->cf32_ring.ptr, sl.sums_dev.ptr)
+                     : launch_iq_moments_raw(c->stream, c->config.format, mp, c->raw.ptr, sl.sums_dev.ptr);
+    if (st) return st;
+    c->stats.launches += 1;
+    if ((st = cuda_status(cudaMemcpyAsync(sl.sums_host.ptr, sl.sums_dev.ptr, floats * sizeof(float),
+                                          cudaMemcpyDeviceToHost, c->stream),
+                          "front-end moments read-back")))
+        return st;
+    sl.sums_count = count;
+    sl.sums_run = c->run_index;
+    sl.sums_pending = true;
+    return RV_OK;
+}
+
+// The table of corrections the fused kernel applies over a coarse window that
+// starts at source sample `window` (which may precede the stream): the runs
+// the window reaches, from the latest that began at or before its start.
+// Uploaded into the run's slot; c->fe_table is null when none applies.
+int32_t fe_table(rv_chain* c, int64_t window, bool keep_pointer) {
+    c->fe_table = nullptr;
+    auto& runs = c->fe_runs;
+    // runs wholly before the window can no longer be read
+    size_t drop = 0;
+    while (drop + 1 < runs.size() && (int64_t)runs[drop + 1].start <= window) ++drop;
+    runs.erase(runs.begin(), runs.begin() + (ptrdiff_t)drop);
+    bool any = false;
+    for (const auto& r : runs) any = any || r.entry.on;
+    if (!any && !keep_pointer) return RV_OK;
+    if (runs.size() > kFrontEndEntries)
+        return set_error_fmt(RV_ERR_UNSUPPORTED,
+                             "rv_chain_run: the channelizer's history spans %zu runs, more than the %u the front-end "
+                             "correction keeps: use longer runs",
+                             runs.size(), kFrontEndEntries);
+    RunSlot& sl = S(c);
+    if (sl.fe_dev.count == 0)
+        if (int32_t st = sl.fe_dev.alloc(1)) return st;
+    if (int32_t st = sl.fe_host.reserve(1)) return st;
+    FrontEndTable* t = sl.fe_host.ptr;
+    memset(t, 0, sizeof *t);
+    t->count = runs.empty() ? 1u : (uint32_t)runs.size();
+    if (runs.empty()) t->e[0] = FrontEndEntry{0u, 0u, 0.0F, 0.0F, 0.0F, 1.0F};
+    for (size_t k = 0; k < runs.size(); ++k) {
+        t->e[k] = runs[k].entry;
+        const int64_t rel = (int64_t)runs[k].start - window;
+        t->e[k].rel_start = rel > 0 ? (uint32_t)rel : 0u;
+    }
+    if (int32_t st = cuda_status(cudaMemcpyAsync(sl.fe_dev.ptr, t, sizeof *t, cudaMemcpyHostToDevice, c->stream),
+                                 "front-end table upload"))
+        return st;
+    c->fe_table = sl.fe_dev.ptr;
+    return RV_OK;
 }
 
 int32_t upload_table(rv_chain* c) {
@@ -381,6 +519,20 @@ int32_t coarse_plain(rv_chain* c, uint64_t first_sample, const uint8_t* src, uin
                                 c->cf32_ring.count))
         return st;
     c->stats.launches += 1;
+    // front end: moments of the converted run, then the run corrected in place
+    bool fe_on = false;
+    const FrontEndEntry fe = fe_prepare(c, first_sample, count, &fe_on);
+    if (fe_on) {
+        if (int32_t st = fe_moments(c, first_sample, (uint32_t)count)) return st;
+        if (fe.on) {
+            rv_iq_correct_params ip{c->raw_mask, (uint32_t)(first_sample & c->raw_mask), (uint32_t)count,
+                                    fe.dc_i, fe.dc_q, fe.cross, fe.scale};
+            if (int32_t st = rv_iq_correct(c->stream, &ip, c->cf32_ring.ptr, c->cf32_ring.count, c->cf32_ring.ptr,
+                                           c->cf32_ring.count))
+                return st;
+            c->stats.launches += 1;
+        }
+    }
     if (blocks == 0) return RV_OK;
     rv_pfb_branch_params bp{c->raw_mask, (uint32_t)(first_block * g.decimation), blocks};
     if (int32_t st = rv_pfb_branch(c->stream, &g, &bp, c->proto.ptr, c->proto.count, c->cf32_ring.ptr,
@@ -403,7 +555,16 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
     if (int32_t st = copy_into_ring(c, c->raw.ptr, (uint64_t)c->raw_mask + 1u, first_sample, src, count, where))
         return st;
     mark(c, 1);
+    // front end: moments of the run's raw samples (the fused kernel below
+    // corrects every sample it converts with its run's parameters)
+    bool fe_on = false;
+    (void)fe_prepare(c, first_sample, count, &fe_on);
+    if (fe_on)
+        if (int32_t st = fe_moments(c, first_sample, (uint32_t)count)) return st;
     if (blocks == 0) return RV_OK;
+    const int64_t window = (int64_t)(first_block * g.decimation) - (int64_t)((uint64_t)g.channels * g.taps_per_branch - 1u);
+    // a captured graph reads the table whenever front-end correction is on
+    if (int32_t st = fe_table(c, window, c->graph && fe_on)) return st;
     // stream-start history reads as zero, as the plain path's zeroed ring does
     const uint64_t support = (uint64_t)g.channels * g.taps_per_branch - 1u;
     const uint64_t centre = first_block * g.decimation;
@@ -415,7 +576,7 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
         return RV_OK;
     }
     if (int32_t st = launch_coarse_fused(c->stream, g, c->config.format, p, c->raw.ptr, c->proto.ptr,
-                                         c->twiddles.ptr, c->channel.ptr))
+                                         c->twiddles.ptr, c->channel.ptr, nullptr, c->fe_table))
         return st;
     c->stats.launches += 1;
     return RV_OK;
@@ -594,7 +755,8 @@ int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
     if (int32_t st = cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "graph capture begin"))
         return st;
     int32_t st = launch_coarse_fused(c->stream, c->config.grid, c->config.format, coarse, c->raw.ptr, c->proto.ptr,
-                                     c->twiddles.ptr, c->channel.ptr, &rc->coarse);
+                                     c->twiddles.ptr, c->channel.ptr, &rc->coarse,
+                                     sh.front_end ? S(c).fe_dev.ptr : nullptr);
     if (!st)
         st = launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, sh.tiles, chan, sh.tile_shared,
                                &rc->queues.tiles, &rc->tiles);
@@ -641,6 +803,7 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
     if (int32_t st = upload_spans(c, spans)) return st;
     const bool fits = S(c).exec != nullptr && fine.size() <= sh.fine && carrier.size() <= sh.carrier &&
                       sh.nrx == nrx && sh.spans_ptr == S(c).spans_dev.ptr && unit_items.size() <= sh.unit_items &&
+                      sh.front_end == (c->fe_table != nullptr ? 1u : 0u) &&
                       units.size() <= sh.units && tiles.size() <= sh.tiles && sh.tile_shared == c->tile_shared &&
                       sh.tiles_ptr == S(c).tiles_dev.ptr && window <= sh.fine_window && sh.weights_cap == c->weights_cap &&
                       sh.unit_budget == c->unit_budget && sh.audio_ptr == S(c).audio_dev.ptr &&
@@ -657,6 +820,7 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
         n.carrier = grow(carrier.size(), sh.carrier);
         n.nrx = nrx;
         n.spans_ptr = S(c).spans_dev.ptr;
+        n.front_end = c->fe_table != nullptr ? 1u : 0u;
         n.unit_items = grow(unit_items.size(), sh.unit_items);
         n.units = grow(units.size(), sh.units);
         n.tiles = grow(tiles.size(), sh.tiles);
@@ -767,6 +931,7 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     c->stream = reinterpret_cast<cudaStream_t>(rv_context_stream(context));
     c->config = *config;
     if (c->config.attenuation_db <= 0.0) c->config.attenuation_db = 120.0;
+    rv_front_end_init(&c->fe);
     c->bytes_per_sample = config->format == RV_FORMAT_CS16 ? 4u : 2u;
     const uint64_t history = (uint64_t)g.channels * g.taps_per_branch + g.decimation;
     // pipelined: two runs in the ring beyond the history, so that a run's input
@@ -977,12 +1142,14 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
     c->samples_in += count;
     c->next_block += blocks;
     c->stats.blocks += blocks;
+    c->run_index += 1;
     if (blocks == 0 || c->rx.empty()) {
         mark(c, 3);
         mark(c, 4);
         mark(c, 5);
-        if (!pipelined(c)) {
+        if (!pipelined(c) || S(c).sums_pending) {
             if ((st = cuda_status(cudaStreamSynchronize(c->stream), "run sync"))) return st;
+            fe_collect(c, S(c));
             collect_marks(c);
         }
         return clear_error();
@@ -1264,6 +1431,26 @@ int32_t rv_chain_capture_graph(rv_chain* c) {
                              "rv_chain_capture_graph: a plain chain records one launch per stage per receiver; only "
                              "the batched chain runs from a graph");
     c->graph = true;
+    return clear_error();
+}
+
+int32_t rv_chain_set_front_end(rv_chain* c, int32_t dc_removal, int32_t iq_correction, uint32_t lag) {
+    if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_front_end: NULL");
+    if (lag == 0 || lag > 64) return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_front_end: lag %u outside [1, 64]", lag);
+    if (pipelined(c) && lag < 2)
+        return set_error_fmt(RV_ERR_INVALID,
+                             "rv_chain_set_front_end: a pipelined chain reads a run's moments back two runs later; "
+                             "lag must be at least 2");
+    c->fe_dc = dc_removal != 0;
+    c->fe_iq = iq_correction != 0;
+    c->fe_lag = lag;
+    return clear_error();
+}
+
+int32_t rv_chain_front_end_estimate(rv_chain* c, rv_front_end* out) {
+    if (c == nullptr || out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_front_end_estimate: NULL");
+    if (int32_t st = collect_all(c)) return st;
+    *out = c->fe;
     return clear_error();
 }
 

@@ -31,6 +31,7 @@
 #include <stdlib.h>
 
 #include "common.cuh"
+#include "receivers.cuh"
 #include "revenant_gb300.h"
 
 namespace rv {
@@ -40,28 +41,36 @@ namespace {
 
 constexpr int kChunksPerTile = 8;
 
-__device__ __forceinline__ int32_t sext16(uint32_t raw) { return ((int32_t)(raw << 16)) >> 16; }
-
 // One raw sample at unmasked ring position n, converted exactly as the plain
 // convert kernel converts it; positions in the first lead_zero samples of
 // block 0's support (before the stream began) read as 0.0.
+// With a front-end table (in shared memory), the sample is then corrected
+// with the parameters of the run it arrived in, as the plain path corrects a
+// run's samples in place after converting them (core/shaders/iq_correct.comp).
 template <int FMT>
+__device__ __forceinline__ float2 convert_sample(const uint32_t* __restrict__ raw, uint32_t pos);
+
+template <int FMT, bool FE>
 __device__ __forceinline__ float2 load_sample(const uint32_t* __restrict__ raw, uint32_t n, const rv_coarse_params& p,
-                                              uint32_t window_start) {
-    if (n - window_start < p.lead_zero) return make_float2(0.0F, 0.0F);
-    const uint32_t pos = n & p.ring_mask;
-    if (FMT == RV_FORMAT_CS16) {
-        const uint32_t w = __ldg(&raw[pos]);
-        return make_float2((float)sext16(w & 0xFFFFu) * 0.000030517578125F,
-                           (float)sext16(w >> 16) * 0.000030517578125F);
-    } else {  // RV_FORMAT_CU8
-        const uint32_t w = __ldg(&raw[pos >> 1]);
-        const int shift = (int)((pos & 1u) << 4);
-        const uint32_t i_raw = (w >> shift) & 0xFFu;
-        const uint32_t q_raw = (w >> (shift + 8)) & 0xFFu;
-        return make_float2(((float)i_raw - 127.5F) * 0.00784313772F,
-                           ((float)q_raw - 127.5F) * 0.00784313772F);
-    }
+                                              uint32_t window_start, const FrontEndTable* fe) {
+    const uint32_t rel = n - window_start;
+    if (rel < p.lead_zero) return make_float2(0.0F, 0.0F);
+    const float2 v = convert_sample<FMT>(raw, n & p.ring_mask);
+    if (!FE) return v;
+    uint32_t k = fe->count - 1u;
+    while (k > 0u && rel < fe->e[k].rel_start) --k;
+    const FrontEndEntry& e = fe->e[k];
+    if (!e.on) return v;
+    const float i = v.x - e.dc_i;
+    const float q_dc = v.y - e.dc_q;
+    const float a = e.cross * i;
+    const float b = e.scale * q_dc;
+    return make_float2(i, a + b);
+}
+
+template <int FMT>
+__device__ __forceinline__ float2 convert_sample(const uint32_t* __restrict__ raw, uint32_t pos) {
+    return convert_raw<FMT>(raw, pos);
 }
 
 // acc += s * c for both components: a rounded multiply then a rounded add per
@@ -93,10 +102,11 @@ __device__ __forceinline__ uint32_t group_pos(uint32_t t, uint32_t u, int g) {
     return (t & lo_mask) | (u << (3 * g)) | ((t >> (3 * g)) << (3 * g + 3));
 }
 
-template <int M, int T, int D, int FMT, int S>
+template <int M, int T, int D, int FMT, int S, bool FE>
 __global__ void __launch_bounds__(M*(M / D) * S)
 k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const rv_cf32* __restrict__ tw_g,
-         rv_cf32* __restrict__ ring, rv_coarse_params p_arg, uint32_t tiles_arg, const rv_coarse_params* dyn) {
+         rv_cf32* __restrict__ ring, rv_coarse_params p_arg, uint32_t tiles_arg, const rv_coarse_params* dyn,
+         const FrontEndTable* fe_g) {
     constexpr int P = M / D;          // block phases sharing no samples
     constexpr int NT = M * P * S;     // threads
     constexpr int CB = T * P;         // blocks per chunk per sub-stream
@@ -120,6 +130,12 @@ k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const
 
     const uint32_t tid = threadIdx.x;
     const uint32_t window_start = p.base_offset - (uint32_t)(M * T - 1);
+    __shared__ FrontEndTable fe_s[1];
+    if (FE) {
+        for (uint32_t i = threadIdx.x; i < sizeof(FrontEndTable) / 4u; i += blockDim.x)
+            reinterpret_cast<uint32_t*>(fe_s)[i] = reinterpret_cast<const uint32_t*>(fe_g)[i];
+    }
+    const FrontEndTable* fe = fe_s;  // read only when FE; visible after the barrier below
     for (uint32_t i = tid; i < (uint32_t)M; i += NT) twd[i] = ld_cf32(&tw_g[i]);
 
     const uint32_t r = tid % M;
@@ -136,14 +152,14 @@ k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const
         const uint32_t n0 = p.base_offset + (tile0 + s * NB + par) * (uint32_t)D - r;
         float2 win[T];
 #pragma unroll
-        for (int q = 1; q < T; ++q) win[T - q] = load_sample<FMT>(raw, n0 - (uint32_t)(q * M), p, window_start);
+        for (int q = 1; q < T; ++q) win[T - q] = load_sample<FMT, FE>(raw, n0 - (uint32_t)(q * M), p, window_start, fe);
 
         for (int c = 0; c < kChunksPerTile; ++c) {
             // ---- branch FIR: T steps, window slot of sample q at step i is (i - q) mod T
 #pragma unroll
             for (int i = 0; i < T; ++i) {
                 const uint32_t g = (uint32_t)(c * T + i);
-                win[i] = load_sample<FMT>(raw, n0 + g * (uint32_t)M, p, window_start);
+                win[i] = load_sample<FMT, FE>(raw, n0 + g * (uint32_t)M, p, window_start, fe);
                 float2 acc = make_float2(0.0F, 0.0F);
 #pragma unroll
                 for (int q = 0; q < T; ++q) mac(acc, win[(i - q + T) % T], h[q]);
@@ -221,13 +237,13 @@ k_coarse(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const
     }
 }
 
-template <int M, int T, int D, int FMT, int S>
+template <int M, int T, int D, int FMT, int S, bool FE>
 int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
-               const rv_coarse_params& p, const rv_coarse_params* dyn) {
+               const rv_coarse_params& p, const rv_coarse_params* dyn, const FrontEndTable* fe) {
     constexpr int P = M / D, NT = M * P * S, CB = T * P;
     constexpr int TILE = S * CB * kChunksPerTile;
     const size_t shared = sizeof(float2) * (M + 2 * S * CB * M);
-    auto kern = k_coarse<M, T, D, FMT, S>;
+    auto kern = k_coarse<M, T, D, FMT, S, FE>;
     static int max_grid = 0;
     if (max_grid == 0) {
         if (shared > 48 * 1024) {
@@ -246,7 +262,7 @@ int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, cons
     const uint32_t tiles = (p.block_count + TILE - 1) / TILE;
     // captured: the full resident grid, for whatever block count the run has
     const uint32_t grid = dyn != nullptr ? (uint32_t)max_grid : (tiles < (uint32_t)max_grid ? tiles : (uint32_t)max_grid);
-    kern<<<grid, NT, shared, stream>>>(raw, taps, tw, ring, p, tiles, dyn);
+    kern<<<grid, NT, shared, stream>>>(raw, taps, tw, ring, p, tiles, dyn, fe);
     return cuda_status(cudaGetLastError(), "coarse_fused launch");
 }
 
@@ -256,12 +272,16 @@ int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, cons
 // grid this build has no fused kernel for (the plain kernels cover it).
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
                             const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
-                            const rv_coarse_params* dyn) {
+                            const rv_coarse_params* dyn, const FrontEndTable* fe) {
     const uint32_t* w = static_cast<const uint32_t*>(raw);
 #define RV_COARSE_CASE(MM, TT, DD, SS)                                                                    \
     if (g.channels == MM && g.taps_per_branch == TT && g.decimation == DD) {                             \
-        if (format == RV_FORMAT_CS16) return launch<MM, TT, DD, RV_FORMAT_CS16, SS>(stream, w, taps, tw, ring, p, dyn); \
-        if (format == RV_FORMAT_CU8) return launch<MM, TT, DD, RV_FORMAT_CU8, SS>(stream, w, taps, tw, ring, p, dyn);   \
+        if (format == RV_FORMAT_CS16)                                                                    \
+            return fe ? launch<MM, TT, DD, RV_FORMAT_CS16, SS, true>(stream, w, taps, tw, ring, p, dyn, fe)   \
+                      : launch<MM, TT, DD, RV_FORMAT_CS16, SS, false>(stream, w, taps, tw, ring, p, dyn, fe); \
+        if (format == RV_FORMAT_CU8)                                                                     \
+            return fe ? launch<MM, TT, DD, RV_FORMAT_CU8, SS, true>(stream, w, taps, tw, ring, p, dyn, fe)    \
+                      : launch<MM, TT, DD, RV_FORMAT_CU8, SS, false>(stream, w, taps, tw, ring, p, dyn, fe);  \
     }
     RV_COARSE_CASE(64, 17, 32, 1)
     RV_COARSE_CASE(8, 17, 4, 8)
@@ -319,7 +339,7 @@ extern "C" int32_t rv_coarse_fused(void* stream, const rv_grid_params* grid, int
     if (((uintptr_t)raw_ring_dev & 3u) != 0)
         return rv::set_error_fmt(RV_ERR_INVALID, "rv_coarse_fused: raw ring is not 4-byte aligned");
     if (int32_t st = rv::launch_coarse_fused(reinterpret_cast<cudaStream_t>(stream), *grid, format, *params,
-                                             raw_ring_dev, taps_dev, twiddles_dev, channel_ring_dev, nullptr))
+                                             raw_ring_dev, taps_dev, twiddles_dev, channel_ring_dev, nullptr, nullptr))
         return st;
     return rv::clear_error();
 }

@@ -144,4 +144,25 @@ __device__ __forceinline__ uint32_t brev(uint32_t v, uint32_t stages) {
     return stages == 0 ? 0u : (__brev(v) >> (32u - stages));
 }
 
+__device__ __forceinline__ int32_t sext16(uint32_t raw) { return ((int32_t)(raw << 16)) >> 16; }
+
+// One raw sample at ring position pos (cs16: one 32-bit word per sample,
+// cu8: two per word), converted exactly as the plain convert kernel converts
+// it (core/dsp/convert.h: int16 * 2^-15; (code - 127.5) * 0x3C008081).
+template <int FMT>
+__device__ __forceinline__ float2 convert_raw(const uint32_t* __restrict__ raw, uint32_t pos) {
+    if (FMT == RV_FORMAT_CS16) {
+        const uint32_t w = __ldg(&raw[pos]);
+        return make_float2((float)sext16(w & 0xFFFFu) * 0.000030517578125F,
+                           (float)sext16(w >> 16) * 0.000030517578125F);
+    } else {  // RV_FORMAT_CU8
+        const uint32_t w = __ldg(&raw[pos >> 1]);
+        const int shift = (int)((pos & 1u) << 4);
+        const uint32_t i_raw = (w >> shift) & 0xFFu;
+        const uint32_t q_raw = (w >> (shift + 8)) & 0xFFu;
+        return make_float2(((float)i_raw - 127.5F) * 0.00784313772F,
+                           ((float)q_raw - 127.5F) * 0.00784313772F);
+    }
+}
+
 }  // namespace rv

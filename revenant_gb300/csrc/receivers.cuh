@@ -149,6 +149,20 @@ struct RunCounts {
     uint32_t pad2;
 };
 
+// Front-end correction in force for the raw samples a coarse launch reads
+// (the fused kernel corrects samples as it converts them): entry k covers the
+// samples from `rel_start` (relative to the launch's window start) up to the
+// next entry's, `on` when the correction was applied to that run's samples.
+constexpr uint32_t kFrontEndEntries = 16;
+struct FrontEndEntry {
+    uint32_t rel_start, on;
+    float dc_i, dc_q, cross, scale;
+};
+struct FrontEndTable {
+    uint32_t count, pad;
+    FrontEndEntry e[kFrontEndEntries];
+};
+
 // Every batched launcher takes `dyn`: nullptr for a direct launch, where
 // `nitems` is the item count; or a device pointer to the count inside a
 // RunCounts, for a launch captured in a CUDA graph, where `nitems` is the

@@ -157,6 +157,14 @@ SIGNATURES = {
     "rv_chain_read_audio": (I32, [P, U32, P, U64, ptr(U64)]),
     "rv_chain_get_stats": (I32, [P, ptr(abi.ChainStats)]),
     "rv_chain_capture_graph": (I32, [P]),
+    "rv_chain_set_front_end": (I32, [P, I32, I32, U32]),
+    "rv_chain_front_end_estimate": (I32, [P, ptr(abi.FrontEnd)]),
+    "rv_iq_moments": (I32, [P, ptr(abi.IqMomentsParams), P, U64, P, U64]),
+    "rv_iq_correct": (I32, [P, ptr(abi.IqCorrectParams), P, U64, P, U64]),
+    "rv_front_end_init": (I32, [ptr(abi.FrontEnd)]),
+    "rv_front_end_reset": (I32, [ptr(abi.FrontEnd)]),
+    "rv_front_end_update": (I32, [ptr(abi.FrontEnd), P, U64, U32, I64]),
+    "rv_front_end_correction": (I32, [ptr(abi.FrontEnd), I32, I32, ptr(abi.IqCorrectParams)]),
     "rv_detector_create": (I32, [P, ptr(abi.DetectorConfig), ptr(P)]),
     "rv_detector_destroy": (I32, [P]),
     "rv_detector_consume": (I32, [P, P, U64, U64, I32, ptr(I32)]),

@@ -42,6 +42,8 @@ def _sig(lib, prefix):
     f("vrx_fine", I32, ptr(abi.VrxFineConfig), ptr(abi.VrxFineParams), P, U64, P, U64, P, U64, P, U64)
     f("vrx_demod", I32, ptr(abi.VrxDemodConfig), ptr(abi.VrxDemodParams), P, U64, P, U64, P, U64)
     f("vrx_carrier", I32, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P)
+    f("iq_moments", I32, ptr(abi.IqMomentsParams), P, U64, P, U64)
+    f("iq_correct", I32, ptr(abi.IqCorrectParams), P, U64, P, U64)
 
 
 _oracle = None
@@ -57,6 +59,10 @@ def oracle():
         _sig(lib, "or_")
         lib.or_coarse_cs16.restype = I32
         lib.or_coarse_cs16.argtypes = [ptr(abi.GridParams), P, P, P, U64, U64, U32, U32, P, I32]
+        lib.or_front_end_update.restype = I32
+        lib.or_front_end_update.argtypes = [ptr(abi.FrontEnd), P, U64, U32, I64]
+        lib.or_front_end_correction.restype = I32
+        lib.or_front_end_correction.argtypes = [ptr(abi.FrontEnd), I32, I32, ptr(abi.IqCorrectParams)]
         lib.or_pfb_f64.restype = I32
         lib.or_pfb_f64.argtypes = [ptr(abi.GridParams), P, P, U32, U32, U32, U32, P, P]
         _oracle = Lib(lib, "or_")
@@ -100,6 +106,8 @@ def reference():
         lib.ref_demod_block.restype = I32
         lib.ref_demod_block.argtypes = [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), U32, U64, U32,
                                         ptr(abi.VrxDemodBlock)]
+        lib.ref_front_end_sequence.restype = I32
+        lib.ref_front_end_sequence.argtypes = [P, U64, P, U32, I64, I32, I32, P, P]
         lib.ref_lwdsp_window.restype = I32
         lib.ref_lwdsp_window.argtypes = [U32, U32, P]
         lib.ref_lwdsp_spectrum.restype = I32

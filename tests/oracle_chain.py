@@ -53,6 +53,15 @@ class OracleChain:
         self.fine_mask = (1 << fine_log2) - 1
         self.samples_in = 0
         self.next_block = 0
+        # front-end correction (Graph::record_front_end_correction,
+        # core/engine/graph.cpp:1382-1436): off until set_front_end
+        self.fe_dc = self.fe_iq = False
+        self.fe_lag = 1
+        self.fe_was_on = False
+        self.fe = abi.FrontEnd()
+        _check(lib().rv_front_end_init(C.byref(self.fe)))
+        self.fe_pending = []  # (run index, count, chunk sums) not yet in the estimate
+        self.run_index = 0
         self.rx = []
         for req in requests:
             pl = abi.VrxPlacement()
@@ -67,11 +76,44 @@ class OracleChain:
                                 started=False, reset=True, audio=[],
                                 history=lib().rv_demod_fine_history(C.byref(info.demod))))
 
+    def set_front_end(self, dc, iq, lag=1):
+        self.fe_dc, self.fe_iq, self.fe_lag = bool(dc), bool(iq), lag
+
+    def front_end(self, destination, count):
+        """Moments of this run's samples, the estimate updated with the runs
+        at least `lag` before this one, then this run corrected in place."""
+        o = self.ora
+        on = self.fe_dc or self.fe_iq
+        if on and not self.fe_was_on:
+            _check(lib().rv_front_end_reset(C.byref(self.fe)))
+            self.fe_pending = []
+        self.fe_was_on = on
+        while self.fe_pending and self.fe_pending[0][0] <= self.run_index - self.fe_lag:
+            _, n, sums = self.fe_pending.pop(0)
+            assert o.lib.or_front_end_update(C.byref(self.fe), sums.ctypes.data, sums.size, n, self.rate) == 0
+        if not on or count == 0:
+            return
+        chunks = (count + 63) // 64
+        sums = np.zeros(chunks * 5, np.float32)
+        mp = abi.IqMomentsParams(self.ring_mask, destination, count)
+        assert o.fn("iq_moments")(C.byref(mp), self.ring.ctypes.data, self.ring.shape[0], sums.ctypes.data,
+                                  sums.size) == 0, o.error()
+        self.fe_pending.append((self.run_index, count, sums))
+        if not self.fe.measured:
+            return
+        cp = abi.IqCorrectParams()
+        assert o.lib.or_front_end_correction(C.byref(self.fe), int(self.fe_dc), int(self.fe_iq), C.byref(cp)) == 0
+        cp.ring_mask, cp.offset, cp.count = self.ring_mask, destination, count
+        n = self.ring.shape[0]
+        assert o.fn("iq_correct")(C.byref(cp), self.ring.ctypes.data, n, self.ring.ctypes.data, n) == 0, o.error()
+
     def run(self, packed, count):
         M, D = self.g.channels, self.g.decimation
         o = self.ora
         cp = abi.ConvertParams(self.ring_mask, self.samples_in & 0xFFFFFFFF, 0, count)
         assert o.convert(self.fmt, cp, packed, self.ring) == 0, o.error()
+        self.front_end(self.samples_in & self.ring_mask, count)
+        self.run_index += 1
         first_block = self.next_block
         last_block = (self.samples_in + count - 1) // D
         self.samples_in += count
