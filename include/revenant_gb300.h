@@ -586,6 +586,18 @@ int32_t rv_chain_get_stats(const rv_chain* chain, rv_chain_stats* stats);
  * buffer it names moved (a receiver was added). Outputs are bit-identical to
  * the direct batched run. */
 int32_t rv_chain_capture_graph(rv_chain* chain);
+/* The spectrum stage (Graph::on_block's spectrum dispatch, a6): with
+ * `transform` N > 0, every run that completes N or more channel blocks
+ * computes one frame of the last N blocks (M * N / 2 dB bins, the central half
+ * of each channel's transform), covering source samples [first block * D -
+ * the prototype's group delay, + N * D) (SpectrumFrame). An attached detector
+ * (same context) consumes every frame on the device as it is made.
+ * transform 0 turns the stage off. */
+struct rv_detector;
+int32_t rv_chain_set_spectrum(rv_chain* chain, uint32_t transform, struct rv_detector* detector);
+/* The latest frame (drains first): its bins, start, count and sequence number. */
+int32_t rv_chain_read_spectrum(rv_chain* chain, float* out, uint64_t capacity, uint64_t* bins, uint64_t* start,
+                               uint64_t* count, uint64_t* sequence);
 /* Graph::set_front_end_correction: from the next run on, each run's samples
  * get their moments measured and are corrected with the estimate built from
  * the runs `lag` or more before it (the engine's estimate lags by its frames

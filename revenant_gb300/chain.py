@@ -94,6 +94,23 @@ class Chain:
         check(lib().rv_chain_front_end_estimate(self.handle, C.byref(st)))
         return st
 
+    def set_spectrum(self, transform, detector=None):
+        """One spectrum frame per run over the last `transform` channel blocks;
+        an attached Detector consumes each frame on the device."""
+        check(lib().rv_chain_set_spectrum(self.handle, transform, detector.handle if detector else None))
+
+    def spectrum(self):
+        """(frame dB float32 or None, start, count, sequence) of the latest frame."""
+        bins, start, count, seq = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(lib().rv_chain_read_spectrum(self.handle, None, 0, C.byref(bins), C.byref(start), C.byref(count),
+                                           C.byref(seq)))
+        if bins.value == 0:
+            return None, start.value, count.value, seq.value
+        out = np.zeros(bins.value, np.float32)
+        check(lib().rv_chain_read_spectrum(self.handle, out.ctypes.data, out.size, C.byref(bins), C.byref(start),
+                                           C.byref(count), C.byref(seq)))
+        return out, start.value, count.value, seq.value
+
     def drain(self):
         check(lib().rv_chain_drain(self.handle))
 

@@ -41,6 +41,8 @@ int32_t launch_iq_moments_raw(cudaStream_t s, int32_t format, const rv_iq_moment
                               float* sums);
 void front_end_update(rv_front_end* st, const double totals[5], uint64_t samples, int64_t rate);
 void total_moments(const float* sums, uint64_t chunks, double totals[5]);
+int32_t build_window(uint32_t n, uint32_t t, double a, std::vector<float>& out);
+int32_t detector_wait_for(rv_detector* d, cudaStream_t producer);
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
                             const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
                             const rv_coarse_params* dyn = nullptr, const FrontEndTable* fe = nullptr);
@@ -268,6 +270,15 @@ struct rv_chain {
     };
     std::vector<FeRun> fe_runs;  // the runs a coarse window can still reach
     const FrontEndTable* fe_table = nullptr;  // this run's table on the device, or none
+    // spectrum stage (Graph::on_block's spectrum dispatch) and its consumer
+    uint32_t spec_n = 0;  // transform points per channel; 0 = off
+    DeviceArray<float> spec_window;
+    DeviceArray<rv_cf32> spec_twiddles;
+    DeviceArray<float> spec_frame;
+    uint64_t spec_start = 0, spec_count = 0, spec_sequence = 0;
+    bool spec_recorded = false;
+    uint64_t group_delay = 0;  // the prototype's, in input samples
+    rv_detector* detector = nullptr;
 };
 
 namespace {
@@ -422,6 +433,38 @@ int32_t fe_table(rv_chain* c, int64_t window, bool keep_pointer) {
                                  "front-end table upload"))
         return st;
     c->fe_table = sl.fe_dev.ptr;
+    return RV_OK;
+}
+
+// Graph::on_block's spectrum frame (core/engine/graph.cpp:5077-5095,
+// 5218-5286): when the run completed N or more channel blocks, one frame of
+// the last N (central half of each channel's N-point transform, dB), covering
+// source samples [first * D - group delay, + N * D); then the attached
+// detector consumes it on the device.
+int32_t spectrum_frame(rv_chain* c, uint64_t first_block, uint32_t blocks) {
+    if (c->spec_n == 0 || blocks == 0) return RV_OK;
+    const uint64_t one_past = first_block + blocks, n = c->spec_n;
+    if (one_past < n) return RV_OK;
+    const uint64_t sfb = one_past - n;
+    const rv_grid_params& g = c->config.grid;
+    rv_spectrum_params sp{g.channels, c->spec_n, ilog2(c->spec_n), c->chan_blocks, c->chan_blocks - 1u,
+                          (uint32_t)(sfb & (c->chan_blocks - 1u))};
+    if (int32_t st = rv_spectrum(c->stream, &sp, c->channel.ptr, c->channel.count, c->spec_twiddles.ptr,
+                                 c->spec_twiddles.count, c->spec_window.ptr, c->spec_window.count, c->spec_frame.ptr,
+                                 c->spec_frame.count))
+        return st;
+    c->stats.launches += 1;
+    c->spec_start = sfb * g.decimation - c->group_delay;
+    c->spec_count = n * g.decimation;
+    c->spec_sequence += 1;
+    c->spec_recorded = true;
+    if (c->detector != nullptr) {
+        if (int32_t st = detector_wait_for(c->detector, c->stream)) return st;
+        uint32_t decisions = 0;
+        if (int32_t st = rv_detector_consume_frames(c->detector, c->spec_frame.ptr, 1, c->spec_start, 0, c->spec_count,
+                                                    1, &decisions))
+            return st;
+    }
     return RV_OK;
 }
 
@@ -960,6 +1003,8 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
                               "channel clear");
     std::vector<rv_cf32> tw, nco;
     if (!st) st = design_prototype_table(g, c->config.attenuation_db, c->proto_host);
+    // the linear-phase prototype's delay: its design length (M (T - 1) + 1) over two
+    c->group_delay = (uint64_t)g.channels * (g.taps_per_branch - 1u) / 2u;
     if (!st) st = build_twiddle_table(g.channels, tw);
     if (!st) st = build_nco(16, nco);
     if (!st) st = c->proto.alloc(c->proto_host.size());
@@ -1005,6 +1050,9 @@ int32_t rv_chain_destroy(rv_chain* c) {
     c->nco.release();
     c->rx_table.release();
     for (RunSlot& sl : c->slots) sl.release();
+    c->spec_window.release();
+    c->spec_twiddles.release();
+    c->spec_frame.release();
     if (c->input_ready) cudaEventDestroy(c->input_ready);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (cudaEvent_t e : c->marks)
@@ -1144,6 +1192,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
     c->stats.blocks += blocks;
     c->run_index += 1;
     if (blocks == 0 || c->rx.empty()) {
+        if ((st = spectrum_frame(c, first_block, blocks))) return st;
         mark(c, 3);
         mark(c, 4);
         mark(c, 5);
@@ -1398,6 +1447,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
 
     c->stats.host_ms +=
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_start).count();
+    if ((st = spectrum_frame(c, first_block, blocks))) return st;
     // ---- audio back to the host (the reference's readback copies), into the
     // slot; handed to the receivers now, or when the slot comes round again
     RunSlot& sl = S(c);
@@ -1451,6 +1501,58 @@ int32_t rv_chain_front_end_estimate(rv_chain* c, rv_front_end* out) {
     if (c == nullptr || out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_front_end_estimate: NULL");
     if (int32_t st = collect_all(c)) return st;
     *out = c->fe;
+    return clear_error();
+}
+
+int32_t rv_chain_set_spectrum(rv_chain* c, uint32_t transform, rv_detector* detector) {
+    if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_spectrum: NULL");
+    if (int32_t st = collect_all(c)) return st;
+    if (transform == 0) {
+        c->spec_n = 0;
+        c->detector = nullptr;
+        return clear_error();
+    }
+    if (!is_pow2(transform) || transform < 8 || transform > 2048)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_spectrum: transform %u must be a power of two in [8, 2048]",
+                             transform);
+    if ((uint64_t)transform > c->chan_blocks)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_spectrum: %u points exceed the %u-block channel ring",
+                             transform, c->chan_blocks);
+    const rv_grid_params& g = c->config.grid;
+    std::vector<float> window;
+    std::vector<rv_cf32> tw;
+    if (int32_t st = build_window(transform, g.taps_per_branch, c->config.attenuation_db, window)) return st;
+    if (int32_t st = build_twiddle_table(transform, tw)) return st;
+    int32_t st = c->spec_window.alloc(window.size());
+    if (!st) st = c->spec_twiddles.alloc(tw.size());
+    if (!st) st = c->spec_frame.alloc((uint64_t)g.channels * transform / 2u);
+    if (!st) st = cuda_status(cudaMemcpyAsync(c->spec_window.ptr, window.data(), window.size() * 4, cudaMemcpyHostToDevice,
+                                              c->stream), "spectrum window upload");
+    if (!st) st = cuda_status(cudaMemcpyAsync(c->spec_twiddles.ptr, tw.data(), tw.size() * 8, cudaMemcpyHostToDevice,
+                                              c->stream), "spectrum twiddle upload");
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "spectrum setup");
+    if (st) return st;
+    c->spec_n = transform;
+    c->detector = detector;
+    c->spec_recorded = false;
+    return clear_error();
+}
+
+int32_t rv_chain_read_spectrum(rv_chain* c, float* out, uint64_t capacity, uint64_t* bins, uint64_t* start,
+                               uint64_t* count, uint64_t* sequence) {
+    if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_read_spectrum: NULL");
+    if (int32_t st = collect_all(c)) return st;
+    if (int32_t st = cuda_status(cudaStreamSynchronize(c->stream), "spectrum read")) return st;
+    const uint64_t n = c->spec_n ? (uint64_t)c->config.grid.channels * c->spec_n / 2u : 0u;
+    if (bins) *bins = c->spec_recorded ? n : 0u;
+    if (start) *start = c->spec_start;
+    if (count) *count = c->spec_count;
+    if (sequence) *sequence = c->spec_sequence;
+    if (out && c->spec_recorded && n)
+        if (int32_t st = cuda_status(cudaMemcpy(out, c->spec_frame.ptr, std::min(capacity, n) * sizeof(float),
+                                                cudaMemcpyDeviceToHost),
+                                     "spectrum read"))
+            return st;
     return clear_error();
 }
 
