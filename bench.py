@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--receivers", type=int, default=RECEIVERS)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-detect", action="store_true", help="skip the spectrum + detector measurement")
     ap.add_argument("--run-log2", type=int, default=24, help="log2 samples per rv_chain_run")
     return ap.parse_args()
 
@@ -322,12 +323,55 @@ def run_gb300(args):
     }
     if not args.no_plain and plain:
         line["vs_plain_path"] = round(value / plain["value"], 2)
+    if rank == 0 and not args.no_detect:
+        line["detection"] = detection(dev, d_codes, min(n, 1 << 26))
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(reqs, threads=os.cpu_count())
     if rank == 0:
         print(json.dumps(line))
     chain.close()
     dev.close()
+
+
+def detection(dev, d_codes, samples):
+    """The spectrum stage and the wideband detector over the capture as the
+    engine would run them: 65,536-sample runs (one spectrum frame each, the
+    shipped 64 channels x 2048 points = 65,536 bins), the detector's default
+    1 s average and 0.1 s decisions, consuming every frame on the device."""
+    from revenant_gb300 import abi
+    from revenant_gb300.chain import Chain
+    from revenant_gb300.detector import Detector
+    M, N, run = GRID[0], 2048, 1 << 16
+    bins = M * N // 2
+    cfg = abi.DetectorConfig()
+    cfg.source_rate, cfg.source_center, cfg.bins, cfg.noise_knots = RATE, 100_000_000, bins, 32
+    cfg.bin_width_numerator, cfg.bin_width_denominator = RATE, M * N
+    cfg.bin_zero_numerator, cfg.bin_zero_denominator = -RATE // 2, 1
+    cfg.detection_threshold_db, cfg.average_seconds, cfg.decision_interval_seconds = 6.0, 1.0, 0.1
+    cfg.noise_window_knots, cfg.noise_percentile, cfg.noise_percentile_high = 8, 0.10, 0.40
+    cfg.noise_excision_sigma, cfg.split_gap_bins, cfg.edge_floor_sigma = 4.0, 8, 3.0
+    cfg.occupied_power_fraction, cfg.split_gap_db = 0.99, 1.0
+    cfg.residual_rate_tolerance, cfg.residual_decisions = 0.25, 4
+    det = Detector(dev, cfg)
+    ch = Chain(dev, grid=GRID, rate=RATE, fmt=abi.FORMAT_CS16, mode=abi.CHAIN_BATCHED, max_run_samples=run,
+               keep_audio=False)
+    ch.set_spectrum(N, det)
+    dev.synchronize()
+    t = time.perf_counter()
+    for at in range(0, samples, run):
+        ch.run(_Offset(d_codes, at * 4), run)
+    ch.drain()
+    wall = time.perf_counter() - t
+    st = det.stats()
+    seconds = samples / RATE
+    out = {"signal_seconds": round(seconds, 3), "bins": bins, "frames": int(st.frames), "decisions": int(st.decisions),
+           "candidates_last": int(det.candidates().size), "wall_ms": round(wall * 1e3, 1),
+           "ms_per_signal_second": round(wall * 1e3 / seconds, 2),
+           "detector_stream_ms": round(st.device_ms, 1), "detector_host_ms": round(st.host_ms, 1),
+           "note": "coarse chain + spectrum + detector, no receivers, wall clock including host work"}
+    ch.close()
+    det.close()
+    return out
 
 
 class _Offset:

@@ -623,8 +623,10 @@ int32_t rv_chain_channel_ring(const rv_chain* chain, const rv_cf32** ring, uint3
  * noise floor, the summed-bin width ladder and the candidate bands, then the
  * residual rejection. The per-bin average, the noise-floor percentiles and
  * interpolation, the prefix sums and the ladder's deflections and peaks run
- * on the GPU; the greedy band growth and candidate emission run on the host.
- * Tracking (Detector::update_tracks) is not part of this interface.
+ * on the GPU; the greedy band growth, candidate emission and track
+ * association run on the host. Each live track's band power is measured on
+ * the GPU for every frame (Detector::measure_levels) and folded into the
+ * track at the next decision or tracks() call.
  * ===================================================================== */
 typedef struct rv_detector_config {
     int64_t source_rate;          /* source samples per second */
@@ -651,8 +653,57 @@ typedef struct rv_detector_config {
     double split_gap_db;              /* 1 */
     double residual_rate_tolerance;   /* 0.25 */
     uint32_t residual_decisions;      /* 4 */
-    uint32_t reserved;
+    /* tracking (Detector::update_tracks, core/detect/detector.h:900-1206) */
+    uint32_t birth_hits;              /* 3: consecutive decisions before a track is born */
+    uint32_t max_tracks;              /* 512 */
+    uint32_t grid_channels;           /* 0: tracks carry no coarse channel */
+    double association_overlap;       /* 0.3 */
+    double confidence_rise;           /* 0.35 */
+    double confidence_half_life_seconds; /* 1 */
+    double drop_confidence;           /* 0.05 */
+    double centre_smoothing;          /* 0.4 */
+    double channel_hysteresis;        /* 0.15 */
+    double bootstrap_hold_seconds;    /* 3 */
 } rv_detector_config;
+
+/* TrackState (core/detect/detector.h:271). */
+enum { RV_TRACK_PENDING = 0, RV_TRACK_LIVE = 1, RV_TRACK_HELD = 2, RV_TRACK_MERGED = 3 };
+
+/* Track (core/detect/detector.h:361-577): the fields the tracker maintains
+ * from candidates and frames. Classification, probes, refinement, emitter
+ * memory, spur and HD-hybrid marks come from probing and are not carried. */
+typedef struct rv_detector_track {
+    uint64_t id;                  /* issued from 1, never reused */
+    uint32_t state;               /* RV_TRACK_* */
+    uint32_t held_spells;
+    int64_t center;               /* Hz, smoothed */
+    int64_t bandwidth;            /* Hz, smoothed, >= 1 */
+    double snr_2500_db;           /* smoothed */
+    double margin_confidence;     /* of the smoothed snr */
+    double confidence;
+    uint64_t first_seen;          /* decision instants (source sample indices) */
+    uint64_t last_seen;
+    uint64_t last_detected;
+    uint32_t hits;
+    uint32_t misses;
+    int64_t channel_index;        /* nearest coarse channel, with hysteresis */
+    uint32_t channel;             /* channel_index reduced into [0, grid_channels) */
+    uint32_t channel_valid;
+    uint64_t merged_into;         /* parent id while merged */
+    uint32_t level_first_bin;     /* the bins of its latest candidate */
+    uint32_t level_last_bin;
+    uint32_t level_bins_known;
+    uint32_t level_frames;        /* frames measured over those bins while live */
+    double level_mean_db;         /* running mean and sum of squared deviations */
+    double level_m2;              /* of the band power, dB (Welford) */
+    double peak_to_mean;          /* BandShape of its latest candidate */
+    double concentration;
+    double lower_fraction;
+    double skirt_fraction;
+    uint64_t skirt_bins_available;
+    uint32_t shape_measured;
+    uint32_t reserved;
+} rv_detector_track;
 
 /* Candidate + BandShape (core/detect/detector.h:299-359, shape.h:53-75). */
 typedef struct rv_detector_candidate {
@@ -681,9 +732,14 @@ typedef struct rv_detector_stats {
     uint64_t peaks_overflowed;
     uint64_t candidates_residual;
     uint64_t residual_parts_degenerate;
-    double device_ms;                /* stream time of the consume calls (CUDA events): kernels,
-                                      * read-backs and the waits for the decisions' host part */
+    double device_ms;                /* stream time of the decisions (CUDA events around each
+                                      * decision's kernels, read-back and host part) */
     double host_ms;                  /* host part of the decisions */
+    uint64_t tracks_born;
+    uint64_t tracks_dropped;
+    uint64_t births_refused;
+    uint64_t merges;
+    uint64_t splits;
 } rv_detector_stats;
 
 typedef struct rv_detector rv_detector;
@@ -707,6 +763,35 @@ int32_t rv_detector_candidates(const rv_detector* detector, rv_detector_candidat
 /* Detector::averaged_power / noise_floor (bins doubles each; either may be NULL). */
 int32_t rv_detector_state(rv_detector* detector, double* average, double* floor, uint64_t bins);
 int32_t rv_detector_get_stats(const rv_detector* detector, rv_detector_stats* stats);
+/* Detector::tracks (all = 0: every track but the pending ones, ascending in
+ * centre then id) or every track including pending ones (all = 1). Waits for
+ * the frames in flight, whose band powers the tracks' levels include. */
+int32_t rv_detector_tracks(rv_detector* detector, int32_t all, rv_detector_track* out, uint32_t capacity,
+                           uint32_t* count);
+
+/* The tracker alone, on the host (Detector::update_tracks over candidates
+ * the caller supplies, and measure_levels over band powers it supplies):
+ * the same state machine rv_detector runs after each decision. */
+typedef struct rv_tracker rv_tracker;
+int32_t rv_tracker_create(const rv_detector_config* config, rv_tracker** out);
+int32_t rv_tracker_destroy(rv_tracker* tracker);
+/* One decision at source sample `now`, `elapsed_seconds` after the previous
+ * one, with that decision's candidates (ascending, as rv_detector hands them). */
+int32_t rv_tracker_update(rv_tracker* tracker, uint64_t now, double elapsed_seconds,
+                          const rv_detector_candidate* candidates, uint32_t count);
+/* The bins whose power each frame contributes to a track's level: pairs
+ * (first, last) of the live tracks with known bins below `bins`, in track
+ * order; *count pairs. */
+int32_t rv_tracker_level_bins(const rv_tracker* tracker, uint32_t bins, uint32_t* first_last, uint32_t capacity,
+                              uint32_t* count);
+/* Folds `frames` frames of band powers: sums[f * tracks + k] is the linear
+ * power summed over pair k's bins in frame f, for the pairs level_bins gave
+ * for the same `bins` (tracks = its count). */
+int32_t rv_tracker_fold_levels(rv_tracker* tracker, uint32_t bins, const double* sums, uint32_t frames,
+                               uint32_t tracks);
+int32_t rv_tracker_tracks(const rv_tracker* tracker, int32_t all, rv_detector_track* out, uint32_t capacity,
+                          uint32_t* count);
+int32_t rv_tracker_get_stats(const rv_tracker* tracker, rv_detector_stats* stats);
 
 /* ===================================================================== *
  * Host planning (core/dsp/pfb_design.cpp, vrx_reference.cpp,             *

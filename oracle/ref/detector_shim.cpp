@@ -48,6 +48,16 @@ int32_t refdet_create(const rv_detector_config* c, void** out) {
     cfg.split_gap_db = c->split_gap_db;
     cfg.residual_rate_tolerance = c->residual_rate_tolerance;
     cfg.residual_decisions = c->residual_decisions;
+    cfg.birth_hits = c->birth_hits;
+    cfg.max_tracks = c->max_tracks;
+    cfg.grid_channels = c->grid_channels;
+    cfg.association_overlap = c->association_overlap;
+    cfg.confidence_rise = c->confidence_rise;
+    cfg.confidence_half_life_seconds = c->confidence_half_life_seconds;
+    cfg.drop_confidence = c->drop_confidence;
+    cfg.centre_smoothing = c->centre_smoothing;
+    cfg.channel_hysteresis = c->channel_hysteresis;
+    cfg.bootstrap_hold_seconds = c->bootstrap_hold_seconds;
     auto* r = new RefDetector;
     r->geometry.transform = c->bins;
     r->geometry.bins_per_channel = c->bins;
@@ -113,6 +123,48 @@ int32_t refdet_candidates(void* d, rv_detector_candidate* out, uint32_t capacity
     return 0;
 }
 
+// Detector::tracks(): every track but the pending ones.
+int32_t refdet_tracks(void* d, rv_detector_track* out, uint32_t capacity, uint32_t* count) {
+    auto* r = static_cast<RefDetector*>(d);
+    const auto tracks = r->detector->tracks();
+    *count = (uint32_t)tracks.size();
+    for (size_t i = 0; i < tracks.size() && i < capacity; ++i) {
+        const detect::Track& t = tracks[i];
+        rv_detector_track& o = out[i];
+        std::memset(&o, 0, sizeof o);
+        o.id = t.id;
+        o.state = (uint32_t)t.state;
+        o.held_spells = t.held_spells;
+        o.center = t.center;
+        o.bandwidth = t.bandwidth;
+        o.snr_2500_db = t.snr_2500_db;
+        o.margin_confidence = t.margin_confidence;
+        o.confidence = t.confidence;
+        o.first_seen = t.first_seen;
+        o.last_seen = t.last_seen;
+        o.last_detected = t.last_detected;
+        o.hits = t.hits;
+        o.misses = t.misses;
+        o.channel_index = t.channel_index;
+        o.channel = t.channel;
+        o.channel_valid = t.channel_valid ? 1u : 0u;
+        o.merged_into = t.merged_into;
+        o.level_first_bin = t.level_first_bin;
+        o.level_last_bin = t.level_last_bin;
+        o.level_bins_known = t.level_bins_known ? 1u : 0u;
+        o.level_frames = t.level_frames;
+        o.level_mean_db = t.level_mean_db;
+        o.level_m2 = t.level_m2;
+        o.peak_to_mean = t.shape.peak_to_mean;
+        o.concentration = t.shape.concentration;
+        o.lower_fraction = t.shape.lower_fraction;
+        o.skirt_fraction = t.shape.skirt_fraction;
+        o.skirt_bins_available = t.shape.skirt_bins_available;
+        o.shape_measured = t.shape.measured ? 1u : 0u;
+    }
+    return 0;
+}
+
 int32_t refdet_state(void* d, double* average, double* floor, uint64_t bins) {
     auto* r = static_cast<RefDetector*>(d);
     const auto a = r->detector->averaged_power();
@@ -134,6 +186,11 @@ int32_t refdet_stats(void* d, rv_detector_stats* s) {
     s->peaks_overflowed = st.peaks_overflowed;
     s->candidates_residual = st.candidates_residual;
     s->residual_parts_degenerate = st.residual_parts_degenerate;
+    s->tracks_born = st.tracks_born;
+    s->tracks_dropped = st.tracks_dropped;
+    s->births_refused = st.births_refused;
+    s->merges = st.merges;
+    s->splits = st.splits;
     return 0;
 }
 

@@ -136,7 +136,31 @@ class DetectorConfig(_S):
                 ("noise_percentile", F64), ("noise_percentile_high", F64), ("noise_excision_sigma", F64),
                 ("max_peaks", U32), ("split_gap_bins", U32), ("edge_floor_fraction", F64),
                 ("edge_floor_sigma", F64), ("occupied_power_fraction", F64), ("split_gap_db", F64),
-                ("residual_rate_tolerance", F64), ("residual_decisions", U32), ("reserved", U32)]
+                ("residual_rate_tolerance", F64), ("residual_decisions", U32), ("birth_hits", U32),
+                ("max_tracks", U32), ("grid_channels", U32), ("association_overlap", F64),
+                ("confidence_rise", F64), ("confidence_half_life_seconds", F64), ("drop_confidence", F64),
+                ("centre_smoothing", F64), ("channel_hysteresis", F64), ("bootstrap_hold_seconds", F64)]
+
+
+def tracking_defaults(c):
+    """DetectorConfig's tracking defaults (core/detect/detector.h:900-1206)."""
+    c.birth_hits, c.max_tracks, c.grid_channels = 3, 512, 0
+    c.association_overlap, c.confidence_rise, c.confidence_half_life_seconds = 0.3, 0.35, 1.0
+    c.drop_confidence, c.centre_smoothing, c.channel_hysteresis, c.bootstrap_hold_seconds = 0.05, 0.4, 0.15, 3.0
+    return c
+
+
+TRACK_PENDING, TRACK_LIVE, TRACK_HELD, TRACK_MERGED = 0, 1, 2, 3
+
+
+class DetectorTrack(_S):
+    _fields_ = [("id", U64), ("state", U32), ("held_spells", U32), ("center", I64), ("bandwidth", I64),
+                ("snr_2500_db", F64), ("margin_confidence", F64), ("confidence", F64), ("first_seen", U64),
+                ("last_seen", U64), ("last_detected", U64), ("hits", U32), ("misses", U32), ("channel_index", I64),
+                ("channel", U32), ("channel_valid", U32), ("merged_into", U64), ("level_first_bin", U32),
+                ("level_last_bin", U32), ("level_bins_known", U32), ("level_frames", U32), ("level_mean_db", F64),
+                ("level_m2", F64), ("peak_to_mean", F64), ("concentration", F64), ("lower_fraction", F64),
+                ("skirt_fraction", F64), ("skirt_bins_available", U64), ("shape_measured", U32), ("reserved", U32)]
 
 
 class DetectorCandidate(_S):
@@ -149,7 +173,8 @@ class DetectorCandidate(_S):
 class DetectorStats(_S):
     _fields_ = [("frames", U64), ("decisions", U64), ("frames_rejected", U64), ("candidates", U64),
                 ("peaks_overflowed", U64), ("candidates_residual", U64), ("residual_parts_degenerate", U64),
-                ("device_ms", F64), ("host_ms", F64)]
+                ("device_ms", F64), ("host_ms", F64), ("tracks_born", U64), ("tracks_dropped", U64),
+                ("births_refused", U64), ("merges", U64), ("splits", U64)]
 
 
 class VrxRequest(_S):
@@ -211,6 +236,7 @@ class ChainStats(_S):
 
 EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params": IqCorrectParams,
                  "rv_front_end": FrontEnd, "rv_detector_config": DetectorConfig, "rv_detector_candidate": DetectorCandidate,
+                 "rv_detector_track": DetectorTrack,
                  "rv_detector_stats": DetectorStats, "rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
 
 

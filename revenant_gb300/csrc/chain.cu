@@ -43,6 +43,7 @@ void front_end_update(rv_front_end* st, const double totals[5], uint64_t samples
 void total_moments(const float* sums, uint64_t chunks, double totals[5]);
 int32_t build_window(uint32_t n, uint32_t t, double a, std::vector<float>& out);
 int32_t detector_wait_for(rv_detector* d, cudaStream_t producer);
+int32_t detector_release_to(rv_detector* d, cudaStream_t producer);
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
                             const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
                             const rv_coarse_params* dyn = nullptr, const FrontEndTable* fe = nullptr);
@@ -449,6 +450,10 @@ int32_t spectrum_frame(rv_chain* c, uint64_t first_block, uint32_t blocks) {
     const rv_grid_params& g = c->config.grid;
     rv_spectrum_params sp{g.channels, c->spec_n, ilog2(c->spec_n), c->chan_blocks, c->chan_blocks - 1u,
                           (uint32_t)(sfb & (c->chan_blocks - 1u))};
+    // the attached detector averages frames asynchronously on its own stream:
+    // the previous frame must be read before this one overwrites it
+    if (c->detector != nullptr)
+        if (int32_t st = detector_release_to(c->detector, c->stream)) return st;
     if (int32_t st = rv_spectrum(c->stream, &sp, c->channel.ptr, c->channel.count, c->spec_twiddles.ptr,
                                  c->spec_twiddles.count, c->spec_window.ptr, c->spec_window.count, c->spec_frame.ptr,
                                  c->spec_frame.count))

@@ -12,9 +12,30 @@ import numpy as np
 from . import abi
 from .library import check, lib
 
-CANDIDATE_DTYPE = np.dtype([(name, np.int64 if t is C.c_int64 else np.uint64 if t is C.c_uint64 else
-                             np.uint32 if t is C.c_uint32 else np.float64)
-                            for name, t in abi.DetectorCandidate._fields_])
+
+def _dtype(struct):
+    return np.dtype([(name, np.int64 if t is C.c_int64 else np.uint64 if t is C.c_uint64 else
+                      np.uint32 if t is C.c_uint32 else np.float64) for name, t in struct._fields_])
+
+
+CANDIDATE_DTYPE = _dtype(abi.DetectorCandidate)
+TRACK_DTYPE = _dtype(abi.DetectorTrack)
+
+
+def _to_array(buf, n, struct, dtype):
+    out = np.zeros(n, dtype)
+    for i in range(n):
+        for name, _ in struct._fields_:
+            out[i][name] = getattr(buf[i], name)
+    return out
+
+
+def _read_tracks(fn, handle, all_tracks):
+    n = C.c_uint32()
+    check(fn(handle, int(all_tracks), None, 0, C.byref(n)))
+    buf = (abi.DetectorTrack * max(n.value, 1))()
+    check(fn(handle, int(all_tracks), buf, n.value, C.byref(n)))
+    return _to_array(buf, n.value, abi.DetectorTrack, TRACK_DTYPE)
 
 
 class Detector:
@@ -50,11 +71,11 @@ class Detector:
         check(lib().rv_detector_candidates(self.handle, None, 0, C.byref(n)))
         buf = (abi.DetectorCandidate * max(n.value, 1))()
         check(lib().rv_detector_candidates(self.handle, buf, n.value, C.byref(n)))
-        out = np.zeros(n.value, CANDIDATE_DTYPE)
-        for i in range(n.value):
-            for name, _ in abi.DetectorCandidate._fields_:
-                out[i][name] = getattr(buf[i], name)
-        return out
+        return _to_array(buf, n.value, abi.DetectorCandidate, CANDIDATE_DTYPE)
+
+    def tracks(self, all_tracks=False):
+        """Detector::tracks (pending ones too with all_tracks)."""
+        return _read_tracks(lib().rv_detector_tracks, self.handle, all_tracks)
 
     def state(self):
         avg = np.zeros(self.bins, np.float64)
@@ -70,6 +91,51 @@ class Detector:
     def close(self):
         if self.handle:
             lib().rv_detector_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Tracker:
+    """The tracker alone on the host (rv_tracker_*): candidates in, tracks out."""
+
+    def __init__(self, config):
+        handle = C.c_void_p()
+        check(lib().rv_tracker_create(C.byref(config), C.byref(handle)))
+        self.handle = handle
+
+    def update(self, now, elapsed_seconds, candidates):
+        """candidates: a sequence of abi.DetectorCandidate."""
+        arr = (abi.DetectorCandidate * max(len(candidates), 1))(*candidates)
+        check(lib().rv_tracker_update(self.handle, now, elapsed_seconds, arr, len(candidates)))
+
+    def level_bins(self, bins):
+        n = C.c_uint32()
+        check(lib().rv_tracker_level_bins(self.handle, bins, None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 2), np.uint32)
+        check(lib().rv_tracker_level_bins(self.handle, bins, out.ctypes.data, n.value, C.byref(n)))
+        return out[:n.value]
+
+    def fold_levels(self, bins, sums):
+        """sums: [frames][tracks] float64 band powers for level_bins(bins)."""
+        s = np.ascontiguousarray(sums, np.float64)
+        check(lib().rv_tracker_fold_levels(self.handle, bins, s.ctypes.data, s.shape[0], s.shape[1]))
+
+    def tracks(self, all_tracks=False):
+        return _read_tracks(lib().rv_tracker_tracks, self.handle, all_tracks)
+
+    def stats(self):
+        s = abi.DetectorStats()
+        check(lib().rv_tracker_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def close(self):
+        if self.handle:
+            lib().rv_tracker_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

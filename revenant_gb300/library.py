@@ -174,6 +174,14 @@ SIGNATURES = {
     "rv_detector_candidates": (I32, [P, P, U32, ptr(U32)]),
     "rv_detector_state": (I32, [P, P, P, U64]),
     "rv_detector_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
+    "rv_detector_tracks": (I32, [P, I32, P, U32, ptr(U32)]),
+    "rv_tracker_create": (I32, [ptr(abi.DetectorConfig), ptr(P)]),
+    "rv_tracker_destroy": (I32, [P]),
+    "rv_tracker_update": (I32, [P, U64, F64, P, U32]),
+    "rv_tracker_level_bins": (I32, [P, U32, P, U32, ptr(U32)]),
+    "rv_tracker_fold_levels": (I32, [P, U32, P, U32, U32]),
+    "rv_tracker_tracks": (I32, [P, I32, P, U32, ptr(U32)]),
+    "rv_tracker_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
     "rv_chain_drain": (I32, [P]),
     "rv_chain_channel_ring": (I32, [P, ptr(P), ptr(U32)]),
     "rv_chain_receiver_rings": (I32, [P, U32, ptr(P), ptr(P), ptr(U32)]),

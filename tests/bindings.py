@@ -204,16 +204,38 @@ def detector_reference():
         lib.refdet_state.argtypes = [P, P, P, U64]
         lib.refdet_stats.restype = I32
         lib.refdet_stats.argtypes = [P, ptr(abi.DetectorStats)]
+        lib.refdet_tracks.restype = I32
+        lib.refdet_tracks.argtypes = [P, P, U32, ptr(U32)]
         _detref = lib
     return _detref
 
 
+def _struct_array(rows, struct):
+    dt = np.dtype([(name, np.int64 if t in (C.c_int64,) else np.uint64 if t is C.c_uint64 else
+                    np.uint32 if t is C.c_uint32 else np.float64) for name, t in struct._fields_])
+    out = np.zeros(len(rows), dt)
+    for i, c in enumerate(rows):
+        for name, _ in struct._fields_:
+            out[i][name] = getattr(c, name)
+    return out
+
+
 def candidates_array(cands):
     """ctypes candidates -> numpy structured array (one row each)."""
-    dt = np.dtype([(name, np.int64 if t in (C.c_int64,) else np.uint64 if t is C.c_uint64 else
-                    np.uint32 if t is C.c_uint32 else np.float64) for name, t in abi.DetectorCandidate._fields_])
-    out = np.zeros(len(cands), dt)
-    for i, c in enumerate(cands):
+    return _struct_array(cands, abi.DetectorCandidate)
+
+
+def tracks_array(tracks):
+    """ctypes tracks -> numpy structured array (one row each)."""
+    return _struct_array(tracks, abi.DetectorTrack)
+
+
+def candidates_from_array(arr):
+    """numpy structured candidates -> list of abi.DetectorCandidate."""
+    out = []
+    for row in arr:
+        c = abi.DetectorCandidate()
         for name, _ in abi.DetectorCandidate._fields_:
-            out[i][name] = getattr(c, name)
+            setattr(c, name, row[name].item())
+        out.append(c)
     return out

@@ -12,7 +12,9 @@ QUANTUM = 256.0
 
 
 def scene(bins, frames, seed, bands, floor_db=-100.0, tilt_db=3.0):
-    """bands: (first_bin, width, snr_db, on_frame, off_frame, shape) tuples."""
+    """bands: (first_bin, width, snr_db, on_frame, off_frame, shape) tuples;
+    shape "flat", "cos" (raised cosine) or "keyN" (flat, keyed off every
+    other N frames)."""
     rng = np.random.default_rng(seed)
     k = np.arange(bins, dtype=np.float64)
     floor = 10.0 ** ((floor_db + tilt_db * np.sin(2.0 * np.pi * k / bins)) / 10.0)
@@ -21,6 +23,8 @@ def scene(bins, frames, seed, bands, floor_db=-100.0, tilt_db=3.0):
         p = floor * rng.exponential(1.0, bins)
         for first, width, snr_db, on, off, shape in bands:
             if not (on <= f < off):
+                continue
+            if shape.startswith("key") and (f // int(shape[3:])) % 2 == 1:
                 continue
             idx = np.arange(first, first + width)
             x = (idx - first + 0.5) / width
@@ -53,6 +57,35 @@ FIXTURE_RATE = 2_048_000
 FIXTURE_HOP = 2048
 
 
+# The tracker's scene: 1024 bins of 1 kHz at 1.024 MS/s, one frame per
+# millisecond. Two bands a bridge joins for 40 frames (a merge, then a split),
+# a band that stops (held, then dropped), a keyed carrier (held spells), and a
+# strong narrow band that appears on a wide one (births beside a live track).
+TRACKER = dict(bins=1024, frames=240, seed=7, bands=[
+    (150, 20, 15.0, 0, 240, "flat"),
+    (230, 20, 15.0, 0, 240, "flat"),
+    (170, 60, 15.0, 60, 100, "flat"),
+    (500, 40, 12.0, 0, 100, "cos"),
+    (700, 8, 20.0, 0, 240, "key64"),
+    (860, 60, 10.0, 30, 240, "flat"),
+    (880, 6, 25.0, 120, 200, "flat"),
+])
+
+
+def tracker_config(abi):
+    """The detector configuration of the tracker's scene."""
+    c = fixture_config(abi)
+    bins = TRACKER["bins"]
+    c.bins = bins
+    c.source_rate = bins * 1000
+    c.bin_width_numerator, c.bin_width_denominator = bins * 1000, bins
+    c.bin_zero_numerator = -bins * 1000 // 2
+    c.confidence_half_life_seconds = 0.02
+    c.bootstrap_hold_seconds = 0.12
+    c.grid_channels = 16
+    return c
+
+
 def fixture_config(abi):
     """The detector configuration the fixture was made with."""
     c = abi.DetectorConfig()
@@ -80,4 +113,15 @@ def fixture_config(abi):
     c.split_gap_db = 1.0
     c.residual_rate_tolerance = 0.25
     c.residual_decisions = 4
+    return abi.tracking_defaults(c)
+
+
+def fast_tracking(c):
+    """Tracking fast enough for the fixture's 0.12 s to hold, drop, merge and
+    split tracks: a half-life of 4 ms, a 20 ms hold, a channel grid."""
+    c.confidence_half_life_seconds = 0.004
+    c.bootstrap_hold_seconds = 0.02
+    c.birth_hits = 2
+    c.grid_channels = 64
+    c.max_tracks = 12
     return c

@@ -19,8 +19,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 import detector_scenes as ds  # noqa: E402
-from bindings import candidates_array, detector_reference  # noqa: E402
+from bindings import candidates_array, detector_reference, tracks_array  # noqa: E402
 from revenant_gb300 import abi  # noqa: E402
+
+
+def reference_tracks(lib, det):
+    n = C.c_uint32()
+    buf = (abi.DetectorTrack * 4096)()
+    lib.refdet_tracks(det, buf, 4096, C.byref(n))
+    return tracks_array(list(buf)[:n.value])
 
 
 def run_reference(frames_q, cfg, hop):
@@ -41,7 +48,7 @@ def run_reference(frames_q, cfg, hop):
             n = C.c_uint32()
             buf = (abi.DetectorCandidate * 4096)()
             lib.refdet_candidates(det, buf, 4096, C.byref(n))
-            decisions.append((f, candidates_array(list(buf)[:n.value])))
+            decisions.append((f, candidates_array(list(buf)[:n.value]), reference_tracks(lib, det)))
     bins = frames.shape[1]
     avg, flo = np.zeros(bins), np.zeros(bins)
     lib.refdet_state(det, avg.ctypes.data, flo.ctypes.data, bins)
@@ -56,15 +63,42 @@ def main():
     frames_q = ds.scene(fx["bins"], fx["frames"], fx["seed"], fx["bands"])
     decisions, avg, flo, st = run_reference(frames_q, ds.fixture_config(abi), ds.FIXTURE_HOP)
     out = {"frames_q": frames_q, "average": avg, "floor": flo,
-           "decision_frames": np.array([f for f, _ in decisions], np.int64),
+           "decision_frames": np.array([f for f, _, _ in decisions], np.int64),
            "stats": np.array([st.frames, st.decisions, st.candidates, st.peaks_overflowed,
-                              st.candidates_residual], np.uint64)}
-    for k, (_, cands) in enumerate(decisions):
+                              st.candidates_residual], np.uint64),
+           "track_stats": np.array([st.tracks_born, st.tracks_dropped, st.births_refused, st.merges, st.splits],
+                                   np.uint64)}
+    for k, (_, cands, tracks) in enumerate(decisions):
         out["candidates_%d" % k] = cands
+        out["tracks_%d" % k] = tracks
+    # the same scene with fast tracking: the tracker holds, drops, merges and
+    # splits within the fixture (the candidates do not depend on tracking)
+    fast, _, _, fst = run_reference(frames_q, ds.fast_tracking(ds.fixture_config(abi)), ds.FIXTURE_HOP)
+    for k, ((f, cands, tracks), (f2, cands2, _)) in enumerate(zip(fast, decisions)):
+        assert f == f2 and cands.tobytes() == cands2.tobytes()
+        out["fast_tracks_%d" % k] = tracks
+    out["fast_track_stats"] = np.array([fst.tracks_born, fst.tracks_dropped, fst.births_refused, fst.merges,
+                                        fst.splits], np.uint64)
+    # the tracker's scene: merges, splits, holds, drops, channels
+    tr = ds.TRACKER
+    trk_q = ds.scene(tr["bins"], tr["frames"], tr["seed"], tr["bands"])
+    trk, _, _, tst = run_reference(trk_q, ds.tracker_config(abi), tr["bins"])
+    out["trk_frames_q"] = trk_q
+    out["trk_decision_frames"] = np.array([f for f, _, _ in trk], np.int64)
+    for k, (_, cands, tracks) in enumerate(trk):
+        out["trk_candidates_%d" % k] = cands
+        out["trk_tracks_%d" % k] = tracks
+    out["trk_track_stats"] = np.array([tst.tracks_born, tst.tracks_dropped, tst.births_refused, tst.merges,
+                                       tst.splits], np.uint64)
+    print("tracker scene: %d decisions, stats (born, dropped, refused, merges, splits) %s"
+          % (len(trk), out["trk_track_stats"]))
     np.savez_compressed(os.path.join(HERE, "detector.npz"), **out)
-    print("wrote detector.npz: %d decisions, %d candidates in total" % (len(decisions), sum(len(c) for _, c in decisions)))
-    for f, c in decisions:
+    print("wrote detector.npz: %d decisions, %d candidates in total" % (len(decisions), sum(len(c) for _, c, _ in decisions)))
+    for (f, c, t), (_, _, ft) in zip(decisions, fast):
         print(f, [(int(x["first_bin"]), int(x["last_bin"]), round(float(x["snr_2500_db"]), 2)) for x in c])
+        print("   tracks", [(int(x["id"]), int(x["state"])) for x in t], "fast", [(int(x["id"]), int(x["state"]),
+                                                                             int(x["merged_into"])) for x in ft])
+    print("track stats", out["track_stats"], "fast", out["fast_track_stats"])
 
 
 if __name__ == "__main__":
