@@ -352,6 +352,8 @@ def detection(dev, d_codes, samples):
     cfg.noise_excision_sigma, cfg.split_gap_bins, cfg.edge_floor_sigma = 4.0, 8, 3.0
     cfg.occupied_power_fraction, cfg.split_gap_db = 0.99, 1.0
     cfg.residual_rate_tolerance, cfg.residual_decisions = 0.25, 4
+    abi.tracking_defaults(cfg)
+    cfg.grid_channels = M
     det = Detector(dev, cfg)
     ch = Chain(dev, grid=GRID, rate=RATE, fmt=abi.FORMAT_CS16, mode=abi.CHAIN_BATCHED, max_run_samples=run,
                keep_audio=False)
@@ -365,10 +367,11 @@ def detection(dev, d_codes, samples):
     st = det.stats()
     seconds = samples / RATE
     out = {"signal_seconds": round(seconds, 3), "bins": bins, "frames": int(st.frames), "decisions": int(st.decisions),
-           "candidates_last": int(det.candidates().size), "wall_ms": round(wall * 1e3, 1),
+           "candidates_last": int(det.candidates().size), "tracks_last": int(det.tracks().size),
+           "tracks_born": int(st.tracks_born), "wall_ms": round(wall * 1e3, 1),
            "ms_per_signal_second": round(wall * 1e3 / seconds, 2),
            "detector_stream_ms": round(st.device_ms, 1), "detector_host_ms": round(st.host_ms, 1),
-           "note": "coarse chain + spectrum + detector, no receivers, wall clock including host work"}
+           "note": "coarse chain + spectrum + detector with tracking, no receivers, wall clock including host work"}
     ch.close()
     det.close()
     return out

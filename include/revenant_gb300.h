@@ -618,6 +618,114 @@ int32_t rv_chain_receiver_rings(const rv_chain* chain, uint32_t id, const rv_cf3
 int32_t rv_chain_channel_ring(const rv_chain* chain, const rv_cf32** ring, uint32_t* ring_blocks);
 
 /* ===================================================================== *
+ * Span-wide impulse excision (core/dsp/impulse_excision.h,
+ * impulse_excision_reference.cpp; core/shaders/impulse_excise.comp): on the
+ * cf32 sample ring, after the front-end correction and before the
+ * channelizer. Segment powers, their running median, per-sample flags, and
+ * the apply pass that zeroes (to -0) every run of marked samples no longer
+ * than max_width and writes what it removed beside it, so cleaned + removed
+ * == raw bit for bit.
+ * ===================================================================== */
+enum {
+    RV_EXCISE_SEGMENT = 0,
+    RV_EXCISE_REFERENCE = 1,
+    RV_EXCISE_FLAG = 2,
+    RV_EXCISE_APPLY = 3,
+    RV_EXCISE_MAX_SEGMENTS = 64,
+    RV_EXCISE_MAX_WIDTH = 4096,
+    RV_EXCISE_MAX_SEG_LOG2 = 12,
+    RV_EXCISE_MAX_GUARD = 16,
+    RV_EXCISE_COUNTER_SAMPLES = 0, /* counters[4]: samples excised, */
+    RV_EXCISE_COUNTER_EVENTS = 1,  /* runs excised, */
+    RV_EXCISE_COUNTER_SPARED = 2,  /* runs left alone as too long */
+    RV_EXCISE_COUNTERS = 4
+};
+
+/* ExcisionConfig (impulse_excision.h:150-160): the kernel's specialisation
+ * constants. `pass` is set by each entry point. */
+typedef struct rv_excision_config {
+    uint32_t pass;
+    uint32_t seg_log2;  /* segment of 2^seg_log2 samples */
+    uint32_t segments;  /* K, the median's window */
+    uint32_t max_width; /* longest run excised */
+    uint32_t hang;
+    uint32_t lead;
+} rv_excision_config;
+
+/* ExcisionParams (impulse_excision.h:176-187): eight packed words. */
+typedef struct rv_excision_params {
+    uint32_t ring_mask;
+    uint32_t first;     /* ring slot of the first sample (segment passes: of the first segment) */
+    uint32_t count;     /* samples (segment passes: segments) */
+    uint32_t seg_mask;
+    uint32_t flag_mask;
+    uint32_t removed_mask;
+    int32_t history;    /* samples of the current run before `first` */
+    float threshold;    /* power ratio */
+} rv_excision_params;
+
+typedef struct rv_excision_rings {
+    uint32_t seg_mask;
+    uint32_t flag_mask;
+    uint32_t removed_mask;
+} rv_excision_rings;
+
+/* ExcisionPlan: one block's four passes (count 0: nothing to do). */
+typedef struct rv_excision_plan {
+    rv_excision_params segment;
+    rv_excision_params reference;
+    rv_excision_params flag;
+    rv_excision_params apply;
+    uint64_t cleaned_end; /* one past the last sample finished: the channelizer reads below it */
+    uint32_t restarted;
+    uint32_t reserved;
+} rv_excision_plan;
+
+/* ExcisionCursor (impulse_excision.h:232-270), as plain state. */
+typedef struct rv_excision_cursor {
+    rv_excision_config config;
+    uint32_t ring_mask;
+    rv_excision_rings rings;
+    float threshold;
+    uint32_t running;
+    uint32_t reserved;
+    uint64_t valid_from;
+    uint64_t next_in;
+    uint64_t seg_next;
+    uint64_t flag_next;
+    uint64_t apply_next;
+} rv_excision_cursor;
+
+/* design_excision / excision_threshold / size_excision_rings (host). */
+int32_t rv_design_excision(int64_t source_rate, double max_width_seconds, rv_excision_config* out);
+float rv_excision_threshold(double threshold_db);
+int32_t rv_size_excision_rings(const rv_excision_config* config, uint64_t max_block, uint32_t frames_in_flight,
+                               uint32_t ring_mask, rv_excision_rings* out);
+/* ExcisionCursor: construct (running = 0), reset (set running = 0), plan. */
+int32_t rv_excision_cursor_init(rv_excision_cursor* cursor, const rv_excision_config* config, uint32_t ring_mask,
+                                const rv_excision_rings* rings, float threshold);
+int32_t rv_excision_plan_block(rv_excision_cursor* cursor, uint64_t start, uint32_t count, rv_excision_plan* out);
+
+/* The four passes on the device (one launch each, validated as the twins
+ * validate; the lengths are the buffers' element counts). `raw` and
+ * `cleaned` may be the same ring. */
+int32_t rv_excise_segment(void* stream, const rv_excision_config* config, const rv_excision_params* params,
+                          const rv_cf32* raw_dev, uint64_t raw_len, float* seg_power_dev, uint64_t seg_len);
+int32_t rv_excise_reference(void* stream, const rv_excision_config* config, const rv_excision_params* params,
+                            const float* seg_power_dev, float* seg_level_dev, uint64_t seg_len);
+int32_t rv_excise_flag(void* stream, const rv_excision_config* config, const rv_excision_params* params,
+                       const rv_cf32* raw_dev, uint64_t raw_len, const float* seg_level_dev, uint64_t seg_len,
+                       uint32_t* flags_dev, uint64_t flags_len);
+int32_t rv_excise_apply(void* stream, const rv_excision_config* config, const rv_excision_params* params,
+                        const rv_cf32* raw_dev, uint64_t raw_len, const uint32_t* flags_dev, uint64_t flags_len,
+                        rv_cf32* cleaned_dev, rv_cf32* removed_dev, uint64_t removed_len, uint32_t* counters_dev);
+/* Graph::record_impulse_excision: a plan's passes in order on one ring, in place. */
+int32_t rv_excise_block(void* stream, const rv_excision_config* config, const rv_excision_plan* plan,
+                        rv_cf32* ring_dev, uint64_t ring_len, float* seg_power_dev, float* seg_level_dev,
+                        uint64_t seg_len, uint32_t* flags_dev, uint64_t flags_len, rv_cf32* removed_dev,
+                        uint64_t removed_len, uint32_t* counters_dev);
+
+/* ===================================================================== *
  * Wideband detector (core/detect/detector.h:1316-1460, detector.cpp:186-1586):
  * the exponential average of the spectrum frames, and at every decision the
  * noise floor, the summed-bin width ladder and the candidate bands, then the

@@ -1095,3 +1095,285 @@ int32_t or_front_end_correction(const rv_front_end* st, int32_t dc, int32_t iq, 
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* impulse excision: core/dsp/impulse_excision_reference.cpp          */
+
+static uint64_t ring_size(uint32_t mask) { return (uint64_t)mask + 1u; }
+
+static uint32_t bit_ceil_u32(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+static uint64_t bit_ceil_u64(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+static double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+/* design_excision (impulse_excision_reference.cpp:57-80) */
+int32_t or_design_excision(int64_t source_rate, double max_width_seconds, rv_excision_config* out) {
+    const double rate = (double)(source_rate > 1 ? source_rate : 1);
+    memset(out, 0, sizeof *out);
+    out->max_width = (uint32_t)clampd(round(max_width_seconds * rate), 1.0, (double)RV_EXCISE_MAX_WIDTH);
+    out->hang = (uint32_t)clampd(round(0.1e-6 * rate), 2.0, 16.0);
+    out->lead = out->hang;
+    const uint32_t quarter = (out->max_width + 3u) / 4u > 16u ? (out->max_width + 3u) / 4u : 16u;
+    uint32_t log2 = 0;
+    while ((1u << log2) < bit_ceil_u32(quarter)) ++log2;
+    out->seg_log2 = log2 < RV_EXCISE_MAX_SEG_LOG2 ? log2 : RV_EXCISE_MAX_SEG_LOG2;
+    out->segments = 32;
+    return ok();
+}
+
+/* excision_threshold (:82-84) */
+float or_excision_threshold(double threshold_db) { return (float)pow(10.0, threshold_db / 10.0); }
+
+static int is_mask32(uint32_t m) { return is_pow2_u64(ring_size(m)); }
+
+/* validate (:86-140) */
+static int32_t excise_validate(const rv_excision_config* c, const rv_excision_params* p) {
+    if (c->pass > RV_EXCISE_APPLY) return fail("excision: bad pass");
+    if (c->seg_log2 < 2 || c->seg_log2 > RV_EXCISE_MAX_SEG_LOG2) return fail("excision: bad segment");
+    if (c->segments < 2 || c->segments > RV_EXCISE_MAX_SEGMENTS) return fail("excision: bad segments");
+    if (c->max_width < 1 || c->max_width > RV_EXCISE_MAX_WIDTH) return fail("excision: bad width");
+    if (c->hang > RV_EXCISE_MAX_GUARD || c->lead > RV_EXCISE_MAX_GUARD) return fail("excision: bad guard");
+    if (!is_mask32(p->ring_mask) || !is_mask32(p->seg_mask) || !is_mask32(p->flag_mask) || !is_mask32(p->removed_mask))
+        return fail("excision: masks");
+    const uint64_t ring = ring_size(p->ring_mask);
+    if ((ring_size(p->seg_mask) << c->seg_log2) > ring || ring_size(p->flag_mask) > ring ||
+        ring_size(p->removed_mask) > ring)
+        return fail("excision: rings larger than the sample ring");
+    if (c->pass == RV_EXCISE_SEGMENT || c->pass == RV_EXCISE_REFERENCE) {
+        if ((p->first & ((1u << c->seg_log2) - 1u)) != 0u) return fail("excision: segment boundary");
+        if ((uint64_t)p->count + c->segments + 2u > ring_size(p->seg_mask)) return fail("excision: segment ring");
+    } else {
+        const uint64_t reach = (uint64_t)p->count + 2u * (uint64_t)c->max_width + c->hang + c->lead;
+        if (reach >= ring_size(p->flag_mask) || (c->pass == RV_EXCISE_APPLY && p->count > ring_size(p->removed_mask)))
+            return fail("excision: flag or removed ring");
+    }
+    if (!(p->threshold > 0.0F)) return fail("excision: threshold");
+    return 0;
+}
+
+/* size_excision_rings (:142-172) */
+int32_t or_size_excision_rings(const rv_excision_config* c, uint64_t max_block, uint32_t frames_in_flight,
+                               uint32_t ring_mask, rv_excision_rings* out) {
+    const uint64_t frames = frames_in_flight > 1u ? frames_in_flight : 1u;
+    const uint64_t segment = 1ull << c->seg_log2;
+    const uint64_t reach = (uint64_t)c->max_width + c->lead;
+    const uint64_t lag = reach > segment ? reach : segment;
+    const uint64_t in_flight = max_block * frames;
+    const uint64_t flags = bit_ceil_u64(in_flight + lag + 2u * (uint64_t)c->max_width + c->hang + c->lead + 1u);
+    const uint64_t segs = bit_ceil_u64(in_flight / segment + c->segments + 4u);
+    const uint64_t removed = bit_ceil_u64((max_block + lag) * frames);
+    const uint64_t ring = ring_size(ring_mask);
+    if (flags > ring || removed > ring || (segs << c->seg_log2) > ring) return fail("excision: ring too small");
+    out->seg_mask = (uint32_t)(segs - 1u);
+    out->flag_mask = (uint32_t)(flags - 1u);
+    out->removed_mask = (uint32_t)(removed - 1u);
+    return ok();
+}
+
+/* ExcisionCursor (:175-245) */
+int32_t or_excision_cursor_init(rv_excision_cursor* k, const rv_excision_config* c, uint32_t ring_mask,
+                                const rv_excision_rings* rings, float threshold) {
+    memset(k, 0, sizeof *k);
+    k->config = *c;
+    k->ring_mask = ring_mask;
+    k->rings = *rings;
+    k->threshold = threshold;
+    return ok();
+}
+
+static rv_excision_params cursor_params(const rv_excision_cursor* k, uint64_t first, uint32_t count) {
+    rv_excision_params o;
+    o.ring_mask = k->ring_mask;
+    o.first = (uint32_t)(first & k->ring_mask);
+    o.count = count;
+    o.seg_mask = k->rings.seg_mask;
+    o.flag_mask = k->rings.flag_mask;
+    o.removed_mask = k->rings.removed_mask;
+    const int64_t clamp = (int64_t)1 << 30;
+    int64_t h = (int64_t)first - (int64_t)k->valid_from;
+    h = h < -clamp ? -clamp : (h > clamp ? clamp : h);
+    o.history = (int32_t)h;
+    o.threshold = k->threshold;
+    return o;
+}
+
+int32_t or_excision_plan_block(rv_excision_cursor* k, uint64_t start, uint32_t count, rv_excision_plan* out) {
+    memset(out, 0, sizeof *out);
+    out->segment.threshold = out->reference.threshold = out->flag.threshold = out->apply.threshold = 31.622776F;
+    const uint64_t segment = 1ull << k->config.seg_log2;
+    if (!k->running || start != k->next_in) {
+        k->running = 1;
+        out->restarted = 1;
+        k->valid_from = start;
+        k->seg_next = (start + segment - 1u) / segment;
+        k->flag_next = start;
+        k->apply_next = start;
+    }
+    const uint64_t end = start + count;
+    k->next_in = end;
+    const uint64_t seg_end = end / segment;
+    if (seg_end > k->seg_next) {
+        out->segment = cursor_params(k, k->seg_next * segment, (uint32_t)(seg_end - k->seg_next));
+        k->seg_next = seg_end;
+    }
+    if (end > k->flag_next) {
+        const uint64_t lo = k->flag_next / segment, hi = (end - 1u) / segment;
+        out->reference = cursor_params(k, lo * segment, (uint32_t)(hi - lo + 1u));
+        out->flag = cursor_params(k, k->flag_next, (uint32_t)(end - k->flag_next));
+        k->flag_next = end;
+    }
+    const uint64_t reach = (uint64_t)k->config.max_width + k->config.lead;
+    const uint64_t by_scan = end > reach ? end - reach : 0;
+    const uint64_t by_segment = (end / segment) * segment;
+    const uint64_t apply_end = by_scan < by_segment ? by_scan : by_segment;
+    if (apply_end > k->apply_next) {
+        out->apply = cursor_params(k, k->apply_next, (uint32_t)(apply_end - k->apply_next));
+        k->apply_next = apply_end;
+    }
+    out->cleaned_end = k->apply_next;
+    return ok();
+}
+
+static rv_excision_config with_pass(const rv_excision_config* c, uint32_t pass) {
+    rv_excision_config o = *c;
+    o.pass = pass;
+    return o;
+}
+
+/* reference_excise_segment (:248-270): sequential fp32 sum of |x|^2 */
+int32_t or_excise_segment(const rv_excision_config* c0, const rv_excision_params* p, const rv_cf32* raw,
+                          uint64_t raw_len, float* seg_power, uint64_t seg_len) {
+    const rv_excision_config c = with_pass(c0, RV_EXCISE_SEGMENT);
+    if (excise_validate(&c, p)) return -1;
+    if (raw_len < ring_size(p->ring_mask) || seg_len < ring_size(p->seg_mask)) return fail("excise_segment: short");
+    flush_scope s;
+    flush_begin(&s);
+    const uint32_t n = 1u << c.seg_log2;
+    for (uint32_t j = 0; j < p->count; ++j) {
+        const uint32_t base = (p->first + (j << c.seg_log2)) & p->ring_mask;
+        float sum = 0.0F;
+        for (uint32_t m = 0; m < n; ++m) {
+            const rv_cf32 v = raw[(base + m) & p->ring_mask];
+            const float q = v.re * v.re + v.im * v.im;
+            sum = sum + q;
+        }
+        seg_power[(base >> c.seg_log2) & p->seg_mask] = sum;
+    }
+    flush_end(&s);
+    return ok();
+}
+
+/* reference_excise_reference (:272-306): the median (element K/2 after an
+ * insertion sort) of the K segments before the guard segment */
+int32_t or_excise_reference(const rv_excision_config* c0, const rv_excision_params* p, const float* seg_power,
+                            float* seg_level, uint64_t seg_len) {
+    const rv_excision_config c = with_pass(c0, RV_EXCISE_REFERENCE);
+    if (excise_validate(&c, p)) return -1;
+    if (seg_len < ring_size(p->seg_mask)) return fail("excise_reference: short");
+    const int64_t segment = (int64_t)1 << c.seg_log2, window = c.segments;
+    for (uint32_t j = 0; j < p->count; ++j) {
+        const uint32_t base = (p->first + (j << c.seg_log2)) & p->ring_mask;
+        const uint32_t slot = base >> c.seg_log2;
+        const int64_t rel = (int64_t)j * segment;
+        if (rel - (window + 1) * segment + p->history < 0) {
+            seg_level[slot & p->seg_mask] = 0.0F;
+            continue;
+        }
+        float v[RV_EXCISE_MAX_SEGMENTS];
+        for (uint32_t m = 0; m < c.segments; ++m) v[m] = seg_power[(slot - 1u - c.segments + m) & p->seg_mask];
+        for (uint32_t a = 1; a < c.segments; ++a) {
+            const float x = v[a];
+            uint32_t b = a;
+            while (b > 0 && v[b - 1u] > x) {
+                v[b] = v[b - 1u];
+                --b;
+            }
+            v[b] = x;
+        }
+        seg_level[slot & p->seg_mask] = v[c.segments / 2u];
+    }
+    return ok();
+}
+
+/* reference_excise_flag (:308-330) */
+int32_t or_excise_flag(const rv_excision_config* c0, const rv_excision_params* p, const rv_cf32* raw,
+                       uint64_t raw_len, const float* seg_level, uint64_t seg_len, uint32_t* flags,
+                       uint64_t flags_len) {
+    const rv_excision_config c = with_pass(c0, RV_EXCISE_FLAG);
+    if (excise_validate(&c, p)) return -1;
+    if (raw_len < ring_size(p->ring_mask) || seg_len < ring_size(p->seg_mask) || flags_len < ring_size(p->flag_mask))
+        return fail("excise_flag: short");
+    flush_scope s;
+    flush_begin(&s);
+    const float samples = (float)(1u << c.seg_log2);
+    for (uint32_t j = 0; j < p->count; ++j) {
+        const uint32_t slot = (p->first + j) & p->ring_mask;
+        const rv_cf32 v = raw[slot];
+        const float pw = v.re * v.re + v.im * v.im;
+        const float level = seg_level[(slot >> c.seg_log2) & p->seg_mask];
+        const float lhs = pw * samples;
+        const float rhs = p->threshold * level;
+        flags[(p->first + j) & p->flag_mask] = (level > 0.0F && lhs > rhs) ? 1u : 0u;
+    }
+    flush_end(&s);
+    return ok();
+}
+
+static int excise_flag_at(const rv_excision_params* p, const uint32_t* flags, int64_t rel) {
+    if (rel + p->history < 0) return 0;
+    return flags[(p->first + (uint32_t)rel) & p->flag_mask] != 0u;
+}
+
+static int excise_marked(const rv_excision_config* c, const rv_excision_params* p, const uint32_t* flags,
+                         int64_t rel) {
+    for (uint32_t m = 0; m <= c->hang + c->lead; ++m)
+        if (excise_flag_at(p, flags, rel - (int64_t)c->hang + m)) return 1;
+    return 0;
+}
+
+/* reference_excise_apply (:332-378) */
+int32_t or_excise_apply(const rv_excision_config* c0, const rv_excision_params* p, const rv_cf32* raw,
+                        uint64_t raw_len, const uint32_t* flags, uint64_t flags_len, rv_cf32* cleaned,
+                        rv_cf32* removed, uint64_t removed_len, uint32_t* counters) {
+    const rv_excision_config c = with_pass(c0, RV_EXCISE_APPLY);
+    if (excise_validate(&c, p)) return -1;
+    if (raw_len < ring_size(p->ring_mask) || flags_len < ring_size(p->flag_mask) ||
+        removed_len < ring_size(p->removed_mask))
+        return fail("excise_apply: short");
+    rv_cf32 nothing;
+    const uint32_t neg_zero = 0x80000000u;
+    memcpy(&nothing.re, &neg_zero, 4);
+    memcpy(&nothing.im, &neg_zero, 4);
+    for (uint32_t j = 0; j < p->count; ++j) {
+        const int64_t rel = j;
+        const uint32_t slot = (p->first + j) & p->ring_mask;
+        const rv_cf32 x = raw[slot];
+        int excise = 0;
+        if (excise_marked(&c, p, flags, rel)) {
+            uint32_t left = 0, right = 0;
+            for (uint32_t k = 1; k <= c.max_width; ++k) {
+                if (!excise_marked(&c, p, flags, rel - k)) break;
+                ++left;
+            }
+            for (uint32_t k = 1; k <= c.max_width; ++k) {
+                if (!excise_marked(&c, p, flags, rel + k)) break;
+                ++right;
+            }
+            excise = left + right + 1u <= c.max_width;
+            if (left == 0u) counters[excise ? RV_EXCISE_COUNTER_EVENTS : RV_EXCISE_COUNTER_SPARED] += 1u;
+        }
+        if (excise) counters[RV_EXCISE_COUNTER_SAMPLES] += 1u;
+        cleaned[slot] = excise ? nothing : x;
+        removed[(p->first + j) & p->removed_mask] = excise ? x : nothing;
+    }
+    return ok();
+}

@@ -93,4 +93,23 @@ int32_t or_iq_correct(const rv_iq_correct_params* p, const rv_cf32* in, uint64_t
                       uint64_t out_len);
 int32_t or_front_end_update(rv_front_end* st, const float* sums, uint64_t sums_len, uint32_t count, int64_t rate);
 int32_t or_front_end_correction(const rv_front_end* st, int32_t dc, int32_t iq, rv_iq_correct_params* out);
+
+/* impulse excision: twins of core/dsp/impulse_excision_reference.cpp */
+int32_t or_design_excision(int64_t source_rate, double max_width_seconds, rv_excision_config* out);
+float or_excision_threshold(double threshold_db);
+int32_t or_size_excision_rings(const rv_excision_config* c, uint64_t max_block, uint32_t frames_in_flight,
+                               uint32_t ring_mask, rv_excision_rings* out);
+int32_t or_excision_cursor_init(rv_excision_cursor* k, const rv_excision_config* c, uint32_t ring_mask,
+                                const rv_excision_rings* rings, float threshold);
+int32_t or_excision_plan_block(rv_excision_cursor* k, uint64_t start, uint32_t count, rv_excision_plan* out);
+int32_t or_excise_segment(const rv_excision_config* c, const rv_excision_params* p, const rv_cf32* raw,
+                          uint64_t raw_len, float* seg_power, uint64_t seg_len);
+int32_t or_excise_reference(const rv_excision_config* c, const rv_excision_params* p, const float* seg_power,
+                            float* seg_level, uint64_t seg_len);
+int32_t or_excise_flag(const rv_excision_config* c, const rv_excision_params* p, const rv_cf32* raw,
+                       uint64_t raw_len, const float* seg_level, uint64_t seg_len, uint32_t* flags,
+                       uint64_t flags_len);
+int32_t or_excise_apply(const rv_excision_config* c, const rv_excision_params* p, const rv_cf32* raw,
+                        uint64_t raw_len, const uint32_t* flags, uint64_t flags_len, rv_cf32* cleaned,
+                        rv_cf32* removed, uint64_t removed_len, uint32_t* counters);
 #endif

@@ -18,6 +18,7 @@
 
 #include "core/dsp/convert.h"
 #include "core/dsp/front_end_correction.h"
+#include "core/dsp/impulse_excision.h"
 #include "core/dsp/pfb.h"
 #include "core/dsp/pfb_branch_reference.h"
 #include "core/dsp/pfb_fft_reference.h"
@@ -446,6 +447,116 @@ int32_t ref_front_end_sequence(const float* sums, uint64_t stride, const uint32_
         corrections[b] = rv_iq_correct_params{0u, 0u, 0u, c.dc_i, c.dc_q, c.cross, c.scale};
     }
     return 0;
+}
+
+// core/dsp/impulse_excision_reference.cpp
+namespace {
+dsp::ExcisionConfig xcfg(const rv_excision_config* c) {
+    dsp::ExcisionConfig o;
+    o.pass = c->pass;
+    o.seg_log2 = c->seg_log2;
+    o.segments = c->segments;
+    o.max_width = c->max_width;
+    o.hang = c->hang;
+    o.lead = c->lead;
+    return o;
+}
+dsp::ExcisionParams xpar(const rv_excision_params* p) {
+    dsp::ExcisionParams o;
+    std::memcpy(&o, p, sizeof o);
+    return o;
+}
+void xout(const dsp::ExcisionParams& p, rv_excision_params* o) { std::memcpy(o, &p, sizeof *o); }
+std::span<const std::complex<float>> xcs(const rv_cf32* p, uint64_t n) {
+    return {reinterpret_cast<const std::complex<float>*>(p), n};
+}
+std::span<std::complex<float>> xms(rv_cf32* p, uint64_t n) { return {reinterpret_cast<std::complex<float>*>(p), n}; }
+}  // namespace
+
+int32_t ref_design_excision(int64_t rate, double max_width_seconds, rv_excision_config* out) {
+    const dsp::ExcisionConfig c = dsp::design_excision(rate, max_width_seconds);
+    out->pass = c.pass;
+    out->seg_log2 = c.seg_log2;
+    out->segments = c.segments;
+    out->max_width = c.max_width;
+    out->hang = c.hang;
+    out->lead = c.lead;
+    return 0;
+}
+
+float ref_excision_threshold(double db) { return dsp::excision_threshold(db); }
+
+int32_t ref_size_excision_rings(const rv_excision_config* c, uint64_t max_block, uint32_t frames, uint32_t ring_mask,
+                                rv_excision_rings* out) {
+    auto r = dsp::size_excision_rings(xcfg(c), max_block, frames, ring_mask);
+    if (!r) return report(r);
+    out->seg_mask = r->seg_mask;
+    out->flag_mask = r->flag_mask;
+    out->removed_mask = r->removed_mask;
+    return 0;
+}
+
+// An ExcisionCursor over `blocks` blocks [starts[b], starts[b] + counts[b]):
+// each block's plan.
+int32_t ref_excision_plans(const rv_excision_config* c, uint32_t ring_mask, const rv_excision_rings* rings,
+                           float threshold, const uint64_t* starts, const uint32_t* counts, uint32_t blocks,
+                           rv_excision_plan* plans) {
+    dsp::ExcisionRings rr;
+    rr.seg_mask = rings->seg_mask;
+    rr.flag_mask = rings->flag_mask;
+    rr.removed_mask = rings->removed_mask;
+    dsp::ExcisionCursor cursor(xcfg(c), ring_mask, rr, threshold);
+    for (uint32_t b = 0; b < blocks; ++b) {
+        const dsp::ExcisionPlan p = cursor.plan(starts[b], counts[b]);
+        rv_excision_plan& o = plans[b];
+        std::memset(&o, 0, sizeof o);
+        xout(p.segment, &o.segment);
+        xout(p.reference, &o.reference);
+        xout(p.flag, &o.flag);
+        xout(p.apply, &o.apply);
+        o.cleaned_end = p.cleaned_end;
+        o.restarted = p.restarted ? 1u : 0u;
+    }
+    return 0;
+}
+
+int32_t ref_excise_segment(const rv_excision_config* c, const rv_excision_params* p, const rv_cf32* raw,
+                           uint64_t raw_len, float* seg, uint64_t seg_len) {
+    dsp::ExcisionConfig cc = xcfg(c);
+    cc.pass = dsp::kExciseSegment;
+    auto st = dsp::reference_excise_segment(cc, xpar(p), xcs(raw, raw_len), std::span<float>(seg, seg_len));
+    return st ? 0 : report(st);
+}
+
+int32_t ref_excise_reference(const rv_excision_config* c, const rv_excision_params* p, const float* seg_power,
+                             float* seg_level, uint64_t seg_len) {
+    dsp::ExcisionConfig cc = xcfg(c);
+    cc.pass = dsp::kExciseReference;
+    auto st = dsp::reference_excise_reference(cc, xpar(p), std::span<const float>(seg_power, seg_len),
+                                              std::span<float>(seg_level, seg_len));
+    return st ? 0 : report(st);
+}
+
+int32_t ref_excise_flag(const rv_excision_config* c, const rv_excision_params* p, const rv_cf32* raw,
+                        uint64_t raw_len, const float* seg_level, uint64_t seg_len, uint32_t* flags,
+                        uint64_t flags_len) {
+    dsp::ExcisionConfig cc = xcfg(c);
+    cc.pass = dsp::kExciseFlag;
+    auto st = dsp::reference_excise_flag(cc, xpar(p), xcs(raw, raw_len), std::span<const float>(seg_level, seg_len),
+                                         std::span<std::uint32_t>(flags, flags_len));
+    return st ? 0 : report(st);
+}
+
+int32_t ref_excise_apply(const rv_excision_config* c, const rv_excision_params* p, const rv_cf32* raw,
+                         uint64_t raw_len, const uint32_t* flags, uint64_t flags_len, rv_cf32* cleaned,
+                         rv_cf32* removed, uint64_t removed_len, uint32_t* counters) {
+    dsp::ExcisionConfig cc = xcfg(c);
+    cc.pass = dsp::kExciseApply;
+    auto st = dsp::reference_excise_apply(cc, xpar(p), xcs(raw, raw_len),
+                                          std::span<const std::uint32_t>(flags, flags_len),
+                                          xms(cleaned, (uint64_t)p->ring_mask + 1u), xms(removed, removed_len),
+                                          std::span<std::uint32_t>(counters, 4));
+    return st ? 0 : report(st);
 }
 
 }  // extern "C"

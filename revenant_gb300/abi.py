@@ -150,6 +150,35 @@ def tracking_defaults(c):
     return c
 
 
+EXCISE_SEGMENT, EXCISE_REFERENCE, EXCISE_FLAG, EXCISE_APPLY = 0, 1, 2, 3
+EXCISE_COUNTER_SAMPLES, EXCISE_COUNTER_EVENTS, EXCISE_COUNTER_SPARED = 0, 1, 2
+
+
+class ExcisionConfig(_S):
+    _fields_ = [("pass_", U32), ("seg_log2", U32), ("segments", U32), ("max_width", U32), ("hang", U32),
+                ("lead", U32)]
+
+
+class ExcisionParams(_S):
+    _fields_ = [("ring_mask", U32), ("first", U32), ("count", U32), ("seg_mask", U32), ("flag_mask", U32),
+                ("removed_mask", U32), ("history", I32), ("threshold", F32)]
+
+
+class ExcisionRings(_S):
+    _fields_ = [("seg_mask", U32), ("flag_mask", U32), ("removed_mask", U32)]
+
+
+class ExcisionPlan(_S):
+    _fields_ = [("segment", ExcisionParams), ("reference", ExcisionParams), ("flag", ExcisionParams),
+                ("apply", ExcisionParams), ("cleaned_end", U64), ("restarted", U32), ("reserved", U32)]
+
+
+class ExcisionCursor(_S):
+    _fields_ = [("config", ExcisionConfig), ("ring_mask", U32), ("rings", ExcisionRings), ("threshold", F32),
+                ("running", U32), ("reserved", U32), ("valid_from", U64), ("next_in", U64), ("seg_next", U64),
+                ("flag_next", U64), ("apply_next", U64)]
+
+
 TRACK_PENDING, TRACK_LIVE, TRACK_HELD, TRACK_MERGED = 0, 1, 2, 3
 
 
@@ -236,7 +265,9 @@ class ChainStats(_S):
 
 EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params": IqCorrectParams,
                  "rv_front_end": FrontEnd, "rv_detector_config": DetectorConfig, "rv_detector_candidate": DetectorCandidate,
-                 "rv_detector_track": DetectorTrack,
+                 "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
+                 "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,
+                 "rv_excision_plan": ExcisionPlan, "rv_excision_cursor": ExcisionCursor,
                  "rv_detector_stats": DetectorStats, "rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
 
 

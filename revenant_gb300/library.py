@@ -175,6 +175,18 @@ SIGNATURES = {
     "rv_detector_state": (I32, [P, P, P, U64]),
     "rv_detector_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
     "rv_detector_tracks": (I32, [P, I32, P, U32, ptr(U32)]),
+    "rv_design_excision": (I32, [I64, F64, ptr(abi.ExcisionConfig)]),
+    "rv_excision_threshold": (F32, [F64]),
+    "rv_size_excision_rings": (I32, [ptr(abi.ExcisionConfig), U64, U32, U32, ptr(abi.ExcisionRings)]),
+    "rv_excision_cursor_init": (I32, [ptr(abi.ExcisionCursor), ptr(abi.ExcisionConfig), U32,
+                                      ptr(abi.ExcisionRings), F32]),
+    "rv_excision_plan_block": (I32, [ptr(abi.ExcisionCursor), U64, U32, ptr(abi.ExcisionPlan)]),
+    "rv_excise_segment": (I32, [P, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, U64, P, U64]),
+    "rv_excise_reference": (I32, [P, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, P, U64]),
+    "rv_excise_flag": (I32, [P, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, U64, P, U64, P, U64]),
+    "rv_excise_apply": (I32, [P, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, U64, P, U64, P, P, U64, P]),
+    "rv_excise_block": (I32, [P, ptr(abi.ExcisionConfig), ptr(abi.ExcisionPlan), P, U64, P, P, U64, P, U64, P, U64,
+                              P]),
     "rv_tracker_create": (I32, [ptr(abi.DetectorConfig), ptr(P)]),
     "rv_tracker_destroy": (I32, [P]),
     "rv_tracker_update": (I32, [P, U64, F64, P, U32]),

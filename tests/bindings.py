@@ -44,6 +44,13 @@ def _sig(lib, prefix):
     f("vrx_carrier", I32, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P)
     f("iq_moments", I32, ptr(abi.IqMomentsParams), P, U64, P, U64)
     f("iq_correct", I32, ptr(abi.IqCorrectParams), P, U64, P, U64)
+    f("design_excision", I32, I64, F64, ptr(abi.ExcisionConfig))
+    f("excision_threshold", F32, F64)
+    f("size_excision_rings", I32, ptr(abi.ExcisionConfig), U64, U32, U32, ptr(abi.ExcisionRings))
+    f("excise_segment", I32, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, U64, P, U64)
+    f("excise_reference", I32, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, P, U64)
+    f("excise_flag", I32, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, U64, P, U64, P, U64)
+    f("excise_apply", I32, ptr(abi.ExcisionConfig), ptr(abi.ExcisionParams), P, U64, P, U64, P, P, U64, P)
 
 
 _oracle = None
@@ -63,6 +70,11 @@ def oracle():
         lib.or_front_end_update.argtypes = [ptr(abi.FrontEnd), P, U64, U32, I64]
         lib.or_front_end_correction.restype = I32
         lib.or_front_end_correction.argtypes = [ptr(abi.FrontEnd), I32, I32, ptr(abi.IqCorrectParams)]
+        lib.or_excision_cursor_init.restype = I32
+        lib.or_excision_cursor_init.argtypes = [ptr(abi.ExcisionCursor), ptr(abi.ExcisionConfig), U32,
+                                                ptr(abi.ExcisionRings), F32]
+        lib.or_excision_plan_block.restype = I32
+        lib.or_excision_plan_block.argtypes = [ptr(abi.ExcisionCursor), U64, U32, ptr(abi.ExcisionPlan)]
         lib.or_pfb_f64.restype = I32
         lib.or_pfb_f64.argtypes = [ptr(abi.GridParams), P, P, U32, U32, U32, U32, P, P]
         _oracle = Lib(lib, "or_")
@@ -110,6 +122,8 @@ def reference():
         lib.ref_front_end_sequence.argtypes = [P, U64, P, U32, I64, I32, I32, P, P]
         lib.ref_lwdsp_window.restype = I32
         lib.ref_lwdsp_window.argtypes = [U32, U32, P]
+        lib.ref_excision_plans.restype = I32
+        lib.ref_excision_plans.argtypes = [ptr(abi.ExcisionConfig), U32, ptr(abi.ExcisionRings), F32, P, P, U32, P]
         lib.ref_lwdsp_spectrum.restype = I32
         lib.ref_lwdsp_spectrum.argtypes = [U32, U32, F32, P, U64, P]
         _reference = Lib(lib, "ref_")
