@@ -606,6 +606,19 @@ int32_t rv_chain_read_spectrum(rv_chain* chain, float* out, uint64_t capacity, u
 int32_t rv_chain_set_front_end(rv_chain* chain, int32_t dc_removal, int32_t iq_correction, uint32_t lag);
 /* The current estimate (Graph::front_end_correction); drains first. */
 int32_t rv_chain_front_end_estimate(rv_chain* chain, rv_front_end* out);
+/* Graph's span-wide impulse excision (EngineConfig::impulse_excision,
+ * core/engine/graph.cpp:1461-1525): from the next run on, every run's samples
+ * are excised in place after the front-end correction (rv_excise_block over
+ * the run's ExcisionCursor plan, the stage designed by design_excision for
+ * the chain's rate and max_width_seconds, threshold in dB: 15 is the
+ * reference's default), and the channelizer reads only the samples the stage
+ * has finished. In the batched mode the samples then pass through a cf32 ring
+ * the fused channelizer reads. Off by default; switching on restarts the
+ * stage. Drains first. */
+int32_t rv_chain_set_impulse_excision(rv_chain* chain, int32_t on, double threshold_db, double max_width_seconds);
+/* Samples excised, runs excised, runs spared and samples examined since the
+ * chain was created (drains first). */
+int32_t rv_chain_excision_counters(rv_chain* chain, uint64_t* out4);
 /* Waits for all of the chain's device work (a run returns with its audio
  * read back already; this is the engine's drain at stop). */
 int32_t rv_chain_drain(rv_chain* chain);

@@ -89,6 +89,16 @@ class Chain:
         """Front-end DC / IQ-imbalance correction from the next run on."""
         check(lib().rv_chain_set_front_end(self.handle, 1 if dc else 0, 1 if iq else 0, lag))
 
+    def set_impulse_excision(self, on=True, threshold_db=15.0, max_width_seconds=20e-6):
+        """Span-wide impulse excision from the next run on (off by default)."""
+        check(lib().rv_chain_set_impulse_excision(self.handle, 1 if on else 0, threshold_db, max_width_seconds))
+
+    def excision_counters(self):
+        """(samples excised, runs excised, runs spared, samples examined)."""
+        out = (C.c_uint64 * 4)()
+        check(lib().rv_chain_excision_counters(self.handle, out))
+        return tuple(int(x) for x in out)
+
     def front_end_estimate(self):
         st = abi.FrontEnd()
         check(lib().rv_chain_front_end_estimate(self.handle, C.byref(st)))

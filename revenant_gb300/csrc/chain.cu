@@ -47,6 +47,8 @@ int32_t detector_release_to(rv_detector* d, cudaStream_t producer);
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
                             const void* raw, const float* taps, const rv_cf32* tw, rv_cf32* ring,
                             const rv_coarse_params* dyn = nullptr, const FrontEndTable* fe = nullptr);
+int32_t launch_convert_ring(cudaStream_t stream, int32_t format, const void* raw, uint32_t mask, uint32_t from,
+                            uint32_t count, uint32_t window_start, const FrontEndTable* fe, rv_cf32* clean);
 }  // namespace rv
 
 using namespace rv;
@@ -151,7 +153,7 @@ struct Receiver {
 // captures again.
 struct GraphShape {
     uint32_t fine = 0, carrier = 0, unit_items = 0, units = 0, tiles = 0, nrx = 0;
-    uint32_t fine_window = 0, weights_cap = 0, unit_budget = 0, tile_shared = 0, front_end = 0;
+    uint32_t fine_window = 0, weights_cap = 0, unit_budget = 0, tile_shared = 0, front_end = 0, excision = 0;
     const void* tiles_ptr = nullptr;
     const void* spans_ptr = nullptr;
     const void* audio_ptr = nullptr;
@@ -280,6 +282,24 @@ struct rv_chain {
     bool spec_recorded = false;
     uint64_t group_delay = 0;  // the prototype's, in input samples
     rv_detector* detector = nullptr;
+    // impulse excision (Graph::plan_impulse_excision / record_impulse_excision)
+    bool ex_on = false, ex_was_on = false;
+    rv_excision_config ex_cfg{};
+    rv_excision_rings ex_rings{};
+    rv_excision_cursor ex_cursor{};
+    float ex_threshold = 0.0F;
+    DeviceArray<rv_cf32> clean;  // batched: the converted, corrected, excised samples (raw ring's slots)
+    DeviceArray<float> ex_seg_power, ex_seg_level;
+    DeviceArray<uint32_t> ex_flags, ex_counters;
+    DeviceArray<rv_cf32> ex_removed;
+    rv_excision_plan ex_plan{};
+    uint64_t ex_converted_end = 0;  // batched: the clean ring holds converted samples up to here
+    // batched: the channelizer reads the clean ring. Set once the stage was
+    // on, and kept after it is switched off, because the channelizer's history
+    // still reaches back into samples the stage excised.
+    bool ex_clean = false;
+    uint64_t ex_examined = 0;
+    uint64_t ex_totals[3] = {0, 0, 0};  // samples, events, spared read back so far
 };
 
 namespace {
@@ -437,6 +457,33 @@ int32_t fe_table(rv_chain* c, int64_t window, bool keep_pointer) {
     return RV_OK;
 }
 
+// Graph::plan_impulse_excision (core/engine/graph.cpp:1468-1488): the plan of
+// this run's excision passes, or null while the stage is off. Switching it on
+// restarts the cursor, which then waits for a full reference window.
+const rv_excision_plan* plan_excision(rv_chain* c, uint64_t start, uint64_t count) {
+    if (!c->ex_on) {
+        c->ex_was_on = false;
+        return nullptr;
+    }
+    if (!c->ex_was_on) c->ex_cursor.running = 0;
+    c->ex_was_on = true;
+    (void)rv_excision_plan_block(&c->ex_cursor, start, (uint32_t)count, &c->ex_plan);
+    return &c->ex_plan;
+}
+
+// Graph::record_impulse_excision: the plan's passes, in place on `ring`.
+int32_t excise(rv_chain* c, const rv_excision_plan& plan, rv_cf32* ring) {
+    const uint64_t n = (uint64_t)c->raw_mask + 1u;
+    if (int32_t st = rv_excise_block(c->stream, &c->ex_cfg, &plan, ring, n, c->ex_seg_power.ptr, c->ex_seg_level.ptr,
+                                     c->ex_seg_power.count, c->ex_flags.ptr, c->ex_flags.count, c->ex_removed.ptr,
+                                     c->ex_removed.count, c->ex_counters.ptr))
+        return st;
+    for (const rv_excision_params* q : {&plan.segment, &plan.reference, &plan.flag, &plan.apply})
+        if (q->count) c->stats.launches += 1;
+    c->ex_examined += plan.apply.count;
+    return RV_OK;
+}
+
 // Graph::on_block's spectrum frame (core/engine/graph.cpp:5077-5095,
 // 5218-5286): when the run completed N or more channel blocks, one frame of
 // the last N (central half of each channel's N-point transform, dB), covering
@@ -557,7 +604,7 @@ int32_t copy_into_ring(rv_chain* c, uint8_t* ring, uint64_t ring_samples, uint64
 }
 
 int32_t coarse_plain(rv_chain* c, uint64_t first_sample, const uint8_t* src, uint64_t count, int32_t where,
-                     uint64_t first_block, uint32_t blocks) {
+                     uint64_t first_block, uint32_t blocks, const rv_excision_plan* excision) {
     const rv_grid_params& g = c->config.grid;
     // staging copy of this run's raw bytes, then convert into the cf32 ring
     if (int32_t st = copy_into_ring(c, c->raw.ptr, count + 1, 0, src, count, where)) return st;
@@ -581,6 +628,9 @@ int32_t coarse_plain(rv_chain* c, uint64_t first_sample, const uint8_t* src, uin
             c->stats.launches += 1;
         }
     }
+    // impulse excision in place on the corrected ring
+    if (excision != nullptr)
+        if (int32_t st = excise(c, *excision, c->cf32_ring.ptr)) return st;
     if (blocks == 0) return RV_OK;
     rv_pfb_branch_params bp{c->raw_mask, (uint32_t)(first_block * g.decimation), blocks};
     if (int32_t st = rv_pfb_branch(c->stream, &g, &bp, c->proto.ptr, c->proto.count, c->cf32_ring.ptr,
@@ -598,7 +648,8 @@ int32_t coarse_plain(rv_chain* c, uint64_t first_sample, const uint8_t* src, uin
 // With `deferred`, the coarse parameters are returned for a captured run to
 // hand to its graph instead of being launched here.
 int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, uint64_t count, int32_t where,
-                       uint64_t first_block, uint32_t blocks, rv_coarse_params* deferred) {
+                       uint64_t first_block, uint32_t blocks, rv_coarse_params* deferred,
+                       const rv_excision_plan* excision) {
     const rv_grid_params& g = c->config.grid;
     if (int32_t st = copy_into_ring(c, c->raw.ptr, (uint64_t)c->raw_mask + 1u, first_sample, src, count, where))
         return st;
@@ -609,10 +660,30 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
     (void)fe_prepare(c, first_sample, count, &fe_on);
     if (fe_on)
         if (int32_t st = fe_moments(c, first_sample, (uint32_t)count)) return st;
-    if (blocks == 0) return RV_OK;
     const int64_t window = (int64_t)(first_block * g.decimation) - (int64_t)((uint64_t)g.channels * g.taps_per_branch - 1u);
+    const bool clean = c->ex_clean;
+    if (clean) {
+        // the run's samples into the cf32 ring, converted and corrected as the
+        // fused kernel would, then excised in place; on a restart also the
+        // channelizer's history behind them, which the ring does not hold yet
+        uint64_t from = first_sample;
+        if (c->ex_converted_end != first_sample) from = std::min<uint64_t>(from, window > 0 ? (uint64_t)window : 0u);
+        const int64_t table_at = std::min<int64_t>((int64_t)from, window);
+        if (int32_t st = fe_table(c, table_at, false)) return st;
+        if (int32_t st = launch_convert_ring(c->stream, c->config.format, c->raw.ptr, c->raw_mask, (uint32_t)from,
+                                             (uint32_t)(first_sample + count - from), (uint32_t)table_at, c->fe_table,
+                                             c->clean.ptr))
+            return st;
+        c->stats.launches += 1;
+        c->fe_table = nullptr;  // applied: the coarse kernel reads corrected samples
+        c->ex_converted_end = first_sample + count;
+        if (excision != nullptr)
+            if (int32_t st = excise(c, *excision, c->clean.ptr)) return st;
+    }
+    if (blocks == 0) return RV_OK;
     // a captured graph reads the table whenever front-end correction is on
-    if (int32_t st = fe_table(c, window, c->graph && fe_on)) return st;
+    if (!clean)
+        if (int32_t st = fe_table(c, window, c->graph && fe_on)) return st;
     // stream-start history reads as zero, as the plain path's zeroed ring does
     const uint64_t support = (uint64_t)g.channels * g.taps_per_branch - 1u;
     const uint64_t centre = first_block * g.decimation;
@@ -623,7 +694,8 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
         *deferred = p;
         return RV_OK;
     }
-    if (int32_t st = launch_coarse_fused(c->stream, g, c->config.format, p, c->raw.ptr, c->proto.ptr,
+    if (int32_t st = launch_coarse_fused(c->stream, g, clean ? kFormatCf32Ring : c->config.format, p,
+                                         clean ? static_cast<const void*>(c->clean.ptr) : c->raw.ptr, c->proto.ptr,
                                          c->twiddles.ptr, c->channel.ptr, nullptr, c->fe_table))
         return st;
     c->stats.launches += 1;
@@ -802,7 +874,8 @@ int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
     cudaGraph_t graph = nullptr;
     if (int32_t st = cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "graph capture begin"))
         return st;
-    int32_t st = launch_coarse_fused(c->stream, c->config.grid, c->config.format, coarse, c->raw.ptr, c->proto.ptr,
+    int32_t st = launch_coarse_fused(c->stream, c->config.grid, sh.excision ? kFormatCf32Ring : c->config.format, coarse,
+                                     sh.excision ? static_cast<const void*>(c->clean.ptr) : c->raw.ptr, c->proto.ptr,
                                      c->twiddles.ptr, c->channel.ptr, &rc->coarse,
                                      sh.front_end ? S(c).fe_dev.ptr : nullptr);
     if (!st)
@@ -851,7 +924,7 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
     if (int32_t st = upload_spans(c, spans)) return st;
     const bool fits = S(c).exec != nullptr && fine.size() <= sh.fine && carrier.size() <= sh.carrier &&
                       sh.nrx == nrx && sh.spans_ptr == S(c).spans_dev.ptr && unit_items.size() <= sh.unit_items &&
-                      sh.front_end == (c->fe_table != nullptr ? 1u : 0u) &&
+                      sh.front_end == (c->fe_table != nullptr ? 1u : 0u) && sh.excision == (c->ex_clean ? 1u : 0u) &&
                       units.size() <= sh.units && tiles.size() <= sh.tiles && sh.tile_shared == c->tile_shared &&
                       sh.tiles_ptr == S(c).tiles_dev.ptr && window <= sh.fine_window && sh.weights_cap == c->weights_cap &&
                       sh.unit_budget == c->unit_budget && sh.audio_ptr == S(c).audio_dev.ptr &&
@@ -869,6 +942,7 @@ int32_t run_captured(rv_chain* c, const rv_coarse_params& coarse, const std::vec
         n.nrx = nrx;
         n.spans_ptr = S(c).spans_dev.ptr;
         n.front_end = c->fe_table != nullptr ? 1u : 0u;
+        n.excision = c->ex_clean ? 1u : 0u;
         n.unit_items = grow(unit_items.size(), sh.unit_items);
         n.units = grow(units.size(), sh.units);
         n.tiles = grow(tiles.size(), sh.tiles);
@@ -981,7 +1055,11 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     if (c->config.attenuation_db <= 0.0) c->config.attenuation_db = 120.0;
     rv_front_end_init(&c->fe);
     c->bytes_per_sample = config->format == RV_FORMAT_CS16 ? 4u : 2u;
-    const uint64_t history = (uint64_t)g.channels * g.taps_per_branch + g.decimation;
+    // the filter history, and room for the impulse excision's lag (the
+    // channelizer then reads up to max_width + lead or a segment behind the
+    // newest sample)
+    const uint64_t history = (uint64_t)g.channels * g.taps_per_branch + g.decimation +
+                             (uint64_t)RV_EXCISE_MAX_WIDTH + RV_EXCISE_MAX_GUARD + (1u << RV_EXCISE_MAX_SEG_LOG2);
     // pipelined: two runs in the ring beyond the history, so that a run's input
     // copy never overwrites samples the run before it still reads
     const uint64_t runs_held = config->pipelined ? 2u : 1u;
@@ -1048,6 +1126,12 @@ int32_t rv_chain_destroy(rv_chain* c) {
     }
     c->raw.release();
     c->cf32_ring.release();
+    c->clean.release();
+    c->ex_seg_power.release();
+    c->ex_seg_level.release();
+    c->ex_flags.release();
+    c->ex_counters.release();
+    c->ex_removed.release();
     c->branch.release();
     c->channel.release();
     c->proto.release();
@@ -1179,17 +1263,22 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
     const bool plain = c->config.mode == RV_CHAIN_PLAIN;
     const uint8_t* src = static_cast<const uint8_t*>(samples);
     const uint64_t first_sample = c->samples_in;
-    const uint64_t newest_sample = first_sample + count - 1u;
-    const uint64_t last_block = newest_sample / g.decimation;
     const uint64_t first_block = c->next_block;
-    const uint32_t blocks = last_block >= first_block ? (uint32_t)(last_block - first_block + 1u) : 0u;
+    // the impulse excision lags the newest sample and the channelizer reads
+    // only what it has finished (Graph::on_block, core/engine/graph.cpp:5025-5052)
+    const rv_excision_plan* excision = plan_excision(c, first_sample, count);
+    const uint64_t limit = excision ? std::min<uint64_t>(first_sample + count, excision->cleaned_end)
+                                    : first_sample + count;
+    uint32_t blocks = 0;
+    if (limit > first_block * g.decimation) blocks = (uint32_t)((limit - 1u) / g.decimation - first_block + 1u);
+    const uint64_t last_block = first_block + blocks - 1u;  // meaningful when blocks > 0
     mark(c, 0);
     // a captured run launches the coarse kernel inside its graph
     c->captured_run = !plain && c->graph && blocks > 0 && !c->rx.empty();
     rv_coarse_params coarse{};
-    int32_t st = plain ? coarse_plain(c, first_sample, src, count, where, first_block, blocks)
+    int32_t st = plain ? coarse_plain(c, first_sample, src, count, where, first_block, blocks, excision)
                        : coarse_batched(c, first_sample, src, count, where, first_block, blocks,
-                                        c->captured_run ? &coarse : nullptr);
+                                        c->captured_run ? &coarse : nullptr, excision);
     if (st) return st;
     if (!c->captured_run) mark(c, 2);
     c->samples_in += count;
@@ -1506,6 +1595,67 @@ int32_t rv_chain_front_end_estimate(rv_chain* c, rv_front_end* out) {
     if (c == nullptr || out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_front_end_estimate: NULL");
     if (int32_t st = collect_all(c)) return st;
     *out = c->fe;
+    return clear_error();
+}
+
+int32_t rv_chain_set_impulse_excision(rv_chain* c, int32_t on, double threshold_db, double max_width_seconds) {
+    if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_impulse_excision: NULL");
+    if (int32_t st = rv_chain_drain(c)) return st;
+    if (!on) {
+        c->ex_on = false;
+        return clear_error();
+    }
+    if (!std::isfinite(threshold_db) || threshold_db < -100.0 || threshold_db > 100.0)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_impulse_excision: threshold %g dB", threshold_db);
+    if (!std::isfinite(max_width_seconds) || max_width_seconds <= 0.0)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_set_impulse_excision: max width %g s", max_width_seconds);
+    rv_excision_config cfg{};
+    if (int32_t st = rv_design_excision(c->config.rate, max_width_seconds, &cfg)) return st;
+    rv_excision_rings rings{};
+    if (int32_t st = rv_size_excision_rings(&cfg, c->config.max_run_samples, pipelined(c) ? 2u : 1u, c->raw_mask, &rings))
+        return st;
+    const uint64_t cap = (uint64_t)c->raw_mask + 1u;
+    int32_t st = RV_OK;
+    if (c->config.mode == RV_CHAIN_BATCHED && c->clean.count < cap) st = c->clean.alloc(cap);
+    if (!st && c->ex_seg_power.count != (uint64_t)rings.seg_mask + 1u) {
+        st = c->ex_seg_power.alloc((uint64_t)rings.seg_mask + 1u);
+        if (!st) st = c->ex_seg_level.alloc((uint64_t)rings.seg_mask + 1u);
+    }
+    if (!st && c->ex_flags.count != (uint64_t)rings.flag_mask + 1u) st = c->ex_flags.alloc((uint64_t)rings.flag_mask + 1u);
+    if (!st && c->ex_removed.count != (uint64_t)rings.removed_mask + 1u)
+        st = c->ex_removed.alloc((uint64_t)rings.removed_mask + 1u);
+    if (!st && c->ex_counters.count == 0) st = c->ex_counters.alloc(RV_EXCISE_COUNTERS);
+    if (!st)
+        st = cuda_status(cudaMemsetAsync(c->ex_counters.ptr, 0, RV_EXCISE_COUNTERS * sizeof(uint32_t), c->stream),
+                         "excision counters");
+    if (st) return st;
+    c->ex_cfg = cfg;
+    c->ex_rings = rings;
+    c->ex_threshold = rv_excision_threshold(threshold_db);
+    if (int32_t e = rv_excision_cursor_init(&c->ex_cursor, &cfg, c->raw_mask, &rings, c->ex_threshold)) return e;
+    c->ex_on = true;
+    c->ex_was_on = false;
+    if (c->config.mode == RV_CHAIN_BATCHED && !c->ex_clean) {
+        c->ex_clean = true;
+        c->ex_converted_end = ~0ull;  // the clean ring holds nothing of this stream yet
+    }
+    return clear_error();
+}
+
+int32_t rv_chain_excision_counters(rv_chain* c, uint64_t* out) {
+    if (c == nullptr || out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_excision_counters: NULL");
+    if (int32_t st = rv_chain_drain(c)) return st;
+    if (c->ex_counters.count) {
+        uint32_t d[RV_EXCISE_COUNTERS] = {0, 0, 0, 0};
+        if (int32_t st = cuda_status(cudaMemcpy(d, c->ex_counters.ptr, sizeof d, cudaMemcpyDeviceToHost),
+                                     "excision counters"))
+            return st;
+        if (int32_t st = cuda_status(cudaMemsetAsync(c->ex_counters.ptr, 0, sizeof d, c->stream), "excision counters"))
+            return st;
+        for (int k = 0; k < 3; ++k) c->ex_totals[k] += d[k];
+    }
+    for (int k = 0; k < 3; ++k) out[k] = c->ex_totals[k];
+    out[3] = c->ex_examined;
     return clear_error();
 }
 

@@ -30,6 +30,8 @@
 #include <stdint.h>
 #include <stdlib.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "receivers.cuh"
 #include "revenant_gb300.h"
@@ -70,6 +72,8 @@ __device__ __forceinline__ float2 load_sample(const uint32_t* __restrict__ raw, 
 
 template <int FMT>
 __device__ __forceinline__ float2 convert_sample(const uint32_t* __restrict__ raw, uint32_t pos) {
+    // a cf32 ring (already converted, corrected and excised) is read as is
+    if (FMT == kFormatCf32Ring) return __ldg(reinterpret_cast<const float2*>(raw) + pos);
     return convert_raw<FMT>(raw, pos);
 }
 
@@ -266,7 +270,53 @@ int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, cons
     return cuda_status(cudaGetLastError(), "coarse_fused launch");
 }
 
+// Source samples [from, from + count) of the raw ring converted into the cf32
+// ring at the same slots, each corrected with the parameters of the run it
+// arrived in (the table's entries are relative to window_start), exactly as
+// the coarse kernel converts and corrects the samples it loads.
+template <int FMT, bool FE>
+__global__ void k_convert_ring(const uint32_t* __restrict__ raw, uint32_t mask, uint32_t from, uint32_t count,
+                               uint32_t window_start, const FrontEndTable* fe_g, float2* __restrict__ clean) {
+    __shared__ FrontEndTable fe_s[1];
+    if (FE) {
+        for (uint32_t i = threadIdx.x; i < sizeof(FrontEndTable) / 4u; i += blockDim.x)
+            reinterpret_cast<uint32_t*>(fe_s)[i] = reinterpret_cast<const uint32_t*>(fe_g)[i];
+        __syncthreads();
+    }
+    rv_coarse_params p{};
+    p.ring_mask = mask;
+    p.lead_zero = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t n = from + i;
+        clean[n & mask] = load_sample<FMT, FE>(raw, n, p, window_start, fe_s);
+    }
+}
+
+template <int FMT>
+int32_t convert_ring(cudaStream_t s, const uint32_t* raw, uint32_t mask, uint32_t from, uint32_t count,
+                     uint32_t window_start, const FrontEndTable* fe, float2* clean) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t grid = std::min<uint32_t>((count + 255u) / 256u, (uint32_t)(sms > 0 ? sms : 1) * 8u);
+    if (fe)
+        k_convert_ring<FMT, true><<<grid, 256, 0, s>>>(raw, mask, from, count, window_start, fe, clean);
+    else
+        k_convert_ring<FMT, false><<<grid, 256, 0, s>>>(raw, mask, from, count, window_start, fe, clean);
+    return cuda_status(cudaGetLastError(), "convert_ring launch");
+}
+
 }  // namespace
+
+int32_t launch_convert_ring(cudaStream_t stream, int32_t format, const void* raw, uint32_t mask, uint32_t from,
+                            uint32_t count, uint32_t window_start, const FrontEndTable* fe, rv_cf32* clean) {
+    if (count == 0) return RV_OK;
+    const uint32_t* w = static_cast<const uint32_t*>(raw);
+    float2* out = reinterpret_cast<float2*>(clean);
+    if (format == RV_FORMAT_CS16) return convert_ring<RV_FORMAT_CS16>(stream, w, mask, from, count, window_start, fe, out);
+    if (format == RV_FORMAT_CU8) return convert_ring<RV_FORMAT_CU8>(stream, w, mask, from, count, window_start, fe, out);
+    return set_error_fmt(RV_ERR_UNSUPPORTED, "convert_ring: format %d", format);
+}
 
 // Dispatch over the instantiated grids. Returns RV_ERR_UNSUPPORTED for a
 // grid this build has no fused kernel for (the plain kernels cover it).
@@ -282,6 +332,8 @@ int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_
         if (format == RV_FORMAT_CU8)                                                                     \
             return fe ? launch<MM, TT, DD, RV_FORMAT_CU8, SS, true>(stream, w, taps, tw, ring, p, dyn, fe)    \
                       : launch<MM, TT, DD, RV_FORMAT_CU8, SS, false>(stream, w, taps, tw, ring, p, dyn, fe);  \
+        if (format == kFormatCf32Ring && fe == nullptr)                                                  \
+            return launch<MM, TT, DD, kFormatCf32Ring, SS, false>(stream, w, taps, tw, ring, p, dyn, fe);   \
     }
     RV_COARSE_CASE(64, 17, 32, 1)
     RV_COARSE_CASE(8, 17, 4, 8)

@@ -154,6 +154,10 @@ struct RunCounts {
 // samples from `rel_start` (relative to the launch's window start) up to the
 // next entry's, `on` when the correction was applied to that run's samples.
 constexpr uint32_t kFrontEndEntries = 16;
+// The fused coarse kernel's input format for a cf32 sample ring that was
+// converted, corrected and excised before it (impulse excision on).
+constexpr int kFormatCf32Ring = 100;
+
 struct FrontEndEntry {
     uint32_t rel_start, on;
     float dc_i, dc_q, cross, scale;

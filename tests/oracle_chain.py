@@ -79,6 +79,55 @@ class OracleChain:
     def set_front_end(self, dc, iq, lag=1):
         self.fe_dc, self.fe_iq, self.fe_lag = bool(dc), bool(iq), lag
 
+    def set_impulse_excision(self, on=True, threshold_db=15.0, max_width_seconds=20e-6, max_block=1 << 16):
+        """The span-wide impulse excision (Graph::plan_impulse_excision and
+        record_impulse_excision, core/engine/graph.cpp:1461-1525) with the
+        oracle's cursor and passes, in place on the ring."""
+        o = self.ora
+        self.ex_on = bool(on)
+        if not on:
+            return
+        self.ex_cfg = abi.ExcisionConfig()
+        assert o.fn("design_excision")(self.rate, max_width_seconds, C.byref(self.ex_cfg)) == 0
+        self.ex_rings = abi.ExcisionRings()
+        assert o.fn("size_excision_rings")(C.byref(self.ex_cfg), max_block, 1, self.ring_mask,
+                                           C.byref(self.ex_rings)) == 0, o.error()
+        self.ex_cursor = abi.ExcisionCursor()
+        thr = o.fn("excision_threshold")(threshold_db)
+        assert o.lib.or_excision_cursor_init(C.byref(self.ex_cursor), C.byref(self.ex_cfg), self.ring_mask,
+                                             C.byref(self.ex_rings), thr) == 0
+        r = self.ex_rings
+        self.ex_seg_power = np.zeros(r.seg_mask + 1, np.float32)
+        self.ex_seg_level = np.zeros(r.seg_mask + 1, np.float32)
+        self.ex_flags = np.zeros(r.flag_mask + 1, np.uint32)
+        self.ex_removed = cf32(r.removed_mask + 1)
+        self.ex_counters = np.zeros(4, np.uint32)
+        self.ex_examined = 0
+
+    def excise(self, start, count):
+        """Plans this run and runs the passes; returns the channel limit."""
+        o = self.ora
+        plan = abi.ExcisionPlan()
+        assert o.lib.or_excision_plan_block(C.byref(self.ex_cursor), start, count, C.byref(plan)) == 0
+        d = lambda a: a.ctypes.data  # noqa: E731
+        n = self.ring.shape[0]
+        c = self.ex_cfg
+        if plan.segment.count:
+            assert o.fn("excise_segment")(C.byref(c), C.byref(plan.segment), d(self.ring), n, d(self.ex_seg_power),
+                                          self.ex_seg_power.size) == 0, o.error()
+        if plan.reference.count:
+            assert o.fn("excise_reference")(C.byref(c), C.byref(plan.reference), d(self.ex_seg_power),
+                                            d(self.ex_seg_level), self.ex_seg_power.size) == 0, o.error()
+        if plan.flag.count:
+            assert o.fn("excise_flag")(C.byref(c), C.byref(plan.flag), d(self.ring), n, d(self.ex_seg_level),
+                                       self.ex_seg_level.size, d(self.ex_flags), self.ex_flags.size) == 0, o.error()
+        if plan.apply.count:
+            assert o.fn("excise_apply")(C.byref(c), C.byref(plan.apply), d(self.ring), n, d(self.ex_flags),
+                                        self.ex_flags.size, d(self.ring), d(self.ex_removed),
+                                        self.ex_removed.shape[0], d(self.ex_counters)) == 0, o.error()
+        self.ex_examined += plan.apply.count
+        return min(start + count, plan.cleaned_end)
+
     def front_end(self, destination, count):
         """Moments of this run's samples, the estimate updated with the runs
         at least `lag` before this one, then this run corrected in place."""
@@ -115,8 +164,13 @@ class OracleChain:
         self.front_end(self.samples_in & self.ring_mask, count)
         self.run_index += 1
         first_block = self.next_block
-        last_block = (self.samples_in + count - 1) // D
+        limit = self.samples_in + count
+        if getattr(self, "ex_on", False):
+            limit = self.excise(self.samples_in, count)
         self.samples_in += count
+        if limit <= first_block * D:
+            return
+        last_block = (limit - 1) // D
         if last_block < first_block:
             return
         blocks = last_block - first_block + 1

@@ -327,7 +327,7 @@ def test_gpu_excision_matches_oracle(gpu, ora, rate, block, log2, nblocks):
     signal = scene(starts[-1] + counts[-1] - origin, 11, rate, c.max_width)
     ps = plans("rv", c, ring_mask, rings, thr, starts, counts)
     r = run_gpu(gpu, c, ps, starts, counts, signal, origin, ring_mask, rings, check_every=1, ora=ora)
-    assert r.counters[abi.EXCISE_COUNTER_EVENTS] > 5
+    assert r.counters[abi.EXCISE_COUNTER_EVENTS] > 2
 
 
 @pytest.mark.gpu
