@@ -739,6 +739,124 @@ int32_t rv_excise_block(void* stream, const rv_excision_config* config, const rv
                         uint64_t removed_len, uint32_t* counters_dev);
 
 /* ===================================================================== *
+ * Per-receiver noise stages (core/dsp/noise_reference.h,
+ * noise_reference.cpp; core/shaders/noise_blank.comp, noise_line.comp,
+ * noise_spectral.comp): the impulse blanker on a receiver's coarse channel,
+ * the line kernel (manual notch cascade and adaptive line enhancer) and the
+ * spectral noise reduction on its mono audio. Same parameter blocks, same
+ * state layouts, same bits as the twins.
+ * ===================================================================== */
+enum {
+    RV_BLANK_DETECT = 0,
+    RV_BLANK_APPLY = 1,
+    RV_BLANK_MIN_WINDOW = 16,
+    RV_BLANK_MAX_WINDOW = 256,
+    RV_LINE_NOTCH = 1,
+    RV_LINE_ALE = 2,
+    RV_LINE_GUARD = 4,
+    RV_LINE_MAX_NOTCHES = 4,
+    RV_LINE_MAX_STRIDE = 8,
+    RV_LINE_NOTCH_COUNT_SHIFT = 8,    /* bits [8, 10): sections after the first */
+    RV_LINE_STATE_POSITION = 4,
+    RV_LINE_STATE_GUARD = 8,
+    RV_LINE_STATE_MORE = 12,
+    RV_LINE_STATE_WEIGHTS = 24,
+    RV_SPECTRAL_MIN_FRAME = 64,
+    RV_SPECTRAL_MAX_FRAME = 512
+};
+
+/* BlankerConfig / BlankerParams (noise_reference.h:117-168). */
+typedef struct rv_blanker_config {
+    uint32_t pass;  /* set by each entry point */
+    uint32_t window;
+    uint32_t guard;
+    uint32_t hang;
+    uint32_t lead;
+} rv_blanker_config;
+
+typedef struct rv_blanker_params {
+    uint32_t chan_base;  /* the channel's first slot in the channel-major ring */
+    uint32_t chan_mask;
+    uint32_t chan_first;
+    uint32_t out_mask;   /* flag and blanked rings */
+    uint32_t out_first;
+    uint32_t count;
+    float threshold;
+} rv_blanker_params;
+
+/* LineConfig / LineSection / LineParams (noise_reference.h:277-385). */
+typedef struct rv_line_config {
+    uint32_t lanes;
+    uint32_t taps;
+    uint32_t history;  /* power of two */
+} rv_line_config;
+
+typedef struct rv_line_section {
+    float b0, b1, b2, a1, a2;
+} rv_line_section;
+
+typedef struct rv_line_params {
+    uint32_t count;
+    uint32_t flags;   /* RV_LINE_* and the section count */
+    uint32_t stride;
+    uint32_t delay;
+    float b0, b1, b2, a1, a2;
+    float mu, leak, eps;
+    float gb0, gb1, gb2, ga1, ga2;
+    rv_line_section more[3];
+} rv_line_params;
+
+/* NotchDesign (noise_reference.h:395-401), before rounding to float. */
+typedef struct rv_notch_design {
+    double b0, b1, b2, a1, a2;
+} rv_notch_design;
+
+/* SpectralConfig / SpectralParams (noise_reference.h:483-524). */
+typedef struct rv_spectral_config {
+    uint32_t frame;  /* N, a power of two in [64, 512]; hop N/2 */
+} rv_spectral_config;
+
+typedef struct rv_spectral_params {
+    uint32_t count;
+    float smoothing, smoothing_complement;
+    float gamma, beta, rise;
+    float bias, alpha, floor_gain, eps;
+} rv_spectral_params;
+
+/* design_blanker / blanker_threshold (noise_reference.cpp:112-125). */
+int32_t rv_design_blanker(int64_t channel_rate, rv_blanker_config* out);
+float rv_blanker_threshold(double threshold_db);
+/* The blanker's two passes (noise_blank.comp): flags (floats 0/1) into
+ * out_mask + 1 slots, then the blanked samples. chan_len counts the whole
+ * channel-major ring (chan_base + chan_mask + 1 at least). */
+int32_t rv_blank_detect(void* stream, const rv_blanker_config* config, const rv_blanker_params* params,
+                        const rv_cf32* channel_ring_dev, uint64_t channel_len, float* flags_dev, uint64_t flags_len);
+int32_t rv_blank_apply(void* stream, const rv_blanker_config* config, const rv_blanker_params* params,
+                       const rv_cf32* channel_ring_dev, uint64_t channel_len, const float* flags_dev,
+                       uint64_t flags_len, rv_cf32* blanked_dev, uint64_t blanked_len);
+
+/* design_notch (noise_reference.cpp:424-459). */
+int32_t rv_design_notch(double audio_hz, double depth_db, double width_hz, int64_t audio_rate, rv_notch_design* out);
+/* line_state_size: floats of the line kernel's state. */
+uint64_t rv_line_state_size(const rv_line_config* config);
+/* The line kernel (noise_line.comp): `count` audio samples in place, the
+ * state (line_state_size floats) read and written. */
+int32_t rv_noise_line(void* stream, const rv_line_config* config, const rv_line_params* params, float* audio_dev,
+                      uint64_t audio_len, float* state_dev, uint64_t state_len);
+
+/* spectral_config_for / design_spectral_tables (4 N floats) / spectral_params
+ * (noise_reference.cpp:493-554) and the state size. */
+int32_t rv_spectral_config_for(int64_t audio_rate, rv_spectral_config* out);
+int32_t rv_design_spectral_tables(const rv_spectral_config* config, float* tables, uint64_t len);
+int32_t rv_spectral_params(double strength, rv_spectral_params* out);
+uint64_t rv_spectral_state_size(const rv_spectral_config* config);
+/* The spectral noise reduction (noise_spectral.comp): in place, one frame
+ * of latency, the state read and written. */
+int32_t rv_noise_spectral(void* stream, const rv_spectral_config* config, const rv_spectral_params* params,
+                          const float* tables_dev, uint64_t tables_len, float* audio_dev, uint64_t audio_len,
+                          float* state_dev, uint64_t state_len);
+
+/* ===================================================================== *
  * Wideband detector (core/detect/detector.h:1316-1460, detector.cpp:186-1586):
  * the exponential average of the spectrum frames, and at every decision the
  * noise floor, the summed-bin width ladder and the candidate bands, then the
