@@ -845,10 +845,11 @@ int32_t rv_noise_line(void* stream, const rv_line_config* config, const rv_line_
                       uint64_t audio_len, float* state_dev, uint64_t state_len);
 
 /* spectral_config_for / design_spectral_tables (4 N floats) / spectral_params
- * (noise_reference.cpp:493-554) and the state size. */
+ * (noise_reference.cpp:493-554; spectral_params as rv_design_spectral_params)
+ * and the state size. */
 int32_t rv_spectral_config_for(int64_t audio_rate, rv_spectral_config* out);
 int32_t rv_design_spectral_tables(const rv_spectral_config* config, float* tables, uint64_t len);
-int32_t rv_spectral_params(double strength, rv_spectral_params* out);
+int32_t rv_design_spectral_params(double strength, rv_spectral_params* out);
 uint64_t rv_spectral_state_size(const rv_spectral_config* config);
 /* The spectral noise reduction (noise_spectral.comp): in place, one frame
  * of latency, the state read and written. */

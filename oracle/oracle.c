@@ -1377,3 +1377,376 @@ int32_t or_excise_apply(const rv_excision_config* c0, const rv_excision_params* 
     }
     return ok();
 }
+
+/* ------------------------------------------------------------------ */
+/* per-receiver noise stages: core/dsp/noise_reference.cpp            */
+
+/* design_blanker (:112-121) */
+int32_t or_design_blanker(int64_t channel_rate, rv_blanker_config* out) {
+    memset(out, 0, sizeof *out);
+    out->window = (uint32_t)clampd(round(0.5e-3 * (double)channel_rate), 16.0, 256.0);
+    out->hang = 2;
+    out->lead = 2;
+    out->guard = out->lead + 2u;
+    return ok();
+}
+
+float or_blanker_threshold(double threshold_db) { return (float)pow(10.0, threshold_db / 10.0); }
+
+static int32_t blanker_valid(const rv_blanker_config* c, const rv_blanker_params* p) {
+    if (c->pass > 1u) return fail("blanker: pass");
+    if (c->window < 16u || c->window > 256u) return fail("blanker: window");
+    if (!is_mask32(p->chan_mask) || !is_mask32(p->out_mask)) return fail("blanker: masks");
+    const uint64_t reach = (uint64_t)c->hang + c->guard + c->window + c->lead + p->count;
+    const uint64_t smaller = (uint64_t)(p->chan_mask < p->out_mask ? p->chan_mask : p->out_mask) + 1u;
+    if (reach >= smaller) return fail("blanker: reach");
+    if (!(p->threshold > 0.0F)) return fail("blanker: threshold");
+    return 0;
+}
+
+/* reference_blank_detect (:158-195) */
+int32_t or_blank_detect(const rv_blanker_config* c0, const rv_blanker_params* p, const rv_cf32* chan,
+                        uint64_t chan_len, float* flags, uint64_t flags_len) {
+    rv_blanker_config c = *c0;
+    c.pass = 0;
+    if (blanker_valid(&c, p)) return -1;
+    if (flags_len < (uint64_t)p->out_mask + 1u || chan_len < (uint64_t)p->chan_base + p->chan_mask + 1u)
+        return fail("blank_detect: short");
+    flush_scope s;
+    flush_begin(&s);
+    const float window = (float)c.window;
+    for (uint32_t i = 0; i < p->count; ++i) {
+        const uint32_t ch = (p->chan_first + i) & p->chan_mask;
+        const uint32_t o = (p->out_first + i) & p->out_mask;
+        const rv_cf32 x = chan[p->chan_base + ch];
+        const float pw = x.re * x.re + x.im * x.im;
+        float sum = 0.0F;
+        for (uint32_t m = 0; m < c.window; ++m) {
+            const rv_cf32 r = chan[p->chan_base + ((ch - c.guard - c.window + m) & p->chan_mask)];
+            const float q = r.re * r.re + r.im * r.im;
+            sum = sum + q;
+        }
+        const float lhs = pw * window;
+        const float rhs = p->threshold * sum;
+        flags[o] = (sum > 0.0F && lhs > rhs) ? 1.0F : 0.0F;
+    }
+    flush_end(&s);
+    return ok();
+}
+
+/* reference_blank_apply (:197-225) */
+int32_t or_blank_apply(const rv_blanker_config* c0, const rv_blanker_params* p, const rv_cf32* chan,
+                       uint64_t chan_len, const float* flags, uint64_t flags_len, rv_cf32* blanked,
+                       uint64_t blanked_len) {
+    rv_blanker_config c = *c0;
+    c.pass = 1;
+    if (blanker_valid(&c, p)) return -1;
+    if (flags_len < (uint64_t)p->out_mask + 1u || blanked_len < (uint64_t)p->out_mask + 1u ||
+        chan_len < (uint64_t)p->chan_base + p->chan_mask + 1u)
+        return fail("blank_apply: short");
+    for (uint32_t i = 0; i < p->count; ++i) {
+        const uint32_t ch = (p->chan_first + i) & p->chan_mask;
+        const uint32_t o = (p->out_first + i) & p->out_mask;
+        int hit = 0;
+        for (uint32_t m = 0; m <= c.hang + c.lead; ++m)
+            if (flags[(o - c.hang + m) & p->out_mask] != 0.0F) hit = 1;
+        if (hit) {
+            blanked[o].re = 0.0F;
+            blanked[o].im = 0.0F;
+        } else {
+            blanked[o] = chan[p->chan_base + ch];
+        }
+    }
+    return ok();
+}
+
+static uint32_t line_sections_of(uint32_t flags) {
+    return (flags & RV_LINE_NOTCH) == 0u ? 0u : 1u + ((flags >> RV_LINE_NOTCH_COUNT_SHIFT) & 3u);
+}
+
+static float biquad_step(float* st, float b0, float b1, float b2, float a1, float a2, float x) {
+    const float t0 = b0 * x;
+    const float t1 = b1 * st[0];
+    const float t2 = b2 * st[1];
+    const float t3 = a1 * st[2];
+    const float t4 = a2 * st[3];
+    float acc = t0 + t1;
+    acc = acc + t2;
+    acc = acc - t3;
+    acc = acc - t4;
+    st[1] = st[0];
+    st[0] = x;
+    st[3] = st[2];
+    st[2] = acc;
+    return acc;
+}
+
+/* reference_line (:265-420) */
+int32_t or_noise_line(const rv_line_config* c, const rv_line_params* p, float* audio, uint64_t audio_len,
+                      float* state, uint64_t state_len) {
+    if (c->lanes == 0 || c->taps == 0 || c->taps % c->lanes != 0) return fail("line: lanes");
+    if (!is_pow2_u64(c->history)) return fail("line: history");
+    if (p->stride == 0 || p->stride > RV_LINE_MAX_STRIDE) return fail("line: stride");
+    if (p->delay == 0) return fail("line: delay");
+    if ((uint64_t)p->delay + (uint64_t)(c->taps - 1u) * p->stride >= c->history) return fail("line: reach");
+    if (!(p->eps > 0.0F)) return fail("line: eps");
+    if ((p->flags & ~(uint32_t)(RV_LINE_NOTCH | RV_LINE_ALE | RV_LINE_GUARD | (3u << RV_LINE_NOTCH_COUNT_SHIFT))) != 0u)
+        return fail("line: flags");
+    if (audio_len < p->count || state_len < (uint64_t)RV_LINE_STATE_WEIGHTS + c->taps + c->history)
+        return fail("line: short");
+    flush_scope s;
+    flush_begin(&s);
+    const int notch = (p->flags & RV_LINE_NOTCH) != 0u;
+    const int ale = (p->flags & RV_LINE_ALE) != 0u;
+    const int guard = ale && (p->flags & RV_LINE_GUARD) != 0u;
+    const uint32_t sections = line_sections_of(p->flags);
+    const uint32_t per_lane = c->taps / c->lanes, hmask = c->history - 1u;
+    float* w = state + RV_LINE_STATE_WEIGHTS;
+    float* hist = w + c->taps;
+    float* ref = (float*)malloc(sizeof(float) * c->taps);
+    float* part_y = (float*)malloc(sizeof(float) * c->lanes);
+    float* part_p = (float*)malloc(sizeof(float) * c->lanes);
+    float n0[4] = {state[0], state[1], state[2], state[3]};
+    float more[3][4];
+    for (uint32_t k = 0; k + 1u < sections; ++k)
+        for (int j = 0; j < 4; ++j) more[k][j] = state[RV_LINE_STATE_MORE + 4 * k + j];
+    float g[4] = {state[RV_LINE_STATE_GUARD], state[RV_LINE_STATE_GUARD + 1], state[RV_LINE_STATE_GUARD + 2],
+                  state[RV_LINE_STATE_GUARD + 3]};
+    uint32_t position = (uint32_t)state[RV_LINE_STATE_POSITION];
+    for (uint32_t n = 0; n < p->count; ++n) {
+        const float x = audio[n];
+        float v = x;
+        if (notch) {
+            v = biquad_step(n0, p->b0, p->b1, p->b2, p->a1, p->a2, x);
+            for (uint32_t k = 0; k + 1u < sections; ++k)
+                v = biquad_step(more[k], p->more[k].b0, p->more[k].b1, p->more[k].b2, p->more[k].a1, p->more[k].a2, v);
+        }
+        float out = v;
+        if (ale) {
+            for (uint32_t lane = 0; lane < c->lanes; ++lane) {
+                float py = 0.0F, pp = 0.0F;
+                for (uint32_t j = 0; j < per_lane; ++j) {
+                    const uint32_t k = lane + j * c->lanes;
+                    const float r = hist[(position - p->delay - k * p->stride) & hmask];
+                    ref[k] = r;
+                    const float wy = w[k] * r;
+                    py = py + wy;
+                    const float rr = r * r;
+                    pp = pp + rr;
+                }
+                part_y[lane] = py;
+                part_p[lane] = pp;
+            }
+            float y = 0.0F, pw = 0.0F;
+            for (uint32_t lane = 0; lane < c->lanes; ++lane) {
+                y = y + part_y[lane];
+                pw = pw + part_p[lane];
+            }
+            const float e = v - y;
+            const float gain = p->mu * det_recip(pw + p->eps);
+            const float ge = gain * e;
+            for (uint32_t k = 0; k < c->taps; ++k) {
+                const float kept = p->leak * w[k];
+                const float step = ge * ref[k];
+                w[k] = kept + step;
+            }
+            hist[position & hmask] = v;
+            out = e;
+            if (guard) out = v - biquad_step(g, p->gb0, p->gb1, p->gb2, p->ga1, p->ga2, y);
+        }
+        audio[n] = out;
+        position = position + 1u;
+    }
+    state[0] = n0[0];
+    state[1] = n0[1];
+    state[2] = n0[2];
+    state[3] = n0[3];
+    for (uint32_t k = 0; k + 1u < sections; ++k)
+        for (int j = 0; j < 4; ++j) state[RV_LINE_STATE_MORE + 4 * k + j] = more[k][j];
+    state[RV_LINE_STATE_POSITION] = (float)(position & hmask);
+    for (int j = 0; j < 4; ++j) state[RV_LINE_STATE_GUARD + j] = g[j];
+    free(ref);
+    free(part_y);
+    free(part_p);
+    flush_end(&s);
+    return ok();
+}
+
+/* design_notch (:424-459) */
+int32_t or_design_notch(double audio_hz, double depth_db, double width_hz, int64_t audio_rate, rv_notch_design* d) {
+    if (audio_rate <= 0) return fail("notch: rate");
+    const double fa = (double)audio_rate, pi = 3.14159265358979323846;
+    if (!(audio_hz > 0.0) || !(audio_hz < 0.5 * fa)) return fail("notch: frequency");
+    if (!(width_hz > 0.0) || !(width_hz < 0.25 * fa)) return fail("notch: width");
+    const double omega = 2.0 * pi * audio_hz / fa;
+    const double rp = 1.0 - pi * width_hz / fa;
+    const double rz = 1.0 - (1.0 - rp) * pow(10.0, -depth_db / 20.0);
+    const double cs = cos(omega);
+    d->b0 = 1.0;
+    d->b1 = -2.0 * rz * cs;
+    d->b2 = rz * rz;
+    d->a1 = -2.0 * rp * cs;
+    d->a2 = rp * rp;
+    const double z = (omega < 0.5 * pi) ? -1.0 : 1.0;
+    const double scale = (1.0 + d->a1 * z + d->a2) / (d->b0 + d->b1 * z + d->b2);
+    d->b0 *= scale;
+    d->b1 *= scale;
+    d->b2 *= scale;
+    return ok();
+}
+
+/* spectral_config_for (:493-501) */
+int32_t or_spectral_config_for(int64_t audio_rate, rv_spectral_config* out) {
+    const uint64_t wanted = audio_rate > 0 ? (uint64_t)audio_rate / 90u : 64u;
+    uint64_t f = 1;
+    while (f * 2u <= (wanted > 1u ? wanted : 1u)) f *= 2u;
+    out->frame = (uint32_t)(f < 64u ? 64u : (f > 512u ? 512u : f));
+    return ok();
+}
+
+/* design_spectral_tables (:503-539) */
+int32_t or_design_spectral_tables(const rv_spectral_config* c, float* t, uint64_t len) {
+    const uint32_t n = c->frame;
+    if (len < 4ull * n) return fail("spectral tables: short");
+    const double pi = 3.14159265358979323846, step = 2.0 * pi / (double)n;
+    for (uint32_t k = 0; k < n; ++k) {
+        double cs = cos(step * (double)k), sn = sin(step * (double)k);
+        if (k == 0) {
+            cs = 1.0;
+            sn = 0.0;
+        } else if (4u * k == n) {
+            cs = 0.0;
+            sn = 1.0;
+        } else if (2u * k == n) {
+            cs = -1.0;
+            sn = 0.0;
+        } else if (4u * k == 3u * n) {
+            cs = 0.0;
+            sn = -1.0;
+        }
+        t[k] = (float)cs;
+        t[n + k] = (float)sn;
+        const double w = sin(pi * ((double)k + 0.5) / (double)n);
+        t[2u * n + k] = (float)w;
+        t[3u * n + k] = (float)(w / (double)n);
+    }
+    return ok();
+}
+
+/* spectral_params (:541-554) */
+int32_t or_design_spectral_params(double strength, rv_spectral_params* o) {
+    const double s = strength < 0.0 ? 0.0 : (strength > 1.0 ? 1.0 : strength);
+    memset(o, 0, sizeof *o);
+    o->smoothing = (float)0.7;
+    o->smoothing_complement = (float)(1.0 - 0.7);
+    o->gamma = (float)0.998;
+    o->beta = (float)0.96;
+    o->rise = (float)((1.0 - 0.998) / (1.0 - 0.96));
+    o->bias = (float)2.4;
+    o->alpha = (float)(1.0 + s);
+    o->floor_gain = (float)pow(10.0, -(6.0 + 12.0 * s) / 20.0);
+    o->eps = (float)1.0e-12;
+    return ok();
+}
+
+/* reference_spectral (:568-684) */
+int32_t or_noise_spectral(const rv_spectral_config* c, const rv_spectral_params* p, const float* tables,
+                          uint64_t tables_len, float* audio, uint64_t audio_len, float* state, uint64_t state_len) {
+    const uint32_t n = c->frame, h = n / 2u, bins = h + 1u, mask = n - 1u;
+    if (!is_pow2_u64(n) || n < 64u || n > 512u) return fail("spectral: frame");
+    if (!(p->eps > 0.0F)) return fail("spectral: eps");
+    if (tables_len < 4ull * n || audio_len < p->count || state_len < 2u + n + h + h + 2u * bins)
+        return fail("spectral: short");
+    flush_scope sc;
+    flush_begin(&sc);
+    const float* cosine = tables;
+    const float* sine = tables + n;
+    const float* analysis = sine + n;
+    const float* synthesis = analysis + n;
+    float* hist = state + 2;
+    float* tail = hist + n;
+    float* queue = tail + h;
+    float* smoothed = queue + h;
+    float* minimum = smoothed + bins;
+    uint32_t phase = (uint32_t)state[0];
+    float seen = state[1];
+    float work[512], y_re[257], y_im[257];
+    uint32_t s = 0;
+    while (s < p->count) {
+        const uint32_t length = (h - phase) < (p->count - s) ? (h - phase) : (p->count - s);
+        for (uint32_t i = 0; i < length; ++i) {
+            const float x = audio[s + i];
+            hist[h + phase + i] = x;
+            audio[s + i] = queue[phase + i];
+        }
+        phase += length;
+        s += length;
+        if (phase != h) continue;
+        for (uint32_t t = 0; t < n; ++t) work[t] = hist[t] * analysis[t];
+        for (uint32_t k = 0; k < bins; ++k) {
+            float re = 0.0F, im = 0.0F;
+            for (uint32_t t = 0; t < n; ++t) {
+                const uint32_t at = (k * t) & mask;
+                const float xc = work[t] * cosine[at];
+                re = re + xc;
+                const float xs = work[t] * sine[at];
+                im = im - xs;
+            }
+            const float rr = re * re;
+            const float ii = im * im;
+            const float power = rr + ii;
+            float level = power, floor_power = power;
+            if (seen != 0.0F) {
+                const float previous = smoothed[k];
+                const float kept = p->smoothing * previous;
+                const float fresh = p->smoothing_complement * power;
+                level = kept + fresh;
+                const float held = minimum[k];
+                if (held < level) {
+                    const float decayed = p->gamma * held;
+                    const float lagged = p->beta * previous;
+                    const float lift = level - lagged;
+                    const float risen = p->rise * lift;
+                    floor_power = decayed + risen;
+                } else {
+                    floor_power = level;
+                }
+            }
+            smoothed[k] = level;
+            minimum[k] = floor_power;
+            const float noise = p->bias * floor_power;
+            const float ratio = noise * det_recip(level + p->eps);
+            const float cut = p->alpha * ratio;
+            float gain = 1.0F - cut;
+            if (gain < p->floor_gain) gain = p->floor_gain;
+            y_re[k] = gain * re;
+            y_im[k] = gain * im;
+        }
+        for (uint32_t t = 0; t < n; ++t) {
+            float acc = 0.0F;
+            for (uint32_t k = 1; k < h; ++k) {
+                const uint32_t at = (k * t) & mask;
+                const float a = y_re[k] * cosine[at];
+                const float b = y_im[k] * sine[at];
+                const float term = a - b;
+                acc = acc + term;
+            }
+            const float nyquist = (t & 1u) != 0u ? -y_re[h] : y_re[h];
+            const float doubled = 2.0F * acc;
+            float sum = y_re[0] + nyquist;
+            sum = sum + doubled;
+            work[t] = sum * synthesis[t];
+        }
+        for (uint32_t t = 0; t < h; ++t) {
+            queue[t] = tail[t] + work[t];
+            tail[t] = work[h + t];
+            hist[t] = hist[h + t];
+        }
+        phase = 0;
+        seen = seen + 1.0F < 2.0F ? seen + 1.0F : 2.0F;
+    }
+    state[0] = (float)phase;
+    state[1] = seen;
+    flush_end(&sc);
+    return ok();
+}

@@ -112,4 +112,21 @@ int32_t or_excise_flag(const rv_excision_config* c, const rv_excision_params* p,
 int32_t or_excise_apply(const rv_excision_config* c, const rv_excision_params* p, const rv_cf32* raw,
                         uint64_t raw_len, const uint32_t* flags, uint64_t flags_len, rv_cf32* cleaned,
                         rv_cf32* removed, uint64_t removed_len, uint32_t* counters);
+
+/* per-receiver noise stages: twins of core/dsp/noise_reference.cpp */
+int32_t or_design_blanker(int64_t channel_rate, rv_blanker_config* out);
+float or_blanker_threshold(double threshold_db);
+int32_t or_blank_detect(const rv_blanker_config* c, const rv_blanker_params* p, const rv_cf32* chan,
+                        uint64_t chan_len, float* flags, uint64_t flags_len);
+int32_t or_blank_apply(const rv_blanker_config* c, const rv_blanker_params* p, const rv_cf32* chan,
+                       uint64_t chan_len, const float* flags, uint64_t flags_len, rv_cf32* blanked,
+                       uint64_t blanked_len);
+int32_t or_noise_line(const rv_line_config* c, const rv_line_params* p, float* audio, uint64_t audio_len,
+                      float* state, uint64_t state_len);
+int32_t or_design_notch(double audio_hz, double depth_db, double width_hz, int64_t audio_rate, rv_notch_design* d);
+int32_t or_spectral_config_for(int64_t audio_rate, rv_spectral_config* out);
+int32_t or_design_spectral_tables(const rv_spectral_config* c, float* t, uint64_t len);
+int32_t or_design_spectral_params(double strength, rv_spectral_params* o);
+int32_t or_noise_spectral(const rv_spectral_config* c, const rv_spectral_params* p, const float* tables,
+                          uint64_t tables_len, float* audio, uint64_t audio_len, float* state, uint64_t state_len);
 #endif

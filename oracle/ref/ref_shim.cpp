@@ -19,6 +19,7 @@
 #include "core/dsp/convert.h"
 #include "core/dsp/front_end_correction.h"
 #include "core/dsp/impulse_excision.h"
+#include "core/dsp/noise_reference.h"
 #include "core/dsp/pfb.h"
 #include "core/dsp/pfb_branch_reference.h"
 #include "core/dsp/pfb_fft_reference.h"
@@ -556,6 +557,110 @@ int32_t ref_excise_apply(const rv_excision_config* c, const rv_excision_params* 
                                           std::span<const std::uint32_t>(flags, flags_len),
                                           xms(cleaned, (uint64_t)p->ring_mask + 1u), xms(removed, removed_len),
                                           std::span<std::uint32_t>(counters, 4));
+    return st ? 0 : report(st);
+}
+
+// core/dsp/noise_reference.cpp: the blanker, the line kernel and the
+// spectral noise reduction, with their designers. The parameter blocks are
+// the reference's own layouts, copied word for word.
+static_assert(sizeof(dsp::BlankerParams) == sizeof(rv_blanker_params));
+static_assert(sizeof(dsp::LineParams) == sizeof(rv_line_params));
+static_assert(sizeof(dsp::SpectralParams) == sizeof(rv_spectral_params));
+
+int32_t ref_design_blanker(int64_t rate, rv_blanker_config* out) {
+    const dsp::BlankerConfig c = dsp::design_blanker(rate);
+    out->pass = c.pass;
+    out->window = c.window;
+    out->guard = c.guard;
+    out->hang = c.hang;
+    out->lead = c.lead;
+    return 0;
+}
+
+float ref_blanker_threshold(double db) { return dsp::blanker_threshold(db); }
+
+namespace {
+dsp::BlankerConfig xbc(const rv_blanker_config* c, uint32_t pass) {
+    dsp::BlankerConfig o;
+    o.pass = pass;
+    o.window = c->window;
+    o.guard = c->guard;
+    o.hang = c->hang;
+    o.lead = c->lead;
+    return o;
+}
+dsp::BlankerParams xbp(const rv_blanker_params* p) {
+    dsp::BlankerParams o;
+    std::memcpy(&o, p, sizeof o);
+    return o;
+}
+}  // namespace
+
+int32_t ref_blank_detect(const rv_blanker_config* c, const rv_blanker_params* p, const rv_cf32* chan, uint64_t chan_len,
+                         float* flags, uint64_t flags_len) {
+    auto st = dsp::reference_blank_detect(xbc(c, dsp::kBlankDetect), xbp(p), xcs(chan, chan_len),
+                                          std::span<float>(flags, flags_len));
+    return st ? 0 : report(st);
+}
+
+int32_t ref_blank_apply(const rv_blanker_config* c, const rv_blanker_params* p, const rv_cf32* chan, uint64_t chan_len,
+                        const float* flags, uint64_t flags_len, rv_cf32* blanked, uint64_t blanked_len) {
+    auto st = dsp::reference_blank_apply(xbc(c, dsp::kBlankApply), xbp(p), xcs(chan, chan_len),
+                                         std::span<const float>(flags, flags_len), xms(blanked, blanked_len));
+    return st ? 0 : report(st);
+}
+
+int32_t ref_noise_line(const rv_line_config* c, const rv_line_params* p, float* audio, uint64_t audio_len,
+                       float* state, uint64_t state_len) {
+    dsp::LineConfig cc;
+    cc.lanes = c->lanes;
+    cc.taps = c->taps;
+    cc.history = c->history;
+    dsp::LineParams pp;
+    std::memcpy(&pp, p, sizeof pp);
+    auto st = dsp::reference_line(cc, pp, std::span<float>(audio, audio_len), std::span<float>(state, state_len));
+    return st ? 0 : report(st);
+}
+
+int32_t ref_design_notch(double audio_hz, double depth_db, double width_hz, int64_t rate, rv_notch_design* out) {
+    auto d = dsp::design_notch(audio_hz, depth_db, width_hz, rate);
+    if (!d) return report(d);
+    out->b0 = d->b0;
+    out->b1 = d->b1;
+    out->b2 = d->b2;
+    out->a1 = d->a1;
+    out->a2 = d->a2;
+    return 0;
+}
+
+int32_t ref_spectral_config_for(int64_t rate, rv_spectral_config* out) {
+    out->frame = dsp::spectral_config_for(rate).frame;
+    return 0;
+}
+
+int32_t ref_design_spectral_tables(const rv_spectral_config* c, float* t, uint64_t len) {
+    dsp::SpectralConfig cc;
+    cc.frame = c->frame;
+    const std::vector<float> v = dsp::design_spectral_tables(cc);
+    if (len < v.size()) return -1;
+    std::memcpy(t, v.data(), v.size() * sizeof(float));
+    return 0;
+}
+
+int32_t ref_design_spectral_params(double strength, rv_spectral_params* out) {
+    const dsp::SpectralParams p = dsp::spectral_params(strength);
+    std::memcpy(out, &p, sizeof *out);
+    return 0;
+}
+
+int32_t ref_noise_spectral(const rv_spectral_config* c, const rv_spectral_params* p, const float* tables,
+                           uint64_t tables_len, float* audio, uint64_t audio_len, float* state, uint64_t state_len) {
+    dsp::SpectralConfig cc;
+    cc.frame = c->frame;
+    dsp::SpectralParams pp;
+    std::memcpy(&pp, p, sizeof pp);
+    auto st = dsp::reference_spectral(cc, pp, std::span<const float>(tables, tables_len),
+                                      std::span<float>(audio, audio_len), std::span<float>(state, state_len));
     return st ? 0 : report(st);
 }
 

@@ -179,6 +179,46 @@ class ExcisionCursor(_S):
                 ("flag_next", U64), ("apply_next", U64)]
 
 
+LINE_NOTCH, LINE_ALE, LINE_GUARD, LINE_NOTCH_COUNT_SHIFT = 1, 2, 4, 8
+LINE_STATE_WEIGHTS = 24
+
+
+class BlankerConfig(_S):
+    _fields_ = [("pass_", U32), ("window", U32), ("guard", U32), ("hang", U32), ("lead", U32)]
+
+
+class BlankerParams(_S):
+    _fields_ = [("chan_base", U32), ("chan_mask", U32), ("chan_first", U32), ("out_mask", U32), ("out_first", U32),
+                ("count", U32), ("threshold", F32)]
+
+
+class LineConfig(_S):
+    _fields_ = [("lanes", U32), ("taps", U32), ("history", U32)]
+
+
+class LineSection(_S):
+    _fields_ = [("b0", F32), ("b1", F32), ("b2", F32), ("a1", F32), ("a2", F32)]
+
+
+class LineParams(_S):
+    _fields_ = [("count", U32), ("flags", U32), ("stride", U32), ("delay", U32), ("b0", F32), ("b1", F32),
+                ("b2", F32), ("a1", F32), ("a2", F32), ("mu", F32), ("leak", F32), ("eps", F32), ("gb0", F32),
+                ("gb1", F32), ("gb2", F32), ("ga1", F32), ("ga2", F32), ("more", LineSection * 3)]
+
+
+class NotchDesign(_S):
+    _fields_ = [("b0", F64), ("b1", F64), ("b2", F64), ("a1", F64), ("a2", F64)]
+
+
+class SpectralConfig(_S):
+    _fields_ = [("frame", U32)]
+
+
+class SpectralParams(_S):
+    _fields_ = [("count", U32), ("smoothing", F32), ("smoothing_complement", F32), ("gamma", F32), ("beta", F32),
+                ("rise", F32), ("bias", F32), ("alpha", F32), ("floor_gain", F32), ("eps", F32)]
+
+
 TRACK_PENDING, TRACK_LIVE, TRACK_HELD, TRACK_MERGED = 0, 1, 2, 3
 
 
@@ -268,6 +308,10 @@ EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params"
                  "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
                  "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,
                  "rv_excision_plan": ExcisionPlan, "rv_excision_cursor": ExcisionCursor,
+                 "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
+                 "rv_line_config": LineConfig, "rv_line_section": LineSection, "rv_line_params": LineParams,
+                 "rv_notch_design": NotchDesign, "rv_spectral_config": SpectralConfig,
+                 "rv_spectral_params": SpectralParams,
                  "rv_detector_stats": DetectorStats, "rv_spectrum_average_params": SpectrumAverageParams, "rv_coarse_params": CoarseParams, "rv_chain_config": ChainConfig, "rv_chain_stats": ChainStats}
 
 

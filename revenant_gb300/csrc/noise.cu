@@ -41,7 +41,7 @@ constexpr uint32_t kBlankHang = 2;
 constexpr uint32_t kBlankThreads = 256;
 
 bool is_mask(uint32_t m) { return rv::is_pow2((uint64_t)m + 1u); }
-uint32_t line_sections(uint32_t flags) {
+__host__ __device__ inline uint32_t line_sections(uint32_t flags) {
     return (flags & RV_LINE_NOTCH) == 0u ? 0u : 1u + ((flags >> RV_LINE_NOTCH_COUNT_SHIFT) & 3u);
 }
 
@@ -480,8 +480,8 @@ int32_t rv_design_spectral_tables(const rv_spectral_config* c, float* tables, ui
     return rv::clear_error();
 }
 
-int32_t rv_spectral_params(double strength, rv_spectral_params* out) {
-    if (out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_spectral_params: NULL");
+int32_t rv_design_spectral_params(double strength, rv_spectral_params* out) {
+    if (out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_design_spectral_params: NULL");
     const double s = std::clamp(strength, 0.0, 1.0);
     memset(out, 0, sizeof *out);
     out->smoothing = (float)0.7;

@@ -177,6 +177,18 @@ SIGNATURES = {
     "rv_detector_state": (I32, [P, P, P, U64]),
     "rv_detector_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
     "rv_detector_tracks": (I32, [P, I32, P, U32, ptr(U32)]),
+    "rv_design_blanker": (I32, [I64, ptr(abi.BlankerConfig)]),
+    "rv_blanker_threshold": (F32, [F64]),
+    "rv_blank_detect": (I32, [P, ptr(abi.BlankerConfig), ptr(abi.BlankerParams), P, U64, P, U64]),
+    "rv_blank_apply": (I32, [P, ptr(abi.BlankerConfig), ptr(abi.BlankerParams), P, U64, P, U64, P, U64]),
+    "rv_design_notch": (I32, [F64, F64, F64, I64, ptr(abi.NotchDesign)]),
+    "rv_line_state_size": (U64, [ptr(abi.LineConfig)]),
+    "rv_noise_line": (I32, [P, ptr(abi.LineConfig), ptr(abi.LineParams), P, U64, P, U64]),
+    "rv_spectral_config_for": (I32, [I64, ptr(abi.SpectralConfig)]),
+    "rv_design_spectral_tables": (I32, [ptr(abi.SpectralConfig), P, U64]),
+    "rv_design_spectral_params": (I32, [F64, ptr(abi.SpectralParams)]),
+    "rv_spectral_state_size": (U64, [ptr(abi.SpectralConfig)]),
+    "rv_noise_spectral": (I32, [P, ptr(abi.SpectralConfig), ptr(abi.SpectralParams), P, U64, P, U64, P, U64]),
     "rv_design_excision": (I32, [I64, F64, ptr(abi.ExcisionConfig)]),
     "rv_excision_threshold": (F32, [F64]),
     "rv_size_excision_rings": (I32, [ptr(abi.ExcisionConfig), U64, U32, U32, ptr(abi.ExcisionRings)]),

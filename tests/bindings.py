@@ -44,6 +44,16 @@ def _sig(lib, prefix):
     f("vrx_carrier", I32, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P)
     f("iq_moments", I32, ptr(abi.IqMomentsParams), P, U64, P, U64)
     f("iq_correct", I32, ptr(abi.IqCorrectParams), P, U64, P, U64)
+    f("design_blanker", I32, I64, ptr(abi.BlankerConfig))
+    f("blanker_threshold", F32, F64)
+    f("blank_detect", I32, ptr(abi.BlankerConfig), ptr(abi.BlankerParams), P, U64, P, U64)
+    f("blank_apply", I32, ptr(abi.BlankerConfig), ptr(abi.BlankerParams), P, U64, P, U64, P, U64)
+    f("noise_line", I32, ptr(abi.LineConfig), ptr(abi.LineParams), P, U64, P, U64)
+    f("design_notch", I32, F64, F64, F64, I64, ptr(abi.NotchDesign))
+    f("spectral_config_for", I32, I64, ptr(abi.SpectralConfig))
+    f("design_spectral_tables", I32, ptr(abi.SpectralConfig), P, U64)
+    f("design_spectral_params", I32, F64, ptr(abi.SpectralParams))
+    f("noise_spectral", I32, ptr(abi.SpectralConfig), ptr(abi.SpectralParams), P, U64, P, U64, P, U64)
     f("design_excision", I32, I64, F64, ptr(abi.ExcisionConfig))
     f("excision_threshold", F32, F64)
     f("size_excision_rings", I32, ptr(abi.ExcisionConfig), U64, U32, U32, ptr(abi.ExcisionRings))
