@@ -1075,6 +1075,40 @@ int32_t rv_demod_block(const rv_vrx_plan_info* plan, uint32_t fine_mask, uint64_
 int32_t rv_carrier_block(const rv_vrx_plan_info* plan, uint32_t fine_mask, uint64_t first_fine,
                          uint32_t count, int32_t reset, float shift,
                          rv_vrx_carrier_params* params);
+/* The display tap (core/dsp/vrx_reference.h:1639-1766): the fine stage
+ * again, one polyphase branch of RV_DISPLAY_TAPS taps and an integer
+ * decimation R from the channel rate's ladder, reading the same channel with
+ * the receiver's own mix, so a passband pane shows the channel before any
+ * receiver filter. Its launches are rv_vrx_fine with `fine` below. */
+enum { RV_DISPLAY_TAPS = 256 };
+typedef struct rv_vrx_display_plan {
+    int64_t channel_rate;
+    int64_t display_rate;
+    uint32_t decimation;
+    uint32_t reserved;
+    int64_t reach_hz;
+    rv_vrx_fine_config fine;  /* taps 256, phases 1, the receiver's nco_log2 */
+    uint32_t reserved2;
+    uint64_t nco_delta;       /* the fine stage's mix at the display rate */
+    double pass_hz;
+    double stop_hz;
+    double attenuation_db;
+    double group_delay_channel_samples;
+    uint64_t tap_count;       /* taps + 1 */
+} rv_vrx_display_plan;
+
+uint32_t rv_display_max_decimation(void);
+/* display_ladder: the rungs R may take, ascending from 1 (*count of them). */
+int32_t rv_display_ladder(int64_t channel_rate, uint32_t* rungs, uint32_t capacity, uint32_t* count);
+uint32_t rv_display_decimation(int64_t channel_rate, int64_t reach_hz);
+/* plan_vrx_display for a receiver's plan; writes the tap table when `taps`
+ * is not NULL (tap_count entries). */
+int32_t rv_plan_vrx_display(const rv_vrx_plan_info* plan, rv_vrx_display_plan* out, rv_cf32* taps, uint64_t taps_len);
+/* display_block: rv_vrx_fine parameters for display outputs
+ * [first_output, first_output + count). */
+int32_t rv_display_block(const rv_vrx_display_plan* plan, uint32_t channel_base, uint32_t channel_mask,
+                         uint32_t display_mask, uint64_t first_output, uint32_t count, rv_vrx_fine_block* block);
+
 /* dsp::demod_fine_history (core/dsp/vrx_reference.h). */
 uint32_t rv_demod_fine_history(const rv_vrx_demod_config* config);
 

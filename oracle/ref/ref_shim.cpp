@@ -664,4 +664,56 @@ int32_t ref_noise_spectral(const rv_spectral_config* c, const rv_spectral_params
     return st ? 0 : report(st);
 }
 
+// core/dsp/vrx_reference.cpp: the display tap
+uint32_t ref_display_max_decimation(void) { return dsp::display_max_decimation(); }
+
+int32_t ref_display_ladder(int64_t rate, uint32_t* rungs, uint32_t capacity, uint32_t* count) {
+    const std::vector<std::uint32_t> v = dsp::display_ladder(rate);
+    *count = (uint32_t)v.size();
+    for (uint32_t i = 0; i < *count && i < capacity; ++i) rungs[i] = v[i];
+    return 0;
+}
+
+uint32_t ref_display_decimation(int64_t rate, int64_t reach) { return dsp::display_decimation(rate, reach); }
+
+// place + plan_vrx + plan_vrx_display for a request, and optionally one
+// display_block
+int32_t ref_plan_vrx_display(const rv_grid_params* g, int64_t rate, const rv_vrx_request* r, rv_vrx_display_plan* out,
+                             rv_cf32* taps, uint64_t taps_len, uint32_t channel_base, uint32_t channel_mask,
+                             uint32_t display_mask, uint64_t first_output, uint32_t count, rv_vrx_fine_block* block) {
+    auto placed = engine::place(grid_of(g), rate, request_of(r));
+    if (!placed) return report(placed);
+    auto planned = dsp::plan_vrx(grid_of(g), rate, request_of(r), *placed);
+    if (!planned) return report(planned);
+    auto disp = dsp::plan_vrx_display(*planned);
+    if (!disp) return report(disp);
+    const dsp::VrxDisplayPlan& d = *disp;
+    std::memset(out, 0, sizeof *out);
+    out->channel_rate = d.channel_rate;
+    out->display_rate = d.display_rate;
+    out->decimation = d.decimation;
+    out->reach_hz = d.reach_hz;
+    out->fine = rv_vrx_fine_config{d.fine.taps, d.fine.phases, d.fine.nco_log2};
+    out->nco_delta = d.nco_delta;
+    out->pass_hz = d.pass_hz;
+    out->stop_hz = d.stop_hz;
+    out->attenuation_db = d.attenuation_db;
+    out->group_delay_channel_samples = d.group_delay_channel_samples;
+    out->tap_count = d.taps.size();
+    if (taps) {
+        if (taps_len != d.taps.size()) return -1;
+        std::memcpy(taps, d.taps.data(), d.taps.size() * sizeof(rv_cf32));
+    }
+    if (block && count) {
+        auto b = dsp::display_block(d, channel_base, channel_mask, display_mask, first_output, count);
+        if (!b) return report(b);
+        std::memset(block, 0, sizeof *block);
+        std::memcpy(&block->params, &b->params, sizeof(block->params));
+        block->first_input = b->first_input;
+        block->oldest_input = b->oldest_input;
+        block->newest_input = b->newest_input;
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -179,6 +179,12 @@ class ExcisionCursor(_S):
                 ("flag_next", U64), ("apply_next", U64)]
 
 
+class VrxDisplayPlan(_S):
+    _fields_ = [("channel_rate", I64), ("display_rate", I64), ("decimation", U32), ("reserved", U32),
+                ("reach_hz", I64), ("fine", VrxFineConfig), ("reserved2", U32), ("nco_delta", U64), ("pass_hz", F64),
+                ("stop_hz", F64), ("attenuation_db", F64), ("group_delay_channel_samples", F64), ("tap_count", U64)]
+
+
 LINE_NOTCH, LINE_ALE, LINE_GUARD, LINE_NOTCH_COUNT_SHIFT = 1, 2, 4, 8
 LINE_STATE_WEIGHTS = 24
 
@@ -308,7 +314,7 @@ EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params"
                  "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
                  "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,
                  "rv_excision_plan": ExcisionPlan, "rv_excision_cursor": ExcisionCursor,
-                 "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
+                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
                  "rv_line_config": LineConfig, "rv_line_section": LineSection, "rv_line_params": LineParams,
                  "rv_notch_design": NotchDesign, "rv_spectral_config": SpectralConfig,
                  "rv_spectral_params": SpectralParams,

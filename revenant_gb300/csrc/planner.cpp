@@ -1051,12 +1051,128 @@ int32_t rv_plan_vrx(const rv_grid_params* grid, int64_t rate, const rv_vrx_reque
 
 // resample_block (core/dsp/vrx_reference.cpp:2786-2850): block parameters
 // from the absolute output index, re-deriving the first input exactly.
+static int32_t resample_block(const rv_vrx_fine_config& fine, int64_t channel_rate, int64_t out_rate, uint64_t nco,
+                              uint32_t channel_base, uint32_t channel_mask, uint32_t fine_mask, uint64_t first_output,
+                              uint32_t count, rv_vrx_fine_block* block);
+
 int32_t rv_fine_block(const rv_vrx_plan_info* plan, uint32_t channel_base, uint32_t channel_mask, uint32_t fine_mask,
                       uint64_t first_output, uint32_t count, rv_vrx_fine_block* block) {
     if (plan == nullptr || block == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_fine_block: NULL");
     if (plan->channel_rate <= 0 || plan->demod_rate <= 0) return set_error_fmt(RV_ERR_INVALID, "fine_block: the plan carries no rates");
     if (count == 0) return set_error_fmt(RV_ERR_INVALID, "fine_block: a dispatch of zero outputs has nothing to do");
-    const uint64_t fc = static_cast<uint64_t>(plan->channel_rate), fd = static_cast<uint64_t>(plan->demod_rate);
+    return resample_block(plan->fine, plan->channel_rate, plan->demod_rate, plan->fine_nco_delta, channel_base,
+                          channel_mask, fine_mask, first_output, count, block);
+}
+
+// ---- the display tap (core/dsp/vrx_reference.cpp:2938-3080) --------------
+
+// The largest R at which 256 taps still reach 80 dB across Fdisp/2.
+uint32_t rv_display_max_decimation(void) {
+    uint32_t best = 1;
+    for (uint32_t r = 1; r <= 4096u; ++r) {
+        if (attenuation_reachable(RV_DISPLAY_TAPS, 1.0 / (2.0 * static_cast<double>(r))) < 80.0) break;
+        best = r;
+    }
+    return best;
+}
+
+static std::vector<uint32_t> display_ladder(int64_t channel_rate) {
+    std::vector<uint32_t> rungs{1u};
+    if (channel_rate <= 0) return rungs;
+    const uint32_t cap = rv_display_max_decimation();
+    for (;;) {
+        uint32_t next = 0;
+        for (uint32_t d = 2u * rungs.back(); d <= cap; ++d)
+            if (channel_rate % static_cast<int64_t>(d) == 0) {
+                next = d;
+                break;
+            }
+        if (next == 0) return rungs;
+        rungs.push_back(next);
+    }
+}
+
+int32_t rv_display_ladder(int64_t channel_rate, uint32_t* rungs, uint32_t capacity, uint32_t* count) {
+    if (count == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_display_ladder: NULL");
+    const std::vector<uint32_t> v = display_ladder(channel_rate);
+    *count = static_cast<uint32_t>(v.size());
+    if (rungs)
+        for (uint32_t i = 0; i < *count && i < capacity; ++i) rungs[i] = v[i];
+    return rv::clear_error();
+}
+
+uint32_t rv_display_decimation(int64_t channel_rate, int64_t reach_hz) {
+    if (channel_rate <= 0 || reach_hz <= 0) return 1u;
+    // Fdisp/4 >= 2 reach: the pane is at least four reaches across
+    const int64_t wanted = channel_rate / (8 * reach_hz);
+    uint32_t chosen = 1u;
+    for (uint32_t rung : display_ladder(channel_rate))
+        if (static_cast<int64_t>(rung) <= wanted) chosen = rung;
+    return chosen;
+}
+
+int32_t rv_plan_vrx_display(const rv_vrx_plan_info* plan, rv_vrx_display_plan* out, rv_cf32* taps, uint64_t taps_len) {
+    if (plan == nullptr || out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_plan_vrx_display: NULL");
+    if (plan->channel_rate <= 0) return set_error_fmt(RV_ERR_INVALID, "plan_vrx_display: the plan carries no channel rate");
+    if (plan->mix_denominator == 0 || plan->placement.residual_denominator == 0)
+        return set_error_fmt(RV_ERR_INVALID, "plan_vrx_display: the plan carries no mix frequency");
+    // the passband in the frame the fine stage mixes to DC
+    const double shift = static_cast<double>(plan->placement.residual_numerator) /
+                             static_cast<double>(plan->placement.residual_denominator) -
+                         static_cast<double>(plan->mix_numerator) / static_cast<double>(plan->mix_denominator);
+    const double reach = std::max(std::fabs(static_cast<double>(plan->passband_low) + shift),
+                                  std::fabs(static_cast<double>(plan->passband_high) + shift));
+    rv_vrx_display_plan d;
+    memset(&d, 0, sizeof d);
+    d.channel_rate = plan->channel_rate;
+    d.reach_hz = std::max<int64_t>(1, static_cast<int64_t>(std::ceil(reach)));
+    d.decimation = rv_display_decimation(plan->channel_rate, d.reach_hz);
+    d.display_rate = plan->channel_rate / static_cast<int64_t>(d.decimation);
+    d.fine.taps = RV_DISPLAY_TAPS;
+    d.fine.phases = 1u;
+    d.fine.nco_log2 = plan->fine.nco_log2;
+    d.group_delay_channel_samples = (static_cast<double>(RV_DISPLAY_TAPS) - 1.0) / 2.0;
+    // flat to the pane's edge Fdisp/4, in stopband by 3 Fdisp/4 (or Fc/2)
+    const double fc = static_cast<double>(plan->channel_rate), fdisp = static_cast<double>(d.display_rate);
+    d.pass_hz = 0.25 * fdisp;
+    d.stop_hz = std::min(0.75 * fdisp, 0.5 * fc);
+    const double reachable = attenuation_reachable(RV_DISPLAY_TAPS, (d.stop_hz - d.pass_hz) / fc);
+    if (reachable < 80.0)
+        return set_error_fmt(RV_ERR_INVALID, "plan_vrx_display: %u taps reach %.1f dB across %.0f to %.0f Hz at %lld S/s",
+                             RV_DISPLAY_TAPS, reachable, d.pass_hz, d.stop_hz, (long long)plan->channel_rate);
+    d.attenuation_db = std::min(100.0, reachable);
+    // the cutoff midway between the edges
+    const int64_t half_width = static_cast<int64_t>(0.5 * (d.pass_hz + d.stop_hz));
+    std::vector<rv_cf32> table;
+    if (int32_t st = design_fine_taps(d.fine, plan->channel_rate, half_width, plan->mix_numerator, plan->mix_denominator,
+                                      d.attenuation_db, table))
+        return st;
+    if (int32_t st = nco_delta(plan->mix_numerator, plan->mix_denominator, d.display_rate, &d.nco_delta)) return st;
+    d.tap_count = table.size();
+    *out = d;
+    if (taps != nullptr) {
+        if (taps_len != table.size())
+            return set_error_fmt(RV_ERR_INVALID, "rv_plan_vrx_display: tap buffer holds %llu, plan has %zu",
+                                 (unsigned long long)taps_len, table.size());
+        memcpy(taps, table.data(), table.size() * sizeof(rv_cf32));
+    }
+    return rv::clear_error();
+}
+
+int32_t rv_display_block(const rv_vrx_display_plan* plan, uint32_t channel_base, uint32_t channel_mask,
+                         uint32_t display_mask, uint64_t first_output, uint32_t count, rv_vrx_fine_block* block) {
+    if (plan == nullptr || block == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_display_block: NULL");
+    if (plan->channel_rate <= 0 || plan->display_rate <= 0)
+        return set_error_fmt(RV_ERR_INVALID, "display_block: the plan carries no rates");
+    if (count == 0) return set_error_fmt(RV_ERR_INVALID, "display_block: a dispatch of zero outputs has nothing to do");
+    return resample_block(plan->fine, plan->channel_rate, plan->display_rate, plan->nco_delta, channel_base,
+                          channel_mask, display_mask, first_output, count, block);
+}
+
+static int32_t resample_block(const rv_vrx_fine_config& fine, int64_t channel_rate, int64_t out_rate, uint64_t nco,
+                              uint32_t channel_base, uint32_t channel_mask, uint32_t fine_mask, uint64_t first_output,
+                              uint32_t count, rv_vrx_fine_block* block) {
+    const uint64_t fc = static_cast<uint64_t>(channel_rate), fd = static_cast<uint64_t>(out_rate);
     const uint64_t step_whole = fc / fd, step_rem = fc % fd;
     const uint64_t whole = first_output / fd, part = first_output % fd;
     const uint64_t carry_product = part * step_rem;
@@ -1075,16 +1191,16 @@ int32_t rv_fine_block(const rv_vrx_plan_info* plan, uint32_t channel_base, uint3
     o.out_rate = static_cast<uint32_t>(fd);
     o.frac0 = static_cast<uint32_t>(frac0);
     o.inv_out_rate = 1.0f / static_cast<float>(fd);
-    const uint64_t phase = plan->fine_nco_delta * first_output;
+    const uint64_t phase = nco * first_output;
     o.nco_phase_high = static_cast<uint32_t>(phase >> 32);
     o.nco_phase_low = static_cast<uint32_t>(phase);
-    o.nco_delta_high = static_cast<uint32_t>(plan->fine_nco_delta >> 32);
-    o.nco_delta_low = static_cast<uint32_t>(plan->fine_nco_delta);
-    if (int32_t st = rv::validate_fine(&plan->fine, &o)) return st;
+    o.nco_delta_high = static_cast<uint32_t>(nco >> 32);
+    o.nco_delta_low = static_cast<uint32_t>(nco);
+    if (int32_t st = rv::validate_fine(&fine, &o)) return st;
     const uint64_t last_acc = frac0 + static_cast<uint64_t>(count - 1u) * step_rem;
     block->first_input = first_input;
     block->newest_input = first_input + static_cast<uint64_t>(count - 1u) * step_whole + last_acc / fd;
-    block->oldest_input = first_input - static_cast<uint64_t>(plan->fine.taps - 1u);
+    block->oldest_input = first_input - static_cast<uint64_t>(fine.taps - 1u);
     return rv::clear_error();
 }
 

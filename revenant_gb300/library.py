@@ -177,6 +177,11 @@ SIGNATURES = {
     "rv_detector_state": (I32, [P, P, P, U64]),
     "rv_detector_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
     "rv_detector_tracks": (I32, [P, I32, P, U32, ptr(U32)]),
+    "rv_display_max_decimation": (U32, []),
+    "rv_display_ladder": (I32, [I64, P, U32, ptr(U32)]),
+    "rv_display_decimation": (U32, [I64, I64]),
+    "rv_plan_vrx_display": (I32, [ptr(abi.VrxPlanInfo), ptr(abi.VrxDisplayPlan), P, U64]),
+    "rv_display_block": (I32, [ptr(abi.VrxDisplayPlan), U32, U32, U32, U64, U32, ptr(abi.VrxFineBlock)]),
     "rv_design_blanker": (I32, [I64, ptr(abi.BlankerConfig)]),
     "rv_blanker_threshold": (F32, [F64]),
     "rv_blank_detect": (I32, [P, ptr(abi.BlankerConfig), ptr(abi.BlankerParams), P, U64, P, U64]),

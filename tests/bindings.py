@@ -132,6 +132,15 @@ def reference():
         lib.ref_front_end_sequence.argtypes = [P, U64, P, U32, I64, I32, I32, P, P]
         lib.ref_lwdsp_window.restype = I32
         lib.ref_lwdsp_window.argtypes = [U32, U32, P]
+        lib.ref_display_max_decimation.restype = U32
+        lib.ref_display_max_decimation.argtypes = []
+        lib.ref_display_ladder.restype = I32
+        lib.ref_display_ladder.argtypes = [I64, P, U32, ptr(U32)]
+        lib.ref_display_decimation.restype = U32
+        lib.ref_display_decimation.argtypes = [I64, I64]
+        lib.ref_plan_vrx_display.restype = I32
+        lib.ref_plan_vrx_display.argtypes = [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), ptr(abi.VrxDisplayPlan),
+                                             P, U64, U32, U32, U32, U64, U32, ptr(abi.VrxFineBlock)]
         lib.ref_excision_plans.restype = I32
         lib.ref_excision_plans.argtypes = [ptr(abi.ExcisionConfig), U32, ptr(abi.ExcisionRings), F32, P, P, U32, P]
         lib.ref_lwdsp_spectrum.restype = I32
