@@ -739,6 +739,50 @@ int32_t rv_excise_block(void* stream, const rv_excision_config* config, const rv
                         uint64_t removed_len, uint32_t* counters_dev);
 
 /* ===================================================================== *
+ * Comb / spur cancellation on the sample ring (core/dsp/comb_cancel.h,
+ * comb_kernels_reference.cpp; core/shaders/comb_project.comp,
+ * comb_subtract.comp): the projection of each tracked line onto the block in
+ * sub-blocks, and the subtraction of the lines' sum with the removed part
+ * written beside it. The tracker that turns projections into amplitudes is
+ * host bookkeeping of the reference's (CombTracker) and not part of this.
+ * ===================================================================== */
+enum { RV_COMB_TABLE_LOG2 = 12, RV_COMB_TABLE_SIZE = 4096, RV_COMB_MAX_LINES = 1024, RV_COMB_MAX_SUB_BLOCKS = 16 };
+
+/* CombLine (comb_cancel.h:248-256): tone_l(n) = table[(phase0 + n step) >> 20]. */
+typedef struct rv_comb_line {
+    uint32_t phase0;
+    uint32_t step;
+    uint32_t pad0;
+    uint32_t pad1;
+    rv_cf32 amplitude;  /* what subtract removes; project ignores it */
+} rv_comb_line;
+
+/* CombParams (comb_cancel.h:276-288): eight packed words. */
+typedef struct rv_comb_params {
+    uint32_t ring_mask;
+    uint32_t first;
+    uint32_t count;
+    uint32_t lines;
+    uint32_t sub_blocks;
+    uint32_t removed_mask;
+    uint32_t pad0;
+    uint32_t pad1;
+} rv_comb_params;
+
+/* comb_step / comb_table (comb_kernels_reference.cpp). */
+uint32_t rv_comb_step(double frequency_hz, int64_t rate);
+int32_t rv_comb_table(rv_cf32* table, uint64_t len);
+/* projections[l * sub_blocks + s] = sum over sub-block s of x(n) conj(tone_l(n)),
+ * in 64-sample chunks added in order. */
+int32_t rv_comb_project(void* stream, const rv_comb_params* params, const rv_cf32* raw_dev, uint64_t raw_len,
+                        const rv_comb_line* lines_dev, uint64_t lines_len, const rv_cf32* table_dev, uint64_t table_len,
+                        rv_cf32* projections_dev, uint64_t projections_len);
+/* cleaned = x - sum_l a_l tone_l(n); removed = the sum (raw and cleaned may be one ring). */
+int32_t rv_comb_subtract(void* stream, const rv_comb_params* params, const rv_cf32* raw_dev, uint64_t raw_len,
+                         const rv_comb_line* lines_dev, uint64_t lines_len, const rv_cf32* table_dev, uint64_t table_len,
+                         rv_cf32* cleaned_dev, uint64_t cleaned_len, rv_cf32* removed_dev, uint64_t removed_len);
+
+/* ===================================================================== *
  * Per-receiver noise stages (core/dsp/noise_reference.h,
  * noise_reference.cpp; core/shaders/noise_blank.comp, noise_line.comp,
  * noise_spectral.comp): the impulse blanker on a receiver's coarse channel,

@@ -1750,3 +1750,112 @@ int32_t or_noise_spectral(const rv_spectral_config* c, const rv_spectral_params*
     flush_end(&sc);
     return ok();
 }
+
+/* ------------------------------------------------------------------ */
+/* comb cancellation: core/dsp/comb_kernels_reference.cpp             */
+
+uint32_t or_comb_step(double frequency_hz, int64_t rate) {
+    if (rate <= 0 || !isfinite(frequency_hz)) return 0;
+    const double cycle = 4294967296.0;
+    double steps = round(frequency_hz / (double)rate * cycle);
+    steps = fmod(steps, cycle);
+    if (steps < 0.0) steps += cycle;
+    return (uint32_t)(uint64_t)steps;
+}
+
+int32_t or_comb_table(rv_cf32* t, uint64_t len) {
+    if (len < RV_COMB_TABLE_SIZE) return fail("comb table: short");
+    const double pi = 3.14159265358979323846;
+    for (uint32_t i = 0; i < RV_COMB_TABLE_SIZE; ++i) {
+        const double angle = 2.0 * pi * (double)i / (double)RV_COMB_TABLE_SIZE;
+        t[i].re = (float)cos(angle);
+        t[i].im = (float)sin(angle);
+    }
+    return ok();
+}
+
+static int32_t comb_valid(const rv_comb_params* p) {
+    if (!is_mask32(p->ring_mask) || !is_mask32(p->removed_mask)) return fail("comb: masks");
+    if (p->removed_mask > p->ring_mask) return fail("comb: removed ring");
+    if (p->lines > RV_COMB_MAX_LINES) return fail("comb: lines");
+    if (p->sub_blocks < 1 || p->sub_blocks > RV_COMB_MAX_SUB_BLOCKS) return fail("comb: sub-blocks");
+    if (p->count == 0 || p->count % p->sub_blocks != 0) return fail("comb: count");
+    if ((uint64_t)p->count > (uint64_t)p->removed_mask + 1u) return fail("comb: removed ring too short");
+    return 0;
+}
+
+static rv_cf32 comb_tone(const rv_cf32* table, const rv_comb_line* l, uint32_t n) {
+    return table[(l->phase0 + n * l->step) >> (32u - RV_COMB_TABLE_LOG2)];
+}
+
+/* reference_comb_project */
+int32_t or_comb_project(const rv_comb_params* p, const rv_cf32* raw, uint64_t raw_len, const rv_comb_line* lines,
+                        uint64_t lines_len, const rv_cf32* table, uint64_t table_len, rv_cf32* proj,
+                        uint64_t proj_len) {
+    if (comb_valid(p)) return -1;
+    if (raw_len < (uint64_t)p->ring_mask + 1u || lines_len < p->lines || table_len != RV_COMB_TABLE_SIZE ||
+        proj_len < (uint64_t)p->lines * p->sub_blocks)
+        return fail("comb_project: short");
+    flush_scope s;
+    flush_begin(&s);
+    const uint32_t length = p->count / p->sub_blocks;
+    for (uint32_t l = 0; l < p->lines; ++l)
+        for (uint32_t sb = 0; sb < p->sub_blocks; ++sb) {
+            const uint32_t begin = sb * length;
+            float tr = 0.0F, ti = 0.0F;
+            for (uint32_t c = 0; c < length; c += 64u) {
+                const uint32_t end = c + 64u < length ? c + 64u : length;
+                float cr = 0.0F, ci = 0.0F;
+                for (uint32_t m = c; m < end; ++m) {
+                    const uint32_t n = begin + m;
+                    const rv_cf32 x = raw[(p->first + n) & p->ring_mask];
+                    const rv_cf32 t = comb_tone(table, &lines[l], n);
+                    const float re = x.re * t.re + x.im * t.im;
+                    const float im = x.im * t.re - x.re * t.im;
+                    cr = cr + re;
+                    ci = ci + im;
+                }
+                tr = tr + cr;
+                ti = ti + ci;
+            }
+            proj[(uint64_t)l * p->sub_blocks + sb].re = tr;
+            proj[(uint64_t)l * p->sub_blocks + sb].im = ti;
+        }
+    flush_end(&s);
+    return ok();
+}
+
+/* reference_comb_subtract */
+int32_t or_comb_subtract(const rv_comb_params* p, const rv_cf32* raw, uint64_t raw_len, const rv_comb_line* lines,
+                         uint64_t lines_len, const rv_cf32* table, uint64_t table_len, rv_cf32* cleaned,
+                         uint64_t cleaned_len, rv_cf32* removed, uint64_t removed_len) {
+    if (comb_valid(p)) return -1;
+    if (raw_len < (uint64_t)p->ring_mask + 1u || cleaned_len < (uint64_t)p->ring_mask + 1u || lines_len < p->lines ||
+        table_len != RV_COMB_TABLE_SIZE || removed_len < (uint64_t)p->removed_mask + 1u)
+        return fail("comb_subtract: short");
+    flush_scope s;
+    flush_begin(&s);
+    for (uint32_t n = 0; n < p->count; ++n) {
+        const uint32_t slot = (p->first + n) & p->ring_mask;
+        const rv_cf32 x = raw[slot];
+        float sr = -0.0F, si = -0.0F;
+        for (uint32_t l = 0; l < p->lines; ++l) {
+            const rv_cf32 t = comb_tone(table, &lines[l], n);
+            const rv_cf32 a = lines[l].amplitude;
+            const float re = a.re * t.re - a.im * t.im;
+            const float im = a.re * t.im + a.im * t.re;
+            sr = sr + re;
+            si = si + im;
+        }
+        if (p->lines == 0) {
+            cleaned[slot] = x;
+        } else {
+            cleaned[slot].re = x.re - sr;
+            cleaned[slot].im = x.im - si;
+        }
+        removed[(p->first + n) & p->removed_mask].re = sr;
+        removed[(p->first + n) & p->removed_mask].im = si;
+    }
+    flush_end(&s);
+    return ok();
+}

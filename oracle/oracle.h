@@ -129,4 +129,14 @@ int32_t or_design_spectral_tables(const rv_spectral_config* c, float* t, uint64_
 int32_t or_design_spectral_params(double strength, rv_spectral_params* o);
 int32_t or_noise_spectral(const rv_spectral_config* c, const rv_spectral_params* p, const float* tables,
                           uint64_t tables_len, float* audio, uint64_t audio_len, float* state, uint64_t state_len);
+
+/* comb cancellation: twins of core/dsp/comb_kernels_reference.cpp */
+uint32_t or_comb_step(double frequency_hz, int64_t rate);
+int32_t or_comb_table(rv_cf32* t, uint64_t len);
+int32_t or_comb_project(const rv_comb_params* p, const rv_cf32* raw, uint64_t raw_len, const rv_comb_line* lines,
+                        uint64_t lines_len, const rv_cf32* table, uint64_t table_len, rv_cf32* proj,
+                        uint64_t proj_len);
+int32_t or_comb_subtract(const rv_comb_params* p, const rv_cf32* raw, uint64_t raw_len, const rv_comb_line* lines,
+                         uint64_t lines_len, const rv_cf32* table, uint64_t table_len, rv_cf32* cleaned,
+                         uint64_t cleaned_len, rv_cf32* removed, uint64_t removed_len);
 #endif

@@ -18,6 +18,7 @@
 
 #include "core/dsp/convert.h"
 #include "core/dsp/front_end_correction.h"
+#include "core/dsp/comb_cancel.h"
 #include "core/dsp/impulse_excision.h"
 #include "core/dsp/noise_reference.h"
 #include "core/dsp/pfb.h"
@@ -714,6 +715,40 @@ int32_t ref_plan_vrx_display(const rv_grid_params* g, int64_t rate, const rv_vrx
         block->newest_input = b->newest_input;
     }
     return 0;
+}
+
+// core/dsp/comb_kernels_reference.cpp
+static_assert(sizeof(dsp::CombLine) == sizeof(rv_comb_line));
+static_assert(sizeof(dsp::CombParams) == sizeof(rv_comb_params));
+
+uint32_t ref_comb_step(double hz, int64_t rate) { return dsp::comb_step(hz, rate); }
+
+int32_t ref_comb_table(rv_cf32* t, uint64_t len) {
+    const std::vector<dsp::Complex32> v = dsp::comb_table();
+    if (len < v.size()) return -1;
+    std::memcpy(t, v.data(), v.size() * sizeof(rv_cf32));
+    return 0;
+}
+
+int32_t ref_comb_project(const rv_comb_params* p, const rv_cf32* raw, uint64_t raw_len, const rv_comb_line* lines,
+                         uint64_t lines_len, const rv_cf32* table, uint64_t table_len, rv_cf32* proj, uint64_t proj_len) {
+    dsp::CombParams pp;
+    std::memcpy(&pp, p, sizeof pp);
+    auto st = dsp::reference_comb_project(
+        pp, xcs(raw, raw_len), std::span<const dsp::CombLine>(reinterpret_cast<const dsp::CombLine*>(lines), lines_len),
+        xcs(table, table_len), xms(proj, proj_len));
+    return st ? 0 : report(st);
+}
+
+int32_t ref_comb_subtract(const rv_comb_params* p, const rv_cf32* raw, uint64_t raw_len, const rv_comb_line* lines,
+                          uint64_t lines_len, const rv_cf32* table, uint64_t table_len, rv_cf32* cleaned,
+                          uint64_t cleaned_len, rv_cf32* removed, uint64_t removed_len) {
+    dsp::CombParams pp;
+    std::memcpy(&pp, p, sizeof pp);
+    auto st = dsp::reference_comb_subtract(
+        pp, xcs(raw, raw_len), std::span<const dsp::CombLine>(reinterpret_cast<const dsp::CombLine*>(lines), lines_len),
+        xcs(table, table_len), xms(cleaned, cleaned_len), xms(removed, removed_len));
+    return st ? 0 : report(st);
 }
 
 }  // extern "C"

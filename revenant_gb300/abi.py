@@ -185,6 +185,18 @@ class VrxDisplayPlan(_S):
                 ("stop_hz", F64), ("attenuation_db", F64), ("group_delay_channel_samples", F64), ("tap_count", U64)]
 
 
+COMB_TABLE_SIZE = 4096
+
+
+class CombLine(_S):
+    _fields_ = [("phase0", U32), ("step", U32), ("pad0", U32), ("pad1", U32), ("amp_re", F32), ("amp_im", F32)]
+
+
+class CombParams(_S):
+    _fields_ = [("ring_mask", U32), ("first", U32), ("count", U32), ("lines", U32), ("sub_blocks", U32),
+                ("removed_mask", U32), ("pad0", U32), ("pad1", U32)]
+
+
 LINE_NOTCH, LINE_ALE, LINE_GUARD, LINE_NOTCH_COUNT_SHIFT = 1, 2, 4, 8
 LINE_STATE_WEIGHTS = 24
 
@@ -314,7 +326,7 @@ EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params"
                  "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
                  "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,
                  "rv_excision_plan": ExcisionPlan, "rv_excision_cursor": ExcisionCursor,
-                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
+                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_comb_line": CombLine, "rv_comb_params": CombParams, "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
                  "rv_line_config": LineConfig, "rv_line_section": LineSection, "rv_line_params": LineParams,
                  "rv_notch_design": NotchDesign, "rv_spectral_config": SpectralConfig,
                  "rv_spectral_params": SpectralParams,

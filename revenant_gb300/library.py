@@ -177,6 +177,10 @@ SIGNATURES = {
     "rv_detector_state": (I32, [P, P, P, U64]),
     "rv_detector_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
     "rv_detector_tracks": (I32, [P, I32, P, U32, ptr(U32)]),
+    "rv_comb_step": (U32, [F64, I64]),
+    "rv_comb_table": (I32, [P, U64]),
+    "rv_comb_project": (I32, [P, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64]),
+    "rv_comb_subtract": (I32, [P, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64, P, U64]),
     "rv_display_max_decimation": (U32, []),
     "rv_display_ladder": (I32, [I64, P, U32, ptr(U32)]),
     "rv_display_decimation": (U32, [I64, I64]),

@@ -44,6 +44,10 @@ def _sig(lib, prefix):
     f("vrx_carrier", I32, ptr(abi.VrxCarrierConfig), ptr(abi.VrxCarrierParams), P, U64, P, U64, P)
     f("iq_moments", I32, ptr(abi.IqMomentsParams), P, U64, P, U64)
     f("iq_correct", I32, ptr(abi.IqCorrectParams), P, U64, P, U64)
+    f("comb_step", U32, F64, I64)
+    f("comb_table", I32, P, U64)
+    f("comb_project", I32, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64)
+    f("comb_subtract", I32, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64, P, U64)
     f("design_blanker", I32, I64, ptr(abi.BlankerConfig))
     f("blanker_threshold", F32, F64)
     f("blank_detect", I32, ptr(abi.BlankerConfig), ptr(abi.BlankerParams), P, U64, P, U64)
