@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-detect", action="store_true", help="skip the spectrum + detector measurement")
+    ap.add_argument("--no-excision", action="store_true", help="skip the timed run with impulse excision on")
     ap.add_argument("--run-log2", type=int, default=24, help="log2 samples per rv_chain_run")
     return ap.parse_args()
 
@@ -162,6 +163,13 @@ def algorithmic_bytes(plans, samples):
         demod += n_fine * (8 + 4 + 4) + n_audio * 4 * p.demod.channels
     audio_out = sum(samples * p.output_rate // RATE * 4 * p.demod.channels for p in plans)
     return dict(compulsory=samples * 4 + audio_out, coarse=coarse, fine=fine, demod=demod, audio=audio_out)
+
+
+def fine_fp32_ops(plans, samples):
+    """FP32 operations of the fine stage for `samples` input samples: per
+    fine output T complex multiply-adds of 8 rounded operations each (the
+    blended tap is precomputed) and the NCO rotation's 6."""
+    return sum((samples * p.demod_rate // RATE) * (p.fine.taps * 8 + 6) for p in plans)
 
 
 def peaks():
@@ -273,6 +281,39 @@ def run_gb300(args):
     pk, pk_kind = peaks()
     achieved = ab[dominant] / (stage_ms[dominant] / 1e3) / 1e9
     hbm_frac = ab["compulsory"] / (ms / 1e3) / 1e9 / pk["hbm_gbs"]
+    # the fine stage against the FP32 issue rate it is bound by: every
+    # multiply and add is its own rounded instruction (no FMA contraction)
+    sms = dev.info.sm_count or 152
+    fp32_peak = sms * 128 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    fp32_achieved = fine_fp32_ops(plans, samples_step * args.steps) / (stage_ms["fine"] / 1e3) / 1e12
+
+    # the same timed run with the span-wide impulse excision on (the
+    # reference engine's default stage before the channelizer): its cost on
+    # this workload
+    excision = None
+    if not args.no_excision:
+        xch = make_chain(abi.CHAIN_BATCHED, run_samples, profile=False, pipelined=True)
+        xch.capture_graph()
+        xch.set_impulse_excision(True, 15.0, 20e-6)
+        for _ in range(args.warmup):
+            step(xch, "device")
+        xch.drain()
+        x0 = torch.cuda.Event(enable_timing=True)
+        x1 = torch.cuda.Event(enable_timing=True)
+        x0.record(stream)
+        for _ in range(args.steps):
+            step(xch, "device")
+        x1.record(stream)
+        x1.synchronize()
+        xms = x0.elapsed_time(x1)
+        counts = xch.excision_counters()
+        excision = {"value": round(samples_step * args.steps / (xms / 1e3) / 1e6, 2), "unit": "MS/s",
+                    "ms_per_step": round(xms / args.steps, 3),
+                    "samples_excised": counts[0], "runs_excised": counts[1], "runs_spared": counts[2],
+                    "samples_examined": counts[3],
+                    "note": "rv_chain_set_impulse_excision(15 dB, 20 us): runs converted into a cf32 ring, four "
+                            "excision passes, the channelizer reading the ring up to the stage's cleaned end"}
+        xch.close()
 
     plain = None
     if not args.no_plain:
@@ -316,9 +357,14 @@ def run_gb300(args):
                      "peak_kind": pk_kind, "algorithmic_bytes_per_step": int(ab[dominant] / args.steps),
                      "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in stage_ms.items()},
                      "host_ms_per_step": round(d["host_ms"] / args.steps, 3),
-                     "compulsory_hbm_frac": round(hbm_frac, 5)},
+                     "compulsory_hbm_frac": round(hbm_frac, 5),
+                     "fp32": {"kernel": "fine", "achieved_tops": round(fp32_achieved, 2),
+                              "peak_tops": round(fp32_peak, 1), "frac": round(fp32_achieved / fp32_peak, 3),
+                              "peak_kind": "derived: SMs x 128 FP32 lanes x max SM clock, one rounded operation "
+                                           "per instruction"}},
         "realtime_factor": round(value * 1e6 / RATE / max(world, 1), 1),
         "plain_path": plain,
+        "with_impulse_excision": excision,
         "clocks": clocks.summary(),
     }
     if not args.no_plain and plain:
