@@ -1086,6 +1086,15 @@ int32_t rv_validate_grid(const rv_grid_params* grid);
 /* design_prototype (core/dsp/pfb_design.cpp:381). taps_len = M*(L+1). */
 int32_t rv_design_prototype(const rv_grid_params* grid, double attenuation_db, float* taps,
                             uint64_t taps_len, double* stopband_db, uint64_t* group_delay);
+/* Grids past the reference's channel cap (kMaxChannels = 2048,
+ * core/dsp/pfb_design.cpp:67), up to 16384 channels: C4's M = 4096 PFB.
+ * design_prototype and the branch dispatch with the same arithmetic; the
+ * FFT dispatch is rv_pfb_fft (up to 16384 channels) with rv_build_fft_twiddles. */
+int32_t rv_design_prototype_wide(const rv_grid_params* grid, double attenuation_db, float* taps,
+                                 uint64_t taps_len, double* stopband_db, uint64_t* group_delay);
+int32_t rv_pfb_branch_wide(void* stream, const rv_grid_params* grid, const rv_pfb_branch_params* params,
+                           const float* taps_dev, uint64_t taps_len, const rv_cf32* ring_dev,
+                           uint64_t ring_len, rv_cf32* out_dev, uint64_t out_len);
 /* build_twiddles (core/dsp/pfb_design.cpp:515); M entries. */
 int32_t rv_build_twiddles(uint32_t channels, rv_cf32* table, uint64_t table_len);
 /* build_twiddles' first-octant construction for any power of two up to 65536

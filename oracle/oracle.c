@@ -305,10 +305,32 @@ static void branch_block(uint32_t M, uint32_t T, uint32_t base, uint32_t mask, c
     }
 }
 
+static int32_t pfb_branch_any(const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                              uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out,
+                              uint64_t out_len);
+
 int32_t or_pfb_branch(const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
                       uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out,
                       uint64_t out_len) {
     if (validate_grid(g) != 0) return -1;
+    return pfb_branch_any(g, p, taps, taps_len, ring, ring_len, out, out_len);
+}
+
+/* the same branch FIR for grids past 2048 channels (C4) */
+int32_t or_pfb_branch_wide(const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                           uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out,
+                           uint64_t out_len) {
+    if (g->channels > 16384) return fail("grid: channel count %u exceeds 16384", g->channels);
+    if (g->channels <= 2048 && validate_grid(g) != 0) return -1;
+    if (g->channels < 2 || !is_pow2_u64(g->channels) || g->taps_per_branch == 0 || g->decimation == 0 ||
+        g->channels % g->decimation != 0)
+        return fail("grid: invalid");
+    return pfb_branch_any(g, p, taps, taps_len, ring, ring_len, out, out_len);
+}
+
+static int32_t pfb_branch_any(const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                              uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out,
+                              uint64_t out_len) {
     const uint32_t M = g->channels, T = g->taps_per_branch, D = g->decimation;
     if (taps_len != (uint64_t)M * T) return fail("pfb_branch: wants %u taps", M * T);
     if (out_len != (uint64_t)p->block_count * M) return fail("pfb_branch: output length");

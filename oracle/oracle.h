@@ -76,6 +76,9 @@ int32_t or_coarse_cs16(const rv_grid_params* g, const float* taps, const rv_cf32
  * correction) of cf32 input x (as double), for blocks [0, block_count):
  * y[k][m] = sum_r branch_r(m) * exp(-2 pi i k (M - r mod M)/M) * exp(-2 pi i k m D / M).
  * Output channel-major [M][block_count] complex double. */
+int32_t or_pfb_branch_wide(const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                           uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out,
+                           uint64_t out_len);
 int32_t or_pfb_f64(const rv_grid_params* g, const float* taps, const rv_cf32* ring,
                    uint32_t ring_mask, uint32_t base_offset, uint32_t block_count,
                    uint32_t block_base, double* out_re, double* out_im);

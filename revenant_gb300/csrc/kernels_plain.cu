@@ -375,11 +375,15 @@ __global__ void k_vrx_carrier(const rv_cf32* __restrict__ nco, rv_cf32* __restri
 // ---------------------------------------------------------------------
 // host-side validation shared with the fused paths
 
-int32_t validate_grid(const rv_grid_params* g) {
+// The reference's grid rules (core/dsp/pfb_design.cpp:301-380) with its
+// channel cap, kMaxChannels = 2048, or a wider one for the *_wide entry
+// points (C4's M = 4096, which the reference refuses).
+int32_t validate_grid_upto(const rv_grid_params* g, uint32_t max_channels) {
     if (g == nullptr) return set_error_fmt(RV_ERR_INVALID, "grid: NULL");
     if (g->channels < 2) return set_error_fmt(RV_ERR_INVALID, "grid: channel count %u is below the minimum of 2", g->channels);
     if (!is_pow2(g->channels)) return set_error_fmt(RV_ERR_INVALID, "grid: channel count %u is not a power of two", g->channels);
-    if (g->channels > 2048) return set_error_fmt(RV_ERR_INVALID, "grid: channel count %u exceeds 2048", g->channels);
+    if (g->channels > max_channels)
+        return set_error_fmt(RV_ERR_INVALID, "grid: channel count %u exceeds %u", g->channels, max_channels);
     if (g->taps_per_branch == 0) return set_error_fmt(RV_ERR_INVALID, "grid: zero taps per branch");
     if (g->decimation == 0) return set_error_fmt(RV_ERR_INVALID, "grid: zero decimation");
     if (g->channels % g->decimation != 0)
@@ -389,6 +393,8 @@ int32_t validate_grid(const rv_grid_params* g) {
                              (unsigned long long)g->channels * g->taps_per_branch);
     return RV_OK;
 }
+
+int32_t validate_grid(const rv_grid_params* g) { return validate_grid_upto(g, 2048); }
 
 int32_t validate_fft(const rv_pfb_fft_params* p) {
     if (!is_pow2(p->channels) || p->channels < 2)
@@ -559,12 +565,27 @@ int32_t rv_convert(void* stream, int32_t format, const rv_convert_params* p, con
     return clear_error();
 }
 
+static int32_t pfb_branch(void* stream, const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                          uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out, uint64_t out_len,
+                          uint32_t max_channels);
+
 int32_t rv_pfb_branch(void* stream, const rv_grid_params* g, const rv_pfb_branch_params* p,
                       const float* taps, uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len,
                       rv_cf32* out, uint64_t out_len) {
+    return pfb_branch(stream, g, p, taps, taps_len, ring, ring_len, out, out_len, 2048);
+}
+
+int32_t rv_pfb_branch_wide(void* stream, const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                           uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out, uint64_t out_len) {
+    return pfb_branch(stream, g, p, taps, taps_len, ring, ring_len, out, out_len, 16384);
+}
+
+static int32_t pfb_branch(void* stream, const rv_grid_params* g, const rv_pfb_branch_params* p, const float* taps,
+                          uint64_t taps_len, const rv_cf32* ring, uint64_t ring_len, rv_cf32* out, uint64_t out_len,
+                          uint32_t max_channels) {
     if (p == nullptr || taps == nullptr || ring == nullptr || out == nullptr)
         return set_error_fmt(RV_ERR_INVALID, "rv_pfb_branch: NULL argument");
-    if (int32_t st = validate_grid(g)) return st;
+    if (int32_t st = validate_grid_upto(g, max_channels)) return st;
     const uint32_t M = g->channels, T = g->taps_per_branch, D = g->decimation;
     if (taps_len != (uint64_t)M * T) return set_error_fmt(RV_ERR_INVALID, "pfb branch: wants %u prototype taps, got %llu", M * T, (unsigned long long)taps_len);
     if (out_len < (uint64_t)p->block_count * M) return set_error_fmt(RV_ERR_INVALID, "pfb branch: output holds %llu values, %llu needed",

@@ -31,6 +31,7 @@ namespace rv {
 int32_t set_error_fmt(int32_t code, const char* fmt, ...);
 int32_t clear_error();
 int32_t validate_grid(const rv_grid_params* g);
+int32_t validate_grid_upto(const rv_grid_params* g, uint32_t max_channels);
 int32_t validate_fine(const rv_vrx_fine_config* c, const rv_vrx_fine_params* p);
 int32_t validate_demod(const rv_vrx_demod_config* c, const rv_vrx_demod_params* p);
 int32_t validate_carrier(const rv_vrx_carrier_config* c, const rv_vrx_carrier_params* p);
@@ -169,8 +170,8 @@ double measure_stopband_db(const std::vector<float>& taps, uint32_t channels) {
 // ---- prototype, twiddles, NCO, spectrum window ---------------------------
 
 int32_t design_prototype(const rv_grid_params& g, double attenuation_db, std::vector<float>& taps,
-                         double* stopband, uint64_t* group_delay) {
-    if (int32_t st = rv::validate_grid(&g)) return st;
+                         double* stopband, uint64_t* group_delay, uint32_t max_channels = 2048) {
+    if (int32_t st = rv::validate_grid_upto(&g, max_channels)) return st;
     if (!isfinite(attenuation_db) || attenuation_db < 0.0 || attenuation_db > 300.0)
         return set_error_fmt(RV_ERR_INVALID, "design_prototype: stopband target %g dB is outside [0, 300]", attenuation_db);
     const uint32_t M = g.channels;
@@ -979,6 +980,20 @@ int32_t rv_design_prototype(const rv_grid_params* grid, double atten, float* tap
     std::vector<float> t;
     if (int32_t st = design_prototype(*grid, atten, t, stopband_db, group_delay)) return st;
     if (taps_len != t.size()) return set_error_fmt(RV_ERR_INVALID, "rv_design_prototype: wants %zu taps, buffer holds %llu", t.size(), (unsigned long long)taps_len);
+    memcpy(taps, t.data(), t.size() * sizeof(float));
+    return rv::clear_error();
+}
+
+// design_prototype for grids past the reference's 2048 channels (C4's
+// M = 4096): the same Kaiser-windowed sinc and normalisation.
+int32_t rv_design_prototype_wide(const rv_grid_params* grid, double atten, float* taps, uint64_t taps_len,
+                                 double* stopband_db, uint64_t* group_delay) {
+    if (grid == nullptr || taps == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_design_prototype_wide: NULL");
+    std::vector<float> t;
+    if (int32_t st = design_prototype(*grid, atten, t, stopband_db, group_delay, 16384)) return st;
+    if (taps_len != t.size())
+        return set_error_fmt(RV_ERR_INVALID, "rv_design_prototype_wide: wants %zu taps, buffer holds %llu", t.size(),
+                             (unsigned long long)taps_len);
     memcpy(taps, t.data(), t.size() * sizeof(float));
     return rv::clear_error();
 }

@@ -177,6 +177,8 @@ SIGNATURES = {
     "rv_detector_state": (I32, [P, P, P, U64]),
     "rv_detector_get_stats": (I32, [P, ptr(abi.DetectorStats)]),
     "rv_detector_tracks": (I32, [P, I32, P, U32, ptr(U32)]),
+    "rv_design_prototype_wide": (I32, [ptr(abi.GridParams), F64, P, U64, ptr(F64), ptr(U64)]),
+    "rv_pfb_branch_wide": (I32, [P, ptr(abi.GridParams), ptr(abi.PfbBranchParams), P, U64, P, U64, P, U64]),
     "rv_comb_step": (U32, [F64, I64]),
     "rv_comb_table": (I32, [P, U64]),
     "rv_comb_project": (I32, [P, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64]),

@@ -89,6 +89,8 @@ def oracle():
                                                 ptr(abi.ExcisionRings), F32]
         lib.or_excision_plan_block.restype = I32
         lib.or_excision_plan_block.argtypes = [ptr(abi.ExcisionCursor), U64, U32, ptr(abi.ExcisionPlan)]
+        lib.or_pfb_branch_wide.restype = I32
+        lib.or_pfb_branch_wide.argtypes = [ptr(abi.GridParams), ptr(abi.PfbBranchParams), P, U64, P, U64, P, U64]
         lib.or_pfb_f64.restype = I32
         lib.or_pfb_f64.argtypes = [ptr(abi.GridParams), P, P, U32, U32, U32, U32, P, P]
         _oracle = Lib(lib, "or_")

@@ -1,0 +1,139 @@
+"""C4: an M = 4096 polyphase channelizer (D = 2048, T = 16) over a seeded
+multitone (64 tones, amplitudes log-uniform over 90 dB, on and off bin
+centres) in noise. M = 4096 is past the reference's channel cap
+(kMaxChannels = 2048, core/dsp/pfb_design.cpp:67), so there is no twin: the
+wide entry points run the reference's channelizer arithmetic (prototype,
+branch FIR, radix-2 DIT FFT with the phase correction) at the wider grid, and
+are checked
+
+  * bit for bit against the FP32 oracle restated for wide grids, and
+  * against an FP64 restatement (direct DFT, oracle/oracle.c or_pfb_f64):
+    REL_RMS = 2e-6 relative RMS of the channel outputs over all channels, and
+    SPUR_DBC = -110 dB for the worst single output error against the
+    strongest output (the spur floor the FP32 arithmetic leaves).
+
+The tensor-core split-precision DFT this config is also named for is not
+built; the FFT path is the one measured here.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from bindings import cf32, oracle, same_bits
+from revenant_gb300 import abi
+from revenant_gb300.library import lib
+
+M, T, D = 4096, 16, 2048
+REL_RMS = 2e-6
+SPUR_DBC = -110.0
+
+
+def prototype():
+    g = abi.GridParams(M, T, D)
+    taps = np.zeros(M * T, np.float32)
+    stop = C.c_double()
+    assert lib().rv_design_prototype_wide(C.byref(g), 120.0, taps.ctypes.data, taps.size, C.byref(stop), None) == 0, \
+        lib().rv_last_error()
+    return g, taps, stop.value
+
+
+def twiddles():
+    tw = cf32(M)
+    assert lib().rv_build_fft_twiddles(M, tw.ctypes.data, M) == 0
+    return tw
+
+
+def multitone(n, seed=4):
+    rng = np.random.default_rng(seed)
+    t = np.arange(n)
+    z = 10 ** (-5) * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    for k in range(64):
+        amp = 10 ** (-rng.uniform(0, 90) / 20)
+        centre = rng.integers(-M // 2, M // 2) / M
+        f = centre + (0.0 if k % 2 else rng.uniform(-0.4, 0.4) / M)
+        z += 0.3 * amp * np.exp(2j * np.pi * (f * t + rng.uniform()))
+    ring = np.zeros((n, 2), np.float32)
+    ring[:, 0], ring[:, 1] = z.real, z.imag
+    return ring
+
+
+def oracle_fp32(g, taps, tw, ring, base_block, blocks, ring_blocks):
+    o = oracle()
+    branch = cf32(blocks * M)
+    bp = abi.PfbBranchParams(ring.shape[0] - 1, base_block * D, blocks)
+    assert o.lib.or_pfb_branch_wide(C.byref(g), C.byref(bp), taps.ctypes.data, taps.size, ring.ctypes.data,
+                                    ring.shape[0], branch.ctypes.data, branch.shape[0]) == 0, o.error()
+    chan = cf32(M * ring_blocks)
+    fp = abi.PfbFftParams(M, D, 12, base_block, blocks, ring_blocks, ring_blocks - 1)
+    assert o.pfb_fft(fp, branch, tw, chan) == 0, o.error()
+    return chan
+
+
+def fp64(g, taps, ring, base_block, blocks):
+    re = np.zeros(M * blocks)
+    im = np.zeros(M * blocks)
+    assert oracle().lib.or_pfb_f64(C.byref(g), taps.ctypes.data, ring.ctypes.data, ring.shape[0] - 1, base_block * D,
+                                   blocks, base_block, re.ctypes.data, im.ctypes.data) == 0
+    return (re + 1j * im).reshape(M, blocks)
+
+
+def check_tolerance(chan32, want, blocks, ring_blocks, first_slot):
+    got = chan32.reshape(M, ring_blocks, 2)[:, first_slot:first_slot + blocks]
+    got = got[..., 0].astype(np.float64) + 1j * got[..., 1]
+    err = got - want
+    rel = np.sqrt(np.mean(np.abs(err) ** 2) / np.mean(np.abs(want) ** 2))
+    spur = 20 * np.log10(np.max(np.abs(err)) / np.max(np.abs(want)))
+    return rel, spur
+
+
+def test_wide_prototype_matches_the_capped_design(rv):
+    """At M <= 2048 the wide designer is the reference's design_prototype."""
+    g = abi.GridParams(1024, 16, 512)
+    a, b = np.zeros(1024 * 16, np.float32), np.zeros(1024 * 16, np.float32)
+    assert rv.rv_design_prototype(C.byref(g), 120.0, a.ctypes.data, a.size, None, None) == 0
+    assert rv.rv_design_prototype_wide(C.byref(g), 120.0, b.ctypes.data, b.size, None, None) == 0
+    assert same_bits(a, b)
+    g4, taps, stop = prototype()
+    assert abs(float(taps.astype(np.float64).sum()) - 1.0) < 1e-5 and stop < -100.0
+    # the capped entry points still refuse M = 4096, as the reference does
+    assert rv.rv_design_prototype(C.byref(g4), 120.0, taps.ctypes.data, taps.size, None, None) == abi.RV_ERR_INVALID
+
+
+def test_oracle_fp32_within_tolerance_of_fp64():
+    g, taps, _ = prototype()
+    tw = twiddles()
+    ring = multitone(1 << 17)
+    base, blocks = M * T // D, 3
+    chan = oracle_fp32(g, taps, tw, ring, base, blocks, 4)
+    rel, spur = check_tolerance(chan, fp64(g, taps, ring, base, blocks), blocks, 4, base & 3)
+    print("C4 oracle FP32 vs FP64: relative RMS %.2e, spur floor %.1f dBc" % (rel, spur))
+    assert rel <= REL_RMS and spur <= SPUR_DBC
+
+
+@pytest.mark.gpu
+def test_gpu_c4_channelizer(gpu):
+    g, taps, _ = prototype()
+    tw = twiddles()
+    n = 1 << 20
+    ring = multitone(n)
+    base, blocks, ring_blocks = M * T // D, 256, 512
+    bp = abi.PfbBranchParams(n - 1, base * D, blocks)
+    d_ring, d_taps, d_tw = gpu.array(ring), gpu.array(taps), gpu.array(tw)
+    d_branch = gpu.zeros(blocks * M * 8)
+    d_chan = gpu.zeros(M * ring_blocks * 8)
+    assert lib().rv_pfb_branch_wide(gpu.stream, C.byref(g), C.byref(bp), d_taps.ptr, taps.size, d_ring.ptr, n,
+                                    d_branch.ptr, blocks * M) == 0, lib().rv_last_error()
+    fp = abi.PfbFftParams(M, D, 12, base, blocks, ring_blocks, ring_blocks - 1)
+    assert lib().rv_pfb_fft(gpu.stream, C.byref(fp), d_branch.ptr, blocks * M, d_tw.ptr, M, d_chan.ptr,
+                            M * ring_blocks) == 0, lib().rv_last_error()
+    gpu.synchronize()
+    got = d_chan.download(np.float32, (M * ring_blocks, 2))
+    # bit for bit against the FP32 oracle on a slice of blocks
+    want = oracle_fp32(g, taps, tw, ring, base, 8, ring_blocks)
+    sl = got.reshape(M, ring_blocks, 2)[:, base:base + 8]
+    assert same_bits(sl, want.reshape(M, ring_blocks, 2)[:, base:base + 8])
+    # and to the stated tolerance against FP64
+    rel, spur = check_tolerance(got, fp64(g, taps, ring, base, 3), 3, ring_blocks, base)
+    print("C4 GPU vs FP64: relative RMS %.2e, spur floor %.1f dBc" % (rel, spur))
+    assert rel <= REL_RMS and spur <= SPUR_DBC
