@@ -49,6 +49,7 @@ int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_
                             const rv_coarse_params* dyn = nullptr, const FrontEndTable* fe = nullptr);
 int32_t launch_convert_ring(cudaStream_t stream, int32_t format, const void* raw, uint32_t mask, uint32_t from,
                             uint32_t count, uint32_t window_start, const FrontEndTable* fe, rv_cf32* clean);
+bool coarse_fused_supported(const rv_grid_params& g);
 }  // namespace rv
 
 using namespace rv;
@@ -298,6 +299,10 @@ struct rv_chain {
     // on, and kept after it is switched off, because the channelizer's history
     // still reaches back into samples the stage excised.
     bool ex_clean = false;
+    // batched: a fused coarse kernel exists for the grid; otherwise the
+    // channelizer runs as the plain branch and FFT dispatches over the clean
+    // ring, and the receivers stay batched
+    bool fused = true;
     uint64_t ex_examined = 0;
     uint64_t ex_totals[3] = {0, 0, 0};  // samples, events, spared read back so far
 };
@@ -694,6 +699,21 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
         *deferred = p;
         return RV_OK;
     }
+    if (!c->fused) {
+        // no fused kernel for this grid: the reference's two dispatches over
+        // the clean ring (stream-start history is the ring's zeroed slots)
+        rv_pfb_branch_params bp{c->raw_mask, (uint32_t)(first_block * g.decimation), blocks};
+        if (int32_t st = rv_pfb_branch(c->stream, &g, &bp, c->proto.ptr, c->proto.count, c->clean.ptr, c->clean.count,
+                                       c->branch.ptr, c->branch.count))
+            return st;
+        rv_pfb_fft_params fp{g.channels, g.decimation, ilog2(g.channels), (uint32_t)first_block, blocks,
+                             c->chan_blocks, c->chan_blocks - 1u};
+        if (int32_t st = rv_pfb_fft(c->stream, &fp, c->branch.ptr, c->branch.count, c->twiddles.ptr, c->twiddles.count,
+                                    c->channel.ptr, c->channel.count))
+            return st;
+        c->stats.launches += 2;
+        return RV_OK;
+    }
     if (int32_t st = launch_coarse_fused(c->stream, g, clean ? kFormatCf32Ring : c->config.format, p,
                                          clean ? static_cast<const void*>(c->clean.ptr) : c->raw.ptr, c->proto.ptr,
                                          c->twiddles.ptr, c->channel.ptr, nullptr, c->fe_table))
@@ -1075,6 +1095,15 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     if (config->mode == RV_CHAIN_BATCHED) {
         st = c->raw.alloc(raw_cap * c->bytes_per_sample);
         if (!st) st = cuda_status(cudaMemsetAsync(c->raw.ptr, 0, raw_cap * c->bytes_per_sample, c->stream), "ring clear");
+        c->fused = coarse_fused_supported(g);
+        if (!st && !c->fused) {
+            // the stream-start history reads as zero, as in the plain chain's ring
+            st = c->clean.alloc(raw_cap);
+            if (!st) st = cuda_status(cudaMemsetAsync(c->clean.ptr, 0, raw_cap * sizeof(rv_cf32), c->stream), "ring clear");
+            if (!st) st = c->branch.alloc(blocks_per_run * g.channels);
+            c->ex_clean = true;
+            c->ex_converted_end = ~0ull;
+        }
     } else {
         st = c->raw.alloc(((uint64_t)config->max_run_samples + 1u) * c->bytes_per_sample);
         if (!st) st = c->cf32_ring.alloc(raw_cap);
@@ -1274,7 +1303,7 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
     const uint64_t last_block = first_block + blocks - 1u;  // meaningful when blocks > 0
     mark(c, 0);
     // a captured run launches the coarse kernel inside its graph
-    c->captured_run = !plain && c->graph && blocks > 0 && !c->rx.empty();
+    c->captured_run = !plain && c->graph && c->fused && blocks > 0 && !c->rx.empty();
     rv_coarse_params coarse{};
     int32_t st = plain ? coarse_plain(c, first_sample, src, count, where, first_block, blocks, excision)
                        : coarse_batched(c, first_sample, src, count, where, first_block, blocks,
@@ -1574,6 +1603,11 @@ int32_t rv_chain_capture_graph(rv_chain* c) {
         return set_error_fmt(RV_ERR_UNSUPPORTED,
                              "rv_chain_capture_graph: a plain chain records one launch per stage per receiver; only "
                              "the batched chain runs from a graph");
+    if (!c->fused)
+        return set_error_fmt(RV_ERR_UNSUPPORTED,
+                             "rv_chain_capture_graph: no fused channelizer kernel for M=%u T=%u D=%u; this chain's "
+                             "channelizer runs as per-run dispatches",
+                             c->config.grid.channels, c->config.grid.taps_per_branch, c->config.grid.decimation);
     c->graph = true;
     return clear_error();
 }
@@ -1616,7 +1650,10 @@ int32_t rv_chain_set_impulse_excision(rv_chain* c, int32_t on, double threshold_
         return st;
     const uint64_t cap = (uint64_t)c->raw_mask + 1u;
     int32_t st = RV_OK;
-    if (c->config.mode == RV_CHAIN_BATCHED && c->clean.count < cap) st = c->clean.alloc(cap);
+    if (c->config.mode == RV_CHAIN_BATCHED && c->clean.count < cap) {
+        st = c->clean.alloc(cap);
+        if (!st) st = cuda_status(cudaMemsetAsync(c->clean.ptr, 0, cap * sizeof(rv_cf32), c->stream), "ring clear");
+    }
     if (!st && c->ex_seg_power.count != (uint64_t)rings.seg_mask + 1u) {
         st = c->ex_seg_power.alloc((uint64_t)rings.seg_mask + 1u);
         if (!st) st = c->ex_seg_level.alloc((uint64_t)rings.seg_mask + 1u);

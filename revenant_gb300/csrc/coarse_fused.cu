@@ -318,6 +318,13 @@ int32_t launch_convert_ring(cudaStream_t stream, int32_t format, const void* raw
     return set_error_fmt(RV_ERR_UNSUPPORTED, "convert_ring: format %d", format);
 }
 
+// Whether a fused kernel is instantiated for the grid.
+bool coarse_fused_supported(const rv_grid_params& g) {
+    return (g.channels == 64 && g.taps_per_branch == 17 && g.decimation == 32) ||
+           (g.channels == 8 && g.taps_per_branch == 17 && g.decimation == 4) ||
+           (g.channels == 64 && g.taps_per_branch == 17 && g.decimation == 64);
+}
+
 // Dispatch over the instantiated grids. Returns RV_ERR_UNSUPPORTED for a
 // grid this build has no fused kernel for (the plain kernels cover it).
 int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_t format, const rv_coarse_params& p,
