@@ -1165,6 +1165,116 @@ int32_t rv_display_block(const rv_vrx_display_plan* plan, uint32_t channel_base,
 /* dsp::demod_fine_history (core/dsp/vrx_reference.h). */
 uint32_t rv_demod_fine_history(const rv_vrx_demod_config* config);
 
+/* ===================================================================== *
+ * Capture segments (core/capture/format.h, core/capture/writer.cpp): the  *
+ * rolling capture's on-disk SigMF recordings, so a capture replays       *
+ * through the chain. Host only.                                          *
+ *   <root>/<YYYY-MM-DD>/<stem>.sigmf-data   raw samples, source format   *
+ *   <root>/<YYYY-MM-DD>/<stem>.sigmf-meta   JSON, written on close       *
+ *   stem = rev-<yyyymmddThhmmss.fffZ>-<centre Hz>-<epoch %016x>-<first>  *
+ * An open segment is <stem>.open.sigmf-data plus <stem>.open.revenant.   *
+ * ===================================================================== */
+
+/* core:recorder is "Revenant " RV_CAPTURE_RECORDER_VERSION. */
+#define RV_CAPTURE_RECORDER_VERSION "gb300"
+
+/* WriterConfig (core/capture/writer.h). Zero disables each limit. */
+typedef struct rv_capture_config {
+    uint64_t max_segment_bytes;    /* a block that would pass it closes "size" first */
+    double max_segment_seconds;    /* a segment holding this much closes "size" */
+    uint64_t retention_bytes;      /* closed + open bytes kept; oldest closed go first */
+    int64_t retention_max_age_ns;  /* age from a segment's first sample */
+    uint64_t stream_epoch;         /* 0 = drawn at open */
+    int32_t recover_on_start;      /* close what a dead writer left open first */
+    int32_t reserved;
+} rv_capture_config;
+
+/* A source block (core/source/source.h SourceBlock with its
+ * BlockTimestamp): sample_count samples from stream index first_index. */
+typedef struct rv_capture_block {
+    uint64_t first_index;
+    int64_t epoch_anchor_ns; /* wall clock of stream index 0 */
+    int64_t rate;            /* samples per second */
+    int64_t center;          /* Hz */
+    uint64_t sample_count;
+    uint64_t dropped_before; /* samples the device lost just before this block */
+    int32_t format;          /* RV_FORMAT_CU8, _CS8, _CS16 or _CS24 */
+    int32_t reserved;
+} rv_capture_block;
+
+/* Annotation (core/capture/format.h) as the detector files it: a track's
+ * extent in samples and Hz. core:label is the family, else "signal". */
+typedef struct rv_capture_annotation {
+    uint64_t sample_count;
+    int64_t freq_lower;
+    int64_t freq_upper;
+    double confidence;
+    double peak_db;
+    double snr_db;
+    uint64_t track_id;
+    int32_t has_track_id;
+    int32_t reserved;
+    char family[32];
+} rv_capture_annotation;
+
+typedef struct rv_capture_writer_stats {
+    uint64_t segments_written;
+    uint64_t bytes_written;
+    uint64_t segments_deleted;
+    uint64_t delete_failures;
+    uint64_t annotations_discarded;
+    uint64_t annotations_merged_late;
+    uint64_t retained_bytes;
+    uint64_t recovered;      /* segments closed as "recovered" at open */
+    uint64_t stream_epoch;
+} rv_capture_writer_stats;
+
+typedef struct rv_capture_segment {
+    char day[16];            /* YYYY-MM-DD directory */
+    char stem[96];
+    char close_reason[16];   /* retune, rate, format, loss, size, stop, recovered */
+    int64_t rate;
+    int64_t center;
+    int32_t format;
+    int32_t has_gain;
+    double gain_db;
+    uint64_t stream_epoch;
+    uint64_t first_index;
+    int64_t epoch_anchor_ns;
+    uint64_t dropped_before;
+    uint64_t samples;
+} rv_capture_segment;
+
+typedef struct rv_capture_writer rv_capture_writer;
+
+/* SegmentWriter::start (core/capture/writer.cpp). hw = core:hw (may be NULL). */
+int32_t rv_capture_writer_open(const char* root, const rv_capture_config* config, const char* hw,
+                               rv_capture_writer** out);
+/* SegmentWriter::consume + process: closes the open segment when the block
+ * does not continue it, opens one when none is open, appends the block.
+ * byte_count = sample_count * bytes per sample of the format. */
+int32_t rv_capture_writer_write(rv_capture_writer* w, const rv_capture_block* block, const void* bytes,
+                                uint64_t byte_count);
+/* SegmentWriter::set_gain_db: in force for segments opened from now. */
+int32_t rv_capture_writer_set_gain(rv_capture_writer* w, int32_t has_gain, double gain_db);
+/* SegmentWriter::add_annotation: [absolute_start, + sample_count) in
+ * stream indices, filed into every segment it overlaps. */
+int32_t rv_capture_writer_annotate(rv_capture_writer* w, uint64_t absolute_start, const rv_capture_annotation* a);
+/* The clock retention ages against; 0 = the system clock. */
+int32_t rv_capture_writer_set_clock(rv_capture_writer* w, int64_t now_ns);
+int32_t rv_capture_writer_get_stats(const rv_capture_writer* w, rv_capture_writer_stats* out);
+/* SegmentWriter::stop: closes the open segment ("stop"), frees the writer. */
+int32_t rv_capture_writer_close(rv_capture_writer* w);
+/* The catalog: closed segments under root, by day then stem; *count = all
+ * of them, the first `capacity` written to out (out may be NULL). */
+int32_t rv_capture_list(const char* root, rv_capture_segment* out, uint32_t capacity, uint32_t* count);
+/* Samples [offset, offset + count) of a listed segment, in its format. */
+int32_t rv_capture_read(const char* root, const rv_capture_segment* segment, uint64_t offset, uint64_t count,
+                        void* out);
+/* recover_open_segments: closes segments a dead writer left open
+ * ("recovered"). counts = {recovered, removed empty, failed}. */
+int32_t rv_capture_recover(const char* root, uint32_t counts[3]);
+
 #ifdef __cplusplus
 }
 #endif

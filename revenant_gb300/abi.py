@@ -197,6 +197,34 @@ class CombParams(_S):
                 ("removed_mask", U32), ("pad0", U32), ("pad1", U32)]
 
 
+class CaptureConfig(_S):
+    _fields_ = [("max_segment_bytes", U64), ("max_segment_seconds", F64), ("retention_bytes", U64),
+                ("retention_max_age_ns", I64), ("stream_epoch", U64), ("recover_on_start", I32), ("reserved", I32)]
+
+
+class CaptureBlock(_S):
+    _fields_ = [("first_index", U64), ("epoch_anchor_ns", I64), ("rate", I64), ("center", I64),
+                ("sample_count", U64), ("dropped_before", U64), ("format", I32), ("reserved", I32)]
+
+
+class CaptureAnnotation(_S):
+    _fields_ = [("sample_count", U64), ("freq_lower", I64), ("freq_upper", I64), ("confidence", F64),
+                ("peak_db", F64), ("snr_db", F64), ("track_id", U64), ("has_track_id", I32), ("reserved", I32),
+                ("family", C.c_char * 32)]
+
+
+class CaptureWriterStats(_S):
+    _fields_ = [(n, U64) for n in ("segments_written", "bytes_written", "segments_deleted", "delete_failures",
+                                   "annotations_discarded", "annotations_merged_late", "retained_bytes",
+                                   "recovered", "stream_epoch")]
+
+
+class CaptureSegment(_S):
+    _fields_ = [("day", C.c_char * 16), ("stem", C.c_char * 96), ("close_reason", C.c_char * 16), ("rate", I64),
+                ("center", I64), ("format", I32), ("has_gain", I32), ("gain_db", F64), ("stream_epoch", U64),
+                ("first_index", U64), ("epoch_anchor_ns", I64), ("dropped_before", U64), ("samples", U64)]
+
+
 LINE_NOTCH, LINE_ALE, LINE_GUARD, LINE_NOTCH_COUNT_SHIFT = 1, 2, 4, 8
 LINE_STATE_WEIGHTS = 24
 
@@ -326,7 +354,9 @@ EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params"
                  "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
                  "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,
                  "rv_excision_plan": ExcisionPlan, "rv_excision_cursor": ExcisionCursor,
-                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_comb_line": CombLine, "rv_comb_params": CombParams, "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
+                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_comb_line": CombLine, "rv_capture_config": CaptureConfig,
+                 "rv_capture_block": CaptureBlock, "rv_capture_annotation": CaptureAnnotation,
+                 "rv_capture_writer_stats": CaptureWriterStats, "rv_capture_segment": CaptureSegment, "rv_comb_params": CombParams, "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
                  "rv_line_config": LineConfig, "rv_line_section": LineSection, "rv_line_params": LineParams,
                  "rv_notch_design": NotchDesign, "rv_spectral_config": SpectralConfig,
                  "rv_spectral_params": SpectralParams,

@@ -183,6 +183,16 @@ SIGNATURES = {
     "rv_comb_table": (I32, [P, U64]),
     "rv_comb_project": (I32, [P, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_comb_subtract": (I32, [P, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64, P, U64]),
+    "rv_capture_writer_open": (I32, [C.c_char_p, ptr(abi.CaptureConfig), C.c_char_p, ptr(P)]),
+    "rv_capture_writer_write": (I32, [P, ptr(abi.CaptureBlock), P, U64]),
+    "rv_capture_writer_set_gain": (I32, [P, I32, F64]),
+    "rv_capture_writer_annotate": (I32, [P, U64, ptr(abi.CaptureAnnotation)]),
+    "rv_capture_writer_set_clock": (I32, [P, I64]),
+    "rv_capture_writer_get_stats": (I32, [P, ptr(abi.CaptureWriterStats)]),
+    "rv_capture_writer_close": (I32, [P]),
+    "rv_capture_list": (I32, [C.c_char_p, P, U32, ptr(U32)]),
+    "rv_capture_read": (I32, [C.c_char_p, ptr(abi.CaptureSegment), U64, U64, P]),
+    "rv_capture_recover": (I32, [C.c_char_p, P]),
     "rv_display_max_decimation": (U32, []),
     "rv_display_ladder": (I32, [I64, P, U32, ptr(U32)]),
     "rv_display_decimation": (U32, [I64, I64]),
