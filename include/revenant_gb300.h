@@ -1092,6 +1092,18 @@ int32_t rv_design_prototype(const rv_grid_params* grid, double attenuation_db, f
  * FFT dispatch is rv_pfb_fft (up to 16384 channels) with rv_build_fft_twiddles. */
 int32_t rv_design_prototype_wide(const rv_grid_params* grid, double attenuation_db, float* taps,
                                  uint64_t taps_len, double* stopband_db, uint64_t* group_delay);
+/* C4's split-precision DFT on the tensor cores (tcgen05): rv_pfb_fft's
+ * outputs for M = 4096 (the channel ring, phase correction included),
+ * computed as two 64-point DFT GEMM stages with hi + lo split operands in
+ * FP16 or BF16 and FP32 accumulators. Accurate to a stated tolerance against
+ * FP64, not bit-identical to rv_pfb_fft. Synchronous on `stream` (it reads
+ * back a flag that a bounded wait on the tensor cores ran out:
+ * RV_ERR_TIMEOUT). */
+#define RV_DFT_FP16 0
+#define RV_DFT_BF16 1
+int32_t rv_pfb_dft_tc(void* stream, const rv_pfb_fft_params* params, const rv_cf32* branch_dev, uint64_t branch_len,
+                      const rv_cf32* twiddles_dev, uint64_t twiddles_len, rv_cf32* ring_dev, uint64_t ring_len,
+                      int32_t precision);
 int32_t rv_pfb_branch_wide(void* stream, const rv_grid_params* grid, const rv_pfb_branch_params* params,
                            const float* taps_dev, uint64_t taps_len, const rv_cf32* ring_dev,
                            uint64_t ring_len, rv_cf32* out_dev, uint64_t out_len);

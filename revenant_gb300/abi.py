@@ -197,6 +197,9 @@ class CombParams(_S):
                 ("removed_mask", U32), ("pad0", U32), ("pad1", U32)]
 
 
+DFT_FP16, DFT_BF16 = 0, 1
+
+
 class CaptureConfig(_S):
     _fields_ = [("max_segment_bytes", U64), ("max_segment_seconds", F64), ("retention_bytes", U64),
                 ("retention_max_age_ns", I64), ("stream_epoch", U64), ("recover_on_start", I32), ("reserved", I32)]

@@ -183,6 +183,7 @@ SIGNATURES = {
     "rv_comb_table": (I32, [P, U64]),
     "rv_comb_project": (I32, [P, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64]),
     "rv_comb_subtract": (I32, [P, ptr(abi.CombParams), P, U64, P, U64, P, U64, P, U64, P, U64]),
+    "rv_pfb_dft_tc": (I32, [P, ptr(abi.PfbFftParams), P, U64, P, U64, P, U64, I32]),
     "rv_capture_writer_open": (I32, [C.c_char_p, ptr(abi.CaptureConfig), C.c_char_p, ptr(P)]),
     "rv_capture_writer_write": (I32, [P, ptr(abi.CaptureBlock), P, U64]),
     "rv_capture_writer_set_gain": (I32, [P, I32, F64]),

@@ -12,8 +12,16 @@ are checked
     SPUR_DBC = -110 dB for the worst single output error against the
     strongest output (the spur floor the FP32 arithmetic leaves).
 
-The tensor-core split-precision DFT this config is also named for is not
-built; the FFT path is the one measured here.
+The split-precision DFT on the tensor cores (rv_pfb_dft_tc: the four-step
+64 x 64 factorisation as two tcgen05 GEMM stages, operands split hi + lo in
+FP16 or in BF16, FP32 accumulators in tensor memory) is checked against the
+same FP64 restatement, to its own stated tolerances:
+
+  * FP16 split: TC_FP16 = (relative RMS 2e-6, spur floor -115 dBc)
+  * BF16 split: TC_BF16 = (relative RMS 2e-5, spur floor -105 dBc)
+
+(measured on a GB300: 5.2e-7 / -123.8 dBc and 4.8e-6 / -114.8 dBc, against
+1.6e-7 / -139 dBc for the FP32 FFT).
 """
 import ctypes as C
 
@@ -27,6 +35,8 @@ from revenant_gb300.library import lib
 M, T, D = 4096, 16, 2048
 REL_RMS = 2e-6
 SPUR_DBC = -110.0
+TC_FP16 = (2e-6, -115.0)
+TC_BF16 = (2e-5, -105.0)
 
 
 def prototype():
@@ -137,3 +147,45 @@ def test_gpu_c4_channelizer(gpu):
     rel, spur = check_tolerance(got, fp64(g, taps, ring, base, 3), 3, ring_blocks, base)
     print("C4 GPU vs FP64: relative RMS %.2e, spur floor %.1f dBc" % (rel, spur))
     assert rel <= REL_RMS and spur <= SPUR_DBC
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_gpu_c4_tensor_core_dft(gpu, precision):
+    """rv_pfb_dft_tc against FP64 at its stated tolerance."""
+    prec, (rel_max, spur_max) = (abi.DFT_FP16, TC_FP16) if precision == "fp16" else (abi.DFT_BF16, TC_BF16)
+    g, taps, _ = prototype()
+    tw = twiddles()
+    n = 1 << 20
+    ring = multitone(n, seed=7)
+    d_ring, d_taps, d_tw = gpu.array(ring), gpu.array(taps), gpu.array(tw)
+    # 256 blocks (128 tiles over the SMs), then an odd count (a half tile)
+    # whose checked blocks wrap an 8-block ring (slots 6, 7, 0)
+    for base, blocks, ring_blocks in ((M * T // D, 256, 512), (38, 5, 8)):
+        checked = 3
+        bp = abi.PfbBranchParams(n - 1, base * D, blocks)
+        d_branch = gpu.zeros(blocks * M * 8)
+        d_chan = gpu.zeros(M * ring_blocks * 8)
+        assert lib().rv_pfb_branch_wide(gpu.stream, C.byref(g), C.byref(bp), d_taps.ptr, taps.size, d_ring.ptr, n,
+                                        d_branch.ptr, blocks * M) == 0, lib().rv_last_error()
+        fp = abi.PfbFftParams(M, D, 12, base, blocks, ring_blocks, ring_blocks - 1)
+        assert lib().rv_pfb_dft_tc(gpu.stream, C.byref(fp), d_branch.ptr, blocks * M, d_tw.ptr, M, d_chan.ptr,
+                                   M * ring_blocks, prec) == 0, lib().rv_last_error()
+        got = d_chan.download(np.float32, (M * ring_blocks, 2)).reshape(M, ring_blocks, 2)
+        slots = [(base + b) & (ring_blocks - 1) for b in range(checked)]
+        rel, spur = check_tolerance(got[:, slots].reshape(-1, 2), fp64(g, taps, ring, base, checked), checked,
+                                    checked, 0)
+        print("C4 tensor-core DFT (%s split) vs FP64, %d blocks: relative RMS %.2e, spur floor %.1f dBc"
+              % (precision, blocks, rel, spur))
+        assert rel <= rel_max and spur <= spur_max
+
+
+def test_tensor_core_dft_rejects_other_grids(rv):
+    fp = abi.PfbFftParams(2048, 1024, 11, 0, 4, 4, 3)
+    assert rv.rv_pfb_dft_tc(None, C.byref(fp), None, 0, None, 0, None, 0, abi.DFT_FP16) == abi.RV_ERR_INVALID
+    one = np.zeros(2, np.float32)
+    p = one.ctypes.data
+    assert rv.rv_pfb_dft_tc(None, C.byref(fp), p, 1 << 30, p, 2048, p, 1 << 30, abi.DFT_FP16) == abi.RV_ERR_UNSUPPORTED
+    fp = abi.PfbFftParams(M, D, 12, 0, 4, 4, 3)
+    assert rv.rv_pfb_dft_tc(None, C.byref(fp), p, 1 << 30, p, M, p, 1 << 30, 7) == abi.RV_ERR_INVALID
+    assert rv.rv_pfb_dft_tc(None, C.byref(fp), p, 1 << 30, p, 100, p, 1 << 30, abi.DFT_FP16) == abi.RV_ERR_INVALID
