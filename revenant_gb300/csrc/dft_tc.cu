@@ -22,13 +22,16 @@
 // just below 2^14 before splitting, and GEMM 2's operand by 2^-6, keeping every
 // hi and lo part in FP16's normal range; the scales are undone on output.
 //
-// One CTA per SM (four warps, 193 KB of shared memory), persistent over pairs
-// of blocks. Operands are written to shared memory by the threads in the
-// canonical no-swizzle K-major layout (8-row x 16-byte core matrices); thread
-// 0 issues the MMAs and commits them to an mbarrier; every warp reads its 32
-// TMEM lanes back with tcgen05.ld. Every mbarrier wait is bounded: a wait that
-// runs out sets an error flag the host reads, and the CTA frees its TMEM and
-// returns.
+// One CTA per SM (225 KB of shared memory), persistent over pairs of blocks.
+// A tile's two blocks (64 contiguous KB of branch outputs) arrive through the
+// bulk-copy engine (cp.async.bulk, completing on an mbarrier) while the
+// previous tile is in the tensor cores. Operands are written to shared memory
+// by the threads in the canonical no-swizzle K-major layout (8-row x 16-byte
+// core matrices); thread 0 issues the MMAs and commits them to an mbarrier;
+// every warp reads its 32 TMEM lanes back with tcgen05.ld, and the Re and Im
+// halves of each accumulator meet through a 33 KB exchange. Every mbarrier
+// wait is bounded: a wait that runs out sets an error flag the host reads,
+// and the CTA lets its copies land, frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -41,21 +44,24 @@ namespace {
 
 constexpr uint32_t kM = 4096;
 constexpr uint32_t kRadix = 64;
-constexpr uint32_t kPair = 2;                       // blocks per tile
-constexpr uint32_t kRows = 128;                     // GEMM M: [Re | Im] x 64
-constexpr uint32_t kK = 128;                        // GEMM K: [Re | Im] x 64
-constexpr uint32_t kCols = kPair * kRadix;          // GEMM N
-constexpr uint32_t kOperand = kRows * kK * 2;       // one 16-bit operand: 32 KB
-constexpr uint32_t kPitch = kCols + 1;              // FP32 staging row pitch
-constexpr uint32_t kStageBytes = kRows * kPitch * 4;  // 66,048
-constexpr uint32_t kOffA = 0;                       // A_hi, A_lo
-constexpr uint32_t kOffX = 2 * kOperand;            // B1_hi, B1_lo | FP32 staging
-constexpr uint32_t kOffB2 = kOffX + kStageBytes;    // B2_hi, B2_lo
-constexpr uint32_t kOffMisc = kOffB2 + 2 * kOperand;
-constexpr uint32_t kSmemBytes = kOffMisc + 64;
+constexpr uint32_t kPair = 2;                        // blocks per tile
+constexpr uint32_t kRows = 128;                      // GEMM M: [Re | Im] x 64
+constexpr uint32_t kK = 128;                         // GEMM K: [Re | Im] x 64
+constexpr uint32_t kCols = kPair * kRadix;           // GEMM N
+constexpr uint32_t kOperand = kRows * kK * 2;        // one 16-bit operand: 32 KB
+constexpr uint32_t kBlockBytes = kM * 8;             // one block of branch outputs: 32 KB
+constexpr uint32_t kXPitch = kRadix + 1;             // exchange row pitch (odd: no bank conflicts)
+constexpr uint32_t kXBytes = kRadix * kXPitch * 4;   // one 64 x 64 FP32 exchange half
+constexpr uint32_t kOffA = 0;                        // A_hi, A_lo
+constexpr uint32_t kOffB = 2 * kOperand;             // B_hi, B_lo: GEMM 1's operand, then GEMM 2's
+constexpr uint32_t kOffRaw = 4 * kOperand;           // the tile's two blocks, prefetched
+constexpr uint32_t kOffX = kOffRaw + kPair * kBlockBytes;  // Re and Im exchange halves
+constexpr uint32_t kOffMisc = kOffX + 2 * kXBytes;
+constexpr uint32_t kSmemBytes = kOffMisc + 64;       // 229,952 bytes
 constexpr uint32_t kThreads = 128;
-constexpr uint32_t kTmemCols = 256;                 // acc0 at column 0, acc1 at 128
+constexpr uint32_t kTmemCols = 256;                  // acc0 at column 0, acc1 at 128
 constexpr uint32_t kWaitLimit = 1u << 20;
+static_assert(kSmemBytes <= 232448, "shared memory per CTA");
 
 __device__ uint32_t g_dft_timeouts;
 
@@ -160,17 +166,31 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// The two accumulators of this thread's row combined into the FP32 staging
-// row: acc0 + acc1 2^-s, times `scale`.
+// This thread's TMEM row, columns [c0, c0 + 32): acc0 + acc1 2^-s.
 template <int P>
-__device__ __forceinline__ void drain_row(uint32_t tmem, uint32_t row, float* stage, float scale) {
-    const uint32_t lane_base = tmem + (((row >> 5) * 32u) << 16);
-    for (uint32_t c = 0; c < kCols; c += 32) {
-        float a[32], b[32];
-        tmem_ld32(lane_base + c, a);
-        tmem_ld32(lane_base + kCols + c, b);
+__device__ __forceinline__ void combined32(uint32_t tmem, uint32_t c0, float* v) {
+    float b[32];
+    tmem_ld32(tmem + c0, v);
+    tmem_ld32(tmem + kCols + c0, b);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) stage[row * kPitch + c + i] = (a[i] + b[i] * Split<P>::kInvLo) * scale;
+    for (int i = 0; i < 32; ++i) v[i] = v[i] + b[i] * Split<P>::kInvLo;
+}
+
+// Rows 0-63 of an accumulator hold Re, rows 64-127 Im, of 64 output indices;
+// columns 0-63 belong to the tile's first block, 64-127 to its second. Each
+// half of the CTA finishes one block: threads 0-63 (Re rows) the first,
+// 64-127 (Im rows) the second. So each hands the other half the part it
+// lacks: Re rows put their second-block columns in xa, Im rows their
+// first-block columns in xb.
+template <int P>
+__device__ __forceinline__ void exchange(uint32_t lane_tmem, uint32_t tid, float* xa, float* xb) {
+    const uint32_t i = tid & 63u, other = tid < 64u ? kRadix : 0u;
+    float* x = tid < 64u ? xa : xb;
+    for (uint32_t c = 0; c < kRadix; c += 32) {
+        float v[32];
+        combined32<P>(lane_tmem, other + c, v);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) x[i * kXPitch + c + (uint32_t)k] = v[k];
     }
 }
 
@@ -188,6 +208,19 @@ __device__ __forceinline__ void issue_gemm(uint32_t tmem, uint32_t a_hi, uint32_
     commit(mbar);
 }
 
+// The tile's valid blocks (contiguous in the branch buffer) into shared
+// memory through the bulk-copy engine, completing on `mbar`.
+__device__ __forceinline__ void prefetch(uint32_t raw, const float2* src, uint32_t nblocks, uint32_t mbar) {
+    const uint32_t bytes = nblocks * kBlockBytes;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+    for (uint32_t k = 0; k < nblocks; ++k)
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                raw + k * kBlockBytes),
+            "l"(src + (uint64_t)k * kM), "r"(kBlockBytes), "r"(mbar)
+            : "memory");
+}
+
 template <int P>
 __global__ void __launch_bounds__(kThreads, 1)
 k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float2* __restrict__ out,
@@ -195,17 +228,22 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* const a_hi = sm + kOffA;
     uint8_t* const a_lo = a_hi + kOperand;
-    uint8_t* const x_hi = sm + kOffX;  // B1 (hi, lo), then the FP32 staging
-    uint8_t* const x_lo = x_hi + kOperand;
-    float* const stage = reinterpret_cast<float*>(sm + kOffX);
-    uint8_t* const b2_hi = sm + kOffB2;
-    uint8_t* const b2_lo = b2_hi + kOperand;
-    uint64_t* const mbar = reinterpret_cast<uint64_t*>(sm + kOffMisc);
-    uint32_t* const tmem_slot = reinterpret_cast<uint32_t*>(sm + kOffMisc + 8);
-    uint32_t* const abort_flag = reinterpret_cast<uint32_t*>(sm + kOffMisc + 12);
-    float* const block_max = reinterpret_cast<float*>(sm + kOffMisc + 16);  // [kPair][2 warps]
+    uint8_t* const b_hi = sm + kOffB;
+    uint8_t* const b_lo = b_hi + kOperand;
+    const float2* const raw = reinterpret_cast<const float2*>(sm + kOffRaw);
+    float* const xa = reinterpret_cast<float*>(sm + kOffX);
+    float* const xb = xa + kRadix * kXPitch;
+    uint64_t* const mbar = reinterpret_cast<uint64_t*>(sm + kOffMisc);  // [0] MMAs, [1] prefetch
+    uint32_t* const tmem_slot = reinterpret_cast<uint32_t*>(sm + kOffMisc + 16);
+    uint32_t* const abort_flag = reinterpret_cast<uint32_t*>(sm + kOffMisc + 20);
+    float* const block_max = reinterpret_cast<float*>(sm + kOffMisc + 32);  // one per warp
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    const uint32_t mbar_addr = smem_addr(mbar);
+    const uint32_t mbar_mma = smem_addr(mbar), mbar_raw = smem_addr(mbar + 1), raw_addr = smem_addr(raw);
+    const uint32_t tiles = (p.block_count + kPair - 1u) / kPair;
+    auto valid_in = [&](uint32_t tile) {
+        const uint32_t b0 = tile * kPair;
+        return p.block_count - b0 < kPair ? p.block_count - b0 : kPair;
+    };
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
@@ -213,10 +251,14 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_addr));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_mma));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_raw));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *abort_flag = 0;
     }
+    __syncthreads();
+    if (tid == 0 && blockIdx.x < tiles)
+        prefetch(raw_addr, branch + (uint64_t)blockIdx.x * kPair * kM, valid_in(blockIdx.x), mbar_raw);
     // A = F in real block form, the same for both stages: row r = [Re | Im]
     // of the output index, column k = [Re | Im] of the summed index.
     {
@@ -237,27 +279,31 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_tmem = tmem + ((warp * 32u) << 16);  // this warp's 32 lanes
 
-    const uint32_t tiles = (p.block_count + kPair - 1u) / kPair;
-    uint32_t parity = 0;
+    uint32_t parity_mma = 0, parity_raw = 0;
+    bool raw_in_flight = blockIdx.x < tiles;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const uint32_t b0 = tile * kPair;
-        // this thread's B1 row: block `blk` of the pair, n2
-        const uint32_t blk = tid >> 6, n2 = tid & 63u, b = b0 + blk;
-        const bool valid = b < p.block_count;
-        const float2* y = branch + (uint64_t)(valid ? b : b0) * kM;
+        const uint32_t b0 = tile * kPair, nvalid = valid_in(tile);
+        const uint32_t blk = tid >> 6, i64 = tid & 63u, b = b0 + blk;
+        const bool valid = blk < nvalid;
+        const float2* y = raw + blk * kM;
         const uint32_t m_abs = p.block_base + b;
         const uint32_t dm = ((m_abs & (kM - 1u)) * p.decimation) & (kM - 1u);
+        if (!wait_parity(mbar_raw, parity_raw)) atomicExch(abort_flag, 1u);
+        parity_raw ^= 1u;
+        raw_in_flight = false;
         // the block's largest component, for the power-of-two scale
         float mx = 0.0F;
         if (valid)
             for (uint32_t n1 = 0; n1 < kRadix; ++n1) {
-                const float2 v = y[(kRadix * n1 + n2 - dm) & (kM - 1u)];
+                const float2 v = y[(kRadix * n1 + i64 - dm) & (kM - 1u)];
                 mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
             }
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
         if (lane == 0) block_max[warp] = mx;
         __syncthreads();
+        if (*abort_flag) break;
         const float bmax = fmaxf(block_max[blk * 2], block_max[blk * 2 + 1]);
         int shift = 0;  // scale = 2^shift puts bmax in [2^13, 2^14)
         if (bmax > 0.0F) {
@@ -266,74 +312,92 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
             shift = shift > 100 ? 100 : (shift < -100 ? -100 : shift);
         }
         const float scale_in = ldexpf(1.0F, shift);
-        // B1 row (blk, n2): K = [Re | Im] of y'[64 n1 + n2], n1 = 0..63
+        // B1 row (blk, n2 = i64): K = [Re | Im] of y'[64 n1 + n2], n1 = 0..63
         for (uint32_t j = 0; j < kRadix / 8; ++j) {
             float re[8], im[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const uint32_t n1 = 8u * j + (uint32_t)i;
-                const float2 v = valid ? y[(kRadix * n1 + n2 - dm) & (kM - 1u)] : make_float2(0.0F, 0.0F);
-                re[i] = v.x * scale_in;
-                im[i] = v.y * scale_in;
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t n1 = 8u * j + (uint32_t)k;
+                const float2 v = valid ? y[(kRadix * n1 + i64 - dm) & (kM - 1u)] : make_float2(0.0F, 0.0F);
+                re[k] = v.x * scale_in;
+                im[k] = v.y * scale_in;
             }
-            store_split8<P>(x_hi, x_lo, tid, 8u * j, re);
-            store_split8<P>(x_hi, x_lo, tid, kRadix + 8u * j, im);
+            store_split8<P>(b_hi, b_lo, tid, 8u * j, re);
+            store_split8<P>(b_hi, b_lo, tid, kRadix + 8u * j, im);
         }
         fence_async_smem();
         __syncthreads();
-        if (tid == 0) issue_gemm<P>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(x_hi), smem_addr(x_lo), mbar_addr);
-        if (!wait_parity(mbar_addr, parity)) atomicExch(abort_flag, 1u);
-        parity ^= 1u;
+        if (tid == 0) {
+            issue_gemm<P>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b_hi), smem_addr(b_lo), mbar_mma);
+            const uint32_t next = tile + gridDim.x;  // the raw blocks are read: fetch the next tile's
+            if (next < tiles) {
+                fence_async_smem();
+                prefetch(raw_addr, branch + (uint64_t)next * kPair * kM, valid_in(next), mbar_raw);
+            }
+        }
+        raw_in_flight = tile + gridDim.x < tiles;
+        if (!wait_parity(mbar_mma, parity_mma)) atomicExch(abort_flag, 1u);
+        parity_mma ^= 1u;
         __syncthreads();
         if (*abort_flag) break;
         fence_after();
-        // GEMM 1 out: row tid = [Re | Im] Z[k1], columns (blk, n2); times 2^-6
-        drain_row<P>(tmem, tid, stage, 1.0F / 64.0F);
-        fence_before();
+        // GEMM 1 out, times 2^-6: Re Z[k1] in rows k1, Im in 64 + k1
+        exchange<P>(lane_tmem, tid, xa, xb);
         __syncthreads();
-        // B2 row (blk, k1): K = [Re | Im] of Z'[k1][n2] = Z[k1][n2] W^(k1 n2)
-        {
-            const uint32_t k1 = tid & 63u, col0 = blk * kRadix;
-            for (uint32_t j = 0; j < kRadix / 8; ++j) {
+        // B2 row (blk, k1 = i64): K = [Re | Im] of Z'[k1][n2] = Z[k1][n2] W^(k1 n2)
+        for (uint32_t c = 0; c < kRadix; c += 32) {
+            float own[32];
+            combined32<P>(lane_tmem, blk * kRadix + c, own);
+            for (uint32_t j = 0; j < 32; j += 8) {
                 float re[8], im[8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const uint32_t c = 8u * j + (uint32_t)i;
-                    const float zr = stage[k1 * kPitch + col0 + c], zi = stage[(64u + k1) * kPitch + col0 + c];
-                    const float2 w = tw[(k1 * c) & (kM - 1u)];
-                    re[i] = zr * w.x - zi * w.y;
-                    im[i] = zr * w.y + zi * w.x;
+                for (int k = 0; k < 8; ++k) {
+                    const uint32_t n2 = c + j + (uint32_t)k;
+                    const float mine = own[j + (uint32_t)k] * (1.0F / 64.0F);
+                    const float theirs = (tid < 64u ? xb : xa)[i64 * kXPitch + n2] * (1.0F / 64.0F);
+                    const float zr = tid < 64u ? mine : theirs, zi = tid < 64u ? theirs : mine;
+                    const float2 w = tw[(i64 * n2) & (kM - 1u)];
+                    re[k] = zr * w.x - zi * w.y;
+                    im[k] = zr * w.y + zi * w.x;
                 }
-                store_split8<P>(b2_hi, b2_lo, tid, 8u * j, re);
-                store_split8<P>(b2_hi, b2_lo, tid, kRadix + 8u * j, im);
+                store_split8<P>(b_hi, b_lo, tid, c + j, re);
+                store_split8<P>(b_hi, b_lo, tid, kRadix + c + j, im);
             }
         }
         fence_async_smem();
+        fence_before();
         __syncthreads();
-        if (tid == 0)
-            issue_gemm<P>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b2_hi), smem_addr(b2_lo), mbar_addr);
-        if (!wait_parity(mbar_addr, parity)) atomicExch(abort_flag, 1u);
-        parity ^= 1u;
+        if (tid == 0) issue_gemm<P>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b_hi), smem_addr(b_lo), mbar_mma);
+        if (!wait_parity(mbar_mma, parity_mma)) atomicExch(abort_flag, 1u);
+        parity_mma ^= 1u;
         __syncthreads();
         if (*abort_flag) break;
         fence_after();
-        // GEMM 2 out: row tid = [Re | Im] Y[k1 + 64 k2] for k2, columns (blk, k1);
-        // undo the scales: 2^6 2^-shift (this row's block differs per column
-        // half, so the scale is applied on output)
-        drain_row<P>(tmem, tid, stage, 64.0F);
-        fence_before();
+        // GEMM 2 out: Re Y[k1 + 64 k2] in rows k2, Im in 64 + k2, columns
+        // (block, k1); times 2^6 2^-shift undoes both scales
+        exchange<P>(lane_tmem, tid, xa, xb);
         __syncthreads();
         if (valid) {
-            const float scale_out = ldexpf(1.0F, -shift);
-            const uint32_t k2 = tid & 63u, slot = m_abs & p.out_ring_mask;
-            for (uint32_t k1 = 0; k1 < kRadix; ++k1) {
-                const float re = stage[k2 * kPitch + blk * kRadix + k1] * scale_out;
-                const float im = stage[(64u + k2) * kPitch + blk * kRadix + k1] * scale_out;
-                out[(uint64_t)(k1 + kRadix * k2) * p.out_ring_blocks + slot] = make_float2(re, im);
+            const float scale_out = ldexpf(64.0F, -shift);
+            const uint32_t slot = m_abs & p.out_ring_mask;
+            for (uint32_t c = 0; c < kRadix; c += 32) {
+                float own[32];
+                combined32<P>(lane_tmem, blk * kRadix + c, own);
+#pragma unroll
+                for (uint32_t k = 0; k < 32; ++k) {
+                    const uint32_t k1 = c + k;
+                    const float mine = own[k], theirs = (tid < 64u ? xb : xa)[i64 * kXPitch + k1];
+                    const float re = (tid < 64u ? mine : theirs) * scale_out;
+                    const float im = (tid < 64u ? theirs : mine) * scale_out;
+                    out[(uint64_t)(k1 + kRadix * i64) * p.out_ring_blocks + slot] = make_float2(re, im);
+                }
             }
         }
-        __syncthreads();  // the staging is B1's space again
+        fence_before();
+        __syncthreads();  // B and the exchange are free for the next tile
     }
+    // a prefetch still in flight (after an abort) lands before the CTA leaves
+    if (tid == 0 && raw_in_flight) wait_parity(mbar_raw, parity_raw);
     if (tid == 0 && *abort_flag) atomicAdd(&g_dft_timeouts, 1u);
     fence_before();
     __syncthreads();
