@@ -57,11 +57,14 @@ constexpr uint32_t kOffB = 2 * kOperand;             // B_hi, B_lo: GEMM 1's ope
 constexpr uint32_t kOffRaw = 4 * kOperand;           // the tile's two blocks, prefetched
 constexpr uint32_t kOffX = kOffRaw + kPair * kBlockBytes;  // Re and Im exchange halves
 constexpr uint32_t kOffMisc = kOffX + 2 * kXBytes;
-constexpr uint32_t kSmemBytes = kOffMisc + 64;       // 229,952 bytes
-constexpr uint32_t kThreads = 128;
+constexpr uint32_t kSmemBytes = kOffMisc + 128;      // 230,016 bytes
+constexpr uint32_t kSplit = 4;                       // threads per accumulator row
+constexpr uint32_t kThreads = kRows * kSplit;        // 16 warps
+constexpr uint32_t kChunk = kRadix / kSplit;         // columns (or K groups of 8 x 2) per thread
 constexpr uint32_t kTmemCols = 256;                  // acc0 at column 0, acc1 at 128
 constexpr uint32_t kWaitLimit = 1u << 20;
 static_assert(kSmemBytes <= 232448, "shared memory per CTA");
+static_assert(kRadix * (kCols + 1) * 4 <= 2 * kXBytes, "the output exchange fits the two halves");
 
 __device__ uint32_t g_dft_timeouts;
 
@@ -150,48 +153,44 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// 32 consecutive FP32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-    uint32_t r[32];
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// This thread's TMEM row, columns [c0, c0 + 32): acc0 + acc1 2^-s.
+// This thread's TMEM row, columns [c0, c0 + 16): acc0 + acc1 2^-s.
 template <int P>
-__device__ __forceinline__ void combined32(uint32_t tmem, uint32_t c0, float* v) {
-    float b[32];
-    tmem_ld32(tmem + c0, v);
-    tmem_ld32(tmem + kCols + c0, b);
+__device__ __forceinline__ void combined16(uint32_t tmem, uint32_t c0, float* v) {
+    float b[16];
+    tmem_ld16(tmem + c0, v);
+    tmem_ld16(tmem + kCols + c0, b);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = v[i] + b[i] * Split<P>::kInvLo;
+    for (int i = 0; i < 16; ++i) v[i] = v[i] + b[i] * Split<P>::kInvLo;
 }
 
 // Rows 0-63 of an accumulator hold Re, rows 64-127 Im, of 64 output indices;
 // columns 0-63 belong to the tile's first block, 64-127 to its second. Each
-// half of the CTA finishes one block: threads 0-63 (Re rows) the first,
-// 64-127 (Im rows) the second. So each hands the other half the part it
-// lacks: Re rows put their second-block columns in xa, Im rows their
-// first-block columns in xb.
+// half of the rows finishes one block: Re rows the first, Im rows the second.
+// So each hands the other the part it lacks: Re rows put their second-block
+// columns in xa, Im rows their first-block columns in xb. Row `row`'s
+// threads split the 64 columns in quarters (q).
 template <int P>
-__device__ __forceinline__ void exchange(uint32_t lane_tmem, uint32_t tid, float* xa, float* xb) {
-    const uint32_t i = tid & 63u, other = tid < 64u ? kRadix : 0u;
-    float* x = tid < 64u ? xa : xb;
-    for (uint32_t c = 0; c < kRadix; c += 32) {
-        float v[32];
-        combined32<P>(lane_tmem, other + c, v);
+__device__ __forceinline__ void exchange(uint32_t lane_tmem, uint32_t row, uint32_t q, float* xa, float* xb) {
+    const uint32_t i = row & 63u, other = row < 64u ? kRadix : 0u, c = q * kChunk;
+    float* x = row < 64u ? xa : xb;
+    float v[16];
+    combined16<P>(lane_tmem, other + c, v);
 #pragma unroll
-        for (int k = 0; k < 32; ++k) x[i * kXPitch + c + (uint32_t)k] = v[k];
-    }
+    for (int k = 0; k < 16; ++k) x[i * kXPitch + c + (uint32_t)k] = v[k];
 }
 
 // Both GEMMs of one stage: 8 K-steps of 16 for each of the three products.
@@ -236,8 +235,11 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
     uint64_t* const mbar = reinterpret_cast<uint64_t*>(sm + kOffMisc);  // [0] MMAs, [1] prefetch
     uint32_t* const tmem_slot = reinterpret_cast<uint32_t*>(sm + kOffMisc + 16);
     uint32_t* const abort_flag = reinterpret_cast<uint32_t*>(sm + kOffMisc + 20);
-    float* const block_max = reinterpret_cast<float*>(sm + kOffMisc + 32);  // one per warp
+    float* const block_max = reinterpret_cast<float*>(sm + kOffMisc + 32);  // one per warp (16)
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    // thread = (TMEM row, quarter): warp w reads lanes 32 (w % 4) ..; its
+    // quarter q = w / 4 takes columns (or K groups) [16 q, 16 q + 16)
+    const uint32_t row = tid & (kRows - 1u), q = tid >> 7;
     const uint32_t mbar_mma = smem_addr(mbar), mbar_raw = smem_addr(mbar + 1), raw_addr = smem_addr(raw);
     const uint32_t tiles = (p.block_count + kPair - 1u) / kPair;
     auto valid_in = [&](uint32_t tile) {
@@ -262,16 +264,16 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
     // A = F in real block form, the same for both stages: row r = [Re | Im]
     // of the output index, column k = [Re | Im] of the summed index.
     {
-        const uint32_t r = tid, kr = r & 63u;
-        for (uint32_t j = 0; j < kK / 8; ++j) {
+        const uint32_t kr = row & 63u;
+        for (uint32_t j = 4u * q; j < 4u * q + 4u; ++j) {
             float v[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const uint32_t k = 8u * j + (uint32_t)i, kn = k & 63u;
                 const float2 f = tw[(kRadix * kr * kn) & (kM - 1u)];
-                v[i] = (r < 64u) ? (k < 64u ? f.x : -f.y) : (k < 64u ? f.y : f.x);
+                v[i] = (row < 64u) ? (k < 64u ? f.x : -f.y) : (k < 64u ? f.y : f.x);
             }
-            store_split8<P>(a_hi, a_lo, r, 8u * j, v);
+            store_split8<P>(a_hi, a_lo, row, 8u * j, v);
         }
     }
     fence_async_smem();
@@ -279,13 +281,15 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t lane_tmem = tmem + ((warp * 32u) << 16);  // this warp's 32 lanes
+    const uint32_t lane_tmem = tmem + (((warp & 3u) * 32u) << 16);  // this warp's 32 lanes
+    const bool re_row = row < 64u;
+    const float* const theirs_x = re_row ? xb : xa;
 
     uint32_t parity_mma = 0, parity_raw = 0;
     bool raw_in_flight = blockIdx.x < tiles;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t b0 = tile * kPair, nvalid = valid_in(tile);
-        const uint32_t blk = tid >> 6, i64 = tid & 63u, b = b0 + blk;
+        const uint32_t blk = row >> 6, i64 = row & 63u, b = b0 + blk;
         const bool valid = blk < nvalid;
         const float2* y = raw + blk * kM;
         const uint32_t m_abs = p.block_base + b;
@@ -296,7 +300,7 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         // the block's largest component, for the power-of-two scale
         float mx = 0.0F;
         if (valid)
-            for (uint32_t n1 = 0; n1 < kRadix; ++n1) {
+            for (uint32_t n1 = kChunk * q; n1 < kChunk * q + kChunk; ++n1) {
                 const float2 v = y[(kRadix * n1 + i64 - dm) & (kM - 1u)];
                 mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
             }
@@ -304,7 +308,10 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         if (lane == 0) block_max[warp] = mx;
         __syncthreads();
         if (*abort_flag) break;
-        const float bmax = fmaxf(block_max[blk * 2], block_max[blk * 2 + 1]);
+        float bmax = 0.0F;  // warps whose lanes are this block's rows: (w % 4) / 2 == blk
+#pragma unroll
+        for (uint32_t w = 0; w < kThreads / 32u; ++w)
+            if (((w & 3u) >> 1) == blk) bmax = fmaxf(bmax, block_max[w]);
         int shift = 0;  // scale = 2^shift puts bmax in [2^13, 2^14)
         if (bmax > 0.0F) {
             const int e = (int)((__float_as_uint(bmax) >> 23) & 0xFFu) - 127;
@@ -312,8 +319,9 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
             shift = shift > 100 ? 100 : (shift < -100 ? -100 : shift);
         }
         const float scale_in = ldexpf(1.0F, shift);
-        // B1 row (blk, n2 = i64): K = [Re | Im] of y'[64 n1 + n2], n1 = 0..63
-        for (uint32_t j = 0; j < kRadix / 8; ++j) {
+        // B1 row (blk, n2 = i64): K = [Re | Im] of y'[64 n1 + n2]; this
+        // quarter's n1 = 16 q .. 16 q + 15
+        for (uint32_t j = 2u * q; j < 2u * q + 2u; ++j) {
             float re[8], im[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -322,8 +330,8 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
                 re[k] = v.x * scale_in;
                 im[k] = v.y * scale_in;
             }
-            store_split8<P>(b_hi, b_lo, tid, 8u * j, re);
-            store_split8<P>(b_hi, b_lo, tid, kRadix + 8u * j, im);
+            store_split8<P>(b_hi, b_lo, row, 8u * j, re);
+            store_split8<P>(b_hi, b_lo, row, kRadix + 8u * j, im);
         }
         fence_async_smem();
         __syncthreads();
@@ -342,26 +350,30 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         if (*abort_flag) break;
         fence_after();
         // GEMM 1 out, times 2^-6: Re Z[k1] in rows k1, Im in 64 + k1
-        exchange<P>(lane_tmem, tid, xa, xb);
+        exchange<P>(lane_tmem, row, q, xa, xb);
         __syncthreads();
         // B2 row (blk, k1 = i64): K = [Re | Im] of Z'[k1][n2] = Z[k1][n2] W^(k1 n2)
-        for (uint32_t c = 0; c < kRadix; c += 32) {
-            float own[32];
-            combined32<P>(lane_tmem, blk * kRadix + c, own);
-            for (uint32_t j = 0; j < 32; j += 8) {
+        {
+            const uint32_t c = kChunk * q;
+            float own[16];
+            combined16<P>(lane_tmem, blk * kRadix + c, own);
+#pragma unroll
+            for (uint32_t j = 0; j < 16; j += 8) {
+                float2 w[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) w[k] = tw[(i64 * (c + j + (uint32_t)k)) & (kM - 1u)];
                 float re[8], im[8];
 #pragma unroll
                 for (int k = 0; k < 8; ++k) {
                     const uint32_t n2 = c + j + (uint32_t)k;
                     const float mine = own[j + (uint32_t)k] * (1.0F / 64.0F);
-                    const float theirs = (tid < 64u ? xb : xa)[i64 * kXPitch + n2] * (1.0F / 64.0F);
-                    const float zr = tid < 64u ? mine : theirs, zi = tid < 64u ? theirs : mine;
-                    const float2 w = tw[(i64 * n2) & (kM - 1u)];
-                    re[k] = zr * w.x - zi * w.y;
-                    im[k] = zr * w.y + zi * w.x;
+                    const float theirs = theirs_x[i64 * kXPitch + n2] * (1.0F / 64.0F);
+                    const float zr = re_row ? mine : theirs, zi = re_row ? theirs : mine;
+                    re[k] = zr * w[k].x - zi * w[k].y;
+                    im[k] = zr * w[k].y + zi * w[k].x;
                 }
-                store_split8<P>(b_hi, b_lo, tid, c + j, re);
-                store_split8<P>(b_hi, b_lo, tid, kRadix + c + j, im);
+                store_split8<P>(b_hi, b_lo, row, c + j, re);
+                store_split8<P>(b_hi, b_lo, row, kRadix + c + j, im);
             }
         }
         fence_async_smem();
@@ -374,22 +386,54 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         if (*abort_flag) break;
         fence_after();
         // GEMM 2 out: Re Y[k1 + 64 k2] in rows k2, Im in 64 + k2, columns
-        // (block, k1); times 2^6 2^-shift undoes both scales
-        exchange<P>(lane_tmem, tid, xa, xb);
-        __syncthreads();
-        if (valid) {
-            const float scale_out = ldexpf(64.0F, -shift);
-            const uint32_t slot = m_abs & p.out_ring_mask;
-            for (uint32_t c = 0; c < kRadix; c += 32) {
-                float own[32];
-                combined32<P>(lane_tmem, blk * kRadix + c, own);
+        // (block, k1). The Im rows hand over both blocks' columns; the Re
+        // rows then write each channel's two adjacent ring slots together.
+        {
+            const uint32_t c = kChunk * q;
+            float own0[16], own1[16];
+            combined16<P>(lane_tmem, c, own0);
+            combined16<P>(lane_tmem, kRadix + c, own1);
+            float* const x2 = xa;  // [64][kCols + 1]: both halves of the exchange
+            if (!re_row) {
 #pragma unroll
-                for (uint32_t k = 0; k < 32; ++k) {
+                for (int k = 0; k < 16; ++k) {
+                    x2[i64 * (kCols + 1u) + c + (uint32_t)k] = own0[k];
+                    x2[i64 * (kCols + 1u) + kRadix + c + (uint32_t)k] = own1[k];
+                }
+            }
+            __syncthreads();
+            if (re_row) {
+                // times 2^6 2^-shift undoes both scales, per block
+                float s_out[kPair];
+#pragma unroll
+                for (uint32_t bb = 0; bb < kPair; ++bb) {
+                    float bm = 0.0F;
+#pragma unroll
+                    for (uint32_t w = 0; w < kThreads / 32u; ++w)
+                        if (((w & 3u) >> 1) == bb) bm = fmaxf(bm, block_max[w]);
+                    int sh = 0;
+                    if (bm > 0.0F) {
+                        sh = 13 - ((int)((__float_as_uint(bm) >> 23) & 0xFFu) - 127);
+                        sh = sh > 100 ? 100 : (sh < -100 ? -100 : sh);
+                    }
+                    s_out[bb] = ldexpf(64.0F, -sh);
+                }
+                const uint32_t slot0 = (p.block_base + b0) & p.out_ring_mask;
+                const uint32_t slot1 = (p.block_base + b0 + 1u) & p.out_ring_mask;
+                const bool pair = nvalid == kPair && slot1 == slot0 + 1u && (slot0 & 1u) == 0u &&
+                                  (reinterpret_cast<uintptr_t>(out) & 15u) == 0u;
+#pragma unroll
+                for (uint32_t k = 0; k < 16; ++k) {
                     const uint32_t k1 = c + k;
-                    const float mine = own[k], theirs = (tid < 64u ? xb : xa)[i64 * kXPitch + k1];
-                    const float re = (tid < 64u ? mine : theirs) * scale_out;
-                    const float im = (tid < 64u ? theirs : mine) * scale_out;
-                    out[(uint64_t)(k1 + kRadix * i64) * p.out_ring_blocks + slot] = make_float2(re, im);
+                    const float r0 = own0[k] * s_out[0], i0 = x2[i64 * (kCols + 1u) + k1] * s_out[0];
+                    const float r1 = own1[k] * s_out[1], i1 = x2[i64 * (kCols + 1u) + kRadix + k1] * s_out[1];
+                    float2* const dst = out + (uint64_t)(k1 + kRadix * i64) * p.out_ring_blocks;
+                    if (pair) {
+                        *reinterpret_cast<float4*>(dst + slot0) = make_float4(r0, i0, r1, i1);
+                    } else {
+                        dst[slot0] = make_float2(r0, i0);
+                        if (nvalid == kPair) dst[slot1] = make_float2(r1, i1);
+                    }
                 }
             }
         }
