@@ -20,7 +20,7 @@ same FP64 restatement, to its own stated tolerances:
   * FP16 split: TC_FP16 = (relative RMS 2e-6, spur floor -115 dBc)
   * BF16 split: TC_BF16 = (relative RMS 2e-5, spur floor -105 dBc)
 
-(measured on a GB300: 5.2e-7 / -123.8 dBc and 4.8e-6 / -114.8 dBc, against
+(measured on a GB300: 4.8e-7 / -125.8 dBc and 4.6e-6 / -116.9 dBc, against
 1.6e-7 / -139 dBc for the FP32 FFT).
 """
 import ctypes as C
