@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-detect", action="store_true", help="skip the spectrum + detector measurement")
     ap.add_argument("--no-excision", action="store_true", help="skip the timed run with impulse excision on")
     ap.add_argument("--no-c4", action="store_true", help="skip the M = 4096 channelizer DFT comparison")
+    ap.add_argument("--no-noise", action="store_true", help="skip the scene noise field measurement")
     ap.add_argument("--run-log2", type=int, default=24, help="log2 samples per rv_chain_run")
     return ap.parse_args()
 
@@ -372,6 +373,8 @@ def run_gb300(args):
         line["vs_plain_path"] = round(value / plain["value"], 2)
     if rank == 0 and not args.no_detect:
         line["detection"] = detection(dev, d_codes, min(n, 1 << 26))
+    if rank == 0 and not args.no_noise:
+        line["scene_noise"] = scene_noise(dev, stream, n, max(args.steps, 1))
     if rank == 0 and not args.no_c4:
         line["c4_dft"] = c4_dft(dev, stream, d_codes, n, max(args.steps, 1))
     if rank == 0 and not args.no_cpu:
@@ -424,6 +427,46 @@ def detection(dev, d_codes, samples):
     ch.close()
     det.close()
     return out
+
+
+def scene_noise(dev, stream, n, reps):
+    """a16: the synthesiser's noise field (siggen::Scene::fill_noise) for the
+    capture's 2^n samples on the GPU (CUDA events, `reps` renders), and the
+    oracle's C restatement of the reference's loop on one host core over a
+    2^18-sample sample."""
+    import ctypes as C
+    import torch
+    from revenant_gb300.library import check, lib
+    sigma = lib().rv_scene_noise_sigma(-60.0)
+    out = dev.zeros(n * 8)
+    check(lib().rv_scene_noise(dev.stream, 1, sigma, 0, n, out.address, n))
+    dev.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        check(lib().rv_scene_noise(dev.stream, 1, sigma, 0, n, out.address, n))
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    out.free()
+    res = {"samples": n, "ms": round(ms, 3), "value": round(n / ms / 1e3, 1), "unit": "MS/s",
+           "note": "4096-sample noise blocks, one warp each: MT19937-64 twisted cooperatively in shared memory, "
+                   "FP64 Box-Muller"}
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import build as oracle_build
+        o = C.CDLL(oracle_build.build())
+        o.or_scene_noise.argtypes = [C.c_uint64, C.c_double, C.c_uint64, C.c_uint64, C.c_void_p]
+        m = 1 << 18
+        buf = np.zeros((m, 2), np.float32)
+        t = time.perf_counter()
+        o.or_scene_noise(1, sigma, 0, m, buf.ctypes.data)
+        dt = time.perf_counter() - t
+        res["cpu_oracle"] = {"value": round(m / dt / 1e6, 2), "unit": "MS/s", "cores": 1,
+                             "sample": "2^18 samples, the reference's per-sample loop restated in C"}
+    except Exception as e:  # the oracle is a reported baseline; its absence does not stop the bench
+        res["cpu_oracle"] = {"unavailable": str(e)}
+    return res
 
 
 def c4_dft(dev, stream, d_codes, n, reps):

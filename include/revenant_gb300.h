@@ -1178,6 +1178,26 @@ int32_t rv_display_block(const rv_vrx_display_plan* plan, uint32_t channel_base,
 uint32_t rv_demod_fine_history(const rv_vrx_demod_config* config);
 
 /* ===================================================================== *
+ * Scene noise (core/dsp/synth/wideband.cpp siggen::Scene::fill_noise):   *
+ * the synthesiser's Gaussian noise field, 4096-sample blocks each drawn  *
+ * from its own MT19937-64 seeded from (seed ^ block), two draws per      *
+ * sample, Box-Muller in FP64. The draws equal the reference's bit for    *
+ * bit; a sample can differ from the reference's in its last FP32 bit     *
+ * (CUDA's FP64 log/sin/cos against the C library's).                   *
+ * ===================================================================== */
+
+/* The per-component sigma of a noise floor of `dbfs` over the full band
+ * (wideband.cpp:108-111, :200-203). */
+double rv_scene_noise_sigma(double noise_power_full_band_dbfs);
+/* Samples [start, start + count) of the noise field into out_dev (cf32). */
+int32_t rv_scene_noise(void* stream, uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out_dev,
+                       uint64_t out_len);
+/* The raw draws of the same samples, two per sample (draws_len >= 2 count),
+ * for pinning the generator. */
+int32_t rv_scene_noise_draws(void* stream, uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws_dev,
+                             uint64_t draws_len);
+
+/* ===================================================================== *
  * Capture segments (core/capture/format.h, core/capture/writer.cpp): the  *
  * rolling capture's on-disk SigMF recordings, so a capture replays       *
  * through the chain. Host only.                                          *

@@ -1881,3 +1881,92 @@ int32_t or_comb_subtract(const rv_comb_params* p, const rv_cf32* raw, uint64_t r
     flush_end(&s);
     return ok();
 }
+
+/* ---- scene noise: siggen::Scene::fill_noise ------------------------------
+ * core/dsp/synth/wideband.cpp:535-580 restated: 4096-sample noise blocks,
+ * block b drawing from an MT19937-64 (the C++ standard's mt19937_64, the
+ * published algorithm of Matsumoto and Nishimura) seeded with
+ * derive_stream_seed(seed ^ b, noise domain) (wideband.cpp:46-53), two draws
+ * per sample, Box-Muller in FP64 with the C library's log, sqrt, cos, sin. */
+
+#define OR_NOISE_BLOCK 4096u
+#define OR_MT_N 312u
+#define OR_MT_M 156u
+
+static uint64_t or_derive_stream_seed(uint64_t master, uint64_t domain) {
+    uint64_t z = master + domain * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+typedef struct {
+    uint64_t mt[OR_MT_N];
+    uint32_t index;
+} or_mt64;
+
+static void or_mt64_seed(or_mt64* g, uint64_t seed) {
+    g->mt[0] = seed;
+    for (uint32_t i = 1; i < OR_MT_N; ++i) g->mt[i] = 6364136223846793005ull * (g->mt[i - 1] ^ (g->mt[i - 1] >> 62)) + i;
+    g->index = OR_MT_N;
+}
+
+static uint64_t or_mt64_next(or_mt64* g) {
+    if (g->index >= OR_MT_N) {
+        for (uint32_t i = 0; i < OR_MT_N; ++i) {
+            const uint64_t y = (g->mt[i] & 0xFFFFFFFF80000000ull) | (g->mt[(i + 1) % OR_MT_N] & 0x7FFFFFFFull);
+            g->mt[i] = g->mt[(i + OR_MT_M) % OR_MT_N] ^ (y >> 1) ^ ((y & 1ull) ? 0xB5026F5AA96619E9ull : 0ull);
+        }
+        g->index = 0;
+    }
+    uint64_t y = g->mt[g->index++];
+    y ^= (y >> 29) & 0x5555555555555555ull;
+    y ^= (y << 17) & 0x71D67FFFEDA60000ull;
+    y ^= (y << 37) & 0xFFF7EEE000000000ull;
+    return y ^ (y >> 43);
+}
+
+double or_scene_noise_sigma(double dbfs) { return sqrt(pow(10.0, dbfs * 0.1) * 0.5); }
+
+/* draws (2 per sample) or samples of [start, start + count) */
+static int32_t scene_noise_any(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out,
+                               uint64_t* draws) {
+    const double step = 1.0 / 9007199254740992.0, two_pi = 6.283185307179586476925286766559;
+    const uint64_t end = start + count;
+    uint64_t index = start;
+    or_mt64* g = (or_mt64*)malloc(sizeof(or_mt64));
+    if (g == NULL) return fail("scene noise: out of memory");
+    while (index < end) {
+        const uint64_t block = index / OR_NOISE_BLOCK, block_start = block * OR_NOISE_BLOCK;
+        const uint64_t stop = end < block_start + OR_NOISE_BLOCK ? end : block_start + OR_NOISE_BLOCK;
+        or_mt64_seed(g, or_derive_stream_seed(seed ^ block, 0x1a59017e55ce0d02ull));
+        for (uint64_t skipped = block_start; skipped < index; ++skipped) {
+            (void)or_mt64_next(g);
+            (void)or_mt64_next(g);
+        }
+        for (; index < stop; ++index) {
+            const uint64_t first = or_mt64_next(g), second = or_mt64_next(g);
+            if (draws) {
+                draws[2 * (index - start)] = first;
+                draws[2 * (index - start) + 1] = second;
+                continue;
+            }
+            const double radial = (double)((first >> 11) + 1ull) * step;
+            const double angular = (double)(second >> 11) * step;
+            const double magnitude = sigma * sqrt(-2.0 * log(radial));
+            const double angle = two_pi * angular;
+            out[index - start].re = (float)(magnitude * cos(angle));
+            out[index - start].im = (float)(magnitude * sin(angle));
+        }
+    }
+    free(g);
+    return ok();
+}
+
+int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out) {
+    return scene_noise_any(seed, sigma, start, count, out, NULL);
+}
+
+int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws) {
+    return scene_noise_any(seed, 0.0, start, count, NULL, draws);
+}

@@ -29,6 +29,11 @@
 
 #ifdef __cplusplus
 extern "C" {
+
+/* scene noise field: siggen::Scene::fill_noise (core/dsp/synth/wideband.cpp:535-580) */
+double or_scene_noise_sigma(double dbfs);
+int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out);
+int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
 #endif
 
 const char* or_last_error(void);
@@ -85,6 +90,11 @@ int32_t or_pfb_f64(const rv_grid_params* g, const float* taps, const rv_cf32* ri
 
 #ifdef __cplusplus
 }
+
+/* scene noise field: siggen::Scene::fill_noise (core/dsp/synth/wideband.cpp:535-580) */
+double or_scene_noise_sigma(double dbfs);
+int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out);
+int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
 #endif
 
 
@@ -142,4 +152,9 @@ int32_t or_comb_project(const rv_comb_params* p, const rv_cf32* raw, uint64_t ra
 int32_t or_comb_subtract(const rv_comb_params* p, const rv_cf32* raw, uint64_t raw_len, const rv_comb_line* lines,
                          uint64_t lines_len, const rv_cf32* table, uint64_t table_len, rv_cf32* cleaned,
                          uint64_t cleaned_len, rv_cf32* removed, uint64_t removed_len);
+
+/* scene noise field: siggen::Scene::fill_noise (core/dsp/synth/wideband.cpp:535-580) */
+double or_scene_noise_sigma(double dbfs);
+int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out);
+int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
 #endif

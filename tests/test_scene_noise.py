@@ -1,0 +1,172 @@
+"""a16's noise field: siggen::Scene::fill_noise (core/dsp/synth/wideband.cpp
+:535-580) on the GPU.
+
+The oracle (or_scene_noise, oracle/oracle.c) restates it: 4096-sample noise
+blocks, each an MT19937-64 seeded from derive_stream_seed(seed ^ block), two
+draws per sample, Box-Muller in FP64 with the C library's functions. It is
+pinned against the reference's own Scene (oracle/_ref/libsynref.so) bit for
+bit on this machine, its draws against libstdc++'s std::mt19937_64, and
+against tests/golden/scene_noise.npz (made by tests/golden/make_scene_noise.py)
+everywhere.
+
+On the GPU (rv_scene_noise, rv_scene_noise_draws):
+  * the draws equal the oracle's bit for bit (integers);
+  * the samples equal the oracle's bit for bit except where CUDA's FP64 log,
+    sine or cosine rounds differently from the C library's and that moves the
+    FP32 result: at most MAX_MISMATCH_FRACTION of the samples, each within
+    ULP_TOLERANCE FP32 ulp;
+  * the field is a function of the absolute range: a render in pieces equals
+    the render in one piece, bit for bit, at 2^24 samples.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from bindings import cf32, oracle
+from revenant_gb300.library import lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SYNREF = os.path.join(ROOT, "oracle", "_ref", "libsynref.so")
+GOLDEN = os.path.join(ROOT, "tests", "golden", "scene_noise.npz")
+NOISE_DOMAIN = 0x1A59017E55CE0D02
+MAX_MISMATCH_FRACTION = 1e-4
+ULP_TOLERANCE = 1
+
+
+def derive_stream_seed(master, domain):
+    """wideband.cpp:46-53, restated for the draw pin."""
+    m = (1 << 64) - 1
+    z = (master + domain * 0x9E3779B97F4A7C15) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    return z ^ (z >> 31)
+
+
+def ora_lib():
+    o = oracle().lib
+    o.or_scene_noise_sigma.restype = C.c_double
+    o.or_scene_noise_sigma.argtypes = [C.c_double]
+    o.or_scene_noise.argtypes = [C.c_uint64, C.c_double, C.c_uint64, C.c_uint64, C.c_void_p]
+    o.or_scene_noise_draws.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]
+    return o
+
+
+def ora_noise(seed, sigma, start, count):
+    out = cf32(count)
+    assert ora_lib().or_scene_noise(seed, sigma, start, count, out.ctypes.data) == 0
+    return out
+
+
+def ora_draws(seed, start, count):
+    out = np.zeros(2 * count, np.uint64)
+    assert ora_lib().or_scene_noise_draws(seed, start, count, out.ctypes.data) == 0
+    return out
+
+
+@pytest.fixture(scope="module")
+def synref():
+    if not os.path.exists(SYNREF):
+        pytest.skip("reference synthesiser not built (reference sources absent on this machine)")
+    s = C.CDLL(SYNREF, mode=os.RTLD_LAZY)  # its emitter code paths are never called
+    s.refsyn_noise.argtypes = [C.c_uint64, C.c_int64, C.c_double, C.c_uint64, C.c_uint64, C.c_void_p]
+    s.refsyn_mt64.argtypes = [C.c_uint64, C.c_uint64, C.c_void_p]
+    return s
+
+
+def golden_cases():
+    g = np.load(GOLDEN)
+    for i in range(len([k for k in g.files if k.startswith("case")])):
+        seed, rate, start, count = (int(x) for x in g["params%d" % i])
+        yield seed, rate, float(g["dbfs%d" % i][0]), start, count, g["case%d" % i]
+
+
+@pytest.mark.parametrize("seed,dbfs,start,count", [(1, -60.0, 0, 5000), (0xDEADBEEF, -40.0, 4095, 9000),
+                                                   (5, -75.5, (1 << 31) + 17, 4096), (2, 10.0, 8192, 1)])
+def test_oracle_matches_reference_scene(synref, seed, dbfs, start, count):
+    want = np.zeros((count, 2), np.float32)
+    assert synref.refsyn_noise(seed, 20_000_000, dbfs, start, count, want.ctypes.data) == 0
+    sigma = ora_lib().or_scene_noise_sigma(dbfs)
+    assert lib().rv_scene_noise_sigma(dbfs) == sigma
+    got = ora_noise(seed, sigma, start, count)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_oracle_draws_are_the_standard_mt19937_64(synref):
+    for seed, block in ((7, 0), (7, 3), (2**63 + 5, 1 << 20)):
+        want = np.zeros(8192, np.uint64)
+        synref.refsyn_mt64(derive_stream_seed(seed ^ block, NOISE_DOMAIN), 8192, want.ctypes.data)
+        assert np.array_equal(ora_draws(seed, block * 4096, 4096), want)
+
+
+def test_oracle_matches_golden_fixture():
+    for seed, rate, dbfs, start, count, want in golden_cases():
+        got = ora_noise(seed, ora_lib().or_scene_noise_sigma(dbfs), start, count)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (seed, start)
+
+
+def ulp_distance(a, b):
+    """FP32 ulps between a and b, elementwise (ordered integer view)."""
+    def key(x):
+        i = x.view(np.int32).astype(np.int64)
+        return np.where(i < 0, -(i & 0x7FFFFFFF), i)
+    return np.abs(key(a) - key(b))
+
+
+def check_close(got, want):
+    d = ulp_distance(got.reshape(-1), want.reshape(-1))
+    mismatched = np.count_nonzero(d)
+    assert d.max() <= ULP_TOLERANCE, d.max()
+    assert mismatched <= max(1, MAX_MISMATCH_FRACTION * d.size), mismatched
+    return mismatched
+
+
+@pytest.mark.gpu
+def test_gpu_draws_match_oracle(gpu):
+    for seed, start, count in ((9, 0, 4096), (9, 4000, 10_000), (2**64 - 1, (1 << 33) + 123, 5000)):
+        d = gpu.zeros(2 * count * 8)
+        assert lib().rv_scene_noise_draws(gpu.stream, seed, start, count, d.ptr, 2 * count) == 0, lib().rv_last_error()
+        gpu.synchronize()
+        assert np.array_equal(d.download(np.uint64, (2 * count,)), ora_draws(seed, start, count))
+
+
+@pytest.mark.gpu
+def test_gpu_noise_matches_oracle_and_golden(gpu):
+    cases = [(seed, dbfs, start, count, None) for seed, _, dbfs, start, count, _ in golden_cases()]
+    cases += [(g[0], g[2], g[3], g[4], g[5]) for g in golden_cases()]
+    cases += [(77, -60.0, 123_456, 200_000, None)]
+    for seed, dbfs, start, count, want in cases:
+        sigma = lib().rv_scene_noise_sigma(dbfs)
+        d = gpu.zeros(count * 8)
+        assert lib().rv_scene_noise(gpu.stream, seed, sigma, start, count, d.ptr, count) == 0, lib().rv_last_error()
+        gpu.synchronize()
+        got = d.download(np.float32, (count, 2))
+        n = check_close(got, ora_noise(seed, sigma, start, count) if want is None else want)
+        print("scene noise seed %d, %d samples from %d: %d of %d components off by one FP32 ulp"
+              % (seed, count, start, n, 2 * count))
+
+
+@pytest.mark.gpu
+def test_gpu_noise_is_a_function_of_the_range(gpu):
+    n, seed, sigma = 1 << 24, 11, lib().rv_scene_noise_sigma(-50.0)
+    whole = gpu.zeros(n * 8)
+    assert lib().rv_scene_noise(gpu.stream, seed, sigma, 0, n, whole.ptr, n) == 0
+    parts = gpu.zeros(n * 8)
+    cuts = [0, 1, 4095, 4097, 1_000_001, n // 2, n - 3, n]
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        assert lib().rv_scene_noise(gpu.stream, seed, sigma, a, b - a, parts.address + 8 * a, b - a) == 0
+    gpu.synchronize()
+    x = whole.download(np.float32, (n, 2))
+    assert np.array_equal(x.view(np.uint32), parts.download(np.float32, (n, 2)).view(np.uint32))
+    # and it is the noise it claims to be: zero mean, sigma per component
+    assert abs(float(x.mean())) < 5 * sigma / np.sqrt(2 * n)
+    assert abs(float(x.std()) / sigma - 1.0) < 1e-3
+
+
+def test_entry_points_reject_bad_arguments(rv):
+    one = np.zeros(4, np.float32)
+    assert rv.rv_scene_noise(None, 1, -1.0, 0, 1, one.ctypes.data, 1) == -1
+    assert rv.rv_scene_noise(None, 1, 1.0, 0, 2, one.ctypes.data, 1) == -1
+    assert rv.rv_scene_noise_draws(None, 1, 0, 2, one.ctypes.data, 3) == -1
+    assert rv.rv_scene_noise(None, 1, 1.0, 2**64 - 2, 5, one.ctypes.data, 5) == -1
