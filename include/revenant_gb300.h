@@ -1197,6 +1197,29 @@ int32_t rv_scene_noise(void* stream, uint64_t seed, double sigma, uint64_t start
 int32_t rv_scene_noise_draws(void* stream, uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws_dev,
                              uint64_t draws_len);
 
+/* A tone-modulated emitter of the scene synthesiser (siggen::ModulatorSpec
+ * with no supplied audio; core/dsp/synth/modulators.h). */
+#define RV_EMITTER_AM 1  /* siggen::Modulation::Am */
+#define RV_EMITTER_NFM 2 /* siggen::Modulation::Nfm */
+typedef struct rv_tone_emitter {
+    int32_t modulation;      /* RV_EMITTER_AM or RV_EMITTER_NFM */
+    int32_t reserved;
+    int64_t rate;            /* samples per second */
+    int64_t carrier_offset;  /* Hz from DC */
+    int64_t tone_hz;         /* the modulating tone */
+    int64_t deviation;       /* NFM peak deviation, Hz */
+    double amplitude;        /* peak carrier amplitude */
+    double initial_phase;    /* radians */
+    double modulation_index; /* AM */
+} rv_tone_emitter;
+/* Modulator::accumulate (modulators.cpp:1204-1323): adds `gain` times the
+ * emitter's samples at emitter indices [first, first + count) to
+ * out_dev[0 .. count), as Scene::render_range does for a burst (first = the
+ * range's start less the burst's). Synchronous on `stream` (its host anchor
+ * table is copied first). */
+int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* emitter, uint64_t first, uint64_t count,
+                              double gain, rv_cf32* out_dev, uint64_t out_len);
+
 /* ===================================================================== *
  * Capture segments (core/capture/format.h, core/capture/writer.cpp): the  *
  * rolling capture's on-disk SigMF recordings, so a capture replays       *

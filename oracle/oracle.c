@@ -1970,3 +1970,59 @@ int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t cou
 int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws) {
     return scene_noise_any(seed, 0.0, start, count, NULL, draws);
 }
+
+/* ---- tone emitters: siggen::Modulator::accumulate_am / accumulate_nfm -----
+ * core/dsp/synth/modulators.cpp:1244-1323 restated, with walk_anchored
+ * (:99-122: phasors re-anchored every 1024 emitter samples from exact_phase,
+ * :439-449, and advanced by complex multiply) and Phasor (:58-83). */
+
+static double or_exact_phase(int64_t frequency, int64_t rate, uint64_t index) {
+    int64_t reduced = frequency % rate;
+    if (reduced < 0) reduced += rate;
+    const int64_t position = (int64_t)(index % (uint64_t)rate);
+    const int64_t turns = (reduced * position) % rate;
+    return 6.283185307179586476925286766559 * (double)turns / (double)rate;
+}
+
+int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io) {
+    const double two_pi = 6.283185307179586476925286766559;
+    if (e->modulation != RV_EMITTER_AM && e->modulation != RV_EMITTER_NFM) return fail("emitter: modulation");
+    const double level = gain * e->amplitude;
+    const double cs = two_pi * (double)e->carrier_offset / (double)e->rate;
+    const double ts = two_pi * (double)e->tone_hz / (double)e->rate;
+    const double c_re = cos(cs), c_im = sin(cs), t_re = cos(ts), t_im = sin(ts);
+    const double beta = (double)e->deviation / (double)e->tone_hz;
+    const uint64_t end = first + count;
+    uint64_t index = first;
+    while (index < end) {
+        const uint64_t anchor = index - index % 1024u;
+        const uint64_t stop = end < anchor + 1024u ? end : anchor + 1024u;
+        const double cp = e->initial_phase + or_exact_phase(e->carrier_offset, e->rate, anchor);
+        const double tp = or_exact_phase(e->tone_hz, e->rate, anchor);
+        double cr = cos(cp), ci = sin(cp), tr = cos(tp), ti = sin(tp);
+        for (uint64_t k = anchor; k < stop; ++k) {
+            if (k >= index) {
+                float ar, ai;
+                if (e->modulation == RV_EMITTER_AM) {
+                    const double envelope = level * (1.0 + e->modulation_index * tr);
+                    ar = (float)(envelope * cr);
+                    ai = (float)(envelope * ci);
+                } else {
+                    const double deviation = beta * ti;
+                    const double cosine = cos(deviation), sine = sin(deviation);
+                    const double re = cr * cosine - ci * sine;
+                    const double im = cr * sine + ci * cosine;
+                    ar = (float)(level * re);
+                    ai = (float)(level * im);
+                }
+                io[k - first].re = io[k - first].re + ar;
+                io[k - first].im = io[k - first].im + ai;
+            }
+            const double ncr = cr * c_re - ci * c_im, nci = cr * c_im + ci * c_re;
+            const double ntr = tr * t_re - ti * t_im, nti = tr * t_im + ti * t_re;
+            cr = ncr, ci = nci, tr = ntr, ti = nti;
+        }
+        index = stop;
+    }
+    return ok();
+}

@@ -1,10 +1,12 @@
 // extern "C" access to the reference's scene synthesiser
 // (core/dsp/synth/wideband.cpp siggen::Scene), compiled from the reference
-// sources into oracle/_ref/libsynref.so. Test infrastructure only: the noise
-// tests render noise-only scenes with it and compare the library's GPU noise
-// field against them. Only wideband.cpp is compiled; the modulators it can
-// call for emitters are left unresolved and the library is loaded lazily, so
-// a scene here must have no emitters.
+// sources into oracle/_ref/libsynref.so. Test infrastructure only: the
+// scene tests render noise-only scenes, tone AM and NFM emitters, and scenes
+// of noise plus such emitters with it, and compare the library's GPU noise
+// field and emitters against them. wideband.cpp and modulators.cpp are
+// compiled; what the other modes and the FM stations would call is left
+// unresolved and the library is loaded lazily, so only those emitters may be
+// used here.
 #include <complex>
 #include <cstdint>
 #include <random>
@@ -27,6 +29,67 @@ int refsyn_noise(std::uint64_t seed, std::int64_t rate, double noise_dbfs, std::
     spec.noise_power_full_band_dbfs = noise_dbfs;
     spec.duration_samples = start + count;
     spec.worker_threads = 1;
+    auto scene = siggen::Scene::create(spec);
+    if (!scene) return -1;
+    std::vector<std::complex<float>> buf(count);
+    scene->render(start, std::span<std::complex<float>>(buf));
+    for (std::uint64_t i = 0; i < count; ++i) {
+        out[2 * i] = buf[i].real();
+        out[2 * i + 1] = buf[i].imag();
+    }
+    return 0;
+}
+
+static siggen::ModulatorSpec tone_spec(int kind, std::int64_t rate, std::int64_t carrier, std::int64_t tone,
+                                      std::int64_t deviation, double amplitude, double phase, double index) {
+    siggen::ModulatorSpec spec;
+    spec.kind = kind == 1 ? siggen::Modulation::Am : siggen::Modulation::Nfm;
+    spec.common.rate = rate;
+    spec.common.carrier_offset = carrier;
+    spec.common.amplitude = amplitude;
+    spec.common.initial_phase = phase;
+    spec.am.modulation_index = index;
+    spec.am.tone_hz = tone;
+    spec.nfm.tone_hz = tone;
+    spec.nfm.deviation = deviation;
+    return spec;
+}
+
+// Modulator::accumulate of a tone AM (kind 1) or NFM (kind 2) emitter into
+// `io` (count cf32, added to), emitter indices [first, first + count).
+int refsyn_tone(int kind, std::int64_t rate, std::int64_t carrier, std::int64_t tone, std::int64_t deviation,
+                double amplitude, double phase, double index, std::uint64_t first, std::uint64_t count, double gain,
+                float* io) {
+    auto m = siggen::Modulator::create(tone_spec(kind, rate, carrier, tone, deviation, amplitude, phase, index));
+    if (!m) return -1;
+    std::vector<std::complex<float>> buf(count);
+    for (std::uint64_t i = 0; i < count; ++i) buf[i] = {io[2 * i], io[2 * i + 1]};
+    m->accumulate(first, std::span<std::complex<float>>(buf), gain);
+    for (std::uint64_t i = 0; i < count; ++i) {
+        io[2 * i] = buf[i].real();
+        io[2 * i + 1] = buf[i].imag();
+    }
+    return 0;
+}
+
+// Scene::render of noise plus one tone emitter placed by amplitude (gain 1)
+// over emitter window [on, off).
+int refsyn_scene_tone(std::uint64_t seed, std::int64_t rate, double noise_dbfs, int kind, std::int64_t carrier,
+                      std::int64_t tone, std::int64_t deviation, double amplitude, double phase, double index,
+                      std::uint64_t on, std::uint64_t off, std::uint64_t start, std::uint64_t count, float* out) {
+    siggen::SceneSpec spec;
+    spec.rate = rate;
+    spec.seed = seed;
+    spec.add_noise = true;
+    spec.noise_power_full_band_dbfs = noise_dbfs;
+    spec.duration_samples = start + count;
+    spec.worker_threads = 1;
+    siggen::EmitterPlacement e;
+    e.modulator = tone_spec(kind, rate, carrier, tone, deviation, amplitude, phase, index);
+    e.use_snr = false;
+    e.start_sample = on;
+    e.end_sample = off;
+    spec.emitters.push_back(e);
     auto scene = siggen::Scene::create(spec);
     if (!scene) return -1;
     std::vector<std::complex<float>> buf(count);

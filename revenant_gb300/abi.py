@@ -198,6 +198,12 @@ class CombParams(_S):
 
 
 DFT_FP16, DFT_BF16 = 0, 1
+EMITTER_AM, EMITTER_NFM = 1, 2
+
+
+class ToneEmitter(_S):
+    _fields_ = [("modulation", I32), ("reserved", I32), ("rate", I64), ("carrier_offset", I64), ("tone_hz", I64),
+                ("deviation", I64), ("amplitude", F64), ("initial_phase", F64), ("modulation_index", F64)]
 
 
 class CaptureConfig(_S):
@@ -357,7 +363,7 @@ EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params"
                  "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
                  "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,
                  "rv_excision_plan": ExcisionPlan, "rv_excision_cursor": ExcisionCursor,
-                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_comb_line": CombLine, "rv_capture_config": CaptureConfig,
+                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_comb_line": CombLine, "rv_capture_config": CaptureConfig, "rv_tone_emitter": ToneEmitter,
                  "rv_capture_block": CaptureBlock, "rv_capture_annotation": CaptureAnnotation,
                  "rv_capture_writer_stats": CaptureWriterStats, "rv_capture_segment": CaptureSegment, "rv_comb_params": CombParams, "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
                  "rv_line_config": LineConfig, "rv_line_section": LineSection, "rv_line_params": LineParams,

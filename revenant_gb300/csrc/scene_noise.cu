@@ -20,7 +20,10 @@
 // sample can differ from the reference's in its last FP32 bit where the FP64
 // value sits within an FP64 ulp of an FP32 rounding boundary.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
+
+#include <vector>
 
 #include "common.cuh"
 
@@ -135,10 +138,128 @@ int32_t launch(cudaStream_t s, uint64_t seed, double sigma, uint64_t start, uint
     return cuda_status(cudaGetLastError(), "scene noise");
 }
 
+// ---- tone-modulated emitters: siggen::Modulator::accumulate_am / _nfm ----
+// (core/dsp/synth/modulators.cpp:1244-1323). The carrier and tone are unit
+// phasors advanced by complex multiply and re-anchored every 1024 emitter
+// samples from the exact phase of the anchor index (walk_anchored,
+// modulators.cpp:99-122, so a sample's value does not depend on where a render
+// starts). One thread walks one anchored segment. The anchors' cos/sin and the
+// steps' are computed on the host with the C library, as the reference does,
+// so the recurrence and every sample of AM are the reference's bit for bit;
+// NFM's per-sample cos/sin of the phase deviation are CUDA's.
+
+constexpr uint32_t kAnchorInterval = 1024;  // kPhaseAnchorInterval, modulators.cpp:34
+
+struct Anchor {
+    double cr, ci, tr, ti;  // carrier and tone phasors at an anchor index
+};
+
+struct ToneRun {
+    double level, index, beta;                           // gain x amplitude; AM index; NFM beta
+    double c_step_re, c_step_im, t_step_re, t_step_im;   // per-sample rotations
+    uint64_t first, count, first_anchor;                 // emitter indices; anchor of segment 0
+    int32_t kind;
+};
+
+__global__ void k_tone_emitter(ToneRun r, const Anchor* __restrict__ anchors, uint32_t segments,
+                               float2* __restrict__ out) {
+    const uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seg >= segments) return;
+    const uint64_t anchor = r.first_anchor + (uint64_t)seg * kAnchorInterval;
+    const uint64_t end = r.first + r.count;
+    const uint64_t stop = anchor + kAnchorInterval < end ? anchor + kAnchorInterval : end;
+    const Anchor a = anchors[seg];
+    double cr = a.cr, ci = a.ci, tr = a.tr, ti = a.ti;
+    for (uint64_t index = anchor; index < stop; ++index) {
+        if (index >= r.first) {
+            float2 add;
+            if (r.kind == RV_EMITTER_AM) {
+                const double envelope = r.level * (1.0 + r.index * tr);
+                add = make_float2((float)(envelope * cr), (float)(envelope * ci));
+            } else {
+                const double deviation = r.beta * ti;
+                const double cosine = cos(deviation), sine = sin(deviation);
+                const double re = cr * cosine - ci * sine;
+                const double im = cr * sine + ci * cosine;
+                add = make_float2((float)(r.level * re), (float)(r.level * im));
+            }
+            float2& o = out[index - r.first];
+            o = make_float2(o.x + add.x, o.y + add.y);
+        }
+        const double ncr = cr * r.c_step_re - ci * r.c_step_im, nci = cr * r.c_step_im + ci * r.c_step_re;
+        const double ntr = tr * r.t_step_re - ti * r.t_step_im, nti = tr * r.t_step_im + ti * r.t_step_re;
+        cr = ncr, ci = nci, tr = ntr, ti = nti;
+    }
+}
+
+// modulators.cpp:439-449 exact_phase: the phase of `frequency` at `index`,
+// reduced in integers so it stays exact at any index.
+double exact_phase(int64_t frequency, int64_t rate, uint64_t index) {
+    int64_t reduced = frequency % rate;
+    if (reduced < 0) reduced += rate;
+    const int64_t position = (int64_t)(index % (uint64_t)rate);
+    const int64_t turns = (reduced * position) % rate;
+    return kTwoPi * (double)turns / (double)rate;
+}
+
 }  // namespace
 }  // namespace rv
 
 using namespace rv;
+
+extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e, uint64_t first, uint64_t count,
+                                         double gain, rv_cf32* out, uint64_t out_len) {
+    if (e == nullptr || (out == nullptr && count > 0)) return set_error_fmt(RV_ERR_INVALID, "emitter: NULL argument");
+    if (e->modulation != RV_EMITTER_AM && e->modulation != RV_EMITTER_NFM)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (tone AM or NFM)", e->modulation);
+    // modulators.cpp:310-332 validate_common, :334-343 the tone, :517-546 the mode
+    if (e->rate <= 0 || e->rate > 1000000000) return set_error_fmt(RV_ERR_INVALID, "emitter: rate %lld", (long long)e->rate);
+    if (!isfinite(e->amplitude) || e->amplitude < 0.0 || !isfinite(e->initial_phase))
+        return set_error_fmt(RV_ERR_INVALID, "emitter: amplitude and initial phase must be finite (amplitude >= 0)");
+    if (llabs(e->carrier_offset) * 2 > e->rate) return set_error_fmt(RV_ERR_INVALID, "emitter: carrier past Nyquist");
+    if (e->tone_hz <= 0 || e->tone_hz * 2 >= e->rate) return set_error_fmt(RV_ERR_INVALID, "emitter: tone past Nyquist");
+    if (e->modulation == RV_EMITTER_AM && (!isfinite(e->modulation_index) || e->modulation_index < 0.0))
+        return set_error_fmt(RV_ERR_INVALID, "emitter: AM modulation index must be finite and >= 0");
+    if (e->modulation == RV_EMITTER_NFM && e->deviation <= 0)
+        return set_error_fmt(RV_ERR_INVALID, "emitter: NFM deviation must be positive");
+    if (out_len < count) return set_error_fmt(RV_ERR_INVALID, "emitter: output too short");
+    if (count == 0) return clear_error();
+    if (first + count < first) return set_error_fmt(RV_ERR_INVALID, "emitter: range wraps");
+    ToneRun r{};
+    r.kind = e->modulation;
+    r.level = gain * e->amplitude;
+    r.index = e->modulation_index;
+    r.beta = (double)e->deviation / (double)e->tone_hz;
+    const double c_step = kTwoPi * (double)e->carrier_offset / (double)e->rate;
+    const double t_step = kTwoPi * (double)e->tone_hz / (double)e->rate;
+    r.c_step_re = cos(c_step), r.c_step_im = sin(c_step);
+    r.t_step_re = cos(t_step), r.t_step_im = sin(t_step);
+    r.first = first, r.count = count;
+    r.first_anchor = first - first % kAnchorInterval;
+    const uint64_t segs = (first + count - r.first_anchor + kAnchorInterval - 1) / kAnchorInterval;
+    if (segs > (1u << 30)) return set_error_fmt(RV_ERR_INVALID, "emitter: range too long");
+    std::vector<Anchor> anchors(segs);
+    for (uint64_t k = 0; k < segs; ++k) {
+        const uint64_t a = r.first_anchor + k * kAnchorInterval;
+        const double cp = e->initial_phase + exact_phase(e->carrier_offset, e->rate, a);
+        const double tp = exact_phase(e->tone_hz, e->rate, a);
+        anchors[k] = Anchor{cos(cp), sin(cp), cos(tp), sin(tp)};
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    Anchor* d_anchors = nullptr;
+    if (int32_t st = cuda_status(cudaMallocAsync(&d_anchors, segs * sizeof(Anchor), s), "emitter anchors")) return st;
+    int32_t st = cuda_status(cudaMemcpyAsync(d_anchors, anchors.data(), segs * sizeof(Anchor), cudaMemcpyHostToDevice, s),
+                             "emitter anchors");
+    if (st == RV_OK) {
+        k_tone_emitter<<<(unsigned)((segs + 127) / 128), 128, 0, s>>>(r, d_anchors, (uint32_t)segs,
+                                                                      reinterpret_cast<float2*>(out));
+        st = cuda_status(cudaGetLastError(), "emitter");
+    }
+    cudaFreeAsync(d_anchors, s);
+    // the host table must outlive the copy
+    if (st == RV_OK) st = cuda_status(cudaStreamSynchronize(s), "emitter");
+    return st ? st : clear_error();
+}
 
 extern "C" double rv_scene_noise_sigma(double noise_power_full_band_dbfs) {
     // wideband.cpp:108-111 db_to_power and :200-203: the power split evenly

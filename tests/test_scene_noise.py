@@ -170,3 +170,121 @@ def test_entry_points_reject_bad_arguments(rv):
     assert rv.rv_scene_noise(None, 1, 1.0, 0, 2, one.ctypes.data, 1) == -1
     assert rv.rv_scene_noise_draws(None, 1, 0, 2, one.ctypes.data, 3) == -1
     assert rv.rv_scene_noise(None, 1, 1.0, 2**64 - 2, 5, one.ctypes.data, 5) == -1
+
+
+# ---- tone emitters (Modulator::accumulate_am / _nfm) and scenes of them ----
+
+TONES = [dict(modulation=1, rate=2_400_000, carrier_offset=100_000, tone_hz=1000, deviation=0, amplitude=0.5,
+              initial_phase=0.3, modulation_index=0.8),
+         dict(modulation=2, rate=20_000_000, carrier_offset=-3_000_000, tone_hz=1234, deviation=5000, amplitude=0.25,
+              initial_phase=2.0, modulation_index=0.0),
+         dict(modulation=1, rate=61_440_000, carrier_offset=-30_720_000, tone_hz=30_000, deviation=0, amplitude=1.0,
+              initial_phase=-1.0, modulation_index=1.0),
+         dict(modulation=2, rate=2_400_000, carrier_offset=1_200_000, tone_hz=3000, deviation=75_000, amplitude=1.0,
+              initial_phase=0.0, modulation_index=0.0)]
+
+
+def tone(d):
+    from revenant_gb300 import abi
+    e = abi.ToneEmitter()
+    for k, v in d.items():
+        setattr(e, k, v)
+    return e
+
+
+def ora_tone(d, first, count, gain, io):
+    from revenant_gb300 import abi
+    o = oracle().lib
+    o.or_emitter_accumulate.argtypes = [C.POINTER(abi.ToneEmitter), C.c_uint64, C.c_uint64, C.c_double, C.c_void_p]
+    out = io.copy()
+    assert o.or_emitter_accumulate(C.byref(tone(d)), first, count, gain, out.ctypes.data) == 0
+    return out
+
+
+def ora_scene(seed, dbfs, d, on, off, start, count):
+    """Scene::render_range for noise plus one emitter burst over [on, off)."""
+    out = ora_noise(seed, ora_lib().or_scene_noise_sigma(dbfs), start, count)
+    lo, hi = max(on, start), min(off, start + count)
+    if lo < hi:
+        out[lo - start:hi - start] = ora_tone(d, lo - on, hi - lo, 1.0, out[lo - start:hi - start])
+    return out
+
+
+def ref_args(synref):
+    synref.refsyn_tone.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double,
+                                   C.c_double, C.c_uint64, C.c_uint64, C.c_double, C.c_void_p]
+    synref.refsyn_scene_tone.argtypes = [C.c_uint64, C.c_int64, C.c_double, C.c_int, C.c_int64, C.c_int64, C.c_int64,
+                                         C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_uint64, C.c_uint64,
+                                         C.c_uint64, C.c_void_p]
+    return synref
+
+
+def tone_args(d):
+    return (d["modulation"], d["rate"], d["carrier_offset"], d["tone_hz"], d["deviation"], d["amplitude"],
+            d["initial_phase"], d["modulation_index"])
+
+
+@pytest.mark.parametrize("d", TONES, ids=["am", "nfm", "am-edge", "wide-nfm"])
+def test_oracle_tone_emitter_matches_reference(synref, d):
+    s = ref_args(synref)
+    rng = np.random.default_rng(3)
+    for first, count, gain in ((0, 5000, 1.0), (1023, 3000, 0.37), ((1 << 32) + 77, 2500, 2.5)):
+        io = (1e-3 * rng.standard_normal((count, 2))).astype(np.float32)
+        want = io.copy()
+        assert s.refsyn_tone(*tone_args(d), first, count, gain, want.ctypes.data) == 0
+        got = ora_tone(d, first, count, gain, io)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (first, gain)
+
+
+@pytest.mark.parametrize("d", TONES[:2], ids=["am", "nfm"])
+def test_oracle_scene_with_emitter_matches_reference(synref, d):
+    s = ref_args(synref)
+    seed, dbfs, on, off, start, count = 21, -50.0, 5000, 20_000, 3000, 20_000
+    want = np.zeros((count, 2), np.float32)
+    assert s.refsyn_scene_tone(seed, d["rate"], dbfs, *tone_args(d)[:1], *tone_args(d)[2:], on, off, start, count,
+                               want.ctypes.data) == 0
+    assert np.array_equal(ora_scene(seed, dbfs, d, on, off, start, count).view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("d", TONES, ids=["am", "nfm", "am-edge", "wide-nfm"])
+def test_gpu_tone_emitter_matches_oracle(gpu, d):
+    rng = np.random.default_rng(4)
+    for first, count, gain in ((0, 100_000, 1.0), (1023, 30_000, 0.37), ((1 << 32) + 77, 25_000, 2.5)):
+        io = (1e-3 * rng.standard_normal((count, 2))).astype(np.float32)
+        buf = gpu.array(io)
+        assert lib().rv_emitter_accumulate(gpu.stream, C.byref(tone(d)), first, count, gain, buf.ptr, count) == 0, \
+            lib().rv_last_error()
+        got = buf.download(np.float32, (count, 2))
+        want = ora_tone(d, first, count, gain, io)
+        if d["modulation"] == 1:  # AM: the anchors come from the C library, the rest is + and *
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), first
+        else:  # NFM: CUDA's FP64 cos/sin of the deviation per sample
+            n = check_close(got, want)
+            print("NFM emitter %s, %d samples from %d: %d of %d components off by one FP32 ulp"
+                  % (d["tone_hz"], count, first, n, 2 * count))
+
+
+@pytest.mark.gpu
+def test_gpu_scene_with_emitter_matches_oracle(gpu):
+    """Scene::render of noise plus an AM burst, composed as the scene does:
+    the noise field, then the burst's emitter indices added over its window."""
+    d = TONES[0]
+    seed, dbfs, on, off, start, count = 21, -50.0, 5000, 200_000, 3000, 300_000
+    sigma = lib().rv_scene_noise_sigma(dbfs)
+    buf = gpu.zeros(count * 8)
+    assert lib().rv_scene_noise(gpu.stream, seed, sigma, start, count, buf.ptr, count) == 0
+    lo, hi = max(on, start), min(off, start + count)
+    assert lib().rv_emitter_accumulate(gpu.stream, C.byref(tone(d)), lo - on, hi - lo, 1.0,
+                                       buf.address + 8 * (lo - start), hi - lo) == 0, lib().rv_last_error()
+    got = buf.download(np.float32, (count, 2))
+    check_close(got, ora_scene(seed, dbfs, d, on, off, start, count))
+
+
+def test_emitter_rejects_bad_specs(rv):
+    one = np.zeros(4, np.float32)
+    for bad in (dict(modulation=0), dict(tone_hz=0), dict(tone_hz=1_200_000), dict(carrier_offset=1_300_000),
+                dict(amplitude=-1.0), dict(modulation=2, deviation=0), dict(rate=0)):
+        d = dict(TONES[0])
+        d.update(bad)
+        assert rv.rv_emitter_accumulate(None, C.byref(tone(d)), 0, 1, 1.0, one.ctypes.data, 1) < 0, bad
