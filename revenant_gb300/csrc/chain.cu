@@ -1269,8 +1269,9 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
         return st;
     }
     {
-        const uint32_t nw = (p.demod.channels == 2u && p.demod.pilot_taps != 0u) ? (uint32_t)r.weights.size()
-                                                                                : mono_weight_floats(p.demod.audio_taps);
+        const uint32_t nw = (p.demod.channels == 2u && p.demod.pilot_taps != 0u)
+                                ? stereo_weight_floats(p.demod.audio_taps, p.demod.pilot_taps)
+                                : mono_weight_floats(p.demod.audio_taps);
         c->weights_cap = std::max<uint32_t>(c->weights_cap, (nw + 31u) & ~31u);
     }
     c->rx.push_back(std::move(r));

@@ -393,8 +393,20 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
             sd[e] = rx.det[(start + e) & rx.fine_mask];
         float* ws = sd + window_cap;
         if (rx.channels == 2u) {
-            const uint32_t nw = rx.audio_taps + rx.dc_taps + 2u * rx.pilot_taps + 2u * rx.audio_taps;
-            for (uint32_t e = threadIdx.x; e < nw && e < weights_cap; e += blockDim.x) ws[e] = rx.weights[e];
+            // packed: {w[t], rotation[2t], rotation[2t + 1], 0} per tap, then the pilot pairs
+            const uint32_t Ta = rx.audio_taps, pilot_base = Ta + rx.dc_taps;
+            const uint32_t rotation_base = pilot_base + 2u * rx.pilot_taps;
+            const uint32_t nw = stereo_weight_floats(Ta, rx.pilot_taps);
+            for (uint32_t e = threadIdx.x; e < nw && e < weights_cap; e += blockDim.x) {
+                float v;
+                if (e < 4u * Ta) {
+                    const uint32_t t = e >> 2, c = e & 3u;
+                    v = c == 0u ? rx.weights[t] : c == 3u ? 0.0F : rx.weights[rotation_base + 2u * t + (c - 1u)];
+                } else {
+                    v = rx.weights[pilot_base + (e - 4u * Ta)];
+                }
+                ws[e] = v;
+            }
         } else {
             // the taps, then the four shifted copies (mono_weight_floats)
             const uint32_t Ta = rx.audio_taps, C0 = mono_copy_base(Ta), S = mono_copy_stride(Ta);
@@ -415,14 +427,15 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
             const float* v = sd + rx.reach + i * dec;  // v[-t] = detector at (index - t)
             const float* w = ws;
             if (rx.channels == 2u) {
-                const uint32_t pilot_base = rx.audio_taps + rx.dc_taps;
-                const uint32_t rotation_base = pilot_base + 2u * rx.pilot_taps;
+                const float4* wq = reinterpret_cast<const float4*>(w);
+                const float2* wp = reinterpret_cast<const float2*>(w + 4u * rx.audio_taps);
                 const float* pv = v - (int)(rx.audio_taps / 2u);
                 float pr = 0.0F, pi = 0.0F;
                 for (uint32_t k = 0; k < rx.pilot_taps; ++k) {
                     const float comp = pv[-(int)k];
-                    const float tr = comp * w[pilot_base + 2u * k];
-                    const float ti = comp * w[pilot_base + 2u * k + 1u];
+                    const float2 pw = wp[k];
+                    const float tr = comp * pw.x;
+                    const float ti = comp * pw.y;
                     pr = pr + tr;
                     pi = pi + ti;
                 }
@@ -436,9 +449,10 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
                 const float locked = (power >= 2.0e-5F) ? 1.0F : 0.0F;
                 float sum = 0.0F, diff = 0.0F;
                 for (uint32_t t = 0; t < rx.audio_taps; ++t) {
-                    const float weighted = v[-(int)t] * w[t];
+                    const float4 q = wq[t];
+                    const float weighted = v[-(int)t] * q.x;
                     sum = sum + weighted;
-                    const float ref = sin_two * w[rotation_base + 2u * t] - cos_two * w[rotation_base + 2u * t + 1u];
+                    const float ref = sin_two * q.y - cos_two * q.z;
                     const float term = weighted * ref;
                     diff = diff + term;
                 }

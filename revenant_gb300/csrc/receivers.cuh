@@ -135,6 +135,11 @@ constexpr int kRxThreads = 256;
 // samples every lane reads its weights as aligned four-tap vectors.
 __host__ __device__ inline uint32_t mono_copy_base(uint32_t taps) { return (taps + 31u) & ~31u; }
 __host__ __device__ inline uint32_t mono_copy_stride(uint32_t taps) { return ((taps + 3u + 31u) & ~31u) + 4u; }
+// Stereo weights as the audio kernel stages them: per audio tap one float4
+// {w[t], rotation[2t], rotation[2t + 1], 0}, then the pilot's (re, im) pairs.
+__host__ __device__ inline uint32_t stereo_weight_floats(uint32_t taps, uint32_t pilot_taps) {
+    return 4u * taps + 2u * pilot_taps;
+}
 __host__ __device__ inline uint32_t mono_weight_floats(uint32_t taps) {
     return mono_copy_base(taps) + 4u * mono_copy_stride(taps);
 }
