@@ -254,6 +254,14 @@ __global__ void k_carrier_batched(const RxDev* __restrict__ rxs, const WorkItem*
 
 // ---- detector, once per fine sample ---------------------------------------
 
+// acc = (acc.lo + lo, acc.hi + hi), two rounded adds in one instruction
+__device__ __forceinline__ void add_pair(uint64_t& acc, float lo, float hi) {
+    asm("{\n .reg .b64 t;\n mov.b64 t, {%1, %2};\n add.rn.ftz.f32x2 %0, %0, t;\n}\n" : "+l"(acc) : "f"(lo), "f"(hi));
+}
+__device__ __forceinline__ void unpack_pair(uint64_t acc, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc));
+}
+
 __global__ void __launch_bounds__(kRxThreads)
 k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, uint32_t window_cap, uint32_t* queue,
                  const uint32_t* dyn) {
@@ -302,7 +310,11 @@ k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems,
                 //   step w+3: a_r += v[r-w-3] * wt[w+3]  -> u  z  y  x0
                 // with (n, u, z, y) = v[-w-4 .. -w-1], one aligned 16-byte load,
                 // and the next group's x0..x3 = n, u, z, y.
-                float a0 = 0.0F, a1 = 0.0F, a2 = 0.0F, a3 = 0.0F;
+                // a01 = (a0, a1) and a23 = (a2, a3) are packed pairs: each step
+                // makes its four products with rounded scalar multiplies and
+                // adds them with two rounded packed adds (add.rn.ftz.f32x2,
+                // lane for lane the scalar add), so every output keeps its bits
+                uint64_t a01 = 0, a23 = 0;
                 const float4 first4 = *reinterpret_cast<const float4*>(v);
                 float x0 = first4.x, x1 = first4.y, x2 = first4.z, x3 = first4.w;
                 uint32_t w = 0;
@@ -313,15 +325,18 @@ k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems,
                     const float4 nz = *reinterpret_cast<const float4*>(v - (int)w - 4);
                     const float4 wt = *reinterpret_cast<const float4*>(dws + w);
                     const float y = nz.w, z = nz.z, u = nz.y;
-                    a0 = a0 + x0 * wt.x; a1 = a1 + x1 * wt.x; a2 = a2 + x2 * wt.x; a3 = a3 + x3 * wt.x;
-                    a0 = a0 + y * wt.y; a1 = a1 + x0 * wt.y; a2 = a2 + x1 * wt.y; a3 = a3 + x2 * wt.y;
-                    a0 = a0 + z * wt.z; a1 = a1 + y * wt.z; a2 = a2 + x0 * wt.z; a3 = a3 + x1 * wt.z;
-                    a0 = a0 + u * wt.w; a1 = a1 + z * wt.w; a2 = a2 + y * wt.w; a3 = a3 + x0 * wt.w;
+                    add_pair(a01, x0 * wt.x, x1 * wt.x); add_pair(a23, x2 * wt.x, x3 * wt.x);
+                    add_pair(a01, y * wt.y, x0 * wt.y); add_pair(a23, x1 * wt.y, x2 * wt.y);
+                    add_pair(a01, z * wt.z, y * wt.z); add_pair(a23, x0 * wt.z, x1 * wt.z);
+                    add_pair(a01, u * wt.w, z * wt.w); add_pair(a23, y * wt.w, x0 * wt.w);
                     x3 = y;
                     x2 = z;
                     x1 = u;
                     x0 = nz.x;
                 }
+                float a0, a1, a2, a3;
+                unpack_pair(a01, a0, a1);
+                unpack_pair(a23, a2, a3);
                 for (; w < dc; ++w) {
                     const float wt = dws[w];
                     a0 = a0 + x0 * wt; a1 = a1 + x1 * wt; a2 = a2 + x2 * wt; a3 = a3 + x3 * wt;
