@@ -40,6 +40,13 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+__device__ __forceinline__ void add_pair(uint64_t& acc, float lo, float hi) {
+    asm("{\n .reg .b64 t;\n mov.b64 t, {%1, %2};\n add.rn.ftz.f32x2 %0, %0, t;\n}\n" : "+l"(acc) : "f"(lo), "f"(hi));
+}
+__device__ __forceinline__ void unpack_pair(uint64_t acc, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc));
+}
+
 __device__ __forceinline__ uint32_t next_tile(uint32_t* queue, uint32_t* slot) {
     __syncthreads();
     if (threadIdx.x == 0) *slot = atomicAdd(queue, 1u);
@@ -83,9 +90,12 @@ __device__ __forceinline__ void compute_cols(const float2* tab, const float2* bu
         j[k] = jrow + c;
         act[k] = row < nrows && c < t.width && j[k] >= t.first && j[k] < t.end;
     }
-    float ar[R], ai[R];
+    // (re, im) of each output's sum as one packed pair: the product's two
+    // parts are rounded scalar operations, the two accumulating adds one
+    // add.rn.ftz.f32x2 (lane for lane the scalar add)
+    uint64_t acc[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) ar[k] = ai[k] = 0.0F;
+    for (int k = 0; k < R; ++k) acc[k] = 0;
     // blocks of four taps, every operand loaded before the first multiply;
     // the sums still take q in ascending order
     const float4* tq = reinterpret_cast<const float4*>(tab) + c0;
@@ -108,10 +118,9 @@ __device__ __forceinline__ void compute_cols(const float2* tab, const float2* bu
             const float2 tv[4] = {make_float2(t01[k].x, t01[k].y), make_float2(t01[k].z, t01[k].w),
                                   make_float2(t23[k].x, t23[k].y), make_float2(t23[k].z, t23[k].w)};
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                ar[k] = ar[k] + (sv[u][k].x * tv[u].x - sv[u][k].y * tv[u].y);
-                ai[k] = ai[k] + (sv[u][k].x * tv[u].y + sv[u][k].y * tv[u].x);
-            }
+            for (int u = 0; u < 4; ++u)
+                add_pair(acc[k], sv[u][k].x * tv[u].x - sv[u][k].y * tv[u].y,
+                         sv[u][k].x * tv[u].y + sv[u][k].y * tv[u].x);
         }
     }
 #pragma unroll 1
@@ -121,10 +130,12 @@ __device__ __forceinline__ void compute_cols(const float2* tab, const float2* bu
             const float2 tv = tab[(((q >> 1) * Ap + c0 + (uint32_t)k) << 1) + (q & 1u)];
             const float2 s = sp[k][0];
             sp[k] -= 1;
-            ar[k] = ar[k] + (s.x * tv.x - s.y * tv.y);
-            ai[k] = ai[k] + (s.x * tv.y + s.y * tv.x);
+            add_pair(acc[k], s.x * tv.x - s.y * tv.y, s.x * tv.y + s.y * tv.x);
         }
     }
+    float ar[R], ai[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) unpack_pair(acc[k], ar[k], ai[k]);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (!act[k]) continue;

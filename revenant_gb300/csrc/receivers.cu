@@ -445,15 +445,14 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
                 const float4* wq = reinterpret_cast<const float4*>(w);
                 const float2* wp = reinterpret_cast<const float2*>(w + 4u * rx.audio_taps);
                 const float* pv = v - (int)(rx.audio_taps / 2u);
-                float pr = 0.0F, pi = 0.0F;
+                uint64_t pacc = 0;  // (pr, pi), added as one packed pair
                 for (uint32_t k = 0; k < rx.pilot_taps; ++k) {
                     const float comp = pv[-(int)k];
                     const float2 pw = wp[k];
-                    const float tr = comp * pw.x;
-                    const float ti = comp * pw.y;
-                    pr = pr + tr;
-                    pi = pi + ti;
+                    add_pair(pacc, comp * pw.x, comp * pw.y);
                 }
+                float pr, pi;
+                unpack_pair(pacc, pr, pi);
                 const float sr = pr * rx.gain, si = pi * rx.gain;
                 const float rr = sr * sr, ii = si * si;
                 const float power = rr + ii;
@@ -462,15 +461,15 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
                 const float cos_two = (ii - rr) * inverse;
                 const float sin_two = (-2.0F * cross) * inverse;
                 const float locked = (power >= 2.0e-5F) ? 1.0F : 0.0F;
-                float sum = 0.0F, diff = 0.0F;
+                uint64_t sd_acc = 0;  // (sum, diff), added as one packed pair
                 for (uint32_t t = 0; t < rx.audio_taps; ++t) {
                     const float4 q = wq[t];
                     const float weighted = v[-(int)t] * q.x;
-                    sum = sum + weighted;
                     const float ref = sin_two * q.y - cos_two * q.z;
-                    const float term = weighted * ref;
-                    diff = diff + term;
+                    add_pair(sd_acc, weighted, weighted * ref);
                 }
+                float sum, diff;
+                unpack_pair(sd_acc, sum, diff);
                 const float gated = diff * locked;
                 out[2u * i] = (sum + gated) * rx.gain;
                 out[2u * i + 1u] = (sum - gated) * rx.gain;
