@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-excision", action="store_true", help="skip the timed run with impulse excision on")
     ap.add_argument("--no-c4", action="store_true", help="skip the M = 4096 channelizer DFT comparison")
     ap.add_argument("--no-noise", action="store_true", help="skip the scene noise field measurement")
+    ap.add_argument("--no-c1c2", action="store_true", help="skip the C1 single-receiver and C2 channelizer legs")
     ap.add_argument("--run-log2", type=int, default=24, help="log2 samples per rv_chain_run")
     return ap.parse_args()
 
@@ -373,6 +374,9 @@ def run_gb300(args):
         line["vs_plain_path"] = round(value / plain["value"], 2)
     if rank == 0 and not args.no_detect:
         line["detection"] = detection(dev, d_codes, min(n, 1 << 26))
+    if rank == 0 and not args.no_c1c2:
+        line["c1_chain"] = c1_chain(dev)
+        line["c2_channelizer"] = c2_channelizer(dev, stream, d_codes, max(args.steps, 1), peaks()[0]["hbm_gbs"])
     if rank == 0 and not args.no_noise:
         line["scene_noise"] = scene_noise(dev, stream, n, max(args.steps, 1))
     if rank == 0 and not args.no_c4:
@@ -427,6 +431,113 @@ def detection(dev, d_codes, samples):
     ch.close()
     det.close()
     return out
+
+
+def c1_chain(dev):
+    """C1: the plain single-receiver chain as the reference runs it on the CPU:
+    2^20 cu8 samples at 2.4 MS/s (seed 1), grid M=8 D=4 T=17, one stereo WFM
+    receiver at +200 kHz, fed through rv_chain_run from host memory in
+    16,384-sample blocks (the RTL-SDR's transfer size), launch-bound at this
+    size; per-stage device time from the plain chain's events. Beside it the
+    oracle chain (the reference's twins restated in C) on one host core over
+    the first 2^17 samples."""
+    from bindings import cf32  # noqa: F401  (tests/ on the path for the oracle chain)
+    from oracle_chain import OracleChain
+    from revenant_gb300 import abi
+    from revenant_gb300.chain import Chain
+    n, block, rate, grid = 1 << 20, 1 << 14, 2_400_000, (8, 17, 4)
+    rng = np.random.default_rng(1)
+    t = np.arange(n) / rate
+    phase = 2 * np.pi * 200_000 * t + 75_000 / 1000 * np.sin(2 * np.pi * 1000 * t)
+    z = np.exp(1j * phase) + 10 ** (-25 / 20) * (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+    z *= 0.9 / np.max(np.abs(np.concatenate([z.real, z.imag])))
+    codes = np.empty(2 * n, np.uint8)
+    codes[0::2] = np.clip(np.round(z.real * 127.5 + 127.5), 0, 255)
+    codes[1::2] = np.clip(np.round(z.imag * 127.5 + 127.5), 0, 255)
+    req = abi.request(center=200_000, bandwidth=200_000, demod="wfm", stereo=True)
+    out = {"workload": "2^20 cu8 at 2.4 MS/s (seed 1), M=8 D=4 T=17, one stereo WFM receiver, 16,384-sample "
+                       "blocks from host memory"}
+    for name, mode in (("batched", abi.CHAIN_BATCHED), ("plain", abi.CHAIN_PLAIN)):
+        ch = Chain(dev, grid=grid, rate=rate, fmt=abi.FORMAT_CU8, mode=mode, max_run_samples=block)
+        rid = ch.add_receiver(req)
+        for at in range(0, 8 * block, block):  # warm-up
+            ch.run(codes[2 * at:2 * (at + block)])
+        ch.drain()
+        dev.synchronize()
+        t0 = time.perf_counter()
+        for at in range(8 * block, n, block):
+            ch.run(codes[2 * at:2 * (at + block)])
+        ch.drain()
+        dt = time.perf_counter() - t0
+        frames = ch.audio(rid).size // 2
+        out[name] = {"value": round((n - 8 * block) / dt / 1e6, 2), "unit": "MS/s",
+                     "us_per_block": round(dt / ((n - 8 * block) / block) * 1e6, 1), "audio_frames": int(frames)}
+        ch.close()
+    m = 1 << 17
+    oc = OracleChain(grid, rate, abi.FORMAT_CU8, [req], ring_log2=18, chan_log2=16, fine_log2=17)
+    t0 = time.perf_counter()
+    for at in range(0, m, block):
+        oc.run(codes[2 * at:2 * (at + block)], block)
+    dt = time.perf_counter() - t0
+    out["cpu_oracle"] = {"value": round(m / dt / 1e6, 3), "unit": "MS/s", "cores": 1,
+                         "sample": "the first 2^17 samples, the oracle chain (convert, branch, FFT, fine, WFM "
+                                   "demodulator) in C on one core"}
+    return out
+
+
+def c2_channelizer(dev, stream, d_codes, reps, hbm_gbs):
+    """C2: the M = 1024 (D = 512, T = 16) channelizer over 2^26 cs16 samples
+    (the capture's first 2^26 stand in for C2's 61.44 MS/s scene; the
+    channelizer's time does not depend on the content): convert, branch FIR
+    and FFT dispatches, as the batched chain runs a grid with no fused kernel.
+    Algorithmic bytes 20 per input sample (4 in, 16 out: the 2x-oversampled
+    cf32 channel streams) against the measured HBM bandwidth."""
+    import ctypes as C
+    import torch
+    from revenant_gb300 import abi
+    from revenant_gb300.library import check, lib
+    M, T, D, n = 1024, 16, 512, 1 << 26
+    g = abi.GridParams(M, T, D)
+    taps = np.zeros(M * T, np.float32)
+    check(lib().rv_design_prototype(C.byref(g), 120.0, taps.ctypes.data, taps.size, None, None))
+    tw = np.zeros((M, 2), np.float32)
+    check(lib().rv_build_fft_twiddles(M, tw.ctypes.data, M))
+    d_taps, d_tw = dev.array(taps), dev.array(tw)
+    ring = dev.zeros(n * 8)
+    base = M * T // D
+    blocks = (n - base * D) // D
+    ring_blocks = 1 << (blocks - 1).bit_length()
+    branch = dev.zeros(blocks * M * 8)
+    chan = dev.zeros(M * ring_blocks * 8)
+    cp = abi.ConvertParams(n - 1, 0, 0, n)
+    bp = abi.PfbBranchParams(n - 1, base * D, blocks)
+    fp = abi.PfbFftParams(M, D, 10, base, blocks, ring_blocks, ring_blocks - 1)
+
+    def step():
+        check(lib().rv_convert(dev.stream, abi.FORMAT_CS16, C.byref(cp), d_codes.address, n * 4, ring.address, n))
+        check(lib().rv_pfb_branch(dev.stream, C.byref(g), C.byref(bp), d_taps.address, taps.size, ring.address, n,
+                                  branch.address, blocks * M))
+        check(lib().rv_pfb_fft(dev.stream, C.byref(fp), branch.address, blocks * M, d_tw.address, M, chan.address,
+                               M * ring_blocks))
+
+    step()
+    dev.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    for b in (d_taps, d_tw, ring, branch, chan):
+        b.free()
+    gbs = 20.0 * n / ms / 1e6
+    return {"workload": "M=1024 D=512 T=16 over 2^26 cs16 samples: convert, branch FIR, FFT", "ms": round(ms, 3),
+            "value": round(n / ms / 1e3, 1), "unit": "MS/s", "roofline": {
+                "bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_gbs, "unit": "GB/s",
+                "frac": round(gbs / hbm_gbs, 4), "algorithmic_bytes_per_sample": 20,
+                "note": "the cf32 input ring (8 B/S) and branch outputs (16 B/S written and read) are "
+                        "intermediates in HBM on this path"}}
 
 
 def scene_noise(dev, stream, n, reps):

@@ -128,22 +128,50 @@ __device__ __forceinline__ void shared_fft(float2* x, const rv_cf32* __restrict_
     }
 }
 
+// A CTA transforms the blocks of one pair (2j, 2j + 1), each as the
+// reference does, and writes each channel's two ring slots together: they
+// are adjacent in the channel-major ring, so one 16-byte store replaces two
+// scattered 8-byte ones when the first slot is even (a pair that straddles
+// the ring's wrap, or a lone last block, is stored element by element).
+// `paired` is false when two blocks do not fit in shared memory.
 __global__ void k_pfb_fft(const rv_cf32* __restrict__ branch, const rv_cf32* __restrict__ tw,
-                          rv_cf32* __restrict__ ring, rv_pfb_fft_params p) {
+                          rv_cf32* __restrict__ ring, rv_pfb_fft_params p, bool paired) {
     extern __shared__ float2 x[];
-    const uint32_t M = p.channels;
-    for (uint32_t block = blockIdx.x; block < p.block_count; block += gridDim.x) {
-        const rv_cf32* in = branch + (uint64_t)block * M;
-        for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) x[i] = ld_cf32(&in[brev(i, p.stages)]);
+    const uint32_t M = p.channels, per = paired ? 2u : 1u;
+    const uint32_t groups = (p.block_count + per - 1u) / per;
+    float2* const x1 = x + M;
+    const bool aligned = (reinterpret_cast<uintptr_t>(ring) & 15u) == 0u;
+    for (uint32_t gi = blockIdx.x; gi < groups; gi += gridDim.x) {
+        const uint32_t b0 = gi * per, nb = (p.block_count - b0 < per) ? p.block_count - b0 : per;
+        for (uint32_t h = 0; h < nb; ++h) {
+            const rv_cf32* in = branch + (uint64_t)(b0 + h) * M;
+            float2* xh = h ? x1 : x;
+            for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) xh[i] = ld_cf32(&in[brev(i, p.stages)]);
+        }
         __syncthreads();
         shared_fft(x, tw, M, p.stages);
-        const uint32_t m_abs = p.block_base + block;
-        const uint32_t slot = m_abs & p.out_ring_mask;
-        const uint32_t dm = ((m_abs & (M - 1u)) * p.decimation) & (M - 1u);
+        if (nb == 2u) shared_fft(x1, tw, M, p.stages);
+        const uint32_t m0 = p.block_base + b0, m1 = m0 + 1u;
+        const uint32_t slot0 = m0 & p.out_ring_mask, slot1 = m1 & p.out_ring_mask;
+        const uint32_t dm0 = ((m0 & (M - 1u)) * p.decimation) & (M - 1u);
+        const uint32_t dm1 = ((m1 & (M - 1u)) * p.decimation) & (M - 1u);
+        const bool pair = nb == 2u && aligned && slot1 == slot0 + 1u && (slot0 & 1u) == 0u;
         for (uint32_t k = threadIdx.x; k < M; k += blockDim.x) {
-            float2 v = x[k];
-            if (p.decimation != M) v = cmul(v, ld_cf32(&tw[(k * dm) & (M - 1u)]));
-            st_cf32(&ring[(uint64_t)k * p.out_ring_blocks + slot], v);
+            float2 v0 = x[k];
+            if (p.decimation != M) v0 = cmul(v0, ld_cf32(&tw[(k * dm0) & (M - 1u)]));
+            rv_cf32* row = ring + (uint64_t)k * p.out_ring_blocks;
+            if (nb == 2u) {
+                float2 v1 = x1[k];
+                if (p.decimation != M) v1 = cmul(v1, ld_cf32(&tw[(k * dm1) & (M - 1u)]));
+                if (pair) {
+                    *reinterpret_cast<float4*>(row + slot0) = make_float4(v0.x, v0.y, v1.x, v1.y);
+                } else {
+                    st_cf32(&row[slot0], v0);
+                    st_cf32(&row[slot1], v1);
+                }
+            } else {
+                st_cf32(&row[slot0], v0);
+            }
         }
         __syncthreads();
     }
@@ -509,15 +537,18 @@ int32_t launch_convert(cudaStream_t s, int32_t format, const rv_convert_params& 
 int32_t launch_pfb_fft(cudaStream_t s, const rv_pfb_fft_params& p, const rv_cf32* branch,
                        const rv_cf32* tw, rv_cf32* ring) {
     if (p.block_count == 0) return RV_OK;
-    const size_t shared = (size_t)p.channels * sizeof(float2);
+    const size_t one = (size_t)p.channels * sizeof(float2);
+    const bool paired = 2 * one <= 160 * 1024 && p.block_count > 1;  // two blocks in shared memory
+    const size_t shared = paired ? 2 * one : one;
     if (shared > 48 * 1024) {
         if (int32_t st = cuda_status(cudaFuncSetAttribute(k_pfb_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                           (int)shared), "pfb_fft shared"))
             return st;
     }
     const unsigned threads = p.channels / 2 < 256 ? (p.channels / 2 < 32 ? 32 : p.channels / 2) : 256;
-    const unsigned grid = p.block_count < 152u * 16u ? p.block_count : 152u * 16u;
-    k_pfb_fft<<<grid, threads, shared, s>>>(branch, tw, ring, p);
+    const uint32_t groups = paired ? (p.block_count + 1u) / 2u : p.block_count;
+    const unsigned grid = groups < 152u * 16u ? groups : 152u * 16u;
+    k_pfb_fft<<<grid, threads, shared, s>>>(branch, tw, ring, p, paired);
     return launched("pfb_fft");
 }
 
