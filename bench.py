@@ -457,9 +457,12 @@ def c1_chain(dev):
     req = abi.request(center=200_000, bandwidth=200_000, demod="wfm", stereo=True)
     out = {"workload": "2^20 cu8 at 2.4 MS/s (seed 1), M=8 D=4 T=17, one stereo WFM receiver, 16,384-sample "
                        "blocks from host memory"}
-    for name, mode in (("batched", abi.CHAIN_BATCHED), ("plain", abi.CHAIN_PLAIN)):
-        ch = Chain(dev, grid=grid, rate=rate, fmt=abi.FORMAT_CU8, mode=mode, max_run_samples=block)
+    for name, mode, graph in (("batched_graph_pipelined", abi.CHAIN_BATCHED, True),
+                              ("batched", abi.CHAIN_BATCHED, False), ("plain", abi.CHAIN_PLAIN, False)):
+        ch = Chain(dev, grid=grid, rate=rate, fmt=abi.FORMAT_CU8, mode=mode, max_run_samples=block, pipelined=graph)
         rid = ch.add_receiver(req)
+        if graph:
+            ch.capture_graph()
         for at in range(0, 8 * block, block):  # warm-up
             ch.run(codes[2 * at:2 * (at + block)])
         ch.drain()
