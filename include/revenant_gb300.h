@@ -1201,8 +1201,10 @@ int32_t rv_scene_noise_draws(void* stream, uint64_t seed, uint64_t start, uint64
  * with no supplied audio; core/dsp/synth/modulators.h). */
 #define RV_EMITTER_AM 1  /* siggen::Modulation::Am */
 #define RV_EMITTER_NFM 2 /* siggen::Modulation::Nfm */
+#define RV_EMITTER_USB 3 /* siggen::Modulation::Usb: tone(s) as one exact rotation each */
+#define RV_EMITTER_LSB 4 /* siggen::Modulation::Lsb */
 typedef struct rv_tone_emitter {
-    int32_t modulation;      /* RV_EMITTER_AM or RV_EMITTER_NFM */
+    int32_t modulation;      /* RV_EMITTER_AM, _NFM, _USB or _LSB */
     int32_t reserved;
     int64_t rate;            /* samples per second */
     int64_t carrier_offset;  /* Hz from DC */
@@ -1211,6 +1213,9 @@ typedef struct rv_tone_emitter {
     double amplitude;        /* peak carrier amplitude */
     double initial_phase;    /* radians */
     double modulation_index; /* AM */
+    int64_t tone2_hz;        /* SSB second tone, 0 = one tone */
+    int64_t audio_low_hz;    /* SSB audio passband the tones must sit in */
+    int64_t audio_high_hz;
 } rv_tone_emitter;
 /* Modulator::accumulate (modulators.cpp:1204-1323): adds `gain` times the
  * emitter's samples at emitter indices [first, first + count) to

@@ -1971,8 +1971,8 @@ int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint
     return scene_noise_any(seed, 0.0, start, count, NULL, draws);
 }
 
-/* ---- tone emitters: siggen::Modulator::accumulate_am / accumulate_nfm -----
- * core/dsp/synth/modulators.cpp:1244-1323 restated, with walk_anchored
+/* ---- tone emitters: siggen::Modulator::accumulate_am / _nfm / _ssb -------
+ * core/dsp/synth/modulators.cpp:1244-1366 restated, with walk_anchored
  * (:99-122: phasors re-anchored every 1024 emitter samples from exact_phase,
  * :439-449, and advanced by complex multiply) and Phasor (:58-83). */
 
@@ -1986,10 +1986,18 @@ static double or_exact_phase(int64_t frequency, int64_t rate, uint64_t index) {
 
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io) {
     const double two_pi = 6.283185307179586476925286766559;
-    if (e->modulation != RV_EMITTER_AM && e->modulation != RV_EMITTER_NFM) return fail("emitter: modulation");
-    const double level = gain * e->amplitude;
-    const double cs = two_pi * (double)e->carrier_offset / (double)e->rate;
-    const double ts = two_pi * (double)e->tone_hz / (double)e->rate;
+    if (e->modulation < RV_EMITTER_AM || e->modulation > RV_EMITTER_LSB) return fail("emitter: modulation");
+    /* tone SSB (modulators.cpp:789-803, :1329-1366): one rotation per tone at
+     * carrier +/- tone, both anchored with the initial phase */
+    const int ssb = e->modulation == RV_EMITTER_USB || e->modulation == RV_EMITTER_LSB;
+    const int64_t sense = e->modulation == RV_EMITTER_LSB ? -1 : 1;
+    const int64_t f1 = ssb ? e->carrier_offset + sense * e->tone_hz : e->carrier_offset;
+    const int64_t f2 = ssb ? e->carrier_offset + sense * e->tone2_hz : e->tone_hz;
+    const int two_tone = ssb && e->tone2_hz != 0;
+    double level = gain * e->amplitude;
+    if (two_tone) level = 0.5 * level;
+    const double cs = two_pi * (double)f1 / (double)e->rate;
+    const double ts = two_pi * (double)f2 / (double)e->rate;
     const double c_re = cos(cs), c_im = sin(cs), t_re = cos(ts), t_im = sin(ts);
     const double beta = (double)e->deviation / (double)e->tone_hz;
     const uint64_t end = first + count;
@@ -1997,8 +2005,9 @@ int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t
     while (index < end) {
         const uint64_t anchor = index - index % 1024u;
         const uint64_t stop = end < anchor + 1024u ? end : anchor + 1024u;
-        const double cp = e->initial_phase + or_exact_phase(e->carrier_offset, e->rate, anchor);
-        const double tp = or_exact_phase(e->tone_hz, e->rate, anchor);
+        const double cp = e->initial_phase + or_exact_phase(f1, e->rate, anchor);
+        const double tp = ssb ? e->initial_phase + or_exact_phase(f2, e->rate, anchor)
+                              : or_exact_phase(f2, e->rate, anchor);
         double cr = cos(cp), ci = sin(cp), tr = cos(tp), ti = sin(tp);
         for (uint64_t k = anchor; k < stop; ++k) {
             if (k >= index) {
@@ -2007,6 +2016,14 @@ int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t
                     const double envelope = level * (1.0 + e->modulation_index * tr);
                     ar = (float)(envelope * cr);
                     ai = (float)(envelope * ci);
+                } else if (ssb) {
+                    double re = cr, im = ci;
+                    if (two_tone) {
+                        re += tr;
+                        im += ti;
+                    }
+                    ar = (float)(level * re);
+                    ai = (float)(level * im);
                 } else {
                     const double deviation = beta * ti;
                     const double cosine = cos(deviation), sine = sin(deviation);

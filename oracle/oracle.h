@@ -34,7 +34,7 @@ extern "C" {
 double or_scene_noise_sigma(double dbfs);
 int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out);
 int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
-/* tone emitters: Modulator::accumulate_am / _nfm (core/dsp/synth/modulators.cpp:1244-1323) */
+/* tone emitters: Modulator::accumulate_am / _nfm / _ssb (core/dsp/synth/modulators.cpp:1244-1366) */
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io);
 #endif
 
@@ -97,7 +97,7 @@ int32_t or_pfb_f64(const rv_grid_params* g, const float* taps, const rv_cf32* ri
 double or_scene_noise_sigma(double dbfs);
 int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out);
 int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
-/* tone emitters: Modulator::accumulate_am / _nfm (core/dsp/synth/modulators.cpp:1244-1323) */
+/* tone emitters: Modulator::accumulate_am / _nfm / _ssb (core/dsp/synth/modulators.cpp:1244-1366) */
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io);
 #endif
 
@@ -161,6 +161,6 @@ int32_t or_comb_subtract(const rv_comb_params* p, const rv_cf32* raw, uint64_t r
 double or_scene_noise_sigma(double dbfs);
 int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t count, rv_cf32* out);
 int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
-/* tone emitters: Modulator::accumulate_am / _nfm (core/dsp/synth/modulators.cpp:1244-1323) */
+/* tone emitters: Modulator::accumulate_am / _nfm / _ssb (core/dsp/synth/modulators.cpp:1244-1366) */
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io);
 #endif

@@ -40,10 +40,23 @@ int refsyn_noise(std::uint64_t seed, std::int64_t rate, double noise_dbfs, std::
     return 0;
 }
 
+static std::int64_t g_tone2 = 0, g_low = 300, g_high = 3000;
+
+// The SSB fields of the next tone spec (second tone, audio passband).
+void refsyn_set_ssb(std::int64_t tone2, std::int64_t low, std::int64_t high) {
+    g_tone2 = tone2;
+    g_low = low;
+    g_high = high;
+}
+
 static siggen::ModulatorSpec tone_spec(int kind, std::int64_t rate, std::int64_t carrier, std::int64_t tone,
                                       std::int64_t deviation, double amplitude, double phase, double index) {
     siggen::ModulatorSpec spec;
-    spec.kind = kind == 1 ? siggen::Modulation::Am : siggen::Modulation::Nfm;
+    spec.kind = static_cast<siggen::Modulation>(kind);
+    spec.ssb.tone_hz = tone;
+    spec.ssb.tone2_hz = g_tone2;
+    spec.ssb.audio_low_hz = g_low;
+    spec.ssb.audio_high_hz = g_high;
     spec.common.rate = rate;
     spec.common.carrier_offset = carrier;
     spec.common.amplitude = amplitude;

@@ -138,15 +138,18 @@ int32_t launch(cudaStream_t s, uint64_t seed, double sigma, uint64_t start, uint
     return cuda_status(cudaGetLastError(), "scene noise");
 }
 
-// ---- tone-modulated emitters: siggen::Modulator::accumulate_am / _nfm ----
-// (core/dsp/synth/modulators.cpp:1244-1323). The carrier and tone are unit
+// ---- tone-modulated emitters: siggen::Modulator::accumulate_am / _nfm /
+// _ssb (core/dsp/synth/modulators.cpp:1244-1392). The carrier and tone are unit
 // phasors advanced by complex multiply and re-anchored every 1024 emitter
 // samples from the exact phase of the anchor index (walk_anchored,
 // modulators.cpp:99-122, so a sample's value does not depend on where a render
 // starts). One thread walks one anchored segment. The anchors' cos/sin and the
 // steps' are computed on the host with the C library, as the reference does,
-// so the recurrence and every sample of AM are the reference's bit for bit;
-// NFM's per-sample cos/sin of the phase deviation are CUDA's.
+// so the recurrence and every sample of AM and SSB are the reference's bit for
+// bit; NFM's per-sample cos/sin of the phase deviation are CUDA's. A tone SSB
+// emitter is one rotation per tone at carrier +/- tone (the analytic signal of
+// a cosine, modulators.cpp:789-803); its two phasors take the carrier's and
+// the tone's places here.
 
 constexpr uint32_t kAnchorInterval = 1024;  // kPhaseAnchorInterval, modulators.cpp:34
 
@@ -155,7 +158,8 @@ struct Anchor {
 };
 
 struct ToneRun {
-    double level, index, beta;                           // gain x amplitude; AM index; NFM beta
+    double level, index, beta;                           // gain x amplitude (SSB: its scale); AM index; NFM beta
+    bool two_tone;
     double c_step_re, c_step_im, t_step_re, t_step_im;   // per-sample rotations
     uint64_t first, count, first_anchor;                 // emitter indices; anchor of segment 0
     int32_t kind;
@@ -176,6 +180,13 @@ __global__ void k_tone_emitter(ToneRun r, const Anchor* __restrict__ anchors, ui
             if (r.kind == RV_EMITTER_AM) {
                 const double envelope = r.level * (1.0 + r.index * tr);
                 add = make_float2((float)(envelope * cr), (float)(envelope * ci));
+            } else if (r.kind == RV_EMITTER_USB || r.kind == RV_EMITTER_LSB) {
+                double re = cr, im = ci;
+                if (r.two_tone) {
+                    re += tr;
+                    im += ti;
+                }
+                add = make_float2((float)(r.level * re), (float)(r.level * im));
             } else {
                 const double deviation = r.beta * ti;
                 const double cosine = cos(deviation), sine = sin(deviation);
@@ -210,8 +221,9 @@ using namespace rv;
 extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e, uint64_t first, uint64_t count,
                                          double gain, rv_cf32* out, uint64_t out_len) {
     if (e == nullptr || (out == nullptr && count > 0)) return set_error_fmt(RV_ERR_INVALID, "emitter: NULL argument");
-    if (e->modulation != RV_EMITTER_AM && e->modulation != RV_EMITTER_NFM)
-        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (tone AM or NFM)", e->modulation);
+    if (e->modulation < RV_EMITTER_AM || e->modulation > RV_EMITTER_LSB)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (tone AM, NFM, USB or LSB)", e->modulation);
+    const bool ssb = e->modulation == RV_EMITTER_USB || e->modulation == RV_EMITTER_LSB;
     // modulators.cpp:310-332 validate_common, :334-343 the tone, :517-546 the mode
     if (e->rate <= 0 || e->rate > 1000000000) return set_error_fmt(RV_ERR_INVALID, "emitter: rate %lld", (long long)e->rate);
     if (!isfinite(e->amplitude) || e->amplitude < 0.0 || !isfinite(e->initial_phase))
@@ -222,6 +234,15 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
         return set_error_fmt(RV_ERR_INVALID, "emitter: AM modulation index must be finite and >= 0");
     if (e->modulation == RV_EMITTER_NFM && e->deviation <= 0)
         return set_error_fmt(RV_ERR_INVALID, "emitter: NFM deviation must be positive");
+    if (ssb) {  // modulators.cpp:547-569
+        if (e->audio_low_hz <= 0 || e->audio_high_hz <= e->audio_low_hz)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: SSB audio passband must be a positive increasing range");
+        if (e->tone_hz < e->audio_low_hz || e->tone_hz > e->audio_high_hz)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: SSB tone outside the audio passband");
+        if (e->tone2_hz != 0 && (e->tone2_hz <= 0 || e->tone2_hz * 2 >= e->rate || e->tone2_hz < e->audio_low_hz ||
+                                 e->tone2_hz > e->audio_high_hz))
+            return set_error_fmt(RV_ERR_INVALID, "emitter: SSB second tone outside the audio passband");
+    }
     if (out_len < count) return set_error_fmt(RV_ERR_INVALID, "emitter: output too short");
     if (count == 0) return clear_error();
     if (first + count < first) return set_error_fmt(RV_ERR_INVALID, "emitter: range wraps");
@@ -230,8 +251,15 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
     r.level = gain * e->amplitude;
     r.index = e->modulation_index;
     r.beta = (double)e->deviation / (double)e->tone_hz;
-    const double c_step = kTwoPi * (double)e->carrier_offset / (double)e->rate;
-    const double t_step = kTwoPi * (double)e->tone_hz / (double)e->rate;
+    // the two phasors: carrier and tone, or (SSB) carrier +/- tone 1 and tone 2
+    const int64_t sense = e->modulation == RV_EMITTER_LSB ? -1 : 1;
+    const int64_t f1 = ssb ? e->carrier_offset + sense * e->tone_hz : e->carrier_offset;
+    const int64_t f2 = ssb ? e->carrier_offset + sense * e->tone2_hz : e->tone_hz;
+    const double p2 = ssb ? e->initial_phase : 0.0;
+    r.two_tone = ssb && e->tone2_hz != 0;
+    if (ssb) r.level = r.two_tone ? 0.5 * r.level : r.level;
+    const double c_step = kTwoPi * (double)f1 / (double)e->rate;
+    const double t_step = kTwoPi * (double)f2 / (double)e->rate;
     r.c_step_re = cos(c_step), r.c_step_im = sin(c_step);
     r.t_step_re = cos(t_step), r.t_step_im = sin(t_step);
     r.first = first, r.count = count;
@@ -241,8 +269,8 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
     std::vector<Anchor> anchors(segs);
     for (uint64_t k = 0; k < segs; ++k) {
         const uint64_t a = r.first_anchor + k * kAnchorInterval;
-        const double cp = e->initial_phase + exact_phase(e->carrier_offset, e->rate, a);
-        const double tp = exact_phase(e->tone_hz, e->rate, a);
+        const double cp = e->initial_phase + exact_phase(f1, e->rate, a);
+        const double tp = p2 + exact_phase(f2, e->rate, a);
         anchors[k] = Anchor{cos(cp), sin(cp), cos(tp), sin(tp)};
     }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

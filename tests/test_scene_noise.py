@@ -181,7 +181,12 @@ TONES = [dict(modulation=1, rate=2_400_000, carrier_offset=100_000, tone_hz=1000
          dict(modulation=1, rate=61_440_000, carrier_offset=-30_720_000, tone_hz=30_000, deviation=0, amplitude=1.0,
               initial_phase=-1.0, modulation_index=1.0),
          dict(modulation=2, rate=2_400_000, carrier_offset=1_200_000, tone_hz=3000, deviation=75_000, amplitude=1.0,
-              initial_phase=0.0, modulation_index=0.0)]
+              initial_phase=0.0, modulation_index=0.0),
+         dict(modulation=3, rate=20_000_000, carrier_offset=7_500_000, tone_hz=1000, deviation=0, amplitude=0.5,
+              initial_phase=0.7, modulation_index=0.0, tone2_hz=0, audio_low_hz=300, audio_high_hz=3000),
+         dict(modulation=4, rate=2_400_000, carrier_offset=-100_000, tone_hz=700, deviation=0, amplitude=1.0,
+              initial_phase=-2.5, modulation_index=0.0, tone2_hz=1900, audio_low_hz=300, audio_high_hz=3000)]
+TONE_IDS = ["am", "nfm", "am-edge", "wide-nfm", "usb", "lsb-two-tone"]
 
 
 def tone(d):
@@ -210,7 +215,10 @@ def ora_scene(seed, dbfs, d, on, off, start, count):
     return out
 
 
-def ref_args(synref):
+def ref_args(synref, d=None):
+    synref.refsyn_set_ssb.argtypes = [C.c_int64, C.c_int64, C.c_int64]
+    if d is not None:
+        synref.refsyn_set_ssb(d.get("tone2_hz", 0), d.get("audio_low_hz", 300), d.get("audio_high_hz", 3000))
     synref.refsyn_tone.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double,
                                    C.c_double, C.c_uint64, C.c_uint64, C.c_double, C.c_void_p]
     synref.refsyn_scene_tone.argtypes = [C.c_uint64, C.c_int64, C.c_double, C.c_int, C.c_int64, C.c_int64, C.c_int64,
@@ -224,9 +232,9 @@ def tone_args(d):
             d["initial_phase"], d["modulation_index"])
 
 
-@pytest.mark.parametrize("d", TONES, ids=["am", "nfm", "am-edge", "wide-nfm"])
+@pytest.mark.parametrize("d", TONES, ids=TONE_IDS)
 def test_oracle_tone_emitter_matches_reference(synref, d):
-    s = ref_args(synref)
+    s = ref_args(synref, d)
     rng = np.random.default_rng(3)
     for first, count, gain in ((0, 5000, 1.0), (1023, 3000, 0.37), ((1 << 32) + 77, 2500, 2.5)):
         io = (1e-3 * rng.standard_normal((count, 2))).astype(np.float32)
@@ -236,9 +244,9 @@ def test_oracle_tone_emitter_matches_reference(synref, d):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (first, gain)
 
 
-@pytest.mark.parametrize("d", TONES[:2], ids=["am", "nfm"])
+@pytest.mark.parametrize("d", [TONES[0], TONES[1], TONES[5]], ids=["am", "nfm", "lsb-two-tone"])
 def test_oracle_scene_with_emitter_matches_reference(synref, d):
-    s = ref_args(synref)
+    s = ref_args(synref, d)
     seed, dbfs, on, off, start, count = 21, -50.0, 5000, 20_000, 3000, 20_000
     want = np.zeros((count, 2), np.float32)
     assert s.refsyn_scene_tone(seed, d["rate"], dbfs, *tone_args(d)[:1], *tone_args(d)[2:], on, off, start, count,
@@ -247,7 +255,7 @@ def test_oracle_scene_with_emitter_matches_reference(synref, d):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("d", TONES, ids=["am", "nfm", "am-edge", "wide-nfm"])
+@pytest.mark.parametrize("d", TONES, ids=TONE_IDS)
 def test_gpu_tone_emitter_matches_oracle(gpu, d):
     rng = np.random.default_rng(4)
     for first, count, gain in ((0, 100_000, 1.0), (1023, 30_000, 0.37), ((1 << 32) + 77, 25_000, 2.5)):
@@ -257,7 +265,7 @@ def test_gpu_tone_emitter_matches_oracle(gpu, d):
             lib().rv_last_error()
         got = buf.download(np.float32, (count, 2))
         want = ora_tone(d, first, count, gain, io)
-        if d["modulation"] == 1:  # AM: the anchors come from the C library, the rest is + and *
+        if d["modulation"] != 2:  # AM, SSB: the anchors come from the C library, the rest is + and *
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), first
         else:  # NFM: CUDA's FP64 cos/sin of the deviation per sample
             n = check_close(got, want)
@@ -284,7 +292,10 @@ def test_gpu_scene_with_emitter_matches_oracle(gpu):
 def test_emitter_rejects_bad_specs(rv):
     one = np.zeros(4, np.float32)
     for bad in (dict(modulation=0), dict(tone_hz=0), dict(tone_hz=1_200_000), dict(carrier_offset=1_300_000),
-                dict(amplitude=-1.0), dict(modulation=2, deviation=0), dict(rate=0)):
+                dict(amplitude=-1.0), dict(modulation=2, deviation=0), dict(rate=0), dict(modulation=5),
+                dict(modulation=3, audio_low_hz=300, audio_high_hz=3000, tone_hz=200),
+                dict(modulation=4, audio_low_hz=3000, audio_high_hz=300),
+                dict(modulation=3, audio_low_hz=300, audio_high_hz=3000, tone2_hz=5000)):
         d = dict(TONES[0])
         d.update(bad)
         assert rv.rv_emitter_accumulate(None, C.byref(tone(d)), 0, 1, 1.0, one.ctypes.data, 1) < 0, bad
