@@ -1199,12 +1199,13 @@ int32_t rv_scene_noise_draws(void* stream, uint64_t seed, uint64_t start, uint64
 
 /* A tone-modulated emitter of the scene synthesiser (siggen::ModulatorSpec
  * with no supplied audio; core/dsp/synth/modulators.h). */
+#define RV_EMITTER_CW 0  /* siggen::Modulation::Cw: the text keyed in Morse */
 #define RV_EMITTER_AM 1  /* siggen::Modulation::Am */
 #define RV_EMITTER_NFM 2 /* siggen::Modulation::Nfm */
 #define RV_EMITTER_USB 3 /* siggen::Modulation::Usb: tone(s) as one exact rotation each */
 #define RV_EMITTER_LSB 4 /* siggen::Modulation::Lsb */
 typedef struct rv_tone_emitter {
-    int32_t modulation;      /* RV_EMITTER_AM, _NFM, _USB or _LSB */
+    int32_t modulation;      /* RV_EMITTER_CW, _AM, _NFM, _USB or _LSB */
     int32_t reserved;
     int64_t rate;            /* samples per second */
     int64_t carrier_offset;  /* Hz from DC */
@@ -1216,6 +1217,10 @@ typedef struct rv_tone_emitter {
     int64_t tone2_hz;        /* SSB second tone, 0 = one tone */
     int64_t audio_low_hz;    /* SSB audio passband the tones must sit in */
     int64_t audio_high_hz;
+    double words_per_minute; /* CW (PARIS timing: a dot is 1.2 / WPM seconds) */
+    double rise_fall_ms;     /* CW raised-cosine edges */
+    double message_gap_dots; /* CW silence after the message */
+    char text[64];           /* CW message, NUL-terminated */
 } rv_tone_emitter;
 /* Modulator::accumulate (modulators.cpp:1204-1323): adds `gain` times the
  * emitter's samples at emitter indices [first, first + count) to

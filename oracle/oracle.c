@@ -1984,9 +1984,104 @@ static double or_exact_phase(int64_t frequency, int64_t rate, uint64_t index) {
     return 6.283185307179586476925286766559 * (double)turns / (double)rate;
 }
 
+/* CW: Morse (ITU-R M.1677, the reference's character set) and the keyed
+ * elements of one message cycle (modulators.cpp:124-161, :675-741). */
+static const char* or_morse(char c) {
+    static const char* const letters[26] = {".-", "-...", "-.-.", "-..", ".", "..-.", "--.", "....", "..", ".---",
+                                            "-.-", ".-..", "--", "-.", "---", ".--.", "--.-", ".-.", "...", "-",
+                                            "..-", "...-", ".--", "-..-", "-.--", "--.."};
+    static const char* const digits[10] = {"-----", ".----", "..---", "...--", "....-",
+                                           ".....", "-....", "--...", "---..", "----."};
+    if (c >= 'a' && c <= 'z') c = (char)(c - 'a' + 'A');
+    if (c >= 'A' && c <= 'Z') return letters[c - 'A'];
+    if (c >= '0' && c <= '9') return digits[c - '0'];
+    switch (c) {
+        case '.': return ".-.-.-";
+        case ',': return "--..--";
+        case '?': return "..--..";
+        case '/': return "-..-.";
+        case '=': return "-...-";
+        case '+': return ".-.-.";
+        case '-': return "-....-";
+        case ':': return "---...";
+        default: return NULL;
+    }
+}
+
+typedef struct {
+    int64_t start, stop;
+    int keyed;
+} or_cw_element;
+
+static uint32_t or_cw_elements(const char* text, double dot, double gap, or_cw_element* out, uint32_t cap) {
+    int on[1024];
+    double dots[1024];
+    uint32_t n = 0;
+#define OFF(d)                                           \
+    do {                                                 \
+        const double dd = (d);                           \
+        if (dd > 0.0) {                                  \
+            if (n > 0 && !on[n - 1]) dots[n - 1] += dd;  \
+            else if (n < 1024) on[n] = 0, dots[n++] = dd; \
+        }                                                \
+    } while (0)
+    for (const char* c = text; *c; ++c) {
+        if (*c == ' ') {
+            OFF(4.0);
+            continue;
+        }
+        for (const char* m = or_morse(*c); *m; ++m) {
+            if (n < 1024) on[n] = 1, dots[n++] = (*m == '.') ? 1.0 : 3.0;
+            OFF(1.0);
+        }
+        OFF(2.0);
+    }
+    OFF(gap - 3.0 > 0.0 ? gap - 3.0 : 0.0);
+#undef OFF
+    double cumulative = 0.0;
+    int64_t previous = 0;
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < n && k < cap; ++i) {
+        cumulative += dots[i];
+        int64_t edge = (int64_t)llround(cumulative * dot);
+        if (edge <= previous) edge = previous + 1;
+        out[k].start = previous;
+        out[k].stop = edge;
+        out[k].keyed = on[i];
+        ++k;
+        previous = edge;
+    }
+    return k;
+}
+
+static double or_cw_envelope(const or_cw_element* el, uint32_t n, double ramp_samples, uint64_t index) {
+    const double pi = 3.141592653589793238462643383279502884;
+    const int64_t position = (int64_t)(index % (uint64_t)el[n - 1].stop);
+    uint32_t i = 0;
+    while (i + 1 < n && el[i].stop <= position) ++i;
+    if (!el[i].keyed) return 0.0;
+    const double length = (double)(el[i].stop - el[i].start);
+    const double ramp = ramp_samples < length * 0.5 ? ramp_samples : length * 0.5;
+    if (ramp <= 0.0) return 1.0;
+    const double from_start = (double)(position - el[i].start), to_end = (double)(el[i].stop - position);
+    double envelope = 1.0;
+    if (from_start < ramp) envelope *= 0.5 - 0.5 * cos(pi * from_start / ramp);
+    if (to_end <= ramp) envelope *= 0.5 - 0.5 * cos(pi * to_end / ramp);
+    return envelope;
+}
+
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io) {
     const double two_pi = 6.283185307179586476925286766559;
-    if (e->modulation < RV_EMITTER_AM || e->modulation > RV_EMITTER_LSB) return fail("emitter: modulation");
+    if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_LSB) return fail("emitter: modulation");
+    or_cw_element* elements = NULL;
+    uint32_t nel = 0;
+    const int cw = e->modulation == RV_EMITTER_CW;
+    if (cw) {
+        elements = (or_cw_element*)malloc(1024 * sizeof(or_cw_element));
+        if (elements == NULL) return fail("emitter: out of memory");
+        nel = or_cw_elements(e->text, 1.2 * (double)e->rate / e->words_per_minute, e->message_gap_dots, elements,
+                             1024);
+    }
     /* tone SSB (modulators.cpp:789-803, :1329-1366): one rotation per tone at
      * carrier +/- tone, both anchored with the initial phase */
     const int ssb = e->modulation == RV_EMITTER_USB || e->modulation == RV_EMITTER_LSB;
@@ -2012,7 +2107,12 @@ int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t
         for (uint64_t k = anchor; k < stop; ++k) {
             if (k >= index) {
                 float ar, ai;
-                if (e->modulation == RV_EMITTER_AM) {
+                if (cw) {
+                    const double envelope =
+                        level * or_cw_envelope(elements, nel, e->rise_fall_ms * 0.001 * (double)e->rate, k);
+                    ar = (float)(envelope * cr);
+                    ai = (float)(envelope * ci);
+                } else if (e->modulation == RV_EMITTER_AM) {
                     const double envelope = level * (1.0 + e->modulation_index * tr);
                     ar = (float)(envelope * cr);
                     ai = (float)(envelope * ci);
@@ -2041,5 +2141,6 @@ int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t
         }
         index = stop;
     }
+    free(elements);
     return ok();
 }

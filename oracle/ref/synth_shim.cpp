@@ -8,6 +8,7 @@
 // unresolved and the library is loaded lazily, so only those emitters may be
 // used here.
 #include <complex>
+#include <cstdio>
 #include <cstdint>
 #include <random>
 #include <span>
@@ -42,6 +43,17 @@ int refsyn_noise(std::uint64_t seed, std::int64_t rate, double noise_dbfs, std::
 
 static std::int64_t g_tone2 = 0, g_low = 300, g_high = 3000;
 
+static double g_wpm = 20.0, g_rise = 5.0, g_gap = 7.0;
+static char g_text[64] = "CQ DE REVENANT";
+
+// The CW fields of the next spec.
+void refsyn_set_cw(double wpm, double rise_ms, double gap_dots, const char* text) {
+    g_wpm = wpm;
+    g_rise = rise_ms;
+    g_gap = gap_dots;
+    std::snprintf(g_text, sizeof g_text, "%s", text);
+}
+
 // The SSB fields of the next tone spec (second tone, audio passband).
 void refsyn_set_ssb(std::int64_t tone2, std::int64_t low, std::int64_t high) {
     g_tone2 = tone2;
@@ -57,6 +69,10 @@ static siggen::ModulatorSpec tone_spec(int kind, std::int64_t rate, std::int64_t
     spec.ssb.tone2_hz = g_tone2;
     spec.ssb.audio_low_hz = g_low;
     spec.ssb.audio_high_hz = g_high;
+    spec.cw.words_per_minute = g_wpm;
+    spec.cw.rise_fall_ms = g_rise;
+    spec.cw.message_gap_dots = g_gap;
+    spec.cw.text = g_text;
     spec.common.rate = rate;
     spec.common.carrier_offset = carrier;
     spec.common.amplitude = amplitude;

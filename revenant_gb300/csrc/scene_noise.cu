@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <vector>
 
@@ -213,6 +214,119 @@ double exact_phase(int64_t frequency, int64_t rate, uint64_t index) {
     return kTwoPi * (double)turns / (double)rate;
 }
 
+// International Morse code (ITU-R M.1677): the letters, digits and the
+// punctuation the reference keys (modulators.cpp:124-145), upper case.
+struct MorseCode {
+    char character;
+    const char* code;
+};
+constexpr MorseCode kMorse[] = {
+    {'A', ".-"},    {'B', "-..."},  {'C', "-.-."},  {'D', "-.."},   {'E', "."},      {'F', "..-."},
+    {'G', "--."},   {'H', "...."},  {'I', ".."},    {'J', ".---"},  {'K', "-.-"},    {'L', ".-.."},
+    {'M', "--"},    {'N', "-."},    {'O', "---"},   {'P', ".--."},  {'Q', "--.-"},   {'R', ".-."},
+    {'S', "..."},   {'T', "-"},     {'U', "..-"},   {'V', "...-"},  {'W', ".--"},    {'X', "-..-"},
+    {'Y', "-.--"},  {'Z', "--.."},  {'0', "-----"}, {'1', ".----"}, {'2', "..---"},  {'3', "...--"},
+    {'4', "....-"}, {'5', "....."}, {'6', "-...."}, {'7', "--..."}, {'8', "---.."},  {'9', "----."},
+    {'.', ".-.-.-"}, {',', "--..--"}, {'?', "..--.."}, {'/', "-..-."}, {'=', "-...-"}, {'+', ".-.-."},
+    {'-', "-....-"}, {':', "---..."},
+};
+
+const char* morse(char c) {
+    const char upper = (c >= 'a' && c <= 'z') ? (char)(c - 'a' + 'A') : c;  // no locale
+    for (const MorseCode& m : kMorse)
+        if (m.character == upper) return m.code;
+    return nullptr;
+}
+
+struct CwElement {
+    int64_t start, stop;
+    int32_t keyed, pad;
+};
+
+// The keyed message as elements of [start, stop) samples within one cycle
+// (modulators.cpp:675-741): runs in dot units (a dot on, a dash three; one dot
+// between elements, three between characters, seven between words, then the
+// message gap), their cumulative edges rounded to samples, each edge at least
+// one sample past the last.
+std::vector<CwElement> cw_elements(const char* text, double dot_samples, double gap_dots) {
+    std::vector<std::pair<bool, double>> runs;
+    auto add_off = [&runs](double dots) {
+        if (dots <= 0.0) return;
+        if (!runs.empty() && !runs.back().first) runs.back().second += dots;
+        else runs.emplace_back(false, dots);
+    };
+    for (const char* c = text; *c != '\0'; ++c) {
+        if (*c == ' ') {
+            add_off(4.0);
+            continue;
+        }
+        for (const char* e = morse(*c); *e != '\0'; ++e) {
+            runs.emplace_back(true, *e == '.' ? 1.0 : 3.0);
+            add_off(1.0);
+        }
+        add_off(2.0);
+    }
+    add_off(gap_dots - 3.0 > 0.0 ? gap_dots - 3.0 : 0.0);
+    std::vector<CwElement> out;
+    double cumulative = 0.0;
+    int64_t previous = 0;
+    for (const auto& run : runs) {
+        cumulative += run.second;
+        int64_t edge = (int64_t)llround(cumulative * dot_samples);
+        if (edge <= previous) edge = previous + 1;
+        out.push_back(CwElement{previous, edge, run.first ? 1 : 0, 0});
+        previous = edge;
+    }
+    return out;
+}
+
+// One anchored segment of a CW emitter: the carrier phasor as for the other
+// modes, keyed by the element holding index % cycle, with raised-cosine edges
+// of `ramp` samples (modulators.cpp:1055-1090, cos(pi t / ramp) on the device).
+__global__ void k_cw_emitter(ToneRun r, const Anchor* __restrict__ anchors, uint32_t segments,
+                             const CwElement* __restrict__ el, uint32_t nel, double ramp_samples,
+                             float2* __restrict__ out) {
+    const uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seg >= segments) return;
+    const uint64_t anchor = r.first_anchor + (uint64_t)seg * kAnchorInterval;
+    const uint64_t end = r.first + r.count;
+    const uint64_t stop = anchor + kAnchorInterval < end ? anchor + kAnchorInterval : end;
+    const Anchor a = anchors[seg];
+    double cr = a.cr, ci = a.ci;
+    const int64_t cycle = el[nel - 1].stop;
+    const double pi = 3.141592653589793238462643383279502884;
+    for (uint64_t index = anchor; index < stop; ++index) {
+        if (index >= r.first) {
+            const int64_t position = (int64_t)(index % (uint64_t)cycle);
+            uint32_t lo = 0, hi = nel - 1;  // the element with start <= position < stop
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (el[mid].stop <= position) lo = mid + 1;
+                else hi = mid;
+            }
+            double envelope = 0.0;
+            const CwElement e = el[lo];
+            if (e.keyed) {
+                const double length = (double)(e.stop - e.start);
+                const double ramp = ramp_samples < length * 0.5 ? ramp_samples : length * 0.5;
+                if (ramp <= 0.0) {
+                    envelope = 1.0;
+                } else {
+                    const double from_start = (double)(position - e.start), to_end = (double)(e.stop - position);
+                    envelope = 1.0;
+                    if (from_start < ramp) envelope *= 0.5 - 0.5 * cos(pi * from_start / ramp);
+                    if (to_end <= ramp) envelope *= 0.5 - 0.5 * cos(pi * to_end / ramp);
+                }
+            }
+            const double level = r.level * envelope;
+            float2& o = out[index - r.first];
+            o = make_float2(o.x + (float)(level * cr), o.y + (float)(level * ci));
+        }
+        const double ncr = cr * r.c_step_re - ci * r.c_step_im, nci = cr * r.c_step_im + ci * r.c_step_re;
+        cr = ncr, ci = nci;
+    }
+}
+
 }  // namespace
 }  // namespace rv
 
@@ -221,15 +335,34 @@ using namespace rv;
 extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e, uint64_t first, uint64_t count,
                                          double gain, rv_cf32* out, uint64_t out_len) {
     if (e == nullptr || (out == nullptr && count > 0)) return set_error_fmt(RV_ERR_INVALID, "emitter: NULL argument");
-    if (e->modulation < RV_EMITTER_AM || e->modulation > RV_EMITTER_LSB)
-        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (tone AM, NFM, USB or LSB)", e->modulation);
+    if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_LSB)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (CW, or tone AM, NFM, USB, LSB)",
+                             e->modulation);
     const bool ssb = e->modulation == RV_EMITTER_USB || e->modulation == RV_EMITTER_LSB;
     // modulators.cpp:310-332 validate_common, :334-343 the tone, :517-546 the mode
     if (e->rate <= 0 || e->rate > 1000000000) return set_error_fmt(RV_ERR_INVALID, "emitter: rate %lld", (long long)e->rate);
     if (!isfinite(e->amplitude) || e->amplitude < 0.0 || !isfinite(e->initial_phase))
         return set_error_fmt(RV_ERR_INVALID, "emitter: amplitude and initial phase must be finite (amplitude >= 0)");
     if (llabs(e->carrier_offset) * 2 > e->rate) return set_error_fmt(RV_ERR_INVALID, "emitter: carrier past Nyquist");
-    if (e->tone_hz <= 0 || e->tone_hz * 2 >= e->rate) return set_error_fmt(RV_ERR_INVALID, "emitter: tone past Nyquist");
+    const bool cw = e->modulation == RV_EMITTER_CW;
+    if (!cw && (e->tone_hz <= 0 || e->tone_hz * 2 >= e->rate))
+        return set_error_fmt(RV_ERR_INVALID, "emitter: tone past Nyquist");
+    if (cw) {  // modulators.cpp:485-515
+        if (!isfinite(e->words_per_minute) || e->words_per_minute <= 0.0 || !isfinite(e->rise_fall_ms) ||
+            e->rise_fall_ms < 0.0 || !isfinite(e->message_gap_dots) || e->message_gap_dots < 0.0)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: CW timing must be positive (rise/fall and gap >= 0)");
+        if (1.2 * (double)e->rate / e->words_per_minute < 2.0)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: CW dot shorter than two samples");
+        if (memchr(e->text, 0, sizeof e->text) == nullptr)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: CW text is not NUL-terminated");
+        bool keyed = false;
+        for (const char* c = e->text; *c != '\0'; ++c) {
+            if (*c == ' ') continue;
+            if (morse(*c) == nullptr) return set_error_fmt(RV_ERR_INVALID, "emitter: no Morse code for '%c'", *c);
+            keyed = true;
+        }
+        if (!keyed) return set_error_fmt(RV_ERR_INVALID, "emitter: CW text has nothing to key");
+    }
     if (e->modulation == RV_EMITTER_AM && (!isfinite(e->modulation_index) || e->modulation_index < 0.0))
         return set_error_fmt(RV_ERR_INVALID, "emitter: AM modulation index must be finite and >= 0");
     if (e->modulation == RV_EMITTER_NFM && e->deviation <= 0)
@@ -278,11 +411,27 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
     if (int32_t st = cuda_status(cudaMallocAsync(&d_anchors, segs * sizeof(Anchor), s), "emitter anchors")) return st;
     int32_t st = cuda_status(cudaMemcpyAsync(d_anchors, anchors.data(), segs * sizeof(Anchor), cudaMemcpyHostToDevice, s),
                              "emitter anchors");
+    std::vector<CwElement> elements;
+    CwElement* d_elements = nullptr;
+    if (st == RV_OK && cw) {
+        elements = cw_elements(e->text, 1.2 * (double)e->rate / e->words_per_minute, e->message_gap_dots);
+        st = cuda_status(cudaMallocAsync(&d_elements, elements.size() * sizeof(CwElement), s), "emitter elements");
+        if (st == RV_OK)
+            st = cuda_status(cudaMemcpyAsync(d_elements, elements.data(), elements.size() * sizeof(CwElement),
+                                             cudaMemcpyHostToDevice, s),
+                             "emitter elements");
+    }
     if (st == RV_OK) {
-        k_tone_emitter<<<(unsigned)((segs + 127) / 128), 128, 0, s>>>(r, d_anchors, (uint32_t)segs,
-                                                                      reinterpret_cast<float2*>(out));
+        const unsigned grid = (unsigned)((segs + 127) / 128);
+        if (cw)
+            k_cw_emitter<<<grid, 128, 0, s>>>(r, d_anchors, (uint32_t)segs, d_elements, (uint32_t)elements.size(),
+                                              e->rise_fall_ms * 0.001 * (double)e->rate,
+                                              reinterpret_cast<float2*>(out));
+        else
+            k_tone_emitter<<<grid, 128, 0, s>>>(r, d_anchors, (uint32_t)segs, reinterpret_cast<float2*>(out));
         st = cuda_status(cudaGetLastError(), "emitter");
     }
+    if (d_elements) cudaFreeAsync(d_elements, s);
     cudaFreeAsync(d_anchors, s);
     // the host table must outlive the copy
     if (st == RV_OK) st = cuda_status(cudaStreamSynchronize(s), "emitter");

@@ -186,7 +186,13 @@ TONES = [dict(modulation=1, rate=2_400_000, carrier_offset=100_000, tone_hz=1000
               initial_phase=0.7, modulation_index=0.0, tone2_hz=0, audio_low_hz=300, audio_high_hz=3000),
          dict(modulation=4, rate=2_400_000, carrier_offset=-100_000, tone_hz=700, deviation=0, amplitude=1.0,
               initial_phase=-2.5, modulation_index=0.0, tone2_hz=1900, audio_low_hz=300, audio_high_hz=3000)]
-TONE_IDS = ["am", "nfm", "am-edge", "wide-nfm", "usb", "lsb-two-tone"]
+TONES += [dict(modulation=0, rate=48_000, carrier_offset=3_000, tone_hz=0, deviation=0, amplitude=0.8,
+               initial_phase=0.1, modulation_index=0.0, words_per_minute=30.0, rise_fall_ms=5.0,
+               message_gap_dots=7.0, text=b"CQ DE GB300, K?"),
+          dict(modulation=0, rate=2_400_000, carrier_offset=-250_000, tone_hz=0, deviation=0, amplitude=1.0,
+               initial_phase=0.0, modulation_index=0.0, words_per_minute=45.0, rise_fall_ms=0.0,
+               message_gap_dots=10.5, text=b"test 73")]
+TONE_IDS = ["am", "nfm", "am-edge", "wide-nfm", "usb", "lsb-two-tone", "cw", "cw-hard"]
 
 
 def tone(d):
@@ -217,8 +223,11 @@ def ora_scene(seed, dbfs, d, on, off, start, count):
 
 def ref_args(synref, d=None):
     synref.refsyn_set_ssb.argtypes = [C.c_int64, C.c_int64, C.c_int64]
+    synref.refsyn_set_cw.argtypes = [C.c_double, C.c_double, C.c_double, C.c_char_p]
     if d is not None:
         synref.refsyn_set_ssb(d.get("tone2_hz", 0), d.get("audio_low_hz", 300), d.get("audio_high_hz", 3000))
+        synref.refsyn_set_cw(d.get("words_per_minute", 20.0), d.get("rise_fall_ms", 5.0),
+                             d.get("message_gap_dots", 7.0), d.get("text", b"CQ DE REVENANT"))
     synref.refsyn_tone.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double,
                                    C.c_double, C.c_uint64, C.c_uint64, C.c_double, C.c_void_p]
     synref.refsyn_scene_tone.argtypes = [C.c_uint64, C.c_int64, C.c_double, C.c_int, C.c_int64, C.c_int64, C.c_int64,
@@ -244,7 +253,7 @@ def test_oracle_tone_emitter_matches_reference(synref, d):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (first, gain)
 
 
-@pytest.mark.parametrize("d", [TONES[0], TONES[1], TONES[5]], ids=["am", "nfm", "lsb-two-tone"])
+@pytest.mark.parametrize("d", [TONES[0], TONES[1], TONES[5], TONES[6]], ids=["am", "nfm", "lsb-two-tone", "cw"])
 def test_oracle_scene_with_emitter_matches_reference(synref, d):
     s = ref_args(synref, d)
     seed, dbfs, on, off, start, count = 21, -50.0, 5000, 20_000, 3000, 20_000
@@ -265,12 +274,12 @@ def test_gpu_tone_emitter_matches_oracle(gpu, d):
             lib().rv_last_error()
         got = buf.download(np.float32, (count, 2))
         want = ora_tone(d, first, count, gain, io)
-        if d["modulation"] != 2:  # AM, SSB: the anchors come from the C library, the rest is + and *
+        if d["modulation"] in (1, 3, 4):  # AM, SSB: the anchors come from the C library, the rest is + and *
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), first
-        else:  # NFM: CUDA's FP64 cos/sin of the deviation per sample
+        else:  # NFM, CW: CUDA's FP64 cos/sin of the deviation, or of the keying edges
             n = check_close(got, want)
-            print("NFM emitter %s, %d samples from %d: %d of %d components off by one FP32 ulp"
-                  % (d["tone_hz"], count, first, n, 2 * count))
+            print("%s emitter, %d samples from %d: %d of %d components off by one FP32 ulp"
+                  % ("NFM" if d["modulation"] == 2 else "CW", count, first, n, 2 * count))
 
 
 @pytest.mark.gpu
@@ -291,7 +300,9 @@ def test_gpu_scene_with_emitter_matches_oracle(gpu):
 
 def test_emitter_rejects_bad_specs(rv):
     one = np.zeros(4, np.float32)
-    for bad in (dict(modulation=0), dict(tone_hz=0), dict(tone_hz=1_200_000), dict(carrier_offset=1_300_000),
+    for bad in (dict(modulation=-1), dict(modulation=0, words_per_minute=20.0, rise_fall_ms=5.0, text=b"#"),
+                dict(modulation=0, words_per_minute=20.0, rise_fall_ms=5.0, text=b"   "),
+                dict(modulation=0, words_per_minute=2e6, rise_fall_ms=5.0, text=b"E"), dict(tone_hz=0), dict(tone_hz=1_200_000), dict(carrier_offset=1_300_000),
                 dict(amplitude=-1.0), dict(modulation=2, deviation=0), dict(rate=0), dict(modulation=5),
                 dict(modulation=3, audio_low_hz=300, audio_high_hz=3000, tone_hz=200),
                 dict(modulation=4, audio_low_hz=3000, audio_high_hz=300),
