@@ -1230,6 +1230,45 @@ typedef struct rv_tone_emitter {
 int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* emitter, uint64_t first, uint64_t count,
                               double gain, rv_cf32* out_dev, uint64_t out_len);
 
+/* Scene::create's random population (core/dsp/synth/wideband.cpp:375-482;
+ * RandomPopulation, wideband.h:211-236) for palettes of the built modes
+ * (CW, AM, NFM, USB, LSB): the emitters and their bursts, laid out from
+ * std::mt19937_64 draws exactly as the reference lays them out, sorted by
+ * start. A scene is then rv_scene_noise plus, in this order, each burst's
+ * rv_emitter_accumulate over its window at its gain. */
+typedef struct rv_scene_population {
+    uint64_t seed;
+    int64_t rate;
+    int64_t duration_samples;       /* 0 = unbounded (one always-on burst each) */
+    double noise_dbfs;              /* full-band noise floor */
+    uint32_t emitter_count;
+    uint32_t bursts_per_emitter;
+    int64_t span_low_hz;
+    int64_t span_high_hz;
+    double snr_min_db;              /* in the occupied bandwidth */
+    double snr_max_db;
+    double min_burst_seconds;
+    double max_burst_seconds;
+    uint32_t palette_count;         /* 0 = every modulation (refused: FSK and PSK are not built) */
+    int32_t palette[8];             /* RV_EMITTER_* (siggen::Modulation values) */
+} rv_scene_population;
+
+typedef struct rv_scene_burst {
+    rv_tone_emitter emitter;
+    uint64_t start;                 /* stream indices; end = UINT64_MAX for always on */
+    uint64_t end;
+    double gain;
+    double mean_power;              /* EmitterTruth (wideband.h:82-150) */
+    double snr_in_occupied_bandwidth_db;
+    int64_t extent_low_hz;
+    int64_t extent_high_hz;
+    uint64_t payload_seed;
+} rv_scene_burst;
+
+/* *count = every burst; the first `capacity` written to out (may be NULL). */
+int32_t rv_scene_plan(const rv_scene_population* population, rv_scene_burst* out, uint32_t capacity,
+                      uint32_t* count);
+
 /* ===================================================================== *
  * Capture segments (core/capture/format.h, core/capture/writer.cpp): the  *
  * rolling capture's on-disk SigMF recordings, so a capture replays       *

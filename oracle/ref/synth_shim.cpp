@@ -130,6 +130,57 @@ int refsyn_scene_tone(std::uint64_t seed, std::int64_t rate, double noise_dbfs, 
     return 0;
 }
 
+// Scene::create of a random population over `palette` (siggen::Modulation
+// values) and Scene::render of [start, start + count) into out (may be
+// NULL); the truth rows as 8 doubles each: start, end (-1 = always on),
+// carrier, modulation, mean power, SNR in the occupied band, extent low, high.
+int refsyn_random_scene(std::uint64_t seed, std::int64_t rate, std::int64_t duration, double noise_dbfs,
+                        std::uint32_t emitters, std::uint32_t bursts, std::int64_t span_lo, std::int64_t span_hi,
+                        double snr_min, double snr_max, double min_s, double max_s, std::uint32_t npalette,
+                        const int* palette, std::uint64_t start, std::uint64_t count, float* out, double* truth,
+                        std::uint32_t truth_cap, std::uint32_t* truth_count) {
+    siggen::SceneSpec spec;
+    spec.rate = rate;
+    spec.seed = seed;
+    spec.duration_samples = duration;
+    spec.add_noise = true;
+    spec.noise_power_full_band_dbfs = noise_dbfs;
+    spec.worker_threads = 1;
+    spec.random.emitter_count = emitters;
+    spec.random.bursts_per_emitter = bursts;
+    spec.random.span_low_hz = span_lo;
+    spec.random.span_high_hz = span_hi;
+    spec.random.snr_in_occupied_bandwidth_db_min = snr_min;
+    spec.random.snr_in_occupied_bandwidth_db_max = snr_max;
+    spec.random.min_burst_seconds = min_s;
+    spec.random.max_burst_seconds = max_s;
+    for (std::uint32_t i = 0; i < npalette; ++i) spec.random.palette.push_back(static_cast<siggen::Modulation>(palette[i]));
+    auto scene = siggen::Scene::create(spec);
+    if (!scene) return -1;
+    const auto& t = scene->truth();
+    *truth_count = static_cast<std::uint32_t>(t.size());
+    for (std::uint32_t i = 0; i < t.size() && i < truth_cap; ++i) {
+        double* r = truth + 8 * i;
+        r[0] = static_cast<double>(t[i].start_sample);
+        r[1] = t[i].end_sample == siggen::kAlwaysOn ? -1.0 : static_cast<double>(t[i].end_sample);
+        r[2] = static_cast<double>(t[i].carrier_offset_hz);
+        r[3] = static_cast<double>(t[i].modulation);
+        r[4] = t[i].mean_power;
+        r[5] = t[i].snr_in_occupied_bandwidth_db;
+        r[6] = static_cast<double>(t[i].extent.low_hz);
+        r[7] = static_cast<double>(t[i].extent.high_hz);
+    }
+    if (out != nullptr && count > 0) {
+        std::vector<std::complex<float>> buf(count);
+        scene->render(start, std::span<std::complex<float>>(buf));
+        for (std::uint64_t i = 0; i < count; ++i) {
+            out[2 * i] = buf[i].real();
+            out[2 * i + 1] = buf[i].imag();
+        }
+    }
+    return 0;
+}
+
 // The libstdc++ std::mt19937_64 stream of one noise block, for pinning the
 // GPU generator's draws: the block's seed is given (the reference derives it
 // with derive_stream_seed, which the tests restate).

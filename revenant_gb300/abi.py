@@ -208,6 +208,19 @@ class ToneEmitter(_S):
                 ("rise_fall_ms", F64), ("message_gap_dots", F64), ("text", C.c_char * 64)]
 
 
+class ScenePopulation(_S):
+    _fields_ = [("seed", U64), ("rate", I64), ("duration_samples", I64), ("noise_dbfs", F64), ("emitter_count", U32),
+                ("bursts_per_emitter", U32), ("span_low_hz", I64), ("span_high_hz", I64), ("snr_min_db", F64),
+                ("snr_max_db", F64), ("min_burst_seconds", F64), ("max_burst_seconds", F64), ("palette_count", U32),
+                ("palette", I32 * 8)]
+
+
+class SceneBurst(_S):
+    _fields_ = [("emitter", ToneEmitter), ("start", U64), ("end", U64), ("gain", F64), ("mean_power", F64),
+                ("snr_in_occupied_bandwidth_db", F64), ("extent_low_hz", I64), ("extent_high_hz", I64),
+                ("payload_seed", U64)]
+
+
 class CaptureConfig(_S):
     _fields_ = [("max_segment_bytes", U64), ("max_segment_seconds", F64), ("retention_bytes", U64),
                 ("retention_max_age_ns", I64), ("stream_epoch", U64), ("recover_on_start", I32), ("reserved", I32)]
@@ -365,7 +378,8 @@ EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params"
                  "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
                  "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,
                  "rv_excision_plan": ExcisionPlan, "rv_excision_cursor": ExcisionCursor,
-                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_comb_line": CombLine, "rv_capture_config": CaptureConfig, "rv_tone_emitter": ToneEmitter,
+                 "rv_vrx_display_plan": VrxDisplayPlan, "rv_comb_line": CombLine, "rv_capture_config": CaptureConfig, "rv_tone_emitter": ToneEmitter, "rv_scene_population": ScenePopulation,
+                 "rv_scene_burst": SceneBurst,
                  "rv_capture_block": CaptureBlock, "rv_capture_annotation": CaptureAnnotation,
                  "rv_capture_writer_stats": CaptureWriterStats, "rv_capture_segment": CaptureSegment, "rv_comb_params": CombParams, "rv_blanker_config": BlankerConfig, "rv_blanker_params": BlankerParams,
                  "rv_line_config": LineConfig, "rv_line_section": LineSection, "rv_line_params": LineParams,

@@ -310,3 +310,88 @@ def test_emitter_rejects_bad_specs(rv):
         d = dict(TONES[0])
         d.update(bad)
         assert rv.rv_emitter_accumulate(None, C.byref(tone(d)), 0, 1, 1.0, one.ctypes.data, 1) < 0, bad
+
+
+# ---- random populations (Scene::create's layout) and whole scenes ----------
+
+POPULATIONS = [dict(seed=5, rate=2_400_000, duration=0, noise_dbfs=-60.0, emitters=12, bursts=1,
+                    span=(-1_000_000, 1_000_000), snr=(5.0, 35.0), burst_seconds=(0.05, 2.0), palette=(0, 1, 2, 3, 4)),
+               dict(seed=77, rate=20_000_000, duration=4_000_000, noise_dbfs=-70.0, emitters=20, bursts=3,
+                    span=(-9_000_000, 9_000_000), snr=(-5.0, 30.0), burst_seconds=(0.001, 0.05),
+                    palette=(1, 2, 3, 4)),
+               dict(seed=2, rate=48_000, duration=200_000, noise_dbfs=-50.0, emitters=4, bursts=2,
+                    span=(-20_000, 20_000), snr=(10.0, 20.0), burst_seconds=(0.5, 2.0), palette=(0,))]
+
+
+def ref_random(s, d, start=0, count=0):
+    s.refsyn_random_scene.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_double, C.c_uint32, C.c_uint32,
+                                      C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_uint32, C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
+                                      C.c_uint32, C.POINTER(C.c_uint32)]
+    pal = np.array(d["palette"], np.int32)
+    truth = np.zeros((1024, 8))
+    n = C.c_uint32()
+    out = np.zeros((max(count, 1), 2), np.float32)
+    assert s.refsyn_random_scene(d["seed"], d["rate"], d["duration"], d["noise_dbfs"], d["emitters"], d["bursts"],
+                                 d["span"][0], d["span"][1], d["snr"][0], d["snr"][1], d["burst_seconds"][0],
+                                 d["burst_seconds"][1], len(pal), pal.ctypes.data, start, count,
+                                 out.ctypes.data if count else None, truth.ctypes.data, 1024, C.byref(n)) == 0
+    return truth[:n.value], out[:count]
+
+
+def ora_random_scene(d, start, count):
+    """The scene from the library's plan, rendered by the oracle: noise, then
+    each burst's emitter over its window, in burst order."""
+    from revenant_gb300 import scene
+    pop = scene.population(**d)
+    out = ora_noise(d["seed"], ora_lib().or_scene_noise_sigma(d["noise_dbfs"]), start, count)
+    for b in scene.plan(pop):
+        lo, hi = max(b.start, start), min(b.end, start + count)
+        if lo < hi:
+            from revenant_gb300 import abi
+            o = oracle().lib
+            o.or_emitter_accumulate.argtypes = [C.POINTER(abi.ToneEmitter), C.c_uint64, C.c_uint64, C.c_double,
+                                                C.c_void_p]
+            part = np.ascontiguousarray(out[lo - start:hi - start])
+            assert o.or_emitter_accumulate(C.byref(b.emitter), lo - b.start, hi - lo, b.gain, part.ctypes.data) == 0
+            out[lo - start:hi - start] = part
+    return out
+
+
+@pytest.mark.parametrize("d", POPULATIONS, ids=["always-on", "bursty-20MSps", "cw-only"])
+def test_plan_matches_reference_layout(synref, d):
+    from revenant_gb300 import scene
+    truth, _ = ref_random(synref, d)
+    got = scene.plan(scene.population(**d))
+    assert len(got) == len(truth) > 0
+    for b, t in zip(got, truth):
+        end = -1.0 if b.end == 2**64 - 1 else float(b.end)
+        assert (float(b.start), end, float(b.emitter.carrier_offset), float(b.emitter.modulation)) == tuple(t[:4])
+        assert b.mean_power == t[4] and b.snr_in_occupied_bandwidth_db == t[5]
+        assert (float(b.extent_low_hz), float(b.extent_high_hz)) == tuple(t[6:8])
+
+
+@pytest.mark.parametrize("d,start,count", [(POPULATIONS[0], 1000, 30_000), (POPULATIONS[1], 0, 200_000),
+                                           (POPULATIONS[2], 40_000, 60_000)], ids=["always-on", "bursty", "cw"])
+def test_oracle_random_scene_matches_reference_render(synref, d, start, count):
+    _, want = ref_random(synref, d, start, count)
+    got = ora_random_scene(d, start, count)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_plan_refuses_unbuilt_modes(rv):
+    from revenant_gb300 import abi, scene
+    pop = scene.population(**dict(POPULATIONS[0], palette=(1, 6)))
+    n = C.c_uint32()
+    assert rv.rv_scene_plan(C.byref(pop), None, 0, C.byref(n)) == abi.RV_ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("d,start,count", [(POPULATIONS[0], 1000, 300_000), (POPULATIONS[1], 0, 4_000_000),
+                                           (POPULATIONS[2], 0, 200_000)], ids=["always-on", "bursty", "cw"])
+def test_gpu_random_scene_matches_oracle(gpu, d, start, count):
+    from revenant_gb300 import scene
+    buf = scene.render(gpu, scene.population(**d), start, count)
+    got = buf.download(np.float32, (count, 2))
+    n = check_close(got, ora_random_scene(d, start, count))
+    print("random scene seed %d, %d samples: %d of %d components off by one FP32 ulp" % (d["seed"], count, n, 2 * count))
