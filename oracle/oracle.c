@@ -2070,8 +2070,77 @@ static double or_cw_envelope(const or_cw_element* el, uint32_t n, double ramp_sa
     return envelope;
 }
 
+/* FSK2 (modulators.cpp:216-257 symbol clock, :402-423 index_at, :454-472
+ * random_bits, :850-882 phase prefix, :1393-1441 accumulate_fsk) */
+static int32_t or_fsk_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io) {
+    const double two_pi = 6.283185307179586476925286766559;
+    const uint64_t symbols = e->symbol_count;
+    if (symbols == 0 || symbols > 1000000) return fail("fsk: symbol count");
+    const double rate = (double)e->rate;
+    const double real = (double)symbols * (rate / e->symbol_rate);
+    const int64_t cycle = (int64_t)llround(real);
+    if (cycle < (int64_t)symbols * 2) return fail("fsk: under two samples per symbol");
+    uint8_t* bits = (uint8_t*)malloc(symbols);
+    int64_t* boundary = (int64_t*)malloc((symbols + 1) * sizeof(int64_t));
+    double* prefix = (double*)malloc((symbols + 1) * sizeof(double));
+    or_mt64* g = (or_mt64*)malloc(sizeof(or_mt64));
+    if (!bits || !boundary || !prefix || !g) return fail("fsk: out of memory");
+    or_mt64_seed(g, e->seed);
+    uint64_t word = 0;
+    unsigned remaining = 0;
+    for (uint64_t i = 0; i < symbols; ++i) {
+        if (remaining == 0) word = or_mt64_next(g), remaining = 64;
+        bits[i] = (uint8_t)(word & 1u);
+        word >>= 1;
+        --remaining;
+    }
+    for (uint64_t k = 0; k <= symbols; ++k) boundary[k] = ((int64_t)k * cycle) / (int64_t)symbols;
+    const double upper = two_pi * (double)e->deviation / rate, lower = -upper;
+    double accumulated = 0.0;
+    for (uint64_t k = 0; k < symbols; ++k) {
+        prefix[k] = accumulated;
+        accumulated += (bits[k] != 0 ? upper : lower) * (double)(boundary[k + 1] - boundary[k]);
+        accumulated = fmod(accumulated, two_pi);
+    }
+    const double cycle_phase = accumulated, level = gain * e->amplitude;
+    const double carrier_step = two_pi * (double)e->carrier_offset / rate;
+    const uint64_t end = first + count;
+    uint64_t index = first;
+    while (index < end) {
+        const int64_t repeat = (int64_t)index / cycle, position = (int64_t)index - repeat * cycle;
+        uint64_t sym = (uint64_t)((position * (int64_t)symbols) / cycle);
+        if (sym >= symbols) sym = symbols - 1;
+        while (sym + 1 < symbols && boundary[sym + 1] <= position) ++sym;
+        while (sym > 0 && boundary[sym] > position) --sym;
+        const uint64_t ss = (uint64_t)(repeat * cycle + boundary[sym]), se = (uint64_t)(repeat * cycle + boundary[sym + 1]);
+        const uint64_t grid = index - index % 1024u;
+        const uint64_t anchor = grid > ss ? grid : ss;
+        uint64_t stop = end < se ? end : se;
+        if (grid + 1024u < stop) stop = grid + 1024u;
+        const double sense = bits[sym] != 0 ? 1.0 : -1.0;
+        const double phase = e->initial_phase + or_exact_phase(e->carrier_offset, e->rate, anchor) +
+                             fmod((double)repeat * cycle_phase, two_pi) + prefix[sym] +
+                             sense * upper * (double)(anchor - ss);
+        const double step = carrier_step + sense * upper;
+        double re = cos(phase), im = sin(phase);
+        const double sr = cos(step), si = sin(step);
+        for (uint64_t k = anchor; k < stop; ++k) {
+            if (k >= index) {
+                io[k - first].re = io[k - first].re + (float)(level * re);
+                io[k - first].im = io[k - first].im + (float)(level * im);
+            }
+            const double nre = re * sr - im * si, nim = re * si + im * sr;
+            re = nre, im = nim;
+        }
+        index = stop;
+    }
+    free(bits), free(boundary), free(prefix), free(g);
+    return ok();
+}
+
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io) {
     const double two_pi = 6.283185307179586476925286766559;
+    if (e->modulation == RV_EMITTER_FSK2) return or_fsk_accumulate(e, first, count, gain, io);
     if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_LSB) return fail("emitter: modulation");
     or_cw_element* elements = NULL;
     uint32_t nel = 0;

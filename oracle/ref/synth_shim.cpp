@@ -46,6 +46,17 @@ static std::int64_t g_tone2 = 0, g_low = 300, g_high = 3000;
 static double g_wpm = 20.0, g_rise = 5.0, g_gap = 7.0;
 static char g_text[64] = "CQ DE REVENANT";
 
+static std::uint64_t g_seed = 0;
+static double g_baud = 1200.0;
+static std::uint64_t g_symbols = 256;
+
+// The FSK fields of the next spec (payload seed, baud, payload length).
+void refsyn_set_fsk(std::uint64_t seed, double baud, std::uint64_t symbols) {
+    g_seed = seed;
+    g_baud = baud;
+    g_symbols = symbols;
+}
+
 // The CW fields of the next spec.
 void refsyn_set_cw(double wpm, double rise_ms, double gap_dots, const char* text) {
     g_wpm = wpm;
@@ -69,6 +80,10 @@ static siggen::ModulatorSpec tone_spec(int kind, std::int64_t rate, std::int64_t
     spec.ssb.tone2_hz = g_tone2;
     spec.ssb.audio_low_hz = g_low;
     spec.ssb.audio_high_hz = g_high;
+    spec.fsk.symbol_rate = g_baud;
+    spec.fsk.symbol_count = g_symbols;
+    spec.fsk.deviation = deviation;
+    spec.common.seed = g_seed;
     spec.cw.words_per_minute = g_wpm;
     spec.cw.rise_fall_ms = g_rise;
     spec.cw.message_gap_dots = g_gap;

@@ -198,14 +198,15 @@ class CombParams(_S):
 
 
 DFT_FP16, DFT_BF16 = 0, 1
-EMITTER_CW, EMITTER_AM, EMITTER_NFM, EMITTER_USB, EMITTER_LSB = 0, 1, 2, 3, 4
+EMITTER_CW, EMITTER_AM, EMITTER_NFM, EMITTER_USB, EMITTER_LSB, EMITTER_FSK2 = 0, 1, 2, 3, 4, 5
 
 
 class ToneEmitter(_S):
     _fields_ = [("modulation", I32), ("reserved", I32), ("rate", I64), ("carrier_offset", I64), ("tone_hz", I64),
                 ("deviation", I64), ("amplitude", F64), ("initial_phase", F64), ("modulation_index", F64),
                 ("tone2_hz", I64), ("audio_low_hz", I64), ("audio_high_hz", I64), ("words_per_minute", F64),
-                ("rise_fall_ms", F64), ("message_gap_dots", F64), ("text", C.c_char * 64)]
+                ("rise_fall_ms", F64), ("message_gap_dots", F64), ("text", C.c_char * 64), ("seed", U64),
+                ("symbol_rate", F64), ("symbol_count", U64)]
 
 
 class ScenePopulation(_S):

@@ -4,8 +4,11 @@
 #pragma once
 
 #include <math.h>
+
+#include <cmath>
 #include <stdint.h>
 
+#include <random>
 #include <utility>
 #include <vector>
 
@@ -75,6 +78,53 @@ inline std::vector<CwElement> cw_elements(const char* text, double dot_samples, 
         previous = edge;
     }
     return out;
+}
+
+// modulators.cpp:454-472 random_bits: LSB first from std::mt19937_64(seed)
+inline std::vector<uint8_t> random_bits(size_t count, uint64_t seed) {
+    std::vector<uint8_t> bits(count, 0);
+    std::mt19937_64 engine(seed);
+    uint64_t word = 0;
+    unsigned remaining = 0;
+    for (size_t i = 0; i < count; ++i) {
+        if (remaining == 0) word = engine(), remaining = 64;
+        bits[i] = (uint8_t)(word & 1u);
+        word >>= 1;
+        --remaining;
+    }
+    return bits;
+}
+
+// modulators.cpp:216-257 build_symbol_clock: symbol k spans
+// [floor(k cycle / symbols), floor((k + 1) cycle / symbols)) of a cycle of
+// llround(symbols rate / baud) samples. False when the grid is unusable.
+struct SymbolClock {
+    uint64_t symbols = 0;
+    int64_t cycle = 0;
+    std::vector<int64_t> boundary;
+    // :402-423 index_at
+    uint64_t index_at(int64_t position) const {
+        uint64_t e = (uint64_t)((position * (int64_t)symbols) / cycle);
+        if (e >= symbols) e = symbols - 1;
+        while (e + 1 < symbols && boundary[e + 1] <= position) ++e;
+        while (e > 0 && boundary[e] > position) --e;
+        return e;
+    }
+    double effective_rate(int64_t rate) const { return (double)symbols * (double)rate / (double)cycle; }
+};
+
+inline bool build_symbol_clock(uint64_t symbols, int64_t rate, double baud, SymbolClock& c) {
+    if (symbols == 0 || symbols > 1000000) return false;
+    const double per = (double)rate / baud, real = (double)symbols * per;
+    if (!std::isfinite(real) || real >= 9.0e15) return false;
+    const int64_t cycle = (int64_t)llround(real);
+    if (cycle < (int64_t)symbols * 2) return false;
+    if ((double)symbols * (double)cycle >= 1.8e19) return false;
+    c.symbols = symbols;
+    c.cycle = cycle;
+    c.boundary.resize(symbols + 1);
+    for (uint64_t k = 0; k <= symbols; ++k) c.boundary[k] = ((int64_t)k * cycle) / (int64_t)symbols;
+    return true;
 }
 
 }  // namespace rv

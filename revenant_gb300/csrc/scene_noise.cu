@@ -262,6 +262,73 @@ __global__ void k_cw_emitter(ToneRun r, const Anchor* __restrict__ anchors, uint
     }
 }
 
+// One FSK segment (modulators.cpp:1393-1441): a unit phasor anchored at
+// `anchor` and advanced by one rotation per sample, written over
+// [begin, stop). Segments end at symbol boundaries and at the 1024-sample
+// anchor grid; their anchors' and rotations' cos/sin come from the host.
+struct FskSegment {
+    uint64_t anchor, begin, stop;
+    double re, im, step_re, step_im;
+};
+
+__global__ void k_fsk_emitter(const FskSegment* __restrict__ seg, uint32_t n, double level, uint64_t first,
+                              float2* __restrict__ out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const FskSegment g = seg[k];
+    double re = g.re, im = g.im;
+    for (uint64_t index = g.anchor; index < g.stop; ++index) {
+        if (index >= g.begin) {
+            float2& o = out[index - first];
+            o = make_float2(o.x + (float)(level * re), o.y + (float)(level * im));
+        }
+        const double nre = re * g.step_re - im * g.step_im, nim = re * g.step_im + im * g.step_re;
+        re = nre, im = nim;
+    }
+}
+
+// The FSK segments of emitter indices [first, end): the reference's walk
+// (modulators.cpp:1393-1441) with the bits, symbol clock and per-symbol
+// phase prefix of Modulator::create (:850-882).
+bool fsk_segments(const rv_tone_emitter* e, uint64_t first, uint64_t end, std::vector<FskSegment>& out) {
+    SymbolClock clock;
+    const std::vector<uint8_t> bits = random_bits(e->symbol_count, e->seed);
+    if (!build_symbol_clock(bits.size(), e->rate, e->symbol_rate, clock)) return false;
+    const double rate = (double)e->rate;
+    const double upper = kTwoPi * (double)e->deviation / rate, lower = -upper;
+    std::vector<double> prefix(clock.symbols + 1, 0.0);
+    double accumulated = 0.0;
+    for (uint64_t k = 0; k < clock.symbols; ++k) {
+        prefix[k] = accumulated;
+        accumulated += (bits[k] != 0 ? upper : lower) * (double)(clock.boundary[k + 1] - clock.boundary[k]);
+        accumulated = fmod(accumulated, kTwoPi);
+    }
+    const double cycle_phase = accumulated;
+    const double carrier_step = kTwoPi * (double)e->carrier_offset / rate;
+    const int64_t cycle = clock.cycle;
+    uint64_t index = first;
+    while (index < end) {
+        const int64_t repeat = (int64_t)index / cycle;
+        const int64_t position = (int64_t)index - repeat * cycle;
+        const uint64_t symbol = clock.index_at(position);
+        const int64_t base = repeat * cycle;
+        const uint64_t symbol_start = (uint64_t)(base + clock.boundary[symbol]);
+        const uint64_t symbol_stop = (uint64_t)(base + clock.boundary[symbol + 1]);
+        const uint64_t grid = index - index % kAnchorInterval;
+        const uint64_t anchor = grid > symbol_start ? grid : symbol_start;
+        uint64_t stop = end < symbol_stop ? end : symbol_stop;
+        if (grid + kAnchorInterval < stop) stop = grid + kAnchorInterval;
+        const double sense = bits[symbol] != 0 ? 1.0 : -1.0;
+        const double phase = e->initial_phase + exact_phase(e->carrier_offset, e->rate, anchor) +
+                             fmod((double)repeat * cycle_phase, kTwoPi) + prefix[symbol] +
+                             sense * upper * (double)(anchor - symbol_start);
+        const double step = carrier_step + sense * upper;
+        out.push_back(FskSegment{anchor, index, stop, cos(phase), sin(phase), cos(step), sin(step)});
+        index = stop;
+    }
+    return true;
+}
+
 }  // namespace
 }  // namespace rv
 
@@ -270,9 +337,10 @@ using namespace rv;
 extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e, uint64_t first, uint64_t count,
                                          double gain, rv_cf32* out, uint64_t out_len) {
     if (e == nullptr || (out == nullptr && count > 0)) return set_error_fmt(RV_ERR_INVALID, "emitter: NULL argument");
-    if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_LSB)
-        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (CW, or tone AM, NFM, USB, LSB)",
+    if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_FSK2)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (CW, FSK2, or tone AM, NFM, USB, LSB)",
                              e->modulation);
+    const bool fsk = e->modulation == RV_EMITTER_FSK2;
     const bool ssb = e->modulation == RV_EMITTER_USB || e->modulation == RV_EMITTER_LSB;
     // modulators.cpp:310-332 validate_common, :334-343 the tone, :517-546 the mode
     if (e->rate <= 0 || e->rate > 1000000000) return set_error_fmt(RV_ERR_INVALID, "emitter: rate %lld", (long long)e->rate);
@@ -280,7 +348,13 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
         return set_error_fmt(RV_ERR_INVALID, "emitter: amplitude and initial phase must be finite (amplitude >= 0)");
     if (llabs(e->carrier_offset) * 2 > e->rate) return set_error_fmt(RV_ERR_INVALID, "emitter: carrier past Nyquist");
     const bool cw = e->modulation == RV_EMITTER_CW;
-    if (!cw && (e->tone_hz <= 0 || e->tone_hz * 2 >= e->rate))
+    if (fsk) {  // modulators.cpp:593-609
+        if (!isfinite(e->symbol_rate) || e->symbol_rate <= 0.0 || e->deviation <= 0 || e->symbol_count == 0)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: FSK needs a positive symbol rate, deviation and count");
+        if ((llabs(e->carrier_offset) + e->deviation) * 2 > e->rate)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: FSK tones past Nyquist");
+    }
+    if (!cw && !fsk && (e->tone_hz <= 0 || e->tone_hz * 2 >= e->rate))
         return set_error_fmt(RV_ERR_INVALID, "emitter: tone past Nyquist");
     if (cw) {  // modulators.cpp:485-515
         if (!isfinite(e->words_per_minute) || e->words_per_minute <= 0.0 || !isfinite(e->rise_fall_ms) ||
@@ -331,6 +405,26 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
     r.c_step_re = cos(c_step), r.c_step_im = sin(c_step);
     r.t_step_re = cos(t_step), r.t_step_im = sin(t_step);
     r.first = first, r.count = count;
+    if (fsk) {
+        std::vector<FskSegment> segs;
+        if (!fsk_segments(e, first, first + count, segs))
+            return set_error_fmt(RV_ERR_INVALID, "emitter: FSK symbol clock unusable at this rate and baud");
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        FskSegment* d = nullptr;
+        if (int32_t st = cuda_status(cudaMallocAsync(&d, segs.size() * sizeof(FskSegment), s), "fsk segments"))
+            return st;
+        int32_t st = cuda_status(cudaMemcpyAsync(d, segs.data(), segs.size() * sizeof(FskSegment),
+                                                 cudaMemcpyHostToDevice, s),
+                                 "fsk segments");
+        if (st == RV_OK) {
+            k_fsk_emitter<<<(unsigned)((segs.size() + 127) / 128), 128, 0, s>>>(d, (uint32_t)segs.size(), r.level, first,
+                                                                             reinterpret_cast<float2*>(out));
+            st = cuda_status(cudaGetLastError(), "fsk emitter");
+        }
+        cudaFreeAsync(d, s);
+        if (st == RV_OK) st = cuda_status(cudaStreamSynchronize(s), "fsk emitter");
+        return st ? st : clear_error();
+    }
     r.first_anchor = first - first % kAnchorInterval;
     const uint64_t segs = (first + count - r.first_anchor + kAnchorInterval - 1) / kAnchorInterval;
     if (segs > (1u << 30)) return set_error_fmt(RV_ERR_INVALID, "emitter: range too long");

@@ -62,10 +62,12 @@ T pick(std::mt19937_64& g, const T (&choices)[N]) {
 double db_to_power(double db) { return std::pow(10.0, db * 0.1); }
 double power_to_db(double p) { return 10.0 * std::log10(p); }
 
-// modulators.cpp:261-310 extent_for, for the built modes
-void extent(const rv_tone_emitter& e, int64_t& lo, int64_t& hi) {
+// modulators.cpp:261-310 extent_for, for the built modes; `baud` is FSK's
+// symbol rate (the nominal one when placing, the realised one for the truth)
+void extent(const rv_tone_emitter& e, int64_t& lo, int64_t& hi, double baud = 0.0) {
     int64_t half = 0;
     switch (e.modulation) {
+        case RV_EMITTER_FSK2: half = e.deviation + (int64_t)std::llround(baud * 0.5); break;
         case RV_EMITTER_CW: half = (int64_t)std::llround(1.5 * (e.words_per_minute / 1.2)); break;
         case RV_EMITTER_AM: half = e.tone_hz; break;
         case RV_EMITTER_NFM: half = e.deviation + e.tone_hz; break;
@@ -99,7 +101,8 @@ double nominal_power(const rv_tone_emitter& e) {
             return power * keyed / (double)el.back().stop;
         }
         case RV_EMITTER_AM: return power * (1.0 + e.modulation_index * e.modulation_index * 0.5);
-        case RV_EMITTER_NFM: return power;
+        case RV_EMITTER_NFM:
+        case RV_EMITTER_FSK2: return power;
         default: return e.tone2_hz != 0 ? 0.5 * power : power;
     }
 }
@@ -124,9 +127,9 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
     std::vector<int32_t> palette(p->palette, p->palette + p->palette_count);
     if (palette.empty()) palette = {0, 1, 2, 3, 4, 5, 6, 7};  // all_modulations()
     for (int32_t m : palette)
-        if (m < RV_EMITTER_CW || m > RV_EMITTER_LSB)
-            return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_scene_plan: modulation %d is not built (CW, AM, NFM, USB, LSB)",
-                                 m);
+        if (m < RV_EMITTER_CW || m > RV_EMITTER_FSK2)
+            return set_error_fmt(RV_ERR_UNSUPPORTED,
+                                 "rv_scene_plan: modulation %d is not built (CW, AM, NFM, USB, LSB, FSK2)", m);
     const int64_t window = p->duration_samples / (int64_t)p->bursts_per_emitter;
     if (p->bursts_per_emitter > 1 && window < 2)
         return set_error_fmt(RV_ERR_INVALID, "rv_scene_plan: the bursts do not fit in the scene");
@@ -145,6 +148,8 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
         e.modulation_index = 0.8, e.tone_hz = 1000, e.deviation = 5000;
         e.audio_low_hz = 300, e.audio_high_hz = 3000;
         e.words_per_minute = 20.0, e.rise_fall_ms = 5.0, e.message_gap_dots = 7.0;
+        e.symbol_rate = 1200.0, e.symbol_count = 256;
+        e.seed = payload_seed;
         strcpy(e.text, "CQ DE REVENANT");
         switch (e.modulation) {
             case RV_EMITTER_CW: {
@@ -165,6 +170,16 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
                 e.tone_hz = pick(g, kTone);
                 break;
             }
+            case RV_EMITTER_FSK2: {
+                static const int64_t kBaud[] = {1200, 2400, 4800, 9600};
+                static const double kIndex[] = {0.5, 1.0, 2.0};
+                const int64_t baud = pick(g, kBaud);
+                e.symbol_rate = (double)baud;
+                const double index = pick(g, kIndex);
+                e.deviation = (int64_t)std::llround(0.5 * index * (double)baud);
+                e.symbol_count = 256;
+                break;
+            }
             default: {
                 static const int64_t kTone[] = {700, 1000, 1500, 2200};
                 e.tone_hz = pick(g, kTone);
@@ -175,7 +190,7 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
         }
         // placed by the occupied band measured with the carrier at zero
         int64_t rlo, rhi;
-        extent(e, rlo, rhi);
+        extent(e, rlo, rhi, e.symbol_rate);
         const int64_t nyquist = p->rate / 2;
         const int64_t lowest = std::max(p->span_low_hz, -nyquist) - rlo;
         const int64_t highest = std::min(p->span_high_hz, nyquist) - rhi;
@@ -199,7 +214,14 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
         }
         // level_for with use_snr (wideband.cpp:206-235)
         int64_t lo, hi;
-        extent(e, lo, hi);
+        double realised = 0.0;
+        if (e.modulation == RV_EMITTER_FSK2) {  // the modulator's extent uses the symbol clock's rate
+            rv::SymbolClock clock;
+            if (!rv::build_symbol_clock(e.symbol_count, e.rate, e.symbol_rate, clock))
+                return set_error_fmt(RV_ERR_INVALID, "rv_scene_plan: FSK symbol clock unusable");
+            realised = clock.effective_rate(e.rate);
+        }
+        extent(e, lo, hi, realised);
         const double bandwidth = std::max(1.0, (double)(hi - lo));
         const double in_band = noise_power * bandwidth / (double)p->rate;
         if (noise_power <= 0.0) return set_error_fmt(RV_ERR_INVALID, "rv_scene_plan: SNR placement needs a noise floor");
