@@ -1205,8 +1205,10 @@ int32_t rv_scene_noise_draws(void* stream, uint64_t seed, uint64_t start, uint64
 #define RV_EMITTER_USB 3 /* siggen::Modulation::Usb: tone(s) as one exact rotation each */
 #define RV_EMITTER_LSB 4 /* siggen::Modulation::Lsb */
 #define RV_EMITTER_FSK2 5 /* siggen::Modulation::Fsk2: continuous-phase binary FSK of random bits */
+#define RV_EMITTER_BPSK 6 /* siggen::Modulation::Bpsk: root-raised-cosine pulses of random bits */
+#define RV_EMITTER_QPSK 7 /* siggen::Modulation::Qpsk: two bits a symbol, Gray mapped */
 typedef struct rv_tone_emitter {
-    int32_t modulation;      /* RV_EMITTER_CW, _AM, _NFM, _USB, _LSB or _FSK2 */
+    int32_t modulation;      /* RV_EMITTER_CW, _AM, _NFM, _USB, _LSB, _FSK2, _BPSK or _QPSK */
     int32_t reserved;
     int64_t rate;            /* samples per second */
     int64_t carrier_offset;  /* Hz from DC */
@@ -1222,9 +1224,11 @@ typedef struct rv_tone_emitter {
     double rise_fall_ms;     /* CW raised-cosine edges */
     double message_gap_dots; /* CW silence after the message */
     char text[64];           /* CW message, NUL-terminated */
-    uint64_t seed;           /* FSK payload seed (the random bits) */
-    double symbol_rate;      /* FSK baud */
-    uint64_t symbol_count;   /* FSK payload length in symbols */
+    uint64_t seed;           /* FSK and PSK payload seed (the random bits) */
+    double symbol_rate;      /* FSK and PSK baud */
+    uint64_t symbol_count;   /* FSK and PSK payload length in symbols */
+    double rolloff;          /* PSK root-raised-cosine rolloff, 0..1 */
+    uint64_t span_symbols;   /* PSK pulse span either side, in symbols (the reference's default is 8) */
 } rv_tone_emitter;
 /* Modulator::accumulate (modulators.cpp:1204-1323): adds `gain` times the
  * emitter's samples at emitter indices [first, first + count) to
@@ -1236,7 +1240,7 @@ int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* emitter, uint
 
 /* Scene::create's random population (core/dsp/synth/wideband.cpp:375-482;
  * RandomPopulation, wideband.h:211-236) for palettes of the built modes
- * (CW, AM, NFM, USB, LSB, FSK2): the emitters and their bursts, laid out from
+ * (all eight: CW, AM, NFM, USB, LSB, FSK2, BPSK, QPSK): the emitters and their bursts, laid out from
  * std::mt19937_64 draws exactly as the reference lays them out, sorted by
  * start. A scene is then rv_scene_noise plus, in this order, each burst's
  * rv_emitter_accumulate over its window at its gain. */
@@ -1253,7 +1257,7 @@ typedef struct rv_scene_population {
     double snr_max_db;
     double min_burst_seconds;
     double max_burst_seconds;
-    uint32_t palette_count;         /* 0 = every modulation (refused: FSK and PSK are not built) */
+    uint32_t palette_count;         /* 0 = every modulation */
     int32_t palette[8];             /* RV_EMITTER_* (siggen::Modulation values) */
 } rv_scene_population;
 

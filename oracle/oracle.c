@@ -2138,9 +2138,187 @@ static int32_t or_fsk_accumulate(const rv_tone_emitter* e, uint64_t first, uint6
     return ok();
 }
 
+/* BPSK/QPSK (modulators.cpp:172-196 root_raised_cosine, :885-1016 the
+ * tables, :1092-1156 the pulse lookup and envelope, :1443-1527 accumulate) */
+typedef struct {
+    uint64_t symbols, span;
+    int64_t cycle, stride;
+    int64_t* boundary;
+    double* boundary_d;
+    float *re, *im, *rrc;
+    double scale, base, limit, cycle_span, gain;
+} or_psk;
+
+static double or_rrc(double t, double beta) {
+    const double pi = 3.141592653589793238462643383279502884;
+    if (fabs(t) < 1e-9) return 1.0 + beta * (4.0 / pi - 1.0);
+    if (beta <= 0.0) return sin(pi * t) / (pi * t);
+    const double quarter = 1.0 / (4.0 * beta);
+    if (fabs(fabs(t) - quarter) < 1e-9) {
+        const double leading = (1.0 + 2.0 / pi) * sin(pi / (4.0 * beta));
+        const double trailing = (1.0 - 2.0 / pi) * cos(pi / (4.0 * beta));
+        return (beta / sqrt(2.0)) * (leading + trailing);
+    }
+    const double fbt = 4.0 * beta * t;
+    return (sin(pi * t * (1.0 - beta)) + fbt * cos(pi * t * (1.0 + beta))) / (pi * t * (1.0 - fbt * fbt));
+}
+
+static double or_rrc_tap(const or_psk* p, double position) {
+    if (position <= 0.0 || position >= p->limit) return 0.0;
+    const size_t lower = (size_t)position;
+    const double fraction = position - (double)lower;
+    const double a = (double)p->rrc[lower], b = (double)p->rrc[lower + 1];
+    return a + fraction * (b - a);
+}
+
+static uint64_t or_psk_index(const or_psk* p, int64_t position) {
+    uint64_t e = (uint64_t)((position * (int64_t)p->symbols) / p->cycle);
+    if (e >= p->symbols) e = p->symbols - 1;
+    while (e + 1 < p->symbols && p->boundary[e + 1] <= position) ++e;
+    while (e > 0 && p->boundary[e] > position) --e;
+    return e;
+}
+
+static void or_psk_env(const or_psk* p, int64_t pos_in_cycle, uint64_t symbol, float* er, float* ei) {
+    const int64_t symbols = (int64_t)p->symbols, span = (int64_t)p->span;
+    const double position = (double)pos_in_cycle;
+    double ip = 0.0, qd = 0.0;
+    for (int64_t off = -span; off <= span; ++off) {
+        int64_t w = (int64_t)symbol + off;
+        double shift = 0.0;
+        if (w < 0) w += symbols, shift = -p->cycle_span;
+        else if (w >= symbols) w -= symbols, shift = p->cycle_span;
+        const double tap = or_rrc_tap(p, (position - (p->boundary_d[w] + shift)) * p->scale + p->base);
+        if (tap == 0.0) continue;
+        ip += (double)p->re[w] * tap;
+        qd += (double)p->im[w] * tap;
+    }
+    *er = (float)(ip * p->gain);
+    *ei = (float)(qd * p->gain);
+}
+
+static void or_psk_env_at(const or_psk* p, uint64_t index, float* er, float* ei) {
+    const int64_t position = (int64_t)(index % (uint64_t)p->cycle);
+    or_psk_env(p, position, or_psk_index(p, position), er, ei);
+}
+
+static int32_t or_psk_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io) {
+    const double two_pi = 6.283185307179586476925286766559;
+    const int quad = e->modulation == RV_EMITTER_QPSK;
+    const uint64_t bps = quad ? 2 : 1, nbits = e->symbol_count * bps, symbols = e->symbol_count;
+    if (symbols == 0 || e->span_symbols >= symbols) return fail("psk: payload shorter than the pulse");
+    or_psk p;
+    memset(&p, 0, sizeof p);
+    p.symbols = symbols, p.span = e->span_symbols;
+    const double real = (double)symbols * ((double)e->rate / e->symbol_rate);
+    p.cycle = (int64_t)llround(real);
+    if (p.cycle < (int64_t)symbols * 2) return fail("psk: under two samples per symbol");
+    uint8_t* bits = (uint8_t*)malloc(nbits);
+    p.boundary = (int64_t*)malloc((symbols + 1) * sizeof(int64_t));
+    p.boundary_d = (double*)malloc(symbols * sizeof(double));
+    p.re = (float*)malloc(symbols * sizeof(float));
+    p.im = (float*)malloc(symbols * sizeof(float));
+    const size_t table = 2 * p.span * 512 + 1;
+    p.rrc = (float*)malloc(table * sizeof(float));
+    or_mt64* g = (or_mt64*)malloc(sizeof(or_mt64));
+    if (!bits || !p.boundary || !p.boundary_d || !p.re || !p.im || !p.rrc || !g) return fail("psk: out of memory");
+    or_mt64_seed(g, e->seed);
+    uint64_t word = 0;
+    unsigned remaining = 0;
+    for (uint64_t i = 0; i < nbits; ++i) {
+        if (remaining == 0) word = or_mt64_next(g), remaining = 64;
+        bits[i] = (uint8_t)(word & 1u);
+        word >>= 1;
+        --remaining;
+    }
+    for (uint64_t k = 0; k <= symbols; ++k) p.boundary[k] = ((int64_t)k * p.cycle) / (int64_t)symbols;
+    const double unit = 1.0 / sqrt(2.0);
+    for (uint64_t k = 0; k < symbols; ++k) {
+        p.boundary_d[k] = (double)p.boundary[k];
+        if (quad) {
+            p.re[k] = (float)(bits[2 * k] ? -unit : unit);
+            p.im[k] = (float)(bits[2 * k + 1] ? -unit : unit);
+        } else {
+            p.re[k] = bits[k] ? 1.0f : -1.0f;
+            p.im[k] = 0.0f;
+        }
+    }
+    for (size_t i = 0; i < table; ++i) p.rrc[i] = (float)or_rrc((double)i / 512.0 - (double)p.span, e->rolloff);
+    p.rrc[0] = 0.0f;
+    p.rrc[table - 1] = 0.0f;
+    const double sps = (double)p.cycle / (double)symbols;
+    p.scale = 512.0 / sps, p.base = (double)p.span * 512.0, p.limit = (double)(table - 1);
+    p.cycle_span = (double)p.cycle;
+    const int64_t reach = (int64_t)ceil((double)p.span * sps);
+    double energy = 0.0;
+    for (int64_t off = -reach; off <= reach; ++off) {
+        const double tap = or_rrc_tap(&p, ((double)off / sps) * 512.0 + p.base);
+        energy += tap * tap;
+    }
+    p.gain = energy > 0.0 ? sqrt(sps / energy) : 1.0;
+    p.stride = 1;
+    while (p.stride * 2 <= 1024 && (double)(p.stride * 2) <= sps / 1024.0) p.stride *= 2;
+    const double level = gain * e->amplitude;
+    const double cs = two_pi * (double)e->carrier_offset / (double)e->rate, sr = cos(cs), si = sin(cs);
+    const uint64_t end = first + count;
+    uint64_t index = first;
+    while (index < end) {
+        const uint64_t anchor = index - index % 1024u, stop = end < anchor + 1024u ? end : anchor + 1024u;
+        const double cp = e->initial_phase + or_exact_phase(e->carrier_offset, e->rate, anchor);
+        double cr = cos(cp), ci = sin(cp);
+        for (uint64_t k = anchor; k < index; ++k) {
+            const double a = cr * sr - ci * si, b = cr * si + ci * sr;
+            cr = a, ci = b;
+        }
+        float nr = 0, ni = 0, fr = 0, fi = 0;
+        int64_t position = 0;
+        uint64_t symbol = 0, node = 0;
+        const double inverse = 1.0 / (double)p.stride;
+        if (p.stride == 1) {
+            position = (int64_t)(index % (uint64_t)p.cycle);
+            symbol = or_psk_index(&p, position);
+        } else {
+            node = index - index % (uint64_t)p.stride;
+            or_psk_env_at(&p, node, &nr, &ni);
+            or_psk_env_at(&p, node + (uint64_t)p.stride, &fr, &fi);
+        }
+        for (; index < stop; ++index) {
+            double ip, qd;
+            if (p.stride == 1) {
+                float er, ei;
+                or_psk_env(&p, position, symbol, &er, &ei);
+                ip = (double)er, qd = (double)ei;
+            } else {
+                if (index >= node + (uint64_t)p.stride) {
+                    node += (uint64_t)p.stride;
+                    nr = fr, ni = fi;
+                    or_psk_env_at(&p, node + (uint64_t)p.stride, &fr, &fi);
+                }
+                const double w = (double)(index - node) * inverse;
+                ip = (double)nr + w * ((double)fr - (double)nr);
+                qd = (double)ni + w * ((double)fi - (double)ni);
+            }
+            const double re = ip * cr - qd * ci, im = ip * ci + qd * cr;
+            io[index - first].re = io[index - first].re + (float)(level * re);
+            io[index - first].im = io[index - first].im + (float)(level * im);
+            const double a = cr * sr - ci * si, b = cr * si + ci * sr;
+            cr = a, ci = b;
+            if (p.stride == 1) {
+                ++position;
+                if (position >= p.cycle) position = 0, symbol = 0;
+                else if (position >= p.boundary[symbol + 1]) ++symbol;
+            }
+        }
+    }
+    free(bits), free(p.boundary), free(p.boundary_d), free(p.re), free(p.im), free(p.rrc), free(g);
+    return ok();
+}
+
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io) {
     const double two_pi = 6.283185307179586476925286766559;
     if (e->modulation == RV_EMITTER_FSK2) return or_fsk_accumulate(e, first, count, gain, io);
+    if (e->modulation == RV_EMITTER_BPSK || e->modulation == RV_EMITTER_QPSK)
+        return or_psk_accumulate(e, first, count, gain, io);
     if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_LSB) return fail("emitter: modulation");
     or_cw_element* elements = NULL;
     uint32_t nel = 0;

@@ -57,6 +57,16 @@ void refsyn_set_fsk(std::uint64_t seed, double baud, std::uint64_t symbols) {
     g_symbols = symbols;
 }
 
+static double g_rolloff = 0.35;
+static std::uint64_t g_span = 8;
+
+// The PSK fields of the next spec (rolloff, pulse span; baud, count and seed
+// are the FSK setter's).
+void refsyn_set_psk(double rolloff, std::uint64_t span) {
+    g_rolloff = rolloff;
+    g_span = span;
+}
+
 // The CW fields of the next spec.
 void refsyn_set_cw(double wpm, double rise_ms, double gap_dots, const char* text) {
     g_wpm = wpm;
@@ -80,6 +90,10 @@ static siggen::ModulatorSpec tone_spec(int kind, std::int64_t rate, std::int64_t
     spec.ssb.tone2_hz = g_tone2;
     spec.ssb.audio_low_hz = g_low;
     spec.ssb.audio_high_hz = g_high;
+    spec.psk.symbol_rate = g_baud;
+    spec.psk.symbol_count = g_symbols;
+    spec.psk.rolloff = g_rolloff;
+    spec.psk.span_symbols = g_span;
     spec.fsk.symbol_rate = g_baud;
     spec.fsk.symbol_count = g_symbols;
     spec.fsk.deviation = deviation;

@@ -198,7 +198,7 @@ class CombParams(_S):
 
 
 DFT_FP16, DFT_BF16 = 0, 1
-EMITTER_CW, EMITTER_AM, EMITTER_NFM, EMITTER_USB, EMITTER_LSB, EMITTER_FSK2 = 0, 1, 2, 3, 4, 5
+EMITTER_CW, EMITTER_AM, EMITTER_NFM, EMITTER_USB, EMITTER_LSB, EMITTER_FSK2, EMITTER_BPSK, EMITTER_QPSK = range(8)
 
 
 class ToneEmitter(_S):
@@ -206,7 +206,7 @@ class ToneEmitter(_S):
                 ("deviation", I64), ("amplitude", F64), ("initial_phase", F64), ("modulation_index", F64),
                 ("tone2_hz", I64), ("audio_low_hz", I64), ("audio_high_hz", I64), ("words_per_minute", F64),
                 ("rise_fall_ms", F64), ("message_gap_dots", F64), ("text", C.c_char * 64), ("seed", U64),
-                ("symbol_rate", F64), ("symbol_count", U64)]
+                ("symbol_rate", F64), ("symbol_count", U64), ("rolloff", F64), ("span_symbols", U64)]
 
 
 class ScenePopulation(_S):

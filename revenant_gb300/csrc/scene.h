@@ -127,4 +127,92 @@ inline bool build_symbol_clock(uint64_t symbols, int64_t rate, double baud, Symb
     return true;
 }
 
+// A PSK emitter's tables (Modulator::create, modulators.cpp:885-1016): the
+// symbol constellation (BPSK bit 1 -> +1, QPSK first bit the in-phase sign,
+// second the quadrature, 1/sqrt 2 each), the root-raised-cosine table at 512
+// steps a symbol with its ends pinned to zero, the table scale and base, the
+// energy-normalising gain and the envelope's evaluation stride.
+struct PskPlan {
+    SymbolClock clock;
+    std::vector<float> sym_re, sym_im, rrc;
+    std::vector<double> boundary_d;
+    double scale = 0, base = 0, limit = 0, cycle_span = 0, gain = 1;
+    int64_t stride = 1;
+    uint64_t span = 0;
+};
+
+// modulators.cpp:172-196 root_raised_cosine
+inline double root_raised_cosine(double t, double beta) {
+    const double pi = 3.141592653589793238462643383279502884;
+    if (std::fabs(t) < 1e-9) return 1.0 + beta * (4.0 / pi - 1.0);
+    if (beta <= 0.0) return std::sin(pi * t) / (pi * t);
+    const double quarter = 1.0 / (4.0 * beta);
+    if (std::fabs(std::fabs(t) - quarter) < 1e-9) {
+        const double leading = (1.0 + 2.0 / pi) * std::sin(pi / (4.0 * beta));
+        const double trailing = (1.0 - 2.0 / pi) * std::cos(pi / (4.0 * beta));
+        return (beta / std::sqrt(2.0)) * (leading + trailing);
+    }
+    const double four_beta_t = 4.0 * beta * t;
+    const double numerator = std::sin(pi * t * (1.0 - beta)) + four_beta_t * std::cos(pi * t * (1.0 + beta));
+    const double denominator = pi * t * (1.0 - four_beta_t * four_beta_t);
+    return numerator / denominator;
+}
+
+// modulators.cpp:1092-1101 rrc_tap_at
+inline double rrc_tap_at(const float* rrc, double limit, double position) {
+    if (position <= 0.0 || position >= limit) return 0.0;
+    const size_t lower = (size_t)position;
+    const double fraction = position - (double)lower;
+    const double a = (double)rrc[lower], b = (double)rrc[lower + 1];
+    return a + fraction * (b - a);
+}
+
+inline bool psk_plan(bool quadrature, uint64_t symbol_count, uint64_t seed, int64_t rate, double baud, double rolloff,
+                     uint64_t span, PskPlan& p) {
+    const uint64_t bps = quadrature ? 2u : 1u;
+    const std::vector<uint8_t> bits = random_bits(symbol_count * bps, seed);
+    const uint64_t symbols = bits.size() / bps;
+    if (span >= symbols) return false;
+    if (!build_symbol_clock(symbols, rate, baud, p.clock)) return false;
+    const double unit = 1.0 / std::sqrt(2.0);
+    p.sym_re.resize(symbols);
+    p.sym_im.resize(symbols);
+    for (uint64_t k = 0; k < symbols; ++k) {
+        if (quadrature) {
+            p.sym_re[k] = (float)(bits[2 * k] != 0 ? -unit : unit);
+            p.sym_im[k] = (float)(bits[2 * k + 1] != 0 ? -unit : unit);
+        } else {
+            p.sym_re[k] = bits[k] != 0 ? 1.0f : -1.0f;
+            p.sym_im[k] = 0.0f;
+        }
+    }
+    const size_t steps = 512, table = 2 * span * steps + 1;
+    p.rrc.resize(table);
+    for (size_t i = 0; i < table; ++i) {
+        const double t = (double)i / (double)steps - (double)span;
+        p.rrc[i] = (float)root_raised_cosine(t, rolloff);
+    }
+    p.rrc.front() = 0.0f;
+    p.rrc.back() = 0.0f;
+    const double sps = (double)p.clock.cycle / (double)p.clock.symbols;
+    p.scale = (double)steps / sps;
+    p.base = (double)span * (double)steps;
+    p.limit = (double)(table - 1);
+    p.cycle_span = (double)p.clock.cycle;
+    p.boundary_d.resize(symbols);
+    for (uint64_t k = 0; k < symbols; ++k) p.boundary_d[k] = (double)p.clock.boundary[k];
+    const int64_t reach = (int64_t)std::ceil((double)span * sps);
+    double energy = 0.0;
+    for (int64_t offset = -reach; offset <= reach; ++offset) {
+        const double tap = rrc_tap_at(p.rrc.data(), p.limit, ((double)offset / sps) * (double)steps + p.base);
+        energy += tap * tap;
+    }
+    p.gain = energy > 0.0 ? std::sqrt(sps / energy) : 1.0;
+    p.stride = 1;
+    const double budget = sps / 1024.0;
+    while (p.stride * 2 <= 1024 && (double)(p.stride * 2) <= budget) p.stride *= 2;
+    p.span = span;
+    return true;
+}
+
 }  // namespace rv

@@ -329,6 +329,120 @@ bool fsk_segments(const rv_tone_emitter* e, uint64_t first, uint64_t end, std::v
     return true;
 }
 
+// ---- PSK (Modulator::accumulate_psk, modulators.cpp:1443-1527) ----------
+struct PskDev {
+    const float* sym_re;
+    const float* sym_im;
+    const float* rrc;
+    const double* boundary_d;
+    const int64_t* boundary;
+    double scale, base, limit, cycle_span, gain, level, c_step_re, c_step_im;
+    int64_t cycle, stride;
+    uint64_t symbols, span, first, count, first_anchor;
+};
+
+__device__ double d_rrc_tap(const PskDev& p, double position) {
+    if (position <= 0.0 || position >= p.limit) return 0.0;
+    const uint64_t lower = (uint64_t)position;
+    const double fraction = position - (double)lower;
+    const double a = (double)p.rrc[lower], b = (double)p.rrc[lower + 1];
+    return a + fraction * (b - a);
+}
+
+__device__ uint64_t d_index_at(const PskDev& p, int64_t position) {
+    uint64_t e = (uint64_t)((position * (int64_t)p.symbols) / p.cycle);
+    if (e >= p.symbols) e = p.symbols - 1;
+    while (e + 1 < p.symbols && p.boundary[e + 1] <= position) ++e;
+    while (e > 0 && p.boundary[e] > position) --e;
+    return e;
+}
+
+// modulators.cpp:1104-1151 psk_envelope: the pulses of the 2 span + 1 nearest
+// symbols, wrapped around the repeating payload, in offset order
+__device__ float2 d_psk_envelope(const PskDev& p, int64_t position_in_cycle, uint64_t symbol) {
+    const int64_t symbols = (int64_t)p.symbols, span = (int64_t)p.span;
+    const double position = (double)position_in_cycle;
+    double in_phase = 0.0, quadrature = 0.0;
+    for (int64_t offset = -span; offset <= span; ++offset) {
+        int64_t wrapped = (int64_t)symbol + offset;
+        double shift = 0.0;
+        if (wrapped < 0) {
+            wrapped += symbols;
+            shift = -p.cycle_span;
+        } else if (wrapped >= symbols) {
+            wrapped -= symbols;
+            shift = p.cycle_span;
+        }
+        const double centre = p.boundary_d[wrapped] + shift;
+        const double tap = d_rrc_tap(p, (position - centre) * p.scale + p.base);
+        if (tap == 0.0) continue;
+        in_phase += (double)p.sym_re[wrapped] * tap;
+        quadrature += (double)p.sym_im[wrapped] * tap;
+    }
+    return make_float2((float)(in_phase * p.gain), (float)(quadrature * p.gain));
+}
+
+__device__ float2 d_psk_envelope_at(const PskDev& p, uint64_t index) {
+    const int64_t position = (int64_t)(index % (uint64_t)p.cycle);
+    return d_psk_envelope(p, position, d_index_at(p, position));
+}
+
+__global__ void k_psk_emitter(PskDev p, const Anchor* __restrict__ anchors, uint32_t segments,
+                              float2* __restrict__ out) {
+    const uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seg >= segments) return;
+    const uint64_t anchor = p.first_anchor + (uint64_t)seg * kAnchorInterval;
+    const uint64_t end = p.first + p.count;
+    const uint64_t stop = anchor + kAnchorInterval < end ? anchor + kAnchorInterval : end;
+    uint64_t index = anchor > p.first ? anchor : p.first;
+    double cr = anchors[seg].cr, ci = anchors[seg].ci;
+    for (uint64_t k = anchor; k < index; ++k) {
+        const double ncr = cr * p.c_step_re - ci * p.c_step_im, nci = cr * p.c_step_im + ci * p.c_step_re;
+        cr = ncr, ci = nci;
+    }
+    if (p.stride == 1) {
+        int64_t position = (int64_t)(index % (uint64_t)p.cycle);
+        uint64_t symbol = d_index_at(p, position);
+        for (; index < stop; ++index) {
+            const float2 env = d_psk_envelope(p, position, symbol);
+            const double ip = (double)env.x, qd = (double)env.y;
+            const double re = ip * cr - qd * ci, im = ip * ci + qd * cr;
+            float2& o = out[index - p.first];
+            o = make_float2(o.x + (float)(p.level * re), o.y + (float)(p.level * im));
+            const double ncr = cr * p.c_step_re - ci * p.c_step_im, nci = cr * p.c_step_im + ci * p.c_step_re;
+            cr = ncr, ci = nci;
+            ++position;
+            if (position >= p.cycle) {
+                position = 0;
+                symbol = 0;
+            } else if (position >= p.boundary[symbol + 1]) {
+                ++symbol;
+            }
+        }
+        return;
+    }
+    // the envelope interpolated between evaluations at absolute multiples of the stride
+    const double inverse_stride = 1.0 / (double)p.stride;
+    uint64_t node = index - index % (uint64_t)p.stride;
+    float2 near_point = d_psk_envelope_at(p, node), far_point = d_psk_envelope_at(p, node + (uint64_t)p.stride);
+    for (; index < stop; ++index) {
+        if (index >= node + (uint64_t)p.stride) {
+            node += (uint64_t)p.stride;
+            near_point = far_point;
+            far_point = d_psk_envelope_at(p, node + (uint64_t)p.stride);
+        }
+        const double weight = (double)(index - node) * inverse_stride;
+        const double lr = (double)near_point.x, li = (double)near_point.y;
+        const double ip = lr + weight * ((double)far_point.x - lr);
+        const double qd = li + weight * ((double)far_point.y - li);
+        const double re = ip * cr - qd * ci, im = ip * ci + qd * cr;
+        float2& o = out[index - p.first];
+        o = make_float2(o.x + (float)(p.level * re), o.y + (float)(p.level * im));
+        const double ncr = cr * p.c_step_re - ci * p.c_step_im, nci = cr * p.c_step_im + ci * p.c_step_re;
+        cr = ncr, ci = nci;
+    }
+}
+
 }  // namespace
 }  // namespace rv
 
@@ -337,10 +451,10 @@ using namespace rv;
 extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e, uint64_t first, uint64_t count,
                                          double gain, rv_cf32* out, uint64_t out_len) {
     if (e == nullptr || (out == nullptr && count > 0)) return set_error_fmt(RV_ERR_INVALID, "emitter: NULL argument");
-    if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_FSK2)
-        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (CW, FSK2, or tone AM, NFM, USB, LSB)",
-                             e->modulation);
+    if (e->modulation < RV_EMITTER_CW || e->modulation > RV_EMITTER_QPSK)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter: modulation %d (a siggen::Modulation)", e->modulation);
     const bool fsk = e->modulation == RV_EMITTER_FSK2;
+    const bool psk = e->modulation == RV_EMITTER_BPSK || e->modulation == RV_EMITTER_QPSK;
     const bool ssb = e->modulation == RV_EMITTER_USB || e->modulation == RV_EMITTER_LSB;
     // modulators.cpp:310-332 validate_common, :334-343 the tone, :517-546 the mode
     if (e->rate <= 0 || e->rate > 1000000000) return set_error_fmt(RV_ERR_INVALID, "emitter: rate %lld", (long long)e->rate);
@@ -354,7 +468,12 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
         if ((llabs(e->carrier_offset) + e->deviation) * 2 > e->rate)
             return set_error_fmt(RV_ERR_INVALID, "emitter: FSK tones past Nyquist");
     }
-    if (!cw && !fsk && (e->tone_hz <= 0 || e->tone_hz * 2 >= e->rate))
+    if (psk) {  // modulators.cpp:612-631
+        if (!isfinite(e->symbol_rate) || e->symbol_rate <= 0.0 || !isfinite(e->rolloff) || e->rolloff < 0.0 ||
+            e->rolloff > 1.0 || e->span_symbols == 0 || e->symbol_count == 0)
+            return set_error_fmt(RV_ERR_INVALID, "emitter: PSK needs a positive baud, rolloff in [0, 1], span and count");
+    }
+    if (!cw && !fsk && !psk && (e->tone_hz <= 0 || e->tone_hz * 2 >= e->rate))
         return set_error_fmt(RV_ERR_INVALID, "emitter: tone past Nyquist");
     if (cw) {  // modulators.cpp:485-515
         if (!isfinite(e->words_per_minute) || e->words_per_minute <= 0.0 || !isfinite(e->rise_fall_ms) ||
@@ -427,6 +546,10 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
     }
     r.first_anchor = first - first % kAnchorInterval;
     const uint64_t segs = (first + count - r.first_anchor + kAnchorInterval - 1) / kAnchorInterval;
+    PskPlan plan;
+    if (psk && !psk_plan(e->modulation == RV_EMITTER_QPSK, e->symbol_count, e->seed, e->rate, e->symbol_rate,
+                         e->rolloff, e->span_symbols, plan))
+        return set_error_fmt(RV_ERR_INVALID, "emitter: PSK payload shorter than its pulse, or symbol clock unusable");
     if (segs > (1u << 30)) return set_error_fmt(RV_ERR_INVALID, "emitter: range too long");
     std::vector<Anchor> anchors(segs);
     for (uint64_t k = 0; k < segs; ++k) {
@@ -440,6 +563,39 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
     if (int32_t st = cuda_status(cudaMallocAsync(&d_anchors, segs * sizeof(Anchor), s), "emitter anchors")) return st;
     int32_t st = cuda_status(cudaMemcpyAsync(d_anchors, anchors.data(), segs * sizeof(Anchor), cudaMemcpyHostToDevice, s),
                              "emitter anchors");
+    // PSK tables in one device allocation: symbols (re, im), pulse, boundaries
+    void* d_psk = nullptr;
+    PskDev pd{};
+    if (st == RV_OK && psk) {
+        const size_t n = plan.clock.symbols, t = plan.rrc.size();
+        const size_t bytes = n * 4 * 2 + t * 4 + 64 + n * 8 + (n + 1) * 8 + 64;
+        st = cuda_status(cudaMallocAsync(&d_psk, bytes, s), "psk tables");
+        if (st == RV_OK) {
+            std::vector<uint8_t> blob(bytes, 0);
+            size_t at = 0;
+            auto put = [&](const void* src, size_t len) {
+                const size_t o = (at + 15) & ~size_t(15);
+                memcpy(blob.data() + o, src, len);
+                at = o + len;
+                return o;
+            };
+            const size_t o_re = put(plan.sym_re.data(), n * 4), o_im = put(plan.sym_im.data(), n * 4);
+            const size_t o_rrc = put(plan.rrc.data(), t * 4), o_bd = put(plan.boundary_d.data(), n * 8);
+            const size_t o_b = put(plan.clock.boundary.data(), (n + 1) * 8);
+            st = cuda_status(cudaMemcpyAsync(d_psk, blob.data(), at, cudaMemcpyHostToDevice, s), "psk tables");
+            cudaStreamSynchronize(s);  // the host blob goes out of scope
+            uint8_t* b = static_cast<uint8_t*>(d_psk);
+            pd.sym_re = reinterpret_cast<const float*>(b + o_re);
+            pd.sym_im = reinterpret_cast<const float*>(b + o_im);
+            pd.rrc = reinterpret_cast<const float*>(b + o_rrc);
+            pd.boundary_d = reinterpret_cast<const double*>(b + o_bd);
+            pd.boundary = reinterpret_cast<const int64_t*>(b + o_b);
+        }
+        pd.scale = plan.scale, pd.base = plan.base, pd.limit = plan.limit, pd.cycle_span = plan.cycle_span;
+        pd.gain = plan.gain, pd.level = r.level, pd.c_step_re = r.c_step_re, pd.c_step_im = r.c_step_im;
+        pd.cycle = plan.clock.cycle, pd.stride = plan.stride, pd.symbols = plan.clock.symbols, pd.span = plan.span;
+        pd.first = first, pd.count = count, pd.first_anchor = r.first_anchor;
+    }
     std::vector<CwElement> elements;
     CwElement* d_elements = nullptr;
     if (st == RV_OK && cw) {
@@ -452,7 +608,9 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
     }
     if (st == RV_OK) {
         const unsigned grid = (unsigned)((segs + 127) / 128);
-        if (cw)
+        if (psk)
+            k_psk_emitter<<<grid, 128, 0, s>>>(pd, d_anchors, (uint32_t)segs, reinterpret_cast<float2*>(out));
+        else if (cw)
             k_cw_emitter<<<grid, 128, 0, s>>>(r, d_anchors, (uint32_t)segs, d_elements, (uint32_t)elements.size(),
                                               e->rise_fall_ms * 0.001 * (double)e->rate,
                                               reinterpret_cast<float2*>(out));
@@ -461,6 +619,7 @@ extern "C" int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* e,
         st = cuda_status(cudaGetLastError(), "emitter");
     }
     if (d_elements) cudaFreeAsync(d_elements, s);
+    if (d_psk) cudaFreeAsync(d_psk, s);
     cudaFreeAsync(d_anchors, s);
     // the host table must outlive the copy
     if (st == RV_OK) st = cuda_status(cudaStreamSynchronize(s), "emitter");

@@ -1,7 +1,7 @@
 // The scene synthesiser's random population (siggen::Scene::create,
 // core/dsp/synth/wideband.cpp:375-482, with randomise_mode :124-177, the
 // uniform helpers :62-104, level_for :206-235 and add_bursts :243-266) for
-// palettes of the modes this library renders. Every draw comes from
+// every palette (all eight modulations are rendered). Every draw comes from
 // std::mt19937_64 in the reference's order, so the layout (modes, carriers,
 // levels, burst windows) is the reference's exactly; the bursts come back
 // sorted by start, the order the scene adds them in.
@@ -68,6 +68,8 @@ void extent(const rv_tone_emitter& e, int64_t& lo, int64_t& hi, double baud = 0.
     int64_t half = 0;
     switch (e.modulation) {
         case RV_EMITTER_FSK2: half = e.deviation + (int64_t)std::llround(baud * 0.5); break;
+        case RV_EMITTER_BPSK:
+        case RV_EMITTER_QPSK: half = (int64_t)std::llround((1.0 + e.rolloff) * baud * 0.5); break;
         case RV_EMITTER_CW: half = (int64_t)std::llround(1.5 * (e.words_per_minute / 1.2)); break;
         case RV_EMITTER_AM: half = e.tone_hz; break;
         case RV_EMITTER_NFM: half = e.deviation + e.tone_hz; break;
@@ -102,7 +104,9 @@ double nominal_power(const rv_tone_emitter& e) {
         }
         case RV_EMITTER_AM: return power * (1.0 + e.modulation_index * e.modulation_index * 0.5);
         case RV_EMITTER_NFM:
-        case RV_EMITTER_FSK2: return power;
+        case RV_EMITTER_FSK2:
+        case RV_EMITTER_BPSK:
+        case RV_EMITTER_QPSK: return power;
         default: return e.tone2_hz != 0 ? 0.5 * power : power;
     }
 }
@@ -127,9 +131,8 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
     std::vector<int32_t> palette(p->palette, p->palette + p->palette_count);
     if (palette.empty()) palette = {0, 1, 2, 3, 4, 5, 6, 7};  // all_modulations()
     for (int32_t m : palette)
-        if (m < RV_EMITTER_CW || m > RV_EMITTER_FSK2)
-            return set_error_fmt(RV_ERR_UNSUPPORTED,
-                                 "rv_scene_plan: modulation %d is not built (CW, AM, NFM, USB, LSB, FSK2)", m);
+        if (m < RV_EMITTER_CW || m > RV_EMITTER_QPSK)
+            return set_error_fmt(RV_ERR_INVALID, "rv_scene_plan: modulation %d is not a siggen::Modulation", m);
     const int64_t window = p->duration_samples / (int64_t)p->bursts_per_emitter;
     if (p->bursts_per_emitter > 1 && window < 2)
         return set_error_fmt(RV_ERR_INVALID, "rv_scene_plan: the bursts do not fit in the scene");
@@ -148,7 +151,7 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
         e.modulation_index = 0.8, e.tone_hz = 1000, e.deviation = 5000;
         e.audio_low_hz = 300, e.audio_high_hz = 3000;
         e.words_per_minute = 20.0, e.rise_fall_ms = 5.0, e.message_gap_dots = 7.0;
-        e.symbol_rate = 1200.0, e.symbol_count = 256;
+        e.symbol_rate = 1200.0, e.symbol_count = 256, e.rolloff = 0.35, e.span_symbols = 8;
         e.seed = payload_seed;
         strcpy(e.text, "CQ DE REVENANT");
         switch (e.modulation) {
@@ -177,6 +180,15 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
                 e.symbol_rate = (double)baud;
                 const double index = pick(g, kIndex);
                 e.deviation = (int64_t)std::llround(0.5 * index * (double)baud);
+                e.symbol_count = 256;
+                break;
+            }
+            case RV_EMITTER_BPSK:
+            case RV_EMITTER_QPSK: {
+                static const int64_t kBaud[] = {1200, 2400, 4800, 9600, 19200};
+                static const double kRolloff[] = {0.2, 0.35, 0.5};
+                e.symbol_rate = (double)pick(g, kBaud);
+                e.rolloff = pick(g, kRolloff);
                 e.symbol_count = 256;
                 break;
             }
@@ -215,7 +227,8 @@ extern "C" int32_t rv_scene_plan(const rv_scene_population* p, rv_scene_burst* o
         // level_for with use_snr (wideband.cpp:206-235)
         int64_t lo, hi;
         double realised = 0.0;
-        if (e.modulation == RV_EMITTER_FSK2) {  // the modulator's extent uses the symbol clock's rate
+        if (e.modulation == RV_EMITTER_FSK2 || e.modulation == RV_EMITTER_BPSK ||
+            e.modulation == RV_EMITTER_QPSK) {  // the modulator's extent uses the symbol clock's rate
             rv::SymbolClock clock;
             if (!rv::build_symbol_clock(e.symbol_count, e.rate, e.symbol_rate, clock))
                 return set_error_fmt(RV_ERR_INVALID, "rv_scene_plan: FSK symbol clock unusable");

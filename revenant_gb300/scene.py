@@ -1,5 +1,5 @@
 """Host mirror of the scene synthesiser (siggen::Scene, core/dsp/synth/
-wideband.h) for the modes this library renders.
+wideband.h): its noise field, its eight modulations and its random population.
 
 ``plan(population)`` lays out a random population's bursts as the reference
 does (rv_scene_plan); ``render(device, population, start, count)`` fills a
@@ -15,7 +15,7 @@ from .library import check, lib
 
 
 def population(seed, rate, duration, noise_dbfs=-60.0, emitters=8, bursts=1, span=(-1_000_000, 1_000_000),
-               snr=(5.0, 35.0), burst_seconds=(0.05, 2.0), palette=(0, 1, 2, 3, 4)):
+               snr=(5.0, 35.0), burst_seconds=(0.05, 2.0), palette=()):
     p = abi.ScenePopulation()
     p.seed, p.rate, p.duration_samples, p.noise_dbfs = seed, rate, duration, noise_dbfs
     p.emitter_count, p.bursts_per_emitter = emitters, bursts

@@ -196,7 +196,17 @@ TONES += [dict(modulation=5, rate=48_000, carrier_offset=-5_000, tone_hz=0, devi
                initial_phase=1.3, modulation_index=0.0, seed=12345, symbol_rate=2400.0, symbol_count=64),
           dict(modulation=5, rate=2_400_000, carrier_offset=300_000, tone_hz=0, deviation=9600, amplitude=1.0,
                initial_phase=0.0, modulation_index=0.0, seed=2**64 - 3, symbol_rate=9600.0, symbol_count=256)]
-TONE_IDS = ["am", "nfm", "am-edge", "wide-nfm", "usb", "lsb-two-tone", "cw", "cw-hard", "fsk", "fsk-fast"]
+TONES += [dict(modulation=6, rate=48_000, carrier_offset=4_000, tone_hz=0, deviation=0, amplitude=0.7,
+               initial_phase=0.4, modulation_index=0.0, seed=99, symbol_rate=2400.0, symbol_count=64, rolloff=0.35,
+               span_symbols=8),
+          dict(modulation=7, rate=20_000_000, carrier_offset=-2_000_000, tone_hz=0, deviation=0, amplitude=1.0,
+               initial_phase=2.2, modulation_index=0.0, seed=7, symbol_rate=1200.0, symbol_count=256, rolloff=0.2,
+               span_symbols=8),
+          dict(modulation=7, rate=2_400_000, carrier_offset=50_000, tone_hz=0, deviation=0, amplitude=0.5,
+               initial_phase=0.0, modulation_index=0.0, seed=31, symbol_rate=19200.0, symbol_count=256, rolloff=0.5,
+               span_symbols=8)]
+TONE_IDS = ["am", "nfm", "am-edge", "wide-nfm", "usb", "lsb-two-tone", "cw", "cw-hard", "fsk", "fsk-fast", "bpsk",
+            "qpsk-strided", "qpsk"]
 
 
 def tone(d):
@@ -229,11 +239,13 @@ def ref_args(synref, d=None):
     synref.refsyn_set_ssb.argtypes = [C.c_int64, C.c_int64, C.c_int64]
     synref.refsyn_set_cw.argtypes = [C.c_double, C.c_double, C.c_double, C.c_char_p]
     synref.refsyn_set_fsk.argtypes = [C.c_uint64, C.c_double, C.c_uint64]
+    synref.refsyn_set_psk.argtypes = [C.c_double, C.c_uint64]
     if d is not None:
         synref.refsyn_set_ssb(d.get("tone2_hz", 0), d.get("audio_low_hz", 300), d.get("audio_high_hz", 3000))
         synref.refsyn_set_cw(d.get("words_per_minute", 20.0), d.get("rise_fall_ms", 5.0),
                              d.get("message_gap_dots", 7.0), d.get("text", b"CQ DE REVENANT"))
         synref.refsyn_set_fsk(d.get("seed", 0), d.get("symbol_rate", 1200.0), d.get("symbol_count", 256))
+        synref.refsyn_set_psk(d.get("rolloff", 0.35), d.get("span_symbols", 8))
     synref.refsyn_tone.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double,
                                    C.c_double, C.c_uint64, C.c_uint64, C.c_double, C.c_void_p]
     synref.refsyn_scene_tone.argtypes = [C.c_uint64, C.c_int64, C.c_double, C.c_int, C.c_int64, C.c_int64, C.c_int64,
@@ -259,8 +271,8 @@ def test_oracle_tone_emitter_matches_reference(synref, d):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (first, gain)
 
 
-@pytest.mark.parametrize("d", [TONES[0], TONES[1], TONES[5], TONES[6], TONES[8]],
-                         ids=["am", "nfm", "lsb-two-tone", "cw", "fsk"])
+@pytest.mark.parametrize("d", [TONES[0], TONES[1], TONES[5], TONES[6], TONES[8], TONES[11]],
+                         ids=["am", "nfm", "lsb-two-tone", "cw", "fsk", "qpsk"])
 def test_oracle_scene_with_emitter_matches_reference(synref, d):
     s = ref_args(synref, d)
     seed, dbfs, on, off, start, count = 21, -50.0, 5000, 20_000, 3000, 20_000
@@ -281,7 +293,7 @@ def test_gpu_tone_emitter_matches_oracle(gpu, d):
             lib().rv_last_error()
         got = buf.download(np.float32, (count, 2))
         want = ora_tone(d, first, count, gain, io)
-        if d["modulation"] in (1, 3, 4, 5):  # AM, SSB, FSK: anchors from the C library, the rest + and *
+        if d["modulation"] in (1, 3, 4, 5, 6, 7):  # anchors and tables from the C library, the rest + and *
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), first
         else:  # NFM, CW: CUDA's FP64 cos/sin of the deviation, or of the keying edges
             n = check_close(got, want)
@@ -307,7 +319,8 @@ def test_gpu_scene_with_emitter_matches_oracle(gpu):
 
 def test_emitter_rejects_bad_specs(rv):
     one = np.zeros(4, np.float32)
-    for bad in (dict(modulation=-1), dict(modulation=0, words_per_minute=20.0, rise_fall_ms=5.0, text=b"#"),
+    for bad in (dict(modulation=-1), dict(modulation=8), dict(modulation=6, symbol_rate=1200.0, symbol_count=4,
+                                                               rolloff=0.35, span_symbols=8), dict(modulation=0, words_per_minute=20.0, rise_fall_ms=5.0, text=b"#"),
                 dict(modulation=0, words_per_minute=20.0, rise_fall_ms=5.0, text=b"   "),
                 dict(modulation=0, words_per_minute=2e6, rise_fall_ms=5.0, text=b"E"), dict(tone_hz=0), dict(tone_hz=1_200_000), dict(carrier_offset=1_300_000),
                 dict(amplitude=-1.0), dict(modulation=2, deviation=0), dict(rate=0), dict(modulation=5),
@@ -325,7 +338,7 @@ POPULATIONS = [dict(seed=5, rate=2_400_000, duration=0, noise_dbfs=-60.0, emitte
                     span=(-1_000_000, 1_000_000), snr=(5.0, 35.0), burst_seconds=(0.05, 2.0), palette=(0, 1, 2, 3, 4)),
                dict(seed=77, rate=20_000_000, duration=4_000_000, noise_dbfs=-70.0, emitters=20, bursts=3,
                     span=(-9_000_000, 9_000_000), snr=(-5.0, 30.0), burst_seconds=(0.001, 0.05),
-                    palette=(1, 2, 3, 4, 5)),
+                    palette=()),
                dict(seed=2, rate=48_000, duration=200_000, noise_dbfs=-50.0, emitters=4, bursts=2,
                     span=(-20_000, 20_000), snr=(10.0, 20.0), burst_seconds=(0.5, 2.0), palette=(0,))]
 
@@ -386,11 +399,12 @@ def test_oracle_random_scene_matches_reference_render(synref, d, start, count):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
-def test_plan_refuses_unbuilt_modes(rv):
+def test_plan_refuses_bad_populations(rv):
     from revenant_gb300 import abi, scene
-    pop = scene.population(**dict(POPULATIONS[0], palette=(1, 6)))  # BPSK is not built
     n = C.c_uint32()
-    assert rv.rv_scene_plan(C.byref(pop), None, 0, C.byref(n)) == abi.RV_ERR_UNSUPPORTED
+    for bad in (dict(palette=(1, 9)), dict(span=(5, 5)), dict(bursts=0), dict(snr=(10.0, 5.0))):
+        pop = scene.population(**dict(POPULATIONS[0], **bad))
+        assert rv.rv_scene_plan(C.byref(pop), None, 0, C.byref(n)) == abi.RV_ERR_INVALID, bad
 
 
 @pytest.mark.gpu
