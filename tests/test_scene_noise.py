@@ -1,22 +1,25 @@
-"""a16's noise field: siggen::Scene::fill_noise (core/dsp/synth/wideband.cpp
-:535-580) on the GPU.
+"""a16, the scene synthesiser (core/dsp/synth/wideband.cpp, modulators.cpp)
+on the GPU: its noise field (Scene::fill_noise), its eight modulations
+(Modulator::accumulate for CW, tone AM, NFM, USB, LSB, FSK2, BPSK, QPSK) and
+its random population (Scene::create's layout, rv_scene_plan).
 
-The oracle (or_scene_noise, oracle/oracle.c) restates it: 4096-sample noise
-blocks, each an MT19937-64 seeded from derive_stream_seed(seed ^ block), two
-draws per sample, Box-Muller in FP64 with the C library's functions. It is
-pinned against the reference's own Scene (oracle/_ref/libsynref.so) bit for
-bit on this machine, its draws against libstdc++'s std::mt19937_64, and
-against tests/golden/scene_noise.npz (made by tests/golden/make_scene_noise.py)
-everywhere.
+The oracle (oracle/oracle.c: or_scene_noise, or_emitter_accumulate) restates
+them in C with the C library's transcendentals and is pinned against the
+reference's own Scene and Modulator (oracle/_ref/libsynref.so) bit for bit on
+this machine, the noise draws against libstdc++'s std::mt19937_64, and the
+noise against tests/golden/scene_noise.npz (made by
+tests/golden/make_scene_noise.py) everywhere. The layout is pinned against
+the reference's truth table field for field.
 
-On the GPU (rv_scene_noise, rv_scene_noise_draws):
-  * the draws equal the oracle's bit for bit (integers);
-  * the samples equal the oracle's bit for bit except where CUDA's FP64 log,
-    sine or cosine rounds differently from the C library's and that moves the
-    FP32 result: at most MAX_MISMATCH_FRACTION of the samples, each within
-    ULP_TOLERANCE FP32 ulp;
-  * the field is a function of the absolute range: a render in pieces equals
-    the render in one piece, bit for bit, at 2^24 samples.
+On the GPU:
+  * the noise draws equal the oracle's bit for bit (integers);
+  * AM, SSB, FSK2 and PSK, whose anchors and tables come from the host, equal
+    the oracle bit for bit; the noise, NFM and CW, which take CUDA's FP64
+    log, sine or cosine per sample, equal it except where that rounding
+    moves the FP32 result: at most MAX_MISMATCH_FRACTION of the samples, each
+    within ULP_TOLERANCE FP32 ulp;
+  * the noise field is a function of the absolute range: a render in pieces
+    equals the render in one piece, bit for bit, at 2^24 samples.
 """
 import ctypes as C
 import os
