@@ -1237,6 +1237,14 @@ typedef struct rv_tone_emitter {
  * table is copied first). */
 int32_t rv_emitter_accumulate(void* stream, const rv_tone_emitter* emitter, uint64_t first, uint64_t count,
                               double gain, rv_cf32* out_dev, uint64_t out_len);
+/* The same for an AM, NFM, USB or LSB emitter modulated by supplied audio
+ * (ModulatorSpec::audio: one value per sample at the emitter's rate, zero
+ * past its end; modulators.cpp:1048-1053, :756-781 the FM phase integral,
+ * :807-836 and :1169-1193 the Hilbert phasing network of `hilbert_taps`
+ * (odd, >= 3) taps for SSB). */
+int32_t rv_emitter_accumulate_audio(void* stream, const rv_tone_emitter* emitter, const float* audio,
+                                    uint64_t audio_len, uint32_t hilbert_taps, uint64_t first, uint64_t count,
+                                    double gain, rv_cf32* out_dev, uint64_t out_len);
 
 /* Scene::create's random population (core/dsp/synth/wideband.cpp:375-482;
  * RandomPopulation, wideband.h:211-236) for palettes of the built modes

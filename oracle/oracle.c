@@ -2391,3 +2391,77 @@ int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t
     free(elements);
     return ok();
 }
+
+/* supplied audio (modulators.cpp:1048-1053 audio_at, :756-781 the FM phase
+ * integral, :807-836 and :1169-1193 the Hilbert phasing network, with the
+ * accumulate functions' audio paths) */
+int32_t or_emitter_accumulate_audio(const rv_tone_emitter* e, const float* audio, uint64_t len, uint32_t taps,
+                                    uint64_t first, uint64_t count, double gain, rv_cf32* io) {
+    const double two_pi = 6.283185307179586476925286766559, pi = 3.141592653589793238462643383279502884;
+    const int m = e->modulation;
+    const double rate = (double)e->rate, level = gain * e->amplitude;
+    double* phase = NULL;
+    double* hilbert = NULL;
+    if (m == RV_EMITTER_NFM) {
+        phase = (double*)calloc(len + 1, sizeof(double));
+        const double scale = two_pi * (double)e->deviation / rate;
+        double acc = 0.0;
+        for (uint64_t i = 0; i < len; ++i) {
+            acc += scale * (double)audio[i];
+            acc = fmod(acc, two_pi);
+            phase[i + 1] = acc;
+        }
+    }
+    if (m == RV_EMITTER_USB || m == RV_EMITTER_LSB) {
+        hilbert = (double*)calloc(taps, sizeof(double));
+        const int64_t half = (int64_t)(taps / 2);
+        for (uint32_t i = 0; i < taps; ++i) {
+            const int64_t lag = (int64_t)i - half;
+            if (lag == 0 || lag % 2 == 0) continue;
+            const double position = (double)i / (double)(taps - 1);
+            hilbert[i] = (2.0 / (pi * (double)lag)) *
+                         (0.42 - 0.5 * cos(two_pi * position) + 0.08 * cos(2.0 * two_pi * position));
+        }
+    }
+    const double cs = two_pi * (double)e->carrier_offset / rate, sr = cos(cs), si = sin(cs);
+    const double sense = m == RV_EMITTER_LSB ? -1.0 : 1.0;
+    const uint64_t end = first + count;
+    uint64_t index = first;
+    while (index < end) {
+        const uint64_t anchor = index - index % 1024u, stop = end < anchor + 1024u ? end : anchor + 1024u;
+        const double cp = e->initial_phase + or_exact_phase(e->carrier_offset, e->rate, anchor);
+        double cr = cos(cp), ci = sin(cp);
+        for (uint64_t k = anchor; k < stop; ++k) {
+            if (k >= index) {
+                double re, im;
+                const double a = k < len ? (double)audio[k] : 0.0;
+                if (m == RV_EMITTER_AM) {
+                    const double envelope = level * (1.0 + e->modulation_index * a);
+                    re = envelope * cr, im = envelope * ci;
+                } else if (m == RV_EMITTER_NFM) {
+                    const double dev = phase[k < len ? k : len];
+                    const double c = cos(dev), s = sin(dev);
+                    re = level * (cr * c - ci * s), im = level * (cr * s + ci * c);
+                } else {
+                    const int64_t half = (int64_t)(taps / 2);
+                    double total = 0.0;
+                    for (uint64_t i = (half % 2) == 0 ? 1u : 0u; i < taps; i += 2) {
+                        const int64_t source = (int64_t)k + half - (int64_t)i;
+                        if (source < 0) continue;
+                        total += hilbert[i] * ((uint64_t)source < len ? (double)audio[source] : 0.0);
+                    }
+                    const double q = sense * total;
+                    re = level * (a * cr - q * ci), im = level * (a * ci + q * cr);
+                }
+                io[k - first].re = io[k - first].re + (float)re;
+                io[k - first].im = io[k - first].im + (float)im;
+            }
+            const double ncr = cr * sr - ci * si, nci = cr * si + ci * sr;
+            cr = ncr, ci = nci;
+        }
+        index = stop;
+    }
+    free(phase);
+    free(hilbert);
+    return ok();
+}

@@ -36,6 +36,8 @@ int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t cou
 int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
 /* tone emitters: Modulator::accumulate_am / _nfm / _ssb (core/dsp/synth/modulators.cpp:1244-1366) */
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io);
+int32_t or_emitter_accumulate_audio(const rv_tone_emitter* e, const float* audio, uint64_t len, uint32_t taps,
+                                    uint64_t first, uint64_t count, double gain, rv_cf32* io);
 #endif
 
 const char* or_last_error(void);
@@ -99,6 +101,8 @@ int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t cou
 int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
 /* tone emitters: Modulator::accumulate_am / _nfm / _ssb (core/dsp/synth/modulators.cpp:1244-1366) */
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io);
+int32_t or_emitter_accumulate_audio(const rv_tone_emitter* e, const float* audio, uint64_t len, uint32_t taps,
+                                    uint64_t first, uint64_t count, double gain, rv_cf32* io);
 #endif
 
 
@@ -163,4 +167,6 @@ int32_t or_scene_noise(uint64_t seed, double sigma, uint64_t start, uint64_t cou
 int32_t or_scene_noise_draws(uint64_t seed, uint64_t start, uint64_t count, uint64_t* draws);
 /* tone emitters: Modulator::accumulate_am / _nfm / _ssb (core/dsp/synth/modulators.cpp:1244-1366) */
 int32_t or_emitter_accumulate(const rv_tone_emitter* e, uint64_t first, uint64_t count, double gain, rv_cf32* io);
+int32_t or_emitter_accumulate_audio(const rv_tone_emitter* e, const float* audio, uint64_t len, uint32_t taps,
+                                    uint64_t first, uint64_t count, double gain, rv_cf32* io);
 #endif

@@ -210,6 +210,30 @@ int refsyn_random_scene(std::uint64_t seed, std::int64_t rate, std::int64_t dura
     return 0;
 }
 
+// Modulator::accumulate of an AM, NFM, USB or LSB emitter modulated by
+// supplied audio (ModulatorSpec::audio), SSB through a `taps`-tap Hilbert
+// network over the [low, high] Hz audio passband.
+int refsyn_audio_emitter(int kind, std::int64_t rate, std::int64_t carrier, std::int64_t deviation, double amplitude,
+                         double phase, double index, const float* audio, std::uint64_t len, std::uint32_t taps,
+                         std::int64_t low, std::int64_t high, std::uint64_t first, std::uint64_t count, double gain,
+                         float* io) {
+    siggen::ModulatorSpec spec = tone_spec(kind, rate, carrier, 1000, deviation, amplitude, phase, index);
+    spec.audio.assign(audio, audio + len);
+    spec.ssb.hilbert_taps = taps;
+    spec.ssb.audio_low_hz = low;
+    spec.ssb.audio_high_hz = high;
+    auto m = siggen::Modulator::create(spec);
+    if (!m) return -1;
+    std::vector<std::complex<float>> buf(count);
+    for (std::uint64_t i = 0; i < count; ++i) buf[i] = {io[2 * i], io[2 * i + 1]};
+    m->accumulate(first, std::span<std::complex<float>>(buf), gain);
+    for (std::uint64_t i = 0; i < count; ++i) {
+        io[2 * i] = buf[i].real();
+        io[2 * i + 1] = buf[i].imag();
+    }
+    return 0;
+}
+
 // The libstdc++ std::mt19937_64 stream of one noise block, for pinning the
 // GPU generator's draws: the block's seed is given (the reference derives it
 // with derive_stream_seed, which the tests restate).

@@ -443,6 +443,61 @@ __global__ void k_psk_emitter(PskDev p, const Anchor* __restrict__ anchors, uint
     }
 }
 
+// ---- supplied audio (modulators.cpp:1244-1392 with spec.audio) -----------
+struct AudioRun {
+    const float* audio;      // AM and SSB: the audio; NFM: unused
+    const double* phase;     // NFM: the FM phase integral, audio_len + 1 values
+    const double* hilbert;   // SSB: the transformer's taps
+    uint64_t audio_len, taps, first, count, first_anchor;
+    double level, index, sense, c_step_re, c_step_im;
+    int32_t kind;
+};
+
+__device__ __forceinline__ double audio_at(const AudioRun& r, uint64_t i) {
+    return i < r.audio_len ? (double)r.audio[i] : 0.0;
+}
+
+__global__ void k_audio_emitter(AudioRun r, const Anchor* __restrict__ anchors, uint32_t segments,
+                                float2* __restrict__ out) {
+    const uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seg >= segments) return;
+    const uint64_t anchor = r.first_anchor + (uint64_t)seg * kAnchorInterval;
+    const uint64_t end = r.first + r.count;
+    const uint64_t stop = anchor + kAnchorInterval < end ? anchor + kAnchorInterval : end;
+    double cr = anchors[seg].cr, ci = anchors[seg].ci;
+    for (uint64_t index = anchor; index < stop; ++index) {
+        if (index >= r.first) {
+            float2 add;
+            if (r.kind == RV_EMITTER_AM) {
+                const double envelope = r.level * (1.0 + r.index * audio_at(r, index));
+                add = make_float2((float)(envelope * cr), (float)(envelope * ci));
+            } else if (r.kind == RV_EMITTER_NFM) {
+                const uint64_t last = r.audio_len;  // phase has audio_len + 1 values
+                const double deviation = r.phase[index < last ? index : last];
+                const double cosine = cos(deviation), sine = sin(deviation);
+                const double re = cr * cosine - ci * sine, im = cr * sine + ci * cosine;
+                add = make_float2((float)(r.level * re), (float)(r.level * im));
+            } else {
+                // hilbert_at: odd lags only, ascending tap index
+                const int64_t half = (int64_t)(r.taps / 2), centre = (int64_t)index;
+                double total = 0.0;
+                for (uint64_t i = (half % 2) == 0 ? 1u : 0u; i < r.taps; i += 2) {
+                    const int64_t source = centre + half - (int64_t)i;
+                    if (source < 0) continue;
+                    total += r.hilbert[i] * audio_at(r, (uint64_t)source);
+                }
+                const double in_phase = audio_at(r, index), quadrature = r.sense * total;
+                const double re = in_phase * cr - quadrature * ci, im = in_phase * ci + quadrature * cr;
+                add = make_float2((float)(r.level * re), (float)(r.level * im));
+            }
+            float2& o = out[index - r.first];
+            o = make_float2(o.x + add.x, o.y + add.y);
+        }
+        const double ncr = cr * r.c_step_re - ci * r.c_step_im, nci = cr * r.c_step_im + ci * r.c_step_re;
+        cr = ncr, ci = nci;
+    }
+}
+
 }  // namespace
 }  // namespace rv
 
@@ -654,4 +709,93 @@ extern "C" int32_t rv_scene_noise_draws(void* stream, uint64_t seed, uint64_t st
     if (int32_t st = launch(reinterpret_cast<cudaStream_t>(stream), seed, 0.0, start, count, nullptr, draws))
         return st;
     return clear_error();
+}
+
+extern "C" int32_t rv_emitter_accumulate_audio(void* stream, const rv_tone_emitter* e, const float* audio,
+                                               uint64_t audio_len, uint32_t hilbert_taps, uint64_t first,
+                                               uint64_t count, double gain, rv_cf32* out, uint64_t out_len) {
+    if (e == nullptr || (audio == nullptr && audio_len > 0) || (out == nullptr && count > 0))
+        return set_error_fmt(RV_ERR_INVALID, "emitter audio: NULL argument");
+    const int32_t m = e->modulation;
+    if (m != RV_EMITTER_AM && m != RV_EMITTER_NFM && m != RV_EMITTER_USB && m != RV_EMITTER_LSB)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "emitter audio: AM, NFM, USB or LSB");
+    if (e->rate <= 0 || e->rate > 1000000000 || !isfinite(e->amplitude) || e->amplitude < 0.0 ||
+        !isfinite(e->initial_phase) || llabs(e->carrier_offset) * 2 > e->rate)
+        return set_error_fmt(RV_ERR_INVALID, "emitter audio: rate, amplitude, phase or carrier");
+    if (m == RV_EMITTER_AM && (!isfinite(e->modulation_index) || e->modulation_index < 0.0))
+        return set_error_fmt(RV_ERR_INVALID, "emitter audio: AM modulation index");
+    if (m == RV_EMITTER_NFM && e->deviation <= 0) return set_error_fmt(RV_ERR_INVALID, "emitter audio: NFM deviation");
+    const bool ssb = m == RV_EMITTER_USB || m == RV_EMITTER_LSB;
+    if (ssb) {  // modulators.cpp:550-552, :570-587
+        if (e->audio_low_hz <= 0 || e->audio_high_hz <= e->audio_low_hz)
+            return set_error_fmt(RV_ERR_INVALID, "emitter audio: SSB audio passband must be a positive increasing range");
+        if (hilbert_taps < 3 || hilbert_taps % 2 == 0)
+            return set_error_fmt(RV_ERR_INVALID, "emitter audio: Hilbert transformer length must be odd and >= 3");
+        if ((double)e->audio_low_hz < (double)e->rate / (double)hilbert_taps)
+            return set_error_fmt(RV_ERR_INVALID, "emitter audio: the Hilbert transformer does not reach the passband");
+    }
+    if (out_len < count) return set_error_fmt(RV_ERR_INVALID, "emitter audio: output too short");
+    if (count == 0) return clear_error();
+    const double rate = (double)e->rate;
+    AudioRun r{};
+    r.kind = m, r.level = gain * e->amplitude, r.index = e->modulation_index;
+    r.sense = m == RV_EMITTER_LSB ? -1.0 : 1.0;
+    r.audio_len = audio_len, r.taps = hilbert_taps, r.first = first, r.count = count;
+    r.first_anchor = first - first % kAnchorInterval;
+    const double step = kTwoPi * (double)e->carrier_offset / rate;
+    r.c_step_re = cos(step), r.c_step_im = sin(step);
+    std::vector<double> phase, hilbert;
+    if (m == RV_EMITTER_NFM) {  // modulators.cpp:769-780
+        phase.assign(audio_len + 1, 0.0);
+        const double scale = kTwoPi * (double)e->deviation / rate;
+        double accumulated = 0.0;
+        for (uint64_t i = 0; i < audio_len; ++i) {
+            accumulated += scale * (double)audio[i];
+            accumulated = fmod(accumulated, kTwoPi);
+            phase[i + 1] = accumulated;
+        }
+    }
+    if (ssb) {  // modulators.cpp:807-823: 2 / (pi lag) under a Blackman window, odd lags
+        const double pi = 3.141592653589793238462643383279502884;
+        hilbert.assign(hilbert_taps, 0.0);
+        const int64_t half = (int64_t)(hilbert_taps / 2);
+        for (uint32_t i = 0; i < hilbert_taps; ++i) {
+            const int64_t lag = (int64_t)i - half;
+            if (lag == 0 || lag % 2 == 0) continue;
+            const double ideal = 2.0 / (pi * (double)lag);
+            const double position = (double)i / (double)(hilbert_taps - 1);
+            const double window = 0.42 - 0.5 * cos(kTwoPi * position) + 0.08 * cos(2.0 * kTwoPi * position);
+            hilbert[i] = ideal * window;
+        }
+    }
+    const uint64_t segs = (first + count - r.first_anchor + kAnchorInterval - 1) / kAnchorInterval;
+    std::vector<Anchor> anchors(segs);
+    for (uint64_t k = 0; k < segs; ++k) {
+        const double cp = e->initial_phase + exact_phase(e->carrier_offset, e->rate, r.first_anchor + k * kAnchorInterval);
+        anchors[k] = Anchor{cos(cp), sin(cp), 0.0, 0.0};
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t a_bytes = segs * sizeof(Anchor), au_bytes = audio_len * sizeof(float);
+    const size_t p_bytes = phase.size() * sizeof(double), h_bytes = hilbert.size() * sizeof(double);
+    uint8_t* d = nullptr;
+    const size_t total = a_bytes + au_bytes + p_bytes + h_bytes + 64;
+    if (int32_t st = cuda_status(cudaMallocAsync(reinterpret_cast<void**>(&d), total, s), "emitter audio")) return st;
+    size_t at = 0;
+    auto put = [&](const void* src, size_t len) -> uint8_t* {
+        at = (at + 15) & ~size_t(15);
+        uint8_t* where = d + at;
+        if (len) cudaMemcpyAsync(where, src, len, cudaMemcpyHostToDevice, s);
+        at += len;
+        return where;
+    };
+    const Anchor* d_anchors = reinterpret_cast<const Anchor*>(put(anchors.data(), a_bytes));
+    r.audio = reinterpret_cast<const float*>(put(audio, au_bytes));
+    r.phase = reinterpret_cast<const double*>(put(phase.data(), p_bytes));
+    r.hilbert = reinterpret_cast<const double*>(put(hilbert.data(), h_bytes));
+    k_audio_emitter<<<(unsigned)((segs + 127) / 128), 128, 0, s>>>(r, d_anchors, (uint32_t)segs,
+                                                                  reinterpret_cast<float2*>(out));
+    int32_t st = cuda_status(cudaGetLastError(), "emitter audio");
+    cudaFreeAsync(d, s);
+    if (st == RV_OK) st = cuda_status(cudaStreamSynchronize(s), "emitter audio");
+    return st ? st : clear_error();
 }

@@ -186,6 +186,7 @@ SIGNATURES = {
     "rv_scene_noise_sigma": (F64, [F64]),
     "rv_scene_noise": (I32, [P, U64, F64, U64, U64, P, U64]),
     "rv_scene_plan": (I32, [ptr(abi.ScenePopulation), P, U32, ptr(U32)]),
+    "rv_emitter_accumulate_audio": (I32, [P, ptr(abi.ToneEmitter), P, U64, U32, U64, U64, F64, P, U64]),
     "rv_emitter_accumulate": (I32, [P, ptr(abi.ToneEmitter), U64, U64, F64, P, U64]),
     "rv_scene_noise_draws": (I32, [P, U64, U64, U64, P, U64]),
     "rv_pfb_dft_tc": (I32, [P, ptr(abi.PfbFftParams), P, U64, P, U64, P, U64, I32]),

@@ -419,3 +419,74 @@ def test_gpu_random_scene_matches_oracle(gpu, d, start, count):
     got = buf.download(np.float32, (count, 2))
     n = check_close(got, ora_random_scene(d, start, count))
     print("random scene seed %d, %d samples: %d of %d components off by one FP32 ulp" % (d["seed"], count, n, 2 * count))
+
+
+# ---- supplied audio (AM, NFM, SSB through the Hilbert phasing network) -----
+
+AUDIO_CASES = [dict(modulation=1, rate=48_000, carrier_offset=6_000, deviation=0, amplitude=0.5, initial_phase=0.2,
+                    modulation_index=0.7),
+               dict(modulation=2, rate=48_000, carrier_offset=-9_000, deviation=3_000, amplitude=1.0,
+                    initial_phase=1.0, modulation_index=0.0),
+               dict(modulation=3, rate=48_000, carrier_offset=2_000, deviation=0, amplitude=0.8, initial_phase=0.0,
+                    modulation_index=0.0, audio_low_hz=300, audio_high_hz=3000),
+               dict(modulation=4, rate=48_000, carrier_offset=-12_000, deviation=0, amplitude=1.0, initial_phase=2.5,
+                    modulation_index=0.0, audio_low_hz=300, audio_high_hz=3000)]
+AUDIO_IDS = ["am", "nfm", "usb", "lsb"]
+HILBERT_TAPS = 301
+
+
+def speech_like(n, seed=6):
+    rng = np.random.default_rng(seed)
+    t = np.arange(n) / 48_000
+    a = sum(np.sin(2 * np.pi * f * t + rng.uniform(0, 6)) / k for k, f in enumerate((420, 910, 1700, 2600), 1))
+    return (0.3 * a * (1 + 0.5 * np.sin(2 * np.pi * 3 * t))).astype(np.float32)
+
+
+def ora_audio(d, audio, first, count, gain, io):
+    from revenant_gb300 import abi
+    o = oracle().lib
+    o.or_emitter_accumulate_audio.argtypes = [C.POINTER(abi.ToneEmitter), C.c_void_p, C.c_uint64, C.c_uint32,
+                                              C.c_uint64, C.c_uint64, C.c_double, C.c_void_p]
+    out = io.copy()
+    assert o.or_emitter_accumulate_audio(C.byref(tone(d)), audio.ctypes.data, audio.size, HILBERT_TAPS, first, count,
+                                         gain, out.ctypes.data) == 0
+    return out
+
+
+@pytest.mark.parametrize("d", AUDIO_CASES, ids=AUDIO_IDS)
+def test_oracle_audio_emitter_matches_reference(synref, d):
+    synref.refsyn_audio_emitter.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double,
+                                            C.c_double, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int64, C.c_int64,
+                                            C.c_uint64, C.c_uint64, C.c_double, C.c_void_p]
+    audio = speech_like(30_000)
+    rng = np.random.default_rng(8)
+    for first, count in ((0, 32_000), (1000, 5000), (29_500, 2000)):  # past the audio's end too
+        io = (1e-3 * rng.standard_normal((count, 2))).astype(np.float32)
+        want = io.copy()
+        assert synref.refsyn_audio_emitter(d["modulation"], d["rate"], d["carrier_offset"], d["deviation"],
+                                           d["amplitude"], d["initial_phase"], d["modulation_index"],
+                                           audio.ctypes.data, audio.size, HILBERT_TAPS, d.get("audio_low_hz", 300),
+                                           d.get("audio_high_hz", 3000), first, count, 0.8, want.ctypes.data) == 0
+        got = ora_audio(d, audio, first, count, 0.8, io)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), first
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("d", AUDIO_CASES, ids=AUDIO_IDS)
+def test_gpu_audio_emitter_matches_oracle(gpu, d):
+    audio = speech_like(100_000)
+    rng = np.random.default_rng(9)
+    for first, count in ((0, 120_000), (4097, 50_000)):
+        io = (1e-3 * rng.standard_normal((count, 2))).astype(np.float32)
+        buf = gpu.array(io)
+        assert lib().rv_emitter_accumulate_audio(gpu.stream, C.byref(tone(d)), audio.ctypes.data, audio.size,
+                                                 HILBERT_TAPS, first, count, 0.8, buf.ptr, count) == 0, \
+            lib().rv_last_error()
+        got = buf.download(np.float32, (count, 2))
+        want = ora_audio(d, audio, first, count, 0.8, io)
+        if d["modulation"] == 2:  # NFM: CUDA's FP64 cos/sin of the phase per sample
+            n = check_close(got, want)
+            print("NFM audio emitter, %d samples from %d: %d of %d components off by one FP32 ulp"
+                  % (count, first, n, 2 * count))
+        else:
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), first
