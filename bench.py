@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-c4", action="store_true", help="skip the M = 4096 channelizer DFT comparison")
     ap.add_argument("--no-noise", action="store_true", help="skip the scene noise field measurement")
     ap.add_argument("--no-c1c2", action="store_true", help="skip the C1 single-receiver and C2 channelizer legs")
+    ap.add_argument("--no-c5", action="store_true", help="skip the learned detection proposal (C5)")
+    ap.add_argument("--c5-log2n", type=int, default=30, help="log2 samples of the C5 burst capture")
     ap.add_argument("--run-log2", type=int, default=24, help="log2 samples per rv_chain_run")
     return ap.parse_args()
 
@@ -381,6 +383,8 @@ def run_gb300(args):
         line["scene_noise"] = scene_noise(dev, stream, n, max(args.steps, 1))
     if rank == 0 and not args.no_c4:
         line["c4_dft"] = c4_dft(dev, stream, d_codes, n, max(args.steps, 1))
+    if rank == 0 and not args.no_c5:
+        line["c5_learned_proposal"] = c5_learned(dev, args.c5_log2n)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(reqs, threads=os.cpu_count())
     if rank == 0:
@@ -401,8 +405,10 @@ def detection(dev, d_codes, samples):
     bins = M * N // 2
     cfg = abi.DetectorConfig()
     cfg.source_rate, cfg.source_center, cfg.bins, cfg.noise_knots = RATE, 100_000_000, bins, 32
-    cfg.bin_width_numerator, cfg.bin_width_denominator = RATE, M * N
-    cfg.bin_zero_numerator, cfg.bin_zero_denominator = -RATE // 2, 1
+    # SpectrumGeometry (core/engine/graph.cpp:297-313): rate / (D N) Hz per
+    # bin, bin zero at -rate (M + 1) / (2 M)
+    cfg.bin_width_numerator, cfg.bin_width_denominator = RATE, GRID[2] * N
+    cfg.bin_zero_numerator, cfg.bin_zero_denominator = -RATE * (M + 1), 2 * M
     cfg.detection_threshold_db, cfg.average_seconds, cfg.decision_interval_seconds = 6.0, 1.0, 0.1
     cfg.noise_window_knots, cfg.noise_percentile, cfg.noise_percentile_high = 8, 0.10, 0.40
     cfg.noise_excision_sigma, cfg.split_gap_bins, cfg.edge_floor_sigma = 4.0, 8, 3.0
@@ -430,6 +436,127 @@ def detection(dev, d_codes, samples):
            "note": "coarse chain + spectrum + detector with tracking, no receivers, wall clock including host work"}
     ch.close()
     det.close()
+    return out
+
+
+def c5_learned(dev, log2n, train_scenes=8, train_log2=27, epochs=16):
+    """C5: the learned detection proposal against the plain detector.
+
+    A 2^log2n-sample cs16 burst capture at 20 MS/s (seed 5: 64 emitters of
+    all eight modulations, 24 bursts each per 2^30 samples, 1 ms - 2 s, -5 to
+    30 dB SNR in their occupied band, the scene's burst list kept as truth),
+    rendered on the GPU by the library's own synthesiser; its 65,536-bin
+    spectrum frames (M = 64 channels x 2048-point transforms, one frame per
+    65,536 samples). The network is trained on the GPU from scratch on
+    `train_scenes` other seeded scenes labelled by the plain detector, its
+    threshold set on one more (99 % of that scene's localised candidates).
+    Detection time: wall clock of the detector over every frame (the plain
+    one: accumulate and decide over all bins) against the learned path
+    (tiles and network one row ahead on a second stream, decisions confirmed
+    inside the proposed ranges), per second of signal."""
+    import torch
+    from revenant_gb300 import proposal, scene
+    import c5_workload as w
+    t_all = time.perf_counter()
+    out = {"workload": "2^%d cs16 samples at 20 MS/s (%.1f s), seeded burst scene (seed 5), 65,536-bin frames; "
+                       "network trained on %d scenes of 2^%d samples" % (log2n, (1 << log2n) / w.RATE, train_scenes,
+                                                                         train_log2)}
+    nt = 1 << train_log2
+    tiles, labels = [], []
+    t = time.perf_counter()
+    for seed in range(50, 50 + train_scenes):
+        fr = w.spectrum_frames(dev, w.render_cs16(dev, w.population(seed, nt), nt), nt)
+        inst, cands = w.run_plain(dev, fr)[1:3]
+        tiles.append(w.tile_rows(dev, fr))
+        labels.append(w.labels_for(inst, cands, tiles[-1].shape[0]))
+        del fr
+    tiles = torch.cat(tiles, 0)
+    labels = np.concatenate(labels, 0)
+    data_s = time.perf_counter() - t
+    cnn = proposal.Cnn(dev, max_batch=256, seed=1)
+    t = time.perf_counter()
+    losses = w.train(dev, cnn, tiles, labels, epochs=epochs, lr=2e-3, pos_weight=4.0)
+    train_s = time.perf_counter() - t
+    steps = epochs * (tiles.shape[0] * tiles.shape[1] // 256)
+    del tiles
+    vfr = w.spectrum_frames(dev, w.render_cs16(dev, w.population(99, nt), nt), nt)
+    vinst, vcands = w.run_plain(dev, vfr)[1:3]
+    vz = w.logits(dev, cnn, w.tile_rows(dev, vfr))
+    del vfr
+    vs = proposal.candidate_scores(vinst, vcands, vz.reshape(vz.shape[0], -1), 0, w.ROW_SAMPLES)
+    threshold = float(np.quantile(vs[np.isfinite(vs)], 0.01))
+    out["training"] = {"scenes": train_scenes, "tiles": int(labels.size // proposal.CELLS), "epochs": epochs,
+                       "adam_steps": steps, "batch": 256, "positive_cells": round(float(labels.mean()), 5),
+                       "loss_first_last": [round(losses[0], 4), round(losses[-1], 4)], "train_s": round(train_s, 2),
+                       "data_s": round(data_s, 2), "threshold_logit": round(threshold, 4),
+                       "params": proposal.param_count()}
+    n = 1 << log2n
+    pop = w.population(5, n)
+    bursts = scene.plan(pop)
+    t = time.perf_counter()
+    codes = w.render_cs16(dev, pop, n)
+    render_s = time.perf_counter() - t
+    frames = w.spectrum_frames(dev, codes, n)
+    del codes
+    seconds = n / w.RATE
+    wall_p, inst_p, cands_p, st_p = w.run_plain(dev, frames)
+    wall_l, inst_l, cands_l, st_l, frac = w.run_learned(dev, cnn, frames, threshold)
+    wall_f, inst_f, cands_f, st_f, frac_f = w.run_learned(dev, cnn, frames, threshold, full_every=20)
+    fp = proposal.bursts_found(bursts, inst_p, cands_p, w.BIN_ZERO_HZ, w.BIN_WIDTH_HZ, w.RATE)
+    fl = proposal.bursts_found(bursts, inst_l, cands_l, w.BIN_ZERO_HZ, w.BIN_WIDTH_HZ, w.RATE)
+    ff = proposal.bursts_found(bursts, inst_f, cands_f, w.BIN_ZERO_HZ, w.BIN_WIDTH_HZ, w.RATE)
+    m, tot = proposal.match(cands_p, inst_p, cands_l, inst_l, max_bins=proposal.LOCALISED_BINS)
+    mf, _ = proposal.match(cands_p, inst_p, cands_f, inst_f, max_bins=proposal.LOCALISED_BINS)
+    # the network's forward time per tile row (CUDA events on its stream)
+    rows = frames.shape[0] // proposal.TILE_FRAMES
+    prop = proposal.Proposer(dev, proposal.proposal_config(w.BINS, w.HOP / w.RATE, 1.0, threshold))
+    tbuf = torch.empty(proposal.TILE_VALUES * (w.BINS // proposal.TILE_BINS), dtype=torch.int16, device="cuda")
+    lbuf = torch.empty(32 * (w.BINS // proposal.TILE_BINS), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(cnn.stream)
+    prop.tiles(frames[0].data_ptr(), tbuf.data_ptr())
+    cnn.forward(tbuf.data_ptr(), w.BINS // proposal.TILE_BINS, lbuf.data_ptr(), lbuf.numel())
+    dev.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    reps = min(rows, 64)
+    e0.record(stream)
+    for r in range(reps):
+        prop.tiles(frames[r * proposal.TILE_FRAMES].data_ptr(), tbuf.data_ptr())
+    e1.record(stream)
+    for r in range(reps):
+        cnn.forward(tbuf.data_ptr(), w.BINS // proposal.TILE_BINS, lbuf.data_ptr(), lbuf.numel())
+    e2.record(stream)
+    e2.synchronize()
+    tiles_ms, fwd_ms = e0.elapsed_time(e1) / reps, e1.elapsed_time(e2) / reps
+    prop.close()
+    flops = 2.0 * (w.BINS // proposal.TILE_BINS) * (1024 * 64 * 32 + 256 * 128 * 256 + 128 * 128 * 768 +
+                                                     32 * 64 * 1536 + 32 * 64)
+    out.update({
+        "signal_seconds": round(seconds, 2), "frames": int(frames.shape[0]), "tile_rows": rows,
+        "bursts": len(bursts), "render_s": round(render_s, 2),
+        "plain": {"ms_per_signal_second": round(wall_p * 1e3 / seconds, 3), "wall_s": round(wall_p, 3),
+                  "decisions": int(st_p.decisions), "candidates": len(cands_p),
+                  "localised_candidates": int(proposal.localised(cands_p).sum()),
+                  "bursts_found": int(fp.sum())},
+        "learned": {"ms_per_signal_second": round(wall_l * 1e3 / seconds, 3), "wall_s": round(wall_l, 3),
+                    "decisions": int(st_l.decisions), "candidates": len(cands_l),
+                    "proposed_bin_fraction": round(frac, 4), "bursts_found": int(fl.sum()),
+                    "burst_recall_vs_plain": round(float((fl & fp).sum() / max(fp.sum(), 1)), 4),
+                    "candidate_recall_vs_plain": round(m / max(tot, 1), 4)},
+        "learned_with_fallback": {"full_band_every_rows": 20, "ms_per_signal_second": round(wall_f * 1e3 / seconds, 3),
+                                  "burst_recall_vs_plain": round(float((ff & fp).sum() / max(fp.sum(), 1)), 4),
+                                  "candidate_recall_vs_plain": round(mf / max(tot, 1), 4)},
+        "speedup": round(wall_p / wall_l, 2), "speedup_with_fallback": round(wall_p / wall_f, 2),
+        "truth_recall": {"plain": round(float(fp.mean()), 4), "learned": round(float(fl.mean()), 4)},
+        "network": {"tiles_ms_per_row": round(tiles_ms, 4), "forward_ms_per_row": round(fwd_ms, 4),
+                    "forward_tflops": round(flops / fwd_ms / 1e9, 1), "tiles_per_row": w.BINS // proposal.TILE_BINS},
+        "leg_s": round(time.perf_counter() - t_all, 1),
+        "note": "recall is burst-level (a scene burst counts as found when a candidate of a decision while it is on, "
+                "or within 1 s after, overlaps and localises its band); candidate recall leaves out candidates wider "
+                "than 512 bins (the floor estimate's bias summed over the ladder's widest windows)"})
+    assert cnn.status() == 0
+    cnn.close()
+    del frames
+    torch.cuda.empty_cache()
     return out
 
 

@@ -300,6 +300,11 @@ int32_t rv_context_device_info(const rv_context* context, rv_device_info* out);
 /* The context's own stream (core/gpu Context::submit's queue). */
 void* rv_context_stream(const rv_context* context);
 int32_t rv_context_synchronize(rv_context* context);
+/* A further (non-blocking) stream on the context's device, for work that
+ * overlaps the context stream's. */
+int32_t rv_stream_create(rv_context* context, void** out);
+int32_t rv_stream_destroy(void* stream);
+int32_t rv_stream_synchronize(void* stream);
 
 /* core/gpu/buffer.h:33-39 MemoryKind. */
 #define RV_MEMORY_DEVICE_LOCAL 0
@@ -1394,6 +1399,112 @@ int32_t rv_capture_read(const char* root, const rv_capture_segment* segment, uin
 /* recover_open_segments: closes segments a dead writer left open
  * ("recovered"). counts = {recovered, removed empty, failed}. */
 int32_t rv_capture_recover(const char* root, uint32_t counts[3]);
+
+/* ===================================================================== *
+ * Learned detection proposal. No counterpart in the reference: its       *
+ * detector (core/detect/detector.cpp:526-1942) scans every bin at every  *
+ * decision. Here a small spectrogram CNN proposes the bins worth a look  *
+ * and the detector's own decision rules confirm them there              *
+ * (rv_detector_set_regions), the full-band decision serving as fallback. *
+ * ===================================================================== */
+
+/* Spectrogram tiles: RV_TILE_FRAMES frames x RV_TILE_BINS bins x 2 channels
+ * (the dB of exponential averages of the linear power, frame by frame, with
+ * a tenth of average_seconds and with average_seconds as time constant, both
+ * less the tile row's noise floor and divided by 10), BF16, channels
+ * innermost. A row of tiles covers every bin of RV_TILE_FRAMES consecutive
+ * frames. */
+#define RV_TILE_FRAMES 64u
+#define RV_TILE_BINS 256u
+#define RV_TILE_CHANNELS 2u
+#define RV_CNN_CELLS 32u      /* logits per tile: one per 8-bin cell */
+#define RV_CNN_CELL_BINS 8u
+
+/* The network (fixed): conv 4x4/4 2->64, conv 2x2/2 64->128, conv 2x3/(2,1)
+ * pad (0,1) 128->128, conv 4x3/(4,1) pad (0,1) 128->64 (ReLU after each),
+ * 1x1 64->1; 231,873 FP32 parameters, weights [cout][kh][kw][cin] then the
+ * biases, layer after layer. Forward and backward run as BF16 implicit GEMMs
+ * on the tcgen05 tensor cores with FP32 accumulation, on the context's
+ * stream. */
+typedef struct rv_cnn rv_cnn;
+typedef struct rv_cnn_train_config {
+    float learning_rate;   /* Adam */
+    float beta1;
+    float beta2;
+    float epsilon;
+    float weight_decay;    /* added to the gradient (L2) */
+    float pos_weight;      /* weight of the positive term of the cross-entropy */
+} rv_cnn_train_config;
+
+uint64_t rv_cnn_param_count(void);
+/* He-normal weights from `seed`, zero biases; activations for max_batch tiles. */
+int32_t rv_cnn_create(rv_context* context, uint32_t max_batch, uint64_t seed, rv_cnn** out);
+int32_t rv_cnn_destroy(rv_cnn* cnn);
+int32_t rv_cnn_set_params(rv_cnn* cnn, const float* host, uint64_t count);
+int32_t rv_cnn_get_params(rv_cnn* cnn, float* host, uint64_t count);
+/* The gradient of the last backward or training step. */
+int32_t rv_cnn_get_grads(rv_cnn* cnn, float* host, uint64_t count);
+void* rv_cnn_stream(const rv_cnn* cnn);
+/* Later calls enqueue on `stream` (NULL: the context's); waits for the old one. */
+int32_t rv_cnn_set_stream(rv_cnn* cnn, void* stream);
+/* Logits [batch][RV_CNN_CELLS] of `batch` tiles (BF16, layout above); the
+ * activations stay for rv_cnn_backward. logits_dev may be NULL. */
+int32_t rv_cnn_forward(rv_cnn* cnn, const void* tiles_dev, uint32_t batch, float* logits_dev, uint64_t logits_len);
+/* Parameter gradient of sum(dlogits * logits) for the last forward batch. */
+int32_t rv_cnn_backward(rv_cnn* cnn, const float* dlogits_dev, uint64_t dlogits_len);
+/* Forward, weighted binary cross-entropy against labels [batch][RV_CNN_CELLS]
+ * (0 or 1, mean over the batch), backward and one Adam step. *loss_host (may
+ * be NULL; then nothing waits) receives the batch's loss. */
+int32_t rv_cnn_train_step(rv_cnn* cnn, const void* tiles_dev, const float* labels_dev, uint32_t batch,
+                          const rv_cnn_train_config* config, float* loss_host);
+/* Waits for the stream; RV_ERR_TIMEOUT (count in *timeouts) when a bounded
+ * tensor-core wait ran out since the network was created. */
+int32_t rv_cnn_status(rv_cnn* cnn, uint32_t* timeouts);
+/* The network's GEMM kernel on its own: D[m][n] = sum_k A[m][k] B[n][k],
+ * FP32 row-major operands rounded to BF16, FP32 accumulation. Bounded waits
+ * that run out are counted in *status_dev. */
+int32_t rv_gemm_bf16(void* stream, const float* a_dev, const float* b_dev, uint32_t m, uint32_t n, uint32_t k,
+                     float* d_dev, uint32_t* status_dev);
+
+/* The tile builder and the proposals. */
+typedef struct rv_proposal_config {
+    uint32_t bins;             /* frame bins, a multiple of RV_TILE_BINS */
+    uint32_t hold_rows;        /* a proposed cell stays in force this many further tile rows */
+    double frame_seconds;      /* source seconds between frames */
+    double average_seconds;    /* time constant of the averaged channel (the detector's average_seconds) */
+    float threshold;           /* logit above which a cell is proposed */
+    uint32_t pad_bins;         /* bins added either side of each run of proposed cells */
+} rv_proposal_config;
+
+typedef struct rv_proposer rv_proposer;
+int32_t rv_proposer_create(rv_context* context, const rv_proposal_config* config, rv_proposer** out);
+int32_t rv_proposer_destroy(rv_proposer* proposer);
+/* One row of tiles (bins / RV_TILE_BINS tiles) from RV_TILE_FRAMES frames of
+ * `bins` dB values on the device, advancing the averaged channel. */
+int32_t rv_proposer_tiles(rv_proposer* proposer, const float* frames_dev, uint64_t frames_len, void* tiles_dev,
+                          uint64_t tiles_len);
+/* The cells of one tile row whose logit is above the threshold, held for
+ * hold_rows rows, merged into ascending disjoint bin ranges [lo, hi)
+ * (ranges[2 i], ranges[2 i + 1]) padded by pad_bins; *count = ranges. */
+int32_t rv_proposer_regions(rv_proposer* proposer, const float* logits_dev, uint64_t logits_len, uint32_t* ranges,
+                            uint32_t capacity, uint32_t* count);
+/* Later calls enqueue on `stream` (NULL: the context's); waits for the old one. */
+int32_t rv_proposer_set_stream(rv_proposer* proposer, void* stream);
+/* The averaged channel and the floors start again (a new capture). */
+int32_t rv_proposer_reset(rv_proposer* proposer);
+
+/* Confirmation: the detector's next decisions evaluate the noise floor, the
+ * ladder, the peaks and the candidate growth only inside `count` ascending
+ * disjoint bin ranges [lo, hi); the average keeps accumulating over every
+ * bin. ranges = NULL returns to the full band (the plain detector). */
+int32_t rv_detector_set_regions(rv_detector* detector, const uint32_t* ranges, uint32_t count);
+/* Keeps every decision's candidates, each with its decision instant (the
+ * source sample index), until read; enabling or disabling clears the log. */
+int32_t rv_detector_log_candidates(rv_detector* detector, int32_t enable);
+/* Moves up to `capacity` logged candidates (oldest first) out of the log;
+ * *count = the candidates logged before the call (out = NULL: count only). */
+int32_t rv_detector_read_log(rv_detector* detector, uint64_t* instants, rv_detector_candidate* out, uint32_t capacity,
+                             uint32_t* count);
 
 #ifdef __cplusplus
 }

@@ -374,7 +374,19 @@ class ChainStats(_S):
                 ("graph_captures", U64), ("graph_ms", C.c_double), ("host_ms", C.c_double)]
 
 
-EXTRA_STRUCTS = {"rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params": IqCorrectParams,
+class CnnTrainConfig(_S):
+    _fields_ = [("learning_rate", F32), ("beta1", F32), ("beta2", F32), ("epsilon", F32), ("weight_decay", F32),
+                ("pos_weight", F32)]
+
+
+class ProposalConfig(_S):
+    _fields_ = [("bins", U32), ("hold_rows", U32), ("frame_seconds", F64), ("average_seconds", F64),
+                ("threshold", F32), ("pad_bins", U32)]
+
+
+TILE_FRAMES, TILE_BINS, TILE_CHANNELS, CNN_CELLS, CNN_CELL_BINS = 64, 256, 2, 32, 8
+
+EXTRA_STRUCTS = {"rv_cnn_train_config": CnnTrainConfig, "rv_proposal_config": ProposalConfig, "rv_iq_moments_params": IqMomentsParams, "rv_iq_correct_params": IqCorrectParams,
                  "rv_front_end": FrontEnd, "rv_detector_config": DetectorConfig, "rv_detector_candidate": DetectorCandidate,
                  "rv_detector_track": DetectorTrack, "rv_excision_config": ExcisionConfig,
                  "rv_excision_params": ExcisionParams, "rv_excision_rings": ExcisionRings,

@@ -157,6 +157,29 @@ int32_t rv_context_device_info(const rv_context* ctx, rv_device_info* out) {
 
 void* rv_context_stream(const rv_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
+int32_t rv_stream_create(rv_context* ctx, void** out) {
+    if (ctx == nullptr || out == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_stream_create: NULL");
+    *out = nullptr;
+    cudaStream_t s = nullptr;
+    if (int32_t st = cuda_status(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate")) return st;
+    *out = (void*)s;
+    return rv::clear_error();
+}
+
+int32_t rv_stream_destroy(void* stream) {
+    if (stream == nullptr) return RV_OK;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaStreamSynchronize(s);
+    if (int32_t st = cuda_status(cudaStreamDestroy(s), "cudaStreamDestroy")) return st;
+    return rv::clear_error();
+}
+
+int32_t rv_stream_synchronize(void* stream) {
+    if (int32_t st = cuda_status(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)), "cudaStreamSynchronize"))
+        return st;
+    return rv::clear_error();
+}
+
 int32_t rv_context_synchronize(rv_context* ctx) {
     if (ctx == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_context_synchronize: NULL");
     if (int32_t st = cuda_status(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize")) return st;

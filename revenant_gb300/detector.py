@@ -88,6 +88,26 @@ class Detector:
         check(lib().rv_detector_get_stats(self.handle, C.byref(s)))
         return s
 
+    def set_regions(self, ranges):
+        """Confirm only inside bin ranges ([n][2] lo, hi), or the full band (None)."""
+        if ranges is None:
+            check(lib().rv_detector_set_regions(self.handle, None, 0))
+            return
+        r = np.ascontiguousarray(ranges, np.uint32).reshape(-1, 2)
+        check(lib().rv_detector_set_regions(self.handle, r.ctypes.data, r.shape[0]))
+
+    def log_candidates(self, enable=True):
+        check(lib().rv_detector_log_candidates(self.handle, int(enable)))
+
+    def read_log(self):
+        """(instants, candidates) of every decision since the last read."""
+        n = C.c_uint32()
+        check(lib().rv_detector_read_log(self.handle, None, None, 0, C.byref(n)))
+        buf = (abi.DetectorCandidate * max(n.value, 1))()
+        inst = np.zeros(max(n.value, 1), np.uint64)
+        check(lib().rv_detector_read_log(self.handle, inst.ctypes.data, buf, n.value, C.byref(n)))
+        return inst[:n.value], _to_array(buf, n.value, abi.DetectorCandidate, CANDIDATE_DTYPE)
+
     def close(self):
         if self.handle:
             lib().rv_detector_destroy(self.handle)

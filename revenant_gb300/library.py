@@ -253,6 +253,31 @@ SIGNATURES = {
     "rv_demod_block": (I32, [ptr(abi.VrxPlanInfo), U32, U64, U32, ptr(abi.VrxDemodBlock)]),
     "rv_carrier_block": (I32, [ptr(abi.VrxPlanInfo), U32, U64, U32, I32, F32, ptr(abi.VrxCarrierParams)]),
     "rv_demod_fine_history": (U32, [ptr(abi.VrxDemodConfig)]),
+    "rv_stream_create": (I32, [P, ptr(P)]),
+    "rv_stream_destroy": (I32, [P]),
+    "rv_stream_synchronize": (I32, [P]),
+    "rv_cnn_set_stream": (I32, [P, P]),
+    "rv_proposer_set_stream": (I32, [P, P]),
+    "rv_cnn_param_count": (U64, []),
+    "rv_cnn_create": (I32, [P, U32, U64, ptr(P)]),
+    "rv_cnn_destroy": (I32, [P]),
+    "rv_cnn_set_params": (I32, [P, P, U64]),
+    "rv_cnn_get_params": (I32, [P, P, U64]),
+    "rv_cnn_get_grads": (I32, [P, P, U64]),
+    "rv_cnn_stream": (P, [P]),
+    "rv_cnn_forward": (I32, [P, P, U32, P, U64]),
+    "rv_cnn_backward": (I32, [P, P, U64]),
+    "rv_cnn_train_step": (I32, [P, P, P, U32, ptr(abi.CnnTrainConfig), ptr(F32)]),
+    "rv_cnn_status": (I32, [P, ptr(U32)]),
+    "rv_gemm_bf16": (I32, [P, P, P, U32, U32, U32, P, P]),
+    "rv_proposer_create": (I32, [P, ptr(abi.ProposalConfig), ptr(P)]),
+    "rv_proposer_destroy": (I32, [P]),
+    "rv_proposer_tiles": (I32, [P, P, U64, P, U64]),
+    "rv_proposer_regions": (I32, [P, P, U64, P, U32, ptr(U32)]),
+    "rv_proposer_reset": (I32, [P]),
+    "rv_detector_set_regions": (I32, [P, P, U32]),
+    "rv_detector_log_candidates": (I32, [P, I32]),
+    "rv_detector_read_log": (I32, [P, P, P, U32, ptr(U32)]),
 }
 
 
