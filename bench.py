@@ -487,7 +487,7 @@ def c5_learned(dev, log2n, train_scenes=8, train_log2=27, epochs=16):
     threshold = float(np.quantile(vs[np.isfinite(vs)], 0.01))
     out["training"] = {"scenes": train_scenes, "tiles": int(labels.size // proposal.CELLS), "epochs": epochs,
                        "adam_steps": steps, "batch": 256, "positive_cells": round(float(labels.mean()), 5),
-                       "loss_first_last": [round(losses[0], 4), round(losses[-1], 4)], "train_s": round(train_s, 2),
+                       "epoch_mean_loss_first_last": [round(losses[0], 4), round(losses[-1], 4)], "train_s": round(train_s, 2),
                        "data_s": round(data_s, 2), "threshold_logit": round(threshold, 4),
                        "params": proposal.param_count()}
     n = 1 << log2n
@@ -779,66 +779,113 @@ class _Offset:
         self.address = buf.address + offset
 
 
+class OracleWorkload:
+    """The workload through the oracle (the reference's CPU twins restated in
+    C, planned by the oracle's own planner, pinned to the reference's): one
+    chain converts, branch-filters and FFTs each run, and the receivers'
+    fine stages, carrier loops and demodulators run spread over `threads`
+    host threads (ctypes releases the interpreter lock inside the C). The GPU
+    library is never loaded."""
+
+    def __init__(self, reqs, threads):
+        from concurrent.futures import ThreadPoolExecutor
+        from oracle_chain import OracleChain
+        from revenant_gb300 import abi
+        self.threads = max(1, threads)
+        self.master = OracleChain(GRID, RATE, abi.FORMAT_CS16, [], ring_log2=20, chan_log2=17)
+        self.groups = [OracleChain(GRID, RATE, abi.FORMAT_CS16, reqs[i::self.threads], ring_log2=4, chan_log2=17)
+                       for i in range(self.threads) if reqs[i::self.threads]]
+        for g in self.groups:
+            g.chan = self.master.chan
+        self.pool = ThreadPoolExecutor(max_workers=self.threads) if self.threads > 1 else None
+
+    def run(self, codes, count, run=1 << 16, serial=False):
+        """`count` more samples of the stream; serial: every receiver on the
+        calling thread."""
+        for at in range(0, count, run):
+            m = min(run, count - at)
+            before = self.master.next_block
+            self.master.run(codes[2 * at:2 * (at + m)], m)
+            after = self.master.next_block
+            if after > before:
+                if self.pool and not serial:
+                    list(self.pool.map(lambda g: g.receivers(before, after - 1), self.groups))
+                else:
+                    for g in self.groups:
+                        g.receivers(before, after - 1)
+
+    def close(self):
+        if self.pool:
+            self.pool.shutdown()
+
+
 def cpu_baseline(reqs, threads=None, sample_log2=18):
-    """The oracle (the reference's twins restated in C) on the host cores over
-    a bounded sample of the same workload: the coarse chain over all host
-    threads, then every receiver's fine stage and demodulator with the
-    receivers spread over the threads."""
-    import ctypes as C
-    from concurrent.futures import ThreadPoolExecutor
-
-    from bindings import cf32, oracle
-    from oracle_chain import OracleChain
-    from revenant_gb300 import abi
-
+    """The oracle on the host cores over a bounded sample of the same
+    workload (the first 2^sample_log2 samples of the capture, all
+    receivers)."""
     threads = threads or os.cpu_count() or 1
     n = 1 << sample_log2
-    codes = capture(n, seed=SEED + 100)
-    M, T, D = GRID
-    ora = oracle()
-    proto = OracleChain(GRID, RATE, abi.FORMAT_CS16, [], ring_log2=4, chan_log2=4)
-    blocks = n // D
-    chan_blocks = 1 << int(np.ceil(np.log2(blocks + 300)))
-    chan = cf32(M * chan_blocks)
-    g = abi.GridParams(*GRID)
+    codes = capture(n)
+    wl = OracleWorkload(reqs, threads)
     t = time.perf_counter()
-    st = ora.lib.or_coarse_cs16(C.byref(g), proto.taps.ctypes.data, proto.tw.ctypes.data, codes.ctypes.data, n, 0,
-                                blocks, chan_blocks, chan.ctypes.data, threads)
-    assert st == 0
-    coarse_s = time.perf_counter() - t
-    groups = [g_ for g_ in (reqs[i::threads] for i in range(threads)) if g_]
-    workers = []
-    for group in groups:
-        c = OracleChain(GRID, RATE, abi.FORMAT_CS16, group, ring_log2=4, chan_log2=int(np.log2(chan_blocks)))
-        c.chan = chan
-        workers.append(c)
-    t = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=threads) as pool:
-        list(pool.map(lambda c: c.receivers(0, blocks - 1), workers))
-    rx_s = time.perf_counter() - t
-    total = coarse_s + rx_s
-    return {"value": round(n / total / 1e6, 4), "unit": "MS/s", "cores": threads, "kind": "port",
-            "sample": "2^%d samples (%.1f ms of signal), all %d receivers: coarse %.2f s + receivers %.2f s on %d "
-                      "threads" % (sample_log2, n / RATE * 1e3, len(reqs), coarse_s, rx_s, threads)}
+    wl.run(codes, n)
+    dt = time.perf_counter() - t
+    wl.close()
+    return {"value": round(n / dt / 1e6, 4), "unit": "MS/s", "cores": threads, "kind": "port",
+            "sample": "the capture's first 2^%d samples (%.1f ms of signal), all %d receivers, %.2f s on %d threads"
+                      % (sample_log2, n / RATE * 1e3, len(reqs), dt, threads)}
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path on this host's cores,
+    as the oracle restates it (the reference's twins and planner in C; the
+    reference itself is a C++/Vulkan application with no package to install
+    and is not on this machine). Each step is a bounded sample of the same
+    workload: the next 2^step_log2 samples of the same capture through the
+    same 256 receivers, continuing the stream. Times every step on all host
+    threads, and one sample on a single thread."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    import revenant_gb300 as rg
-    rg.build()
+    threads = os.cpu_count() or 1
+    step_log2 = 16
+    step = 1 << step_log2
     reqs = receivers(args.receivers)
-    vals = []
+    tail = 1 << 13  # the single-thread sample after the timed steps
+    codes = capture((args.warmup + args.steps) * step + tail)
+    wl = OracleWorkload(reqs, threads)
+    at = 0
+    for _ in range(args.warmup):
+        wl.run(codes[2 * at:2 * (at + step)], step)
+        at += step
+    t = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(reqs, threads=os.cpu_count()))
-    v = float(np.median([x["value"] for x in vals]))
+        wl.run(codes[2 * at:2 * (at + step)], step)
+        at += step
+    dt = time.perf_counter() - t
+    v = step * args.steps / dt / 1e6
+    # one thread: the stream's next 2^13 samples with every receiver on this
+    # thread (the same chains, so in the same steady state)
+    m = tail
+    t = time.perf_counter()
+    wl.run(codes[2 * at:2 * (at + m)], m, serial=True)
+    dt1 = time.perf_counter() - t
+    wl.close()
+    ms_per_step = dt * 1e3 / args.steps
     line = {"metric": METRIC, "value": round(v, 4), "unit": "MS/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": {"workload": "batched uneven receivers: 2^%d cs16 samples at 20 MS/s, M=64 D=32 T=17, %d receivers "
-                                   "NFM/AM/USB/LSB/WFM 12.5-200 kHz (seed %d)" % (args.log2n, args.receivers, SEED)},
-            "cpu_baseline": dict(vals[-1], value=round(v, 4)),
+                                   "NFM/AM/USB/LSB/WFM 12.5-200 kHz (seed %d)" % (args.log2n, args.receivers, SEED),
+                       "step": "a bounded sample of the workload: the next 2^%d samples of the capture through all %d "
+                               "receivers (the full 2^%d-sample step would take about %.0f s here)"
+                               % (step_log2, len(reqs), args.log2n, ms_per_step / 1e3 * (1 << args.log2n) / step)},
+            "cpu_baseline": {"value": round(v, 4), "unit": "MS/s", "cores": threads, "kind": "port",
+                             "sample": "%d steps of 2^%d samples after %d warm-up steps, receivers over %d threads"
+                                       % (args.steps, step_log2, args.warmup, threads),
+                             "single_thread": {"value": round(m / dt1 / 1e6, 4), "unit": "MS/s", "cores": 1,
+                                               "sample": "the stream's next 2^13 samples after the timed steps, "
+                                                         "all receivers on one thread"}},
             "e2e": {"value": round(v, 4), "unit": "MS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

@@ -16,25 +16,32 @@ REF_LIB = os.path.join(HERE, "_ref", "libreftwins.so")
 
 
 def build(force=False):
-    src = os.path.join(HERE, "oracle.c")
-    deps = [src, os.path.join(HERE, "oracle.h"),
-            os.path.join(HERE, "..", "include", "revenant_gb300.h")]
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "planner.c")]
+    deps = srcs + [os.path.join(HERE, "oracle.h"), os.path.join(HERE, "..", "include", "revenant_gb300.h")]
     if not force and os.path.exists(LIB) and all(
             os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp.%d" % os.getpid()
     cmd = ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-           "-fno-fast-math", "-Wall", "-Wno-unused-function", "-pthread",
-           src, "-o", tmp, "-lm"]
+           "-fno-fast-math", "-Wall", "-Wno-unused-function", "-pthread"] + srcs + ["-o", tmp, "-lm"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB
 
 
-def build_reference(ref_root="/root/reference"):
+def reference_root():
+    """The reference's source tree: $REVENANT_REFERENCE, else a checkout named
+    `reference` beside this repository; None when neither holds it."""
+    root = os.environ.get("REVENANT_REFERENCE") or os.path.join(HERE, os.pardir, os.pardir, "reference")
+    root = os.path.abspath(root)
+    return root if os.path.isdir(os.path.join(root, "core", "dsp")) else None
+
+
+def build_reference(ref_root=None):
     """Compile the reference's own twins when its sources are present."""
-    if not os.path.isdir(os.path.join(ref_root, "core", "dsp")):
+    ref_root = ref_root or reference_root()
+    if ref_root is None:
         return None
     subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"),
                            "REF=" + ref_root])

@@ -42,6 +42,15 @@ static int32_t ok(void) {
     return 0;
 }
 
+/* The same message slot for the planner restatement (planner.c). */
+int32_t or_fail(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_error, sizeof g_error, fmt, ap);
+    va_end(ap);
+    return -1;
+}
+
 /* ------------------------------------------------------------------ */
 /* scoped denormal flush (core/dsp/denormal_mode.h ScopedDenormalFlush) */
 /* Sets the floating-point environment's flush-to-zero bits through   */

@@ -42,6 +42,23 @@ int32_t or_emitter_accumulate_audio(const rv_tone_emitter* e, const float* audio
 
 const char* or_last_error(void);
 
+/* The planner (planner.c): pfb_design.cpp:381-590 design_prototype and
+ * build_twiddles, vrx_reference.cpp:364 build_nco_table, vrx_place.cpp place,
+ * vrx_reference.cpp plan_vrx with its tables and the block parameters. */
+int32_t or_design_prototype(const rv_grid_params* g, double attenuation_db, float* taps, uint64_t taps_len);
+int32_t or_build_twiddles(uint32_t M, rv_cf32* out, uint64_t len);
+int32_t or_build_nco_table(uint32_t log2, rv_cf32* out, uint64_t len);
+int32_t or_place(const rv_grid_params* g, int64_t rate, const rv_vrx_request* r, rv_vrx_placement* out);
+int32_t or_plan_vrx(const rv_grid_params* g, int64_t rate, const rv_vrx_request* r, const rv_vrx_placement* pl,
+                    rv_vrx_plan_info* p, rv_cf32* taps, uint64_t taps_len, float* weights, uint64_t weights_len);
+int32_t or_fine_block(const rv_vrx_plan_info* plan, uint32_t channel_base, uint32_t channel_mask, uint32_t fine_mask,
+                      uint64_t first_output, uint32_t count, rv_vrx_fine_block* block);
+uint32_t or_demod_fine_history(const rv_vrx_demod_config* c);
+int32_t or_demod_block(const rv_vrx_plan_info* plan, uint32_t fine_mask, uint64_t first_audio, uint32_t count,
+                       rv_vrx_demod_block* block);
+int32_t or_carrier_block(const rv_vrx_plan_info* plan, uint32_t fine_mask, uint64_t first_fine, uint32_t count,
+                         int32_t reset, float shift, rv_vrx_carrier_params* out);
+
 float or_det_rsqrt(float v);
 float or_det_sqrt(float v);
 float or_det_recip(float v);

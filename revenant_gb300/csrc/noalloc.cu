@@ -20,11 +20,16 @@
 // the FFT then reads), but two calls whose work overlaps on the GPU (different
 // streams, no ordering between them) race on it.
 //
-// Set-up: the device address of the array is looked up once per device, on
-// the first call made with that device current (cudaGetSymbolAddress; the host
-// symbol itself is only a stand-in and must never reach a kernel). That first
-// call should therefore come before any stream capture is begun. Nothing here
-// calls cudaMalloc, cudaFree or any allocating routine.
+// Set-up: the device address of the array is looked up once per device
+// context, on the first call made with that context current
+// (cudaGetSymbolAddress; the host symbol itself is only a stand-in and must
+// never reach a kernel). The lookups are kept by the context's unique id
+// (cuCtxGetId, reached through cudaGetDriverEntryPointByVersion, so nothing
+// links the driver library), so a context made after cudaDeviceReset or a
+// different context on the same device gets its own lookup instead of a stale
+// address. The first call in each context should therefore come before any
+// stream capture is begun. Nothing here calls cudaMalloc, cudaFree or any
+// allocating routine.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -41,23 +46,75 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) rv_cf32 g_branch_scratch[kNoAllocBranchValues];
 
 std::mutex g_lock;
-rv_cf32* g_scratch[kMaxDevices] = {};
+struct Lookup {
+    unsigned long long context_id;
+    rv_cf32* address;
+};
+Lookup g_scratch[kMaxDevices] = {};  // most recent contexts first
+int g_lookups = 0;
 
-// Device address of the scratch array on the current device.
-int32_t scratch_address(rv_cf32** out) {
-    int device = 0;
-    if (int32_t st = rv::cuda_status(cudaGetDevice(&device), "rv_pfb_channelize_noalloc: cudaGetDevice")) return st;
-    if (device < 0 || device >= kMaxDevices)
-        return rv::set_error_fmt(RV_ERR_UNSUPPORTED, "rv_pfb_channelize_noalloc: device %d", device);
-    std::lock_guard<std::mutex> guard(g_lock);
-    if (g_scratch[device] == nullptr) {
-        void* address = nullptr;
-        if (int32_t st = rv::cuda_status(cudaGetSymbolAddress(&address, g_branch_scratch),
-                                         "rv_pfb_channelize_noalloc: cudaGetSymbolAddress"))
+using CtxGetCurrent = int (*)(void**);                    // cuCtxGetCurrent
+using CtxGetId = int (*)(void*, unsigned long long*);     // cuCtxGetId
+CtxGetCurrent g_get_current = nullptr;
+CtxGetId g_get_id = nullptr;
+
+// The unique id of the current context; *bound = false when this thread has
+// none yet (the runtime binds it on its next call that needs the device).
+int32_t current_context_id(unsigned long long* id, bool* bound) {
+    if (g_get_current == nullptr || g_get_id == nullptr) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (int32_t st = rv::cuda_status(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa),
+                                         "rv_pfb_channelize_noalloc: cuCtxGetCurrent"))
             return st;
-        g_scratch[device] = static_cast<rv_cf32*>(address);
+        if (int32_t st = rv::cuda_status(cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb),
+                                         "rv_pfb_channelize_noalloc: cuCtxGetId"))
+            return st;
+        if (qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || a == nullptr || b == nullptr)
+            return rv::set_error_fmt(RV_ERR_UNSUPPORTED, "rv_pfb_channelize_noalloc: the driver lacks cuCtxGetId");
+        g_get_current = reinterpret_cast<CtxGetCurrent>(a);
+        g_get_id = reinterpret_cast<CtxGetId>(b);
     }
-    *out = g_scratch[device];
+    void* ctx = nullptr;
+    if (g_get_current(&ctx) != 0) return rv::set_error_fmt(RV_ERR_CUDA, "rv_pfb_channelize_noalloc: cuCtxGetCurrent failed");
+    *bound = ctx != nullptr;
+    if (ctx != nullptr && g_get_id(ctx, id) != 0)
+        return rv::set_error_fmt(RV_ERR_CUDA, "rv_pfb_channelize_noalloc: cuCtxGetId failed");
+    return RV_OK;
+}
+
+// Device address of the scratch array in the current context.
+int32_t scratch_address(rv_cf32** out) {
+    std::lock_guard<std::mutex> guard(g_lock);
+    unsigned long long id = 0;
+    bool bound = false;
+    if (int32_t st = current_context_id(&id, &bound)) return st;
+    if (bound)
+        for (int i = 0; i < g_lookups; ++i)
+            if (g_scratch[i].context_id == id) {
+                *out = g_scratch[i].address;
+                return RV_OK;
+            }
+    void* address = nullptr;
+    if (int32_t st = rv::cuda_status(cudaGetSymbolAddress(&address, g_branch_scratch),
+                                     "rv_pfb_channelize_noalloc: cudaGetSymbolAddress"))
+        return st;
+    if (!bound) {  // the lookup bound the runtime's context to this thread
+        if (int32_t st = current_context_id(&id, &bound)) return st;
+        if (!bound) return rv::set_error_fmt(RV_ERR_CUDA, "rv_pfb_channelize_noalloc: no current context");
+        for (int i = 0; i < g_lookups; ++i)
+            if (g_scratch[i].context_id == id) {
+                *out = g_scratch[i].address;
+                return RV_OK;
+            }
+    }
+    // newest first; the oldest lookup drops out when the table is full
+    const int keep = g_lookups < kMaxDevices ? g_lookups : kMaxDevices - 1;
+    for (int i = keep; i > 0; --i) g_scratch[i] = g_scratch[i - 1];
+    g_scratch[0] = Lookup{id, static_cast<rv_cf32*>(address)};
+    g_lookups = keep + 1;
+    *out = g_scratch[0].address;
     return RV_OK;
 }
 

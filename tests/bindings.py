@@ -93,6 +93,21 @@ def oracle():
         lib.or_pfb_branch_wide.argtypes = [ptr(abi.GridParams), ptr(abi.PfbBranchParams), P, U64, P, U64, P, U64]
         lib.or_pfb_f64.restype = I32
         lib.or_pfb_f64.argtypes = [ptr(abi.GridParams), P, P, U32, U32, U32, U32, P, P]
+        # the planner restatement (oracle/planner.c)
+        for name, res, args in (
+                ("design_prototype", I32, [ptr(abi.GridParams), F64, P, U64]),
+                ("build_twiddles", I32, [U32, P, U64]),
+                ("build_nco_table", I32, [U32, P, U64]),
+                ("place", I32, [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), ptr(abi.VrxPlacement)]),
+                ("plan_vrx", I32, [ptr(abi.GridParams), I64, ptr(abi.VrxRequest), ptr(abi.VrxPlacement),
+                                   ptr(abi.VrxPlanInfo), P, U64, P, U64]),
+                ("fine_block", I32, [ptr(abi.VrxPlanInfo), U32, U32, U32, U64, U32, ptr(abi.VrxFineBlock)]),
+                ("demod_fine_history", U32, [ptr(abi.VrxDemodConfig)]),
+                ("demod_block", I32, [ptr(abi.VrxPlanInfo), U32, U64, U32, ptr(abi.VrxDemodBlock)]),
+                ("carrier_block", I32, [ptr(abi.VrxPlanInfo), U32, U64, U32, I32, F32, ptr(abi.VrxCarrierParams)])):
+            fn = getattr(lib, "or_" + name)
+            fn.restype = res
+            fn.argtypes = args
         _oracle = Lib(lib, "or_")
     return _oracle
 

@@ -159,8 +159,8 @@ def threshold_for(instants, candidates, logits_rows, recall=0.997, pad_bins=64):
 def train(dev, cnn, tiles, labels, epochs=8, batch=256, lr=1e-3, pos_weight=8.0, seed=0, flip=True):
     """Adam over shuffled tiles; tiles [rows][tiles][values], labels numpy
     [rows][tiles][cells]. With `flip`, every other epoch sees each tile and
-    its labels mirrored in frequency. Returns the losses of each epoch's
-    last batch."""
+    its labels mirrored in frequency. Returns each epoch's mean loss over
+    every eighth batch."""
     flat = tiles.reshape(-1, proposal.TILE_VALUES)
     lab = torch.from_numpy(np.ascontiguousarray(labels.reshape(-1, proposal.CELLS))).cuda()
     n = flat.shape[0]
@@ -176,7 +176,7 @@ def train(dev, cnn, tiles, labels, epochs=8, batch=256, lr=1e-3, pos_weight=8.0,
     with torch.cuda.stream(torch.cuda.ExternalStream(cnn.stream)):
         for _ in range(epochs):
             order = torch.from_numpy(rng.permutation(n)).cuda()
-            loss = None
+            seen = []
             for at in range(0, n - batch + 1, batch):
                 idx = order[at:at + batch]
                 torch.index_select(flat, 0, idx, out=xb)
@@ -185,12 +185,13 @@ def train(dev, cnn, tiles, labels, epochs=8, batch=256, lr=1e-3, pos_weight=8.0,
                     xb.copy_(xb.view(batch, proposal.TILE_FRAMES, proposal.TILE_BINS, proposal.TILE_CHANNELS)
                              .flip(2).reshape(batch, proposal.TILE_VALUES))
                     yb.copy_(yb.flip(1))
-                last = at + 2 * batch > n
+                sample = (at // batch) % 8 == 0
                 cfg.learning_rate = lr * (0.05 + 0.95 * 0.5 * (1.0 + np.cos(np.pi * step / max(steps, 1))))
                 step += 1
-                got = cnn.train_step(xb.data_ptr(), yb.data_ptr(), batch, cfg, want_loss=last)
-                loss = got if last else loss
-            losses.append(loss)
+                got = cnn.train_step(xb.data_ptr(), yb.data_ptr(), batch, cfg, want_loss=sample)
+                if sample:
+                    seen.append(got)
+            losses.append(float(np.mean(seen)))
     dev.synchronize()
     return losses
 

@@ -5,9 +5,11 @@ source block (core/engine/graph.cpp:5118-5330, core/engine/vrx_stage.cpp:
 1119-1430): convert the new samples into the ring, branch-filter and FFT the
 new channel blocks, then for every receiver run the fine stage over the
 outputs whose inputs now exist, the carrier loop if the mode has one, and the
-demodulator over the audio frames whose fine history is complete. Block
-parameters come from the library's planner (rv_fine_block / rv_demod_block),
-which tests/test_planner.py pins to the reference's planner. Test
+demodulator over the audio frames whose fine history is complete. Tables
+and block parameters come from the oracle's own planner restatement
+(oracle/planner.c: or_place, or_plan_vrx, or_fine_block, ...), which
+tests/test_oracle_planner.py pins to the reference's planner, so a chain
+without front-end correction never calls the GPU library. Test
 infrastructure only.
 """
 import ctypes as C
@@ -21,6 +23,10 @@ from revenant_gb300.library import lib
 
 def _check(st):
     assert st == 0, lib().rv_last_error().decode()
+
+
+def _ok(o, st):
+    assert st == 0, o.error()
 
 
 def highest_output_for(newest, fc, fd):
@@ -40,12 +46,13 @@ class OracleChain:
         self.g = abi.GridParams(*grid)
         self.rate, self.fmt = rate, fmt
         M, T, D = grid
+        o = self.ora.lib
         self.taps = np.zeros(M * T, np.float32)
-        _check(lib().rv_design_prototype(C.byref(self.g), 120.0, self.taps.ctypes.data, self.taps.size, None, None))
+        _ok(self.ora, o.or_design_prototype(C.byref(self.g), 120.0, self.taps.ctypes.data, self.taps.size))
         self.tw = np.zeros((M, 2), np.float32)
-        _check(lib().rv_build_twiddles(M, self.tw.ctypes.data, M))
+        _ok(self.ora, o.or_build_twiddles(M, self.tw.ctypes.data, M))
         self.nco = np.zeros((1 << 16, 2), np.float32)
-        _check(lib().rv_build_nco_table(16, self.nco.ctypes.data, 1 << 16))
+        _ok(self.ora, o.or_build_nco_table(16, self.nco.ctypes.data, 1 << 16))
         self.ring = cf32(1 << ring_log2)
         self.ring_mask = (1 << ring_log2) - 1
         self.chan_blocks = 1 << chan_log2
@@ -58,23 +65,22 @@ class OracleChain:
         self.fe_dc = self.fe_iq = False
         self.fe_lag = 1
         self.fe_was_on = False
-        self.fe = abi.FrontEnd()
-        _check(lib().rv_front_end_init(C.byref(self.fe)))
+        self.fe = None  # the estimate, made when the correction is first turned on
         self.fe_pending = []  # (run index, count, chunk sums) not yet in the estimate
         self.run_index = 0
         self.rx = []
         for req in requests:
             pl = abi.VrxPlacement()
-            _check(lib().rv_place(C.byref(self.g), rate, C.byref(req), C.byref(pl)))
+            _ok(self.ora, o.or_place(C.byref(self.g), rate, C.byref(req), C.byref(pl)))
             info = abi.VrxPlanInfo()
-            _check(lib().rv_plan_vrx(C.byref(self.g), rate, C.byref(req), C.byref(pl), C.byref(info), None, 0, None, 0))
+            _ok(self.ora, o.or_plan_vrx(C.byref(self.g), rate, C.byref(req), C.byref(pl), C.byref(info), None, 0, None, 0))
             taps = np.zeros((info.fine_tap_count, 2), np.float32)
             w = np.zeros(info.demod_weight_count, np.float32)
-            _check(lib().rv_plan_vrx(C.byref(self.g), rate, C.byref(req), C.byref(pl), C.byref(info), taps.ctypes.data,
+            _ok(self.ora, o.or_plan_vrx(C.byref(self.g), rate, C.byref(req), C.byref(pl), C.byref(info), taps.ctypes.data,
                                      taps.shape[0], w.ctypes.data, w.size))
             self.rx.append(dict(info=info, taps=taps, w=w, fine=cf32(self.fine_mask + 1), state=np.zeros(8, np.uint32),
                                 started=False, reset=True, audio=[],
-                                history=lib().rv_demod_fine_history(C.byref(info.demod))))
+                                history=o.or_demod_fine_history(C.byref(info.demod))))
 
     def set_front_end(self, dc, iq, lag=1):
         self.fe_dc, self.fe_iq, self.fe_lag = bool(dc), bool(iq), lag
@@ -134,6 +140,9 @@ class OracleChain:
         o = self.ora
         on = self.fe_dc or self.fe_iq
         if on and not self.fe_was_on:
+            if self.fe is None:
+                self.fe = abi.FrontEnd()
+                _check(lib().rv_front_end_init(C.byref(self.fe)))
             _check(lib().rv_front_end_reset(C.byref(self.fe)))
             self.fe_pending = []
         self.fe_was_on = on
@@ -204,14 +213,14 @@ class OracleChain:
                 while done < n_total:
                     n = min(n_total - done, per)
                     fb = abi.VrxFineBlock()
-                    _check(lib().rv_fine_block(C.byref(info), info.placement.channel * self.chan_blocks,
+                    _ok(o, o.lib.or_fine_block(C.byref(info), info.placement.channel * self.chan_blocks,
                                                self.chan_blocks - 1, self.fine_mask, r["next_out"] + done, n,
                                                C.byref(fb)))
                     assert o.vrx_fine(info.fine, fb.params, self.chan, r["taps"], self.nco, r["fine"]) == 0, o.error()
                     done += n
                 if info.carrier.power:
                     cpar = abi.VrxCarrierParams()
-                    _check(lib().rv_carrier_block(C.byref(info), self.fine_mask, r["next_out"], n_total,
+                    _ok(o, o.lib.or_carrier_block(C.byref(info), self.fine_mask, r["next_out"], n_total,
                                                   1 if r["reset"] else 0, 0.0, C.byref(cpar)))
                     assert o.vrx_carrier(info.carrier, cpar, self.nco, r["fine"], r["state"]) == 0, o.error()
                     r["reset"] = False
@@ -221,7 +230,7 @@ class OracleChain:
                 if audio_limit + 1 > r["next_audio"]:
                     n = audio_limit + 1 - r["next_audio"]
                     db = abi.VrxDemodBlock()
-                    _check(lib().rv_demod_block(C.byref(info), self.fine_mask, r["next_audio"], n, C.byref(db)))
+                    _ok(o, o.lib.or_demod_block(C.byref(info), self.fine_mask, r["next_audio"], n, C.byref(db)))
                     out = np.zeros(n * info.demod.channels, np.float32)
                     assert o.vrx_demod(info.demod, db.params, r["fine"], r["w"], out) == 0, o.error()
                     r["audio"].append(out)

@@ -71,12 +71,15 @@ def scene(n, rate, emitters, snr_db=30.0, seed=0):
 def random_receivers(count, rate, seed, modes=("nfm", "am", "usb", "lsb", "wfm"), bw=(12_500, 200_000),
                      grid=(64, 17, 32)):
     """Seeded receiver population: offsets uniform over the span, bandwidth
-    uniform in bw, modes uniform; a request the planner refuses is redrawn."""
+    uniform in bw, modes uniform; a request the planner refuses is redrawn.
+    The planner is the oracle's restatement (pinned to the reference's and
+    to the GPU library's), so drawing needs no GPU library."""
     import ctypes as C
 
+    from bindings import oracle
     from revenant_gb300 import abi
-    from revenant_gb300.library import lib
 
+    o = oracle().lib
     rng = np.random.default_rng(seed)
     g = abi.GridParams(*grid)
     out = []
@@ -86,10 +89,10 @@ def random_receivers(count, rate, seed, modes=("nfm", "am", "usb", "lsb", "wfm")
         c = int(rng.uniform(-0.45 * rate, 0.45 * rate))
         req = abi.request(center=c, bandwidth=b, demod=mode, stereo=True)
         pl = abi.VrxPlacement()
-        if lib().rv_place(C.byref(g), rate, C.byref(req), C.byref(pl)) != 0:
+        if o.or_place(C.byref(g), rate, C.byref(req), C.byref(pl)) != 0:
             continue
         info = abi.VrxPlanInfo()
-        if lib().rv_plan_vrx(C.byref(g), rate, C.byref(req), C.byref(pl), C.byref(info), None, 0, None, 0) != 0:
+        if o.or_plan_vrx(C.byref(g), rate, C.byref(req), C.byref(pl), C.byref(info), None, 0, None, 0) != 0:
             continue
         out.append(req)
     return out

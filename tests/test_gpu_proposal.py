@@ -121,7 +121,7 @@ def _scene_frames(gpu, seed, n):
 
 
 def test_learned_proposal_keeps_the_plain_detectors_bursts(gpu):
-    n = 1 << 26
+    n = 1 << 27
     tiles, labels = [], []
     for seed in range(60, 68):
         fr = _scene_frames(gpu, seed, n)
@@ -130,7 +130,8 @@ def test_learned_proposal_keeps_the_plain_detectors_bursts(gpu):
         labels.append(w.labels_for(inst, cands, tiles[-1].shape[0]))
         del fr
     cnn = proposal.Cnn(gpu, max_batch=256, seed=3)
-    losses = w.train(gpu, cnn, torch.cat(tiles, 0), np.concatenate(labels, 0), epochs=12, lr=2e-3, pos_weight=4.0)
+    losses = w.train(gpu, cnn, torch.cat(tiles, 0), np.concatenate(labels, 0), epochs=16, lr=2e-3, pos_weight=4.0)
+    del tiles
     assert losses[-1] < losses[0]
     # threshold: 99 % of the validation scene's localised candidates
     vfr = _scene_frames(gpu, 69, n)

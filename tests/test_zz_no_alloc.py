@@ -57,6 +57,29 @@ def test_noalloc_matches_allocating_path_twice_in_a_row(gpu, calls):
         assert same_bits(got, want), "M=%d blocks=%d" % (M, blocks)
 
 
+@pytest.mark.parametrize("M,T,D,blocks,seed", [(64, 17, 32, 700, 31), (1024, 16, 512, 300, 32)])
+def test_noalloc_matches_the_oracle(gpu, ora, M, T, D, blocks, seed):
+    """The same calls against the oracle's branch filter and FFT (the CPU
+    restatement pinned to the reference's twins), bit for bit."""
+    from bindings import cf32
+    g, bp, taps, ring = cases.branch_case(seed, M, T, D, blocks=blocks)
+    tw = np.zeros((M, 2), np.float32)
+    ok(lib().rv_build_twiddles(M, tw.ctypes.data, M))
+    ring_blocks = 1 << int(np.ceil(np.log2(blocks)))
+    fp = abi.PfbFftParams(M, D, int(np.log2(M)), seed * 131, blocks, ring_blocks, ring_blocks - 1)
+    branch = cf32(blocks * M)
+    assert ora.pfb_branch(g, bp, taps, ring, branch) == 0
+    want = cf32(M * ring_blocks)
+    assert ora.pfb_fft(fp, branch, tw, want) == 0
+    d_taps, d_ring, d_tw = gpu.array(taps), gpu.array(ring), gpu.array(tw)
+    d_out = gpu.zeros(M * ring_blocks * 8)
+    for _ in range(2):
+        ok(lib().rv_pfb_channelize_noalloc(gpu.stream, C.byref(g), C.byref(bp), C.byref(fp), d_taps.ptr, taps.size,
+                                           d_ring.ptr, ring.shape[0], d_tw.ptr, M, d_out.ptr, M * ring_blocks))
+        gpu.synchronize()
+        assert same_bits(d_out.download(np.float32, (M * ring_blocks, 2)), want)
+
+
 def test_noalloc_refuses_requests_beyond_its_scratch(gpu):
     M = 64
     g, bp, taps, ring = cases.branch_case(5, M, 17, 32, blocks=2)
