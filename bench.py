@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-excision", action="store_true", help="skip the timed run with impulse excision on")
     ap.add_argument("--no-c4", action="store_true", help="skip the M = 4096 channelizer DFT comparison")
     ap.add_argument("--no-noise", action="store_true", help="skip the scene noise field measurement")
+    ap.add_argument("--no-fast", action="store_true", help="skip the fast-mode (tensor-core fine stage) leg")
     ap.add_argument("--no-c1c2", action="store_true", help="skip the C1 single-receiver and C2 channelizer legs")
     ap.add_argument("--no-c5", action="store_true", help="skip the learned detection proposal (C5)")
     ap.add_argument("--c5-log2n", type=int, default=30, help="log2 samples of the C5 burst capture")
@@ -236,10 +237,11 @@ def run_gb300(args):
                 ch.run(_Offset(pinned, at * 4), m, host=True)
             at += m
 
-    def timed(source):
+    def timed(source, ch=None):
+        ch = chain if ch is None else ch
         for _ in range(args.warmup):
-            step(chain, source)
-        base = chain.stats()
+            step(ch, source)
+        base = ch.stats()
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
@@ -249,7 +251,7 @@ def run_gb300(args):
         t0.record(stream)
         wall = time.perf_counter()
         for _ in range(args.steps):
-            step(chain, source)
+            step(ch, source)
         t1.record(stream)
         t1.synchronize()
         wall = time.perf_counter() - wall
@@ -259,7 +261,7 @@ def run_gb300(args):
             t = torch.tensor([ms], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             ms = float(t.item())
-        return ms, wall, chain.stats(), base
+        return ms, wall, ch.stats(), base
 
     with Clocks(local) as clocks:
         ms, wall, st, base = timed("device")
@@ -320,6 +322,34 @@ def run_gb300(args):
                             "excision passes, the channelizer reading the ring up to the stage's cleaned end"}
         xch.close()
 
+    # fast mode (RV_CHAIN_FAST): the same timed run with the fine stage as
+    # split-precision BF16 GEMMs on the tensor cores (tolerance-checked, not
+    # bit-exact), and its per-stage split from a directly launched fast chain
+    fast = None
+    if not args.no_fast:
+        fch = make_chain(abi.CHAIN_FAST, run_samples, profile=False, pipelined=True)
+        fch.capture_graph()
+        fms, _, _, _ = timed("device", fch)
+        fms_e2e, _, _, _ = timed("host", fch)
+        fch.close()
+        pfch = make_chain(abi.CHAIN_FAST, run_samples, profile=True)
+        for _ in range(args.warmup):
+            step(pfch, "device")
+        fbase = pfch.stats()
+        for _ in range(args.steps):
+            step(pfch, "device")
+        fst = pfch.stats()
+        pfch.close()
+        fstage = {k: getattr(fst, k + "_ms") - getattr(fbase, k + "_ms") for k in ("coarse", "fine", "demod")}
+        fast = {"value": round(samples_step * world * args.steps / (fms / 1e3) / 1e6, 2), "unit": "MS/s",
+                "ms_per_step": round(fms / args.steps, 3),
+                "e2e": round(samples_step * world * args.steps / (fms_e2e / 1e3) / 1e6, 2),
+                "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in fstage.items()},
+                "fine_speedup_vs_exact": round(stage_ms["fine"] / max(fstage["fine"], 1e-9), 2),
+                "note": "rv_chain_create(RV_CHAIN_FAST): fine stage on tcgen05 (hi*hi + hi*lo + lo*hi BF16 "
+                        "products, FP32 accumulation); fine outputs within 1e-3 relative RMS of the bit-exact "
+                        "chain per receiver (tests/test_gpu_chain_fast.py)"}
+
     plain = None
     if not args.no_plain:
         # the reference's recording, one launch per stage per receiver, on
@@ -369,6 +399,7 @@ def run_gb300(args):
                                            "per instruction"}},
         "realtime_factor": round(value * 1e6 / RATE / max(world, 1), 1),
         "plain_path": plain,
+        "fast_mode": fast,
         "with_impulse_excision": excision,
         "clocks": clocks.summary(),
     }

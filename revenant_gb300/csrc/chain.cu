@@ -134,6 +134,8 @@ struct Receiver {
     uint32_t tile_period = 0;
     uint64_t row_step = 0;
     uint32_t tile_shared = 0;     // float2 of shared memory a tile of this receiver needs
+    uint32_t tc_chunks = 0;       // fast mode: K chunks of its GEMM tiles (0: the exact tiles)
+    DeviceArray<uint16_t> d_tc;   // fast mode: banded tap matrices (fine_tc.cu)
     bool started = false;
     bool carrier_reset = true;
     uint64_t first_output = 0, next_output = 0, next_audio = 0;
@@ -225,6 +227,8 @@ struct rv_chain {
     rv_context* context = nullptr;
     cudaStream_t stream = nullptr;
     rv_chain_config config{};
+    bool fast = false;                 // RV_CHAIN_FAST: a batched chain with the fine stage on the tensor cores
+    DeviceArray<uint32_t> tc_status;   // fast mode: tensor-core waits that ran out
     uint32_t stages = 0;
     uint32_t bytes_per_sample = 0;
     // rings
@@ -571,6 +575,8 @@ int32_t upload_table(rv_chain* c) {
         d.det_item = r.max_det_item;
         d.audio_item = r.max_audio_item;
         d.row_step = r.row_step;
+        d.tc_chunks = r.tc_chunks;
+        d.tc_b = r.d_tc.ptr;
     }
     if (c->rx_table.count < table.size())
         if (int32_t st = c->rx_table.alloc(table.size())) return st;
@@ -774,6 +780,24 @@ void plan_tiles(Receiver& r, uint64_t fc, uint64_t fd, uint32_t budget) {
 void push_tiles(std::vector<FineTile>& list, uint32_t rx, const Receiver& r, uint64_t first, uint64_t count,
                 uint64_t target) {
     if (count == 0) return;
+    if (r.tc_chunks != 0) {
+        // fast mode: GEMM tiles of kFineTcRows rows by kFineTcColumns columns
+        const uint64_t P = r.tile_period, end = first + count;
+        const uint64_t row_lo = first / P, row_hi = (end - 1u) / P + 1u;
+        for (uint64_t b = row_lo; b < row_hi; b += kFineTcRows)
+            for (uint64_t a0 = 0; a0 < P; a0 += kFineTcColumns) {
+                FineTile t{};
+                t.rx = rx;
+                t.a0 = (uint32_t)a0;
+                t.width = (uint32_t)std::min<uint64_t>(kFineTcColumns, P - a0);
+                t.rows = (uint32_t)std::min<uint64_t>(kFineTcRows, row_hi - b);
+                t.row0 = b;
+                t.first = first;
+                t.end = end;
+                list.push_back(t);
+            }
+        return;
+    }
     const uint64_t P = r.tile_period, T = r.plan.fine.taps, end = first + count;
     const uint64_t row_lo = first / P, row_hi = (end - 1u) / P + 1u;
     const uint64_t chunk = kTileRows;
@@ -899,8 +923,10 @@ int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
                                      c->twiddles.ptr, c->channel.ptr, &rc->coarse,
                                      sh.front_end ? S(c).fe_dev.ptr : nullptr);
     if (!st)
-        st = launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, sh.tiles, chan, sh.tile_shared,
-                               &rc->queues.tiles, &rc->tiles);
+        st = c->fast ? launch_fine_tc(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, sh.tiles, chan, &rc->queues.tiles,
+                                      &rc->tiles, c->tc_status.ptr)
+                     : launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, sh.tiles, chan, sh.tile_shared,
+                                         &rc->queues.tiles, &rc->tiles);
     if (!st)
         st = launch_fine_units(c->stream, c->rx_table.ptr, items, S(c).units_dev.ptr, sh.units, chan, c->unit_budget,
                                &rc->queues.units, &rc->units);
@@ -1058,8 +1084,12 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     if (config->format != RV_FORMAT_CS16 && config->format != RV_FORMAT_CU8)
         return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_chain_create: input format %d (cs16 and cu8 are supported)",
                              config->format);
-    if (config->mode != RV_CHAIN_BATCHED && config->mode != RV_CHAIN_PLAIN)
+    if (config->mode != RV_CHAIN_BATCHED && config->mode != RV_CHAIN_PLAIN && config->mode != RV_CHAIN_FAST)
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: mode %d", config->mode);
+    rv_chain_config cfg = *config;
+    const bool fast = cfg.mode == RV_CHAIN_FAST;
+    if (fast) cfg.mode = RV_CHAIN_BATCHED;  // everything but the fine stage runs as batched
+    config = &cfg;
     if (config->rate <= 0 || config->rate % g.decimation != 0)
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: rate %lld must be a positive multiple of D=%u",
                              (long long)config->rate, g.decimation);
@@ -1072,6 +1102,7 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     c->context = context;
     c->stream = reinterpret_cast<cudaStream_t>(rv_context_stream(context));
     c->config = *config;
+    c->fast = fast;
     if (c->config.attenuation_db <= 0.0) c->config.attenuation_db = 120.0;
     rv_front_end_init(&c->fe);
     c->bytes_per_sample = config->format == RV_FORMAT_CS16 ? 4u : 2u;
@@ -1111,6 +1142,8 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
         if (!st) st = c->branch.alloc(blocks_per_run * g.channels);
     }
     if (!st) st = c->channel.alloc((uint64_t)g.channels * c->chan_blocks);
+    if (!st && fast) st = c->tc_status.alloc(1);
+    if (!st && fast) st = cuda_status(cudaMemsetAsync(c->tc_status.ptr, 0, sizeof(uint32_t), c->stream), "status clear");
     if (!st) st = cuda_status(cudaMemsetAsync(c->channel.ptr, 0, (uint64_t)g.channels * c->chan_blocks * sizeof(rv_cf32), c->stream),
                               "channel clear");
     std::vector<rv_cf32> tw, nco;
@@ -1148,6 +1181,7 @@ int32_t rv_chain_destroy(rv_chain* c) {
     for (Receiver& r : c->rx) {
         r.d_taps.release();
         r.d_lerped.release();
+        r.d_tc.release();
         r.d_fine.release();
         r.d_det.release();
         r.d_weights.release();
@@ -1163,6 +1197,7 @@ int32_t rv_chain_destroy(rv_chain* c) {
     c->ex_removed.release();
     c->branch.release();
     c->channel.release();
+    c->tc_status.release();
     c->proto.release();
     c->twiddles.release();
     c->nco.release();
@@ -1258,10 +1293,19 @@ int32_t rv_chain_add_receiver(rv_chain* c, const rv_vrx_request* request, uint32
     if (!st) st = cuda_status(cudaMemcpyAsync(r.d_weights.ptr, r.weights.data(), r.weights.size() * 4, cudaMemcpyHostToDevice, c->stream), "weights upload");
     if (!st) st = r.d_state.alloc(RV_CARRIER_STATE_WORDS);
     if (!st) st = cuda_status(cudaMemsetAsync(r.d_state.ptr, 0, RV_CARRIER_STATE_WORDS * 4, c->stream), "state clear");
+    // fast mode: the tiled receivers' banded tap matrices for the tensor cores
+    if (!st && c->fast && r.tile_cols != 0 && r.d_lerped.ptr) {
+        r.tc_chunks = fine_tc_chunks(p.fine.taps, r.tile_period, (uint32_t)(fc / fd), (uint32_t)rem, (uint32_t)fd);
+        st = r.d_tc.alloc(fine_tc_table_elements(r.tile_period, r.tc_chunks));
+        if (!st)
+            st = launch_fine_tc_tables(c->stream, r.d_lerped.ptr, p.fine.taps, r.period, r.tile_period, (uint32_t)(fc / fd),
+                                       (uint32_t)rem, (uint32_t)fd, r.tc_chunks, r.d_tc.ptr);
+    }
     if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "receiver setup");
     if (st) {
         r.d_taps.release();
         r.d_lerped.release();
+        r.d_tc.release();
         r.d_fine.release();
         r.d_det.release();
         r.d_weights.release();
@@ -1477,11 +1521,14 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             const uint64_t tile_target = std::max<uint64_t>(1, tile_cost_total / (uint64_t)(4 * std::max(sms, 1)));
             for (const TileSpan& ts : tile_spans) push_tiles(tiles, ts.rx, c->rx[ts.rx], ts.first, ts.count, tile_target);
-            // largest first, so the last tiles to start are the short ones
-            std::stable_sort(tiles.begin(), tiles.end(), [&](const FineTile& x, const FineTile& y) {
-                return (uint64_t)x.rows * x.width * c->rx[x.rx].plan.fine.taps >
-                       (uint64_t)y.rows * y.width * c->rx[y.rx].plan.fine.taps;
-            });
+            // largest first, so the last tiles to start are the short ones (a
+            // tensor-core tile costs its K chunks whatever its rows)
+            auto tile_cost = [&](const FineTile& t) {
+                const Receiver& r = c->rx[t.rx];
+                return r.tc_chunks != 0 ? (uint64_t)r.tc_chunks : (uint64_t)t.rows * t.width * r.plan.fine.taps;
+            };
+            std::stable_sort(tiles.begin(), tiles.end(),
+                             [&](const FineTile& x, const FineTile& y) { return tile_cost(x) > tile_cost(y); });
             const uint64_t target = std::max<uint64_t>(1, unit_cost_total / (uint64_t)(4 * std::max(sms, 1)));
             for (const UnitSpan& us : unit_spans) {
                 const uint32_t per = (uint32_t)std::max<uint64_t>(1, target / std::max<uint64_t>(1, us.cost_per_item));
@@ -1540,8 +1587,10 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
         }
         const WorkItem* d = S(c).items_dev.ptr;
         const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
-        if ((st = launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
-                                    c->tile_shared, &S(c).queues.ptr->tiles)))
+        if ((st = c->fast ? launch_fine_tc(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
+                                           &S(c).queues.ptr->tiles, nullptr, c->tc_status.ptr)
+                          : launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
+                                              c->tile_shared, &S(c).queues.ptr->tiles)))
             return st;
         if ((st = launch_fine_units(c->stream, c->rx_table.ptr, S(c).items_dev.ptr, S(c).units_dev.ptr,
                                     (uint32_t)units.size(), chan, c->unit_budget, &S(c).queues.ptr->units)))
@@ -1755,6 +1804,15 @@ int32_t rv_chain_drain(rv_chain* c) {
     if (int32_t st = cuda_status(cudaStreamSynchronize(c->stream), "rv_chain_drain")) return st;
     if (c->copy_stream)
         if (int32_t st = cuda_status(cudaStreamSynchronize(c->copy_stream), "rv_chain_drain")) return st;
+    if (c->fast) {  // a bounded tensor-core wait that ran out
+        uint32_t timeouts = 0;
+        if (int32_t st = cuda_status(cudaMemcpy(&timeouts, c->tc_status.ptr, sizeof timeouts, cudaMemcpyDeviceToHost),
+                                     "rv_chain_drain"))
+            return st;
+        if (timeouts)
+            return set_error_fmt(RV_ERR_TIMEOUT, "rv_chain_drain: %u fine-stage CTAs gave up waiting on the tensor cores",
+                                 timeouts);
+    }
     return clear_error();
 }
 

@@ -48,8 +48,9 @@ struct RxDev {
     uint32_t tile_period;   // P': outputs per row, a multiple of the pattern period
     uint32_t det_item;      // detector item: fine samples (batched detector)
     uint32_t audio_item;    // audio item: frames (batched audio)
-    uint32_t pad;
+    uint32_t tc_chunks;     // fast mode (fine_tc.cu): 64-element K chunks of each column group's GEMM
     uint64_t row_step;      // Dp = P' Fc / Fd: input samples between rows
+    const uint16_t* tc_b;   // fast mode: the banded tap matrices, BF16 hi and lo, per group and chunk
 };
 
 // One receiver's detector and audio work of a run. The device splits it into
@@ -123,6 +124,12 @@ struct FineTile {
     uint64_t end;
 };
 
+// Fast mode's fine stage (fine_tc.cu): GEMM tiles of kFineTcRows rows by
+// kFineTcColumns outputs; a FineTile then has a0 a multiple of the columns,
+// width <= kFineTcColumns and rows <= kFineTcRows.
+constexpr uint32_t kFineTcColumns = 32;
+constexpr uint32_t kFineTcRows = 128;
+
 constexpr int kTileThreads = 256;
 constexpr uint32_t kTileRows = 16;  // rows per staged chunk: one half-warp
 constexpr uint32_t kTileSlots = kTileThreads / kTileRows;  // column slots of R columns each
@@ -192,6 +199,14 @@ uint32_t fine_unit_shared_budget();  // float2 entries of dynamic shared memory 
 // CTA (the largest tiled receiver's table slice plus row buffers).
 int32_t launch_fine_tiles(cudaStream_t s, const RxDev* rxs, const FineTile* tiles, uint32_t ntiles,
                           const float2* chan, uint32_t shared_float2s, uint32_t* queue, const uint32_t* dyn = nullptr);
+// Fast mode: the chunks of a receiver's tables, their size in BF16 values,
+// the table builder (from the blended taps) and the GEMM tiles' launch.
+uint32_t fine_tc_chunks(uint32_t taps, uint32_t P, uint32_t step_whole, uint32_t step_rem, uint32_t fd);
+uint64_t fine_tc_table_elements(uint32_t P, uint32_t chunks);
+int32_t launch_fine_tc_tables(cudaStream_t s, const float2* lerped, uint32_t T, uint32_t period, uint32_t P,
+                              uint32_t step_whole, uint32_t step_rem, uint32_t fd, uint32_t chunks, uint16_t* out);
+int32_t launch_fine_tc(cudaStream_t s, const RxDev* rxs, const FineTile* tiles, uint32_t ntiles, const float2* chan,
+                       uint32_t* queue, const uint32_t* dyn, uint32_t* status);
 int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
                                const uint32_t* dyn = nullptr);
 int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, SpanList spans, uint32_t nitems,

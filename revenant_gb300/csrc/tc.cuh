@@ -1,7 +1,7 @@
 // tcgen05 building blocks shared by the tensor-core kernels: shared-memory
-// matrix descriptors for the canonical no-swizzle K-major layout, the
-// kind::f16 instruction descriptor, MMA issue and commit, bounded mbarrier
-// waits, the tcgen05 fences and TMEM loads.
+// matrix descriptors for the canonical no-swizzle and the 128-byte swizzled
+// K-major layouts, the kind::f16 instruction descriptor, MMA issue and
+// commit, bounded mbarrier waits, the tcgen05 fences and TMEM loads.
 //
 // Layout: a K-major operand of R rows and a K chunk of KC 16-bit elements is
 // stored as 8-row x 16-byte core matrices; core matrix (r / 8, k / 8) sits at
@@ -29,6 +29,22 @@ __device__ __forceinline__ uint32_t core_offset(uint32_t r, uint32_t k, uint32_t
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo_bytes) {
     return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) |
            ((uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// The 128-byte swizzled K-major layout for a K chunk of 64 16-bit elements
+// (one 128-byte row per operand row): row r at r * 128 bytes, its sixteen-
+// byte piece j stored at piece j ^ (r % 8). Eight-row groups are 1024 bytes
+// apart (the stride byte offset); an operand must start on a 1024-byte
+// boundary, and the K step s of an MMA starts 32 * s bytes in.
+__device__ __host__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t k) {
+    return r * 128u + ((((k >> 3) ^ r) & 7u) << 4) + (k & 7u) * 2u;
+}
+
+// Shared-memory matrix descriptor (version 1) for the 128-byte swizzled
+// K-major layout: stride byte offset 1024, leading byte offset unused (1).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | (1ull << 16) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
 }
 
 // kind::f16 instruction descriptor: FP32 accumulator, A and B of type
