@@ -258,7 +258,7 @@ k_fine_tc(const RxDev* __restrict__ rxs, const FineTile* __restrict__ tiles, uin
     if (warp == kMmaWarp) tc::tmem_alloc(tc::smem_addr(&s_tmem), 2u * kTmemCols);
     if (tid == 0) {
         for (uint32_t b = 0; b < kRing; ++b) {
-            tc::mbar_init(tc::smem_addr(full + b), kConvThreads + 1u);  // converters + B's expect
+            tc::mbar_init(tc::smem_addr(full + b), kConvWarps + 1u);  // converter warps + B's expect
             tc::mbar_init(tc::smem_addr(empty + b), 1);
         }
         for (uint32_t b = 0; b < 2u; ++b) {
@@ -299,7 +299,8 @@ k_fine_tc(const RxDev* __restrict__ rxs, const FineTile* __restrict__ tiles, uin
             if (more) load_chunk(nxt, w, warp, lane);
             store_chunk(st, cur, warp, lane);
             tc::fence_async_smem();
-            mbar_arrive(tc::smem_addr(full + slot));
+            __syncwarp();  // the warp's stores before its one arrival
+            if (lane == 0) mbar_arrive(tc::smem_addr(full + slot));
         }
         // after a stop, B copies still landing finish before the stages go
         if (tid == 0)
