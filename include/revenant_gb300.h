@@ -1103,14 +1103,20 @@ int32_t rv_design_prototype_wide(const rv_grid_params* grid, double attenuation_
  * outputs for M = 4096 (the channel ring, phase correction included),
  * computed as two 64-point DFT GEMM stages with hi + lo split operands in
  * FP16 or BF16 and FP32 accumulators. Accurate to a stated tolerance against
- * FP64, not bit-identical to rv_pfb_fft. Synchronous on `stream` (it reads
- * back a flag that a bounded wait on the tensor cores ran out:
- * RV_ERR_TIMEOUT). */
+ * FP64, not bit-identical to rv_pfb_fft. Asynchronous on `stream` (it can be
+ * captured in a graph): a CTA whose bounded wait on the tensor cores or a
+ * bulk copy runs out stops, waits (bounded) for what it has in flight and
+ * counts itself on the device; rv_pfb_dft_tc_status reads and clears that
+ * count (synchronising `stream`) and returns RV_ERR_TIMEOUT when it is not
+ * zero. rv_pfb_dft_tc_stop_for_test makes every later call stop each CTA
+ * before it issues a copy or an MMA (a test of the stop path); 0 clears it. */
 #define RV_DFT_FP16 0
 #define RV_DFT_BF16 1
 int32_t rv_pfb_dft_tc(void* stream, const rv_pfb_fft_params* params, const rv_cf32* branch_dev, uint64_t branch_len,
                       const rv_cf32* twiddles_dev, uint64_t twiddles_len, rv_cf32* ring_dev, uint64_t ring_len,
                       int32_t precision);
+int32_t rv_pfb_dft_tc_status(void* stream, uint32_t* timeouts);
+int32_t rv_pfb_dft_tc_stop_for_test(void* stream, int32_t stop);
 int32_t rv_pfb_branch_wide(void* stream, const rv_grid_params* grid, const rv_pfb_branch_params* params,
                            const float* taps_dev, uint64_t taps_len, const rv_cf32* ring_dev,
                            uint64_t ring_len, rv_cf32* out_dev, uint64_t out_len);

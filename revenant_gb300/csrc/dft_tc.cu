@@ -66,7 +66,8 @@ constexpr uint32_t kWaitLimit = 1u << 20;
 static_assert(kSmemBytes <= 232448, "shared memory per CTA");
 static_assert(kRadix * (kCols + 1) * 4 <= 2 * kXBytes, "the output exchange fits the two halves");
 
-__device__ uint32_t g_dft_timeouts;
+__device__ uint32_t g_dft_timeouts;  // CTAs that stopped on a wait that ran out, since the last status read
+__device__ uint32_t g_dft_stop;      // test hook: every CTA stops before it issues a copy or an MMA
 
 // Element (r, k) of a 128 x 128 K-major operand: core matrix (r/8, k/8) at
 // ((r/8) * 16 + k/8) * 128 bytes, row r%8 at 16 bytes each. K-adjacent core
@@ -256,11 +257,18 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_mma));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_raw));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        *abort_flag = 0;
+        *abort_flag = *reinterpret_cast<volatile uint32_t*>(&g_dft_stop) != 0u ? 1u : 0u;
     }
     __syncthreads();
-    if (tid == 0 && blockIdx.x < tiles)
+    const bool stopped = *abort_flag != 0u;  // read by every thread before any wait can set it
+    // thread 0's copies and MMAs in flight: after a stop it waits for them
+    // (bounded) before the shared and tensor memory go
+    bool raw_pending = false, mma_pending = false;
+    uint32_t raw_pending_parity = 0, mma_pending_parity = 0;
+    if (tid == 0 && blockIdx.x < tiles && !stopped) {
         prefetch(raw_addr, branch + (uint64_t)blockIdx.x * kPair * kM, valid_in(blockIdx.x), mbar_raw);
+        raw_pending = true;
+    }
     // A = F in real block form, the same for both stages: row r = [Re | Im]
     // of the output index, column k = [Re | Im] of the summed index.
     {
@@ -286,17 +294,20 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
     const float* const theirs_x = re_row ? xb : xa;
 
     uint32_t parity_mma = 0, parity_raw = 0;
-    bool raw_in_flight = blockIdx.x < tiles;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (uint32_t tile = stopped ? tiles : blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t b0 = tile * kPair, nvalid = valid_in(tile);
         const uint32_t blk = row >> 6, i64 = row & 63u, b = b0 + blk;
         const bool valid = blk < nvalid;
         const float2* y = raw + blk * kM;
         const uint32_t m_abs = p.block_base + b;
         const uint32_t dm = ((m_abs & (kM - 1u)) * p.decimation) & (kM - 1u);
-        if (!wait_parity(mbar_raw, parity_raw)) atomicExch(abort_flag, 1u);
+        if (wait_parity(mbar_raw, parity_raw)) {
+            if (tid == 0) raw_pending = false;
+        } else {
+            atomicExch(abort_flag, 1u);
+        }
+        if (tid == 0 && raw_pending) raw_pending_parity = parity_raw;
         parity_raw ^= 1u;
-        raw_in_flight = false;
         // the block's largest component, for the power-of-two scale
         float mx = 0.0F;
         if (valid)
@@ -337,14 +348,19 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         __syncthreads();
         if (tid == 0) {
             issue_gemm<P>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b_hi), smem_addr(b_lo), mbar_mma);
+            mma_pending = true, mma_pending_parity = parity_mma;
             const uint32_t next = tile + gridDim.x;  // the raw blocks are read: fetch the next tile's
-            if (next < tiles) {
+            if (next < tiles && !raw_pending) {
                 fence_async_smem();
                 prefetch(raw_addr, branch + (uint64_t)next * kPair * kM, valid_in(next), mbar_raw);
+                raw_pending = true, raw_pending_parity = parity_raw;
             }
         }
-        raw_in_flight = tile + gridDim.x < tiles;
-        if (!wait_parity(mbar_mma, parity_mma)) atomicExch(abort_flag, 1u);
+        if (wait_parity(mbar_mma, parity_mma)) {
+            if (tid == 0) mma_pending = false;
+        } else {
+            atomicExch(abort_flag, 1u);
+        }
         parity_mma ^= 1u;
         __syncthreads();
         if (*abort_flag) break;
@@ -379,8 +395,15 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         fence_async_smem();
         fence_before();
         __syncthreads();
-        if (tid == 0) issue_gemm<P>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b_hi), smem_addr(b_lo), mbar_mma);
-        if (!wait_parity(mbar_mma, parity_mma)) atomicExch(abort_flag, 1u);
+        if (tid == 0) {
+            issue_gemm<P>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b_hi), smem_addr(b_lo), mbar_mma);
+            mma_pending = true, mma_pending_parity = parity_mma;
+        }
+        if (wait_parity(mbar_mma, parity_mma)) {
+            if (tid == 0) mma_pending = false;
+        } else {
+            atomicExch(abort_flag, 1u);
+        }
         parity_mma ^= 1u;
         __syncthreads();
         if (*abort_flag) break;
@@ -440,8 +463,10 @@ k_dft_tc(const float2* __restrict__ branch, const float2* __restrict__ tw, float
         fence_before();
         __syncthreads();  // B and the exchange are free for the next tile
     }
-    // a prefetch still in flight (after an abort) lands before the CTA leaves
-    if (tid == 0 && raw_in_flight) wait_parity(mbar_raw, parity_raw);
+    // after a stop, a prefetch or MMAs still in flight finish (bounded)
+    // before the CTA frees its tensor memory and leaves
+    if (tid == 0 && raw_pending) wait_parity(mbar_raw, raw_pending_parity);
+    if (tid == 0 && mma_pending) wait_parity(mbar_mma, mma_pending_parity);
     if (tid == 0 && *abort_flag) atomicAdd(&g_dft_timeouts, 1u);
     fence_before();
     __syncthreads();
@@ -491,21 +516,32 @@ extern "C" int32_t rv_pfb_dft_tc(void* stream, const rv_pfb_fft_params* p, const
     if (ring_len < (uint64_t)kM * p->out_ring_blocks) return set_error_fmt(RV_ERR_INVALID, "pfb dft tc: channel ring too short");
     if (p->block_count == 0) return clear_error();
     cudaStream_t s = as_stream(stream);
-    const uint32_t zero = 0;
-    if (int32_t st = cuda_status(cudaMemcpyToSymbolAsync(g_dft_timeouts, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, s),
-                                 "dft tc flag"))
-        return st;
     const float2* b = reinterpret_cast<const float2*>(branch);
     const float2* w = reinterpret_cast<const float2*>(tw);
     float2* o = reinterpret_cast<float2*>(ring);
     const int32_t st = precision == RV_DFT_FP16 ? launch<RV_DFT_FP16>(s, *p, b, w, o) : launch<RV_DFT_BF16>(s, *p, b, w, o);
     if (st) return st;
-    uint32_t timeouts = 0;
-    if (int32_t e = cuda_status(cudaMemcpyFromSymbolAsync(&timeouts, g_dft_timeouts, sizeof timeouts, 0,
-                                                          cudaMemcpyDeviceToHost, s),
-                                "dft tc flag"))
-        return e;
-    if (int32_t e = cuda_status(cudaStreamSynchronize(s), "dft tc")) return e;
-    if (timeouts) return set_error_fmt(RV_ERR_TIMEOUT, "pfb dft tc: %u CTAs gave up waiting on the tensor cores", timeouts);
     return clear_error();
+}
+
+extern "C" int32_t rv_pfb_dft_tc_status(void* stream, uint32_t* timeouts) {
+    cudaStream_t s = as_stream(stream);
+    uint32_t count = 0;
+    const uint32_t zero = 0;
+    if (int32_t e = cuda_status(cudaMemcpyFromSymbolAsync(&count, g_dft_timeouts, sizeof count, 0, cudaMemcpyDeviceToHost, s),
+                                "dft tc status"))
+        return e;
+    if (int32_t e = cuda_status(cudaMemcpyToSymbolAsync(g_dft_timeouts, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, s),
+                                "dft tc status"))
+        return e;
+    if (int32_t e = cuda_status(cudaStreamSynchronize(s), "dft tc status")) return e;
+    if (timeouts) *timeouts = count;
+    if (count) return set_error_fmt(RV_ERR_TIMEOUT, "pfb dft tc: %u CTAs gave up waiting on the tensor cores", count);
+    return clear_error();
+}
+
+extern "C" int32_t rv_pfb_dft_tc_stop_for_test(void* stream, int32_t stop) {
+    const uint32_t v = stop ? 1u : 0u;
+    return cuda_status(cudaMemcpyToSymbolAsync(g_dft_stop, &v, sizeof v, 0, cudaMemcpyHostToDevice, as_stream(stream)),
+                       "dft tc stop");
 }

@@ -190,6 +190,8 @@ SIGNATURES = {
     "rv_emitter_accumulate": (I32, [P, ptr(abi.ToneEmitter), U64, U64, F64, P, U64]),
     "rv_scene_noise_draws": (I32, [P, U64, U64, U64, P, U64]),
     "rv_pfb_dft_tc": (I32, [P, ptr(abi.PfbFftParams), P, U64, P, U64, P, U64, I32]),
+    "rv_pfb_dft_tc_status": (I32, [P, ptr(U32)]),
+    "rv_pfb_dft_tc_stop_for_test": (I32, [P, I32]),
     "rv_capture_writer_open": (I32, [C.c_char_p, ptr(abi.CaptureConfig), C.c_char_p, ptr(P)]),
     "rv_capture_writer_write": (I32, [P, ptr(abi.CaptureBlock), P, U64]),
     "rv_capture_writer_set_gain": (I32, [P, I32, F64]),

@@ -171,6 +171,8 @@ def test_gpu_c4_tensor_core_dft(gpu, precision):
         fp = abi.PfbFftParams(M, D, 12, base, blocks, ring_blocks, ring_blocks - 1)
         assert lib().rv_pfb_dft_tc(gpu.stream, C.byref(fp), d_branch.ptr, blocks * M, d_tw.ptr, M, d_chan.ptr,
                                    M * ring_blocks, prec) == 0, lib().rv_last_error()
+        timeouts = C.c_uint32(7)
+        assert lib().rv_pfb_dft_tc_status(gpu.stream, C.byref(timeouts)) == 0 and timeouts.value == 0
         got = d_chan.download(np.float32, (M * ring_blocks, 2)).reshape(M, ring_blocks, 2)
         slots = [(base + b) & (ring_blocks - 1) for b in range(checked)]
         rel, spur = check_tolerance(got[:, slots].reshape(-1, 2), fp64(g, taps, ring, base, checked), checked,
@@ -178,6 +180,50 @@ def test_gpu_c4_tensor_core_dft(gpu, precision):
         print("C4 tensor-core DFT (%s split) vs FP64, %d blocks: relative RMS %.2e, spur floor %.1f dBc"
               % (precision, blocks, rel, spur))
         assert rel <= rel_max and spur <= spur_max
+
+
+@pytest.mark.gpu
+def test_gpu_c4_tensor_core_dft_stop_path(gpu):
+    """The stop path of rv_pfb_dft_tc's bounded waits, without making one run
+    out: the test hook stops every CTA before it issues a copy or an MMA, the
+    status call then reports RV_ERR_TIMEOUT with one count per CTA and clears
+    it, the ring is left untouched, and the next call is bit-identical to one
+    made before the stop."""
+    g, taps, _ = prototype()
+    tw = twiddles()
+    n = 1 << 18
+    ring = multitone(n, seed=9)
+    d_ring, d_taps, d_tw = gpu.array(ring), gpu.array(taps), gpu.array(tw)
+    blocks, ring_blocks, base = 64, 64, M * T // D
+    bp = abi.PfbBranchParams(n - 1, base * D, blocks)
+    d_branch = gpu.zeros(blocks * M * 8)
+    assert lib().rv_pfb_branch_wide(gpu.stream, C.byref(g), C.byref(bp), d_taps.ptr, taps.size, d_ring.ptr, n,
+                                    d_branch.ptr, blocks * M) == 0, lib().rv_last_error()
+    fp = abi.PfbFftParams(M, D, 12, base, blocks, ring_blocks, ring_blocks - 1)
+    d_before, d_stopped, d_after = (gpu.zeros(M * ring_blocks * 8) for _ in range(3))
+
+    def call(d_chan):
+        assert lib().rv_pfb_dft_tc(gpu.stream, C.byref(fp), d_branch.ptr, blocks * M, d_tw.ptr, M, d_chan.ptr,
+                                   M * ring_blocks, abi.DFT_BF16) == 0, lib().rv_last_error()
+
+    timeouts = C.c_uint32(0)
+    call(d_before)
+    assert lib().rv_pfb_dft_tc_status(gpu.stream, C.byref(timeouts)) == 0 and timeouts.value == 0
+    assert lib().rv_pfb_dft_tc_stop_for_test(gpu.stream, 1) == 0
+    try:
+        call(d_stopped)
+        assert lib().rv_pfb_dft_tc_status(gpu.stream, C.byref(timeouts)) == abi.RV_ERR_TIMEOUT
+        ctas = min(blocks // 2, gpu.info.sm_count)
+        assert timeouts.value == ctas, (timeouts.value, ctas)
+    finally:
+        assert lib().rv_pfb_dft_tc_stop_for_test(gpu.stream, 0) == 0
+    assert lib().rv_pfb_dft_tc_status(gpu.stream, C.byref(timeouts)) == 0 and timeouts.value == 0
+    assert not np.any(d_stopped.download(np.uint32, (M * ring_blocks * 2,)))
+    call(d_after)
+    assert lib().rv_pfb_dft_tc_status(gpu.stream, C.byref(timeouts)) == 0
+    before = d_before.download(np.uint32, (M * ring_blocks * 2,))
+    after = d_after.download(np.uint32, (M * ring_blocks * 2,))
+    assert np.array_equal(before, after)
 
 
 def test_tensor_core_dft_rejects_other_grids(rv):
