@@ -352,23 +352,37 @@ def run_gb300(args):
 
     plain = None
     if not args.no_plain:
-        # the reference's recording, one launch per stage per receiver, on
-        # a shorter capture (it is ~two orders of magnitude slower)
-        pn = 1 << 22
-        pch = make_chain(abi.CHAIN_PLAIN, 1 << 20)
-        for at in range(0, 1 << 20, 1 << 20):
-            pch.run(_Offset(d_codes, at * 4), 1 << 20)  # warm-up
-        dev.synchronize()
-        t = time.perf_counter()
-        at = 1 << 20
-        while at < (1 << 20) + pn:
-            pch.run(_Offset(d_codes, at * 4), 1 << 20)
-            at += 1 << 20
-        dt = time.perf_counter() - t
-        pst = pch.stats()
-        plain = {"value": pn / dt / 1e6, "unit": "MS/s", "sample": "2^22 samples after a 2^20 warm-up, same 256 receivers",
-                 "launches_per_run": pst.launches / max(pst.runs, 1)}
-        pch.close()
+        # the reference's recording, one launch per stage per receiver (it
+        # recomputes the detector inside every audio tap, as the reference's
+        # demodulator does), and the same with the detector hoisted (once per
+        # fine sample, still one launch per stage per receiver): the second
+        # isolates what batching adds. Both on the same 2^22 samples after a
+        # 2^20-sample warm-up, CUDA events on the chain's stream.
+        pn, blk = 1 << 22, 1 << 20
+
+        def plain_leg(mode):
+            pch = make_chain(mode, blk)
+            pch.run(_Offset(d_codes, 0), blk)  # warm-up
+            dev.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for at in range(blk, blk + pn, blk):
+                pch.run(_Offset(d_codes, at * 4), blk)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            pst = pch.stats()
+            pch.close()
+            return {"value": round(pn / (ms / 1e3) / 1e6, 3), "unit": "MS/s", "ms": round(ms, 2),
+                    "launches_per_run": round(pst.launches / max(pst.runs, 1), 1)}
+
+        plain = plain_leg(abi.CHAIN_PLAIN)
+        plain["sample"] = "2^22 samples after a 2^20 warm-up, same 256 receivers, CUDA events"
+        hoisted = plain_leg(abi.CHAIN_HOISTED)
+        hoisted["note"] = ("RV_CHAIN_HOISTED: one launch per stage per receiver with the detector once per fine "
+                           "sample; the same audio bit for bit")
+        plain["detector_hoisted"] = hoisted
+        plain["hoisting_gain"] = round(hoisted["value"] / plain["value"], 2)
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "MS/s", "n_gpus": world, "steps": args.steps,
@@ -405,6 +419,7 @@ def run_gb300(args):
     }
     if not args.no_plain and plain:
         line["vs_plain_path"] = round(value / plain["value"], 2)
+        line["vs_plain_path_detector_hoisted"] = round(value / plain["detector_hoisted"]["value"], 2)
     if rank == 0 and not args.no_detect:
         line["detection"] = detection(dev, d_codes, min(n, 1 << 26))
     if rank == 0 and not args.no_c1c2:
@@ -591,6 +606,23 @@ def c5_learned(dev, log2n, train_scenes=8, train_log2=27, epochs=16):
     return out
 
 
+C1_RATE, C1_GRID = 2_400_000, (8, 17, 4)
+
+
+def c1_capture(n, seed=1):
+    """C1's input: cu8 IQ at 2.4 MS/s (offset 127.5), a WFM carrier at
+    +200 kHz (75 kHz deviation, 1 kHz tone) plus AWGN at 25 dB SNR."""
+    rng = np.random.default_rng(seed)
+    t = np.arange(n) / C1_RATE
+    phase = 2 * np.pi * 200_000 * t + 75_000 / 1000 * np.sin(2 * np.pi * 1000 * t)
+    z = np.exp(1j * phase) + 10 ** (-25 / 20) * (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+    z *= 0.9 / np.max(np.abs(np.concatenate([z.real, z.imag])))
+    codes = np.empty(2 * n, np.uint8)
+    codes[0::2] = np.clip(np.round(z.real * 127.5 + 127.5), 0, 255)
+    codes[1::2] = np.clip(np.round(z.imag * 127.5 + 127.5), 0, 255)
+    return codes
+
+
 def c1_chain(dev):
     """C1: the plain single-receiver chain as the reference runs it on the CPU:
     2^20 cu8 samples at 2.4 MS/s (seed 1), grid M=8 D=4 T=17, one stereo WFM
@@ -603,15 +635,8 @@ def c1_chain(dev):
     from oracle_chain import OracleChain
     from revenant_gb300 import abi
     from revenant_gb300.chain import Chain
-    n, block, rate, grid = 1 << 20, 1 << 14, 2_400_000, (8, 17, 4)
-    rng = np.random.default_rng(1)
-    t = np.arange(n) / rate
-    phase = 2 * np.pi * 200_000 * t + 75_000 / 1000 * np.sin(2 * np.pi * 1000 * t)
-    z = np.exp(1j * phase) + 10 ** (-25 / 20) * (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
-    z *= 0.9 / np.max(np.abs(np.concatenate([z.real, z.imag])))
-    codes = np.empty(2 * n, np.uint8)
-    codes[0::2] = np.clip(np.round(z.real * 127.5 + 127.5), 0, 255)
-    codes[1::2] = np.clip(np.round(z.imag * 127.5 + 127.5), 0, 255)
+    n, block, rate, grid = 1 << 20, 1 << 14, C1_RATE, C1_GRID
+    codes = c1_capture(n)
     req = abi.request(center=200_000, bandwidth=200_000, demod="wfm", stereo=True)
     out = {"workload": "2^20 cu8 at 2.4 MS/s (seed 1), M=8 D=4 T=17, one stereo WFM receiver, 16,384-sample "
                        "blocks from host memory"}
@@ -634,6 +659,47 @@ def c1_chain(dev):
         out[name] = {"value": round((n - 8 * block) / dt / 1e6, 2), "unit": "MS/s",
                      "us_per_block": round(dt / ((n - 8 * block) / block) * 1e6, 1), "audio_frames": int(frames)}
         ch.close()
+    # the 1024-point Hann spectrum averaged over 16 frames (lw-radio-dsp's
+    # Spectrum with a 16-frame mean, rv_spectrum_average) over the capture
+    import ctypes as C
+    import torch
+    from revenant_gb300.library import check, lib
+    size, avg = 1024, 16
+    frames = n // size
+    iq = ((codes.astype(np.float32) - 127.5) / 127.5)
+    w = np.zeros(size, np.float32)
+    norm = C.c_double()
+    check(lib().rv_build_lwdsp_window(1, size, w.ctypes.data, C.byref(norm)))
+    tw = np.zeros((size, 2), np.float32)
+    check(lib().rv_build_fft_twiddles(size, tw.ctypes.data, size))
+    sp = abi.SpectrumAverageParams(size=size, frames=frames, average=avg, mode=abi.AVERAGE_MEAN, alpha=0.0,
+                                   norm=norm.value, resume=0)
+    spectra = frames // avg
+    d_iq, d_w, d_tw = dev.array(iq), dev.array(w), dev.array(tw)
+    d_db, d_avg = dev.zeros(spectra * size * 4), dev.zeros(spectra * size * 4)
+
+    def spectrum():
+        check(lib().rv_spectrum_average(dev.stream, C.byref(sp), d_iq.address, n, d_w.address, size, d_tw.address,
+                                        size, d_db.address, spectra * size, d_avg.address, spectra * size))
+
+    stream = torch.cuda.ExternalStream(dev.stream)
+    spectrum()
+    dev.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(10):
+        spectrum()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    out["spectrum_1024_hann_mean16"] = {"ms": round(ms, 4), "spectra": spectra, "frames": frames,
+                                        "value": round(n / ms / 1e3, 1), "unit": "MS/s",
+                                        "note": "rv_spectrum_average over the whole 2^20-sample capture (cf32 on "
+                                                "the device), within the a13 tolerance of the FP64 mean "
+                                                "(tests/test_spectrum_average.py)"}
+    out["baseline_shape"] = ("the 240 kS/s, 64-tap fine stage and decimation by 5 to 48 kHz: bit-exact against the "
+                             "oracle end to end in tests/test_gpu_c1_shape.py; the chain legs above run the planner's "
+                             "own WFM shape (336 kS/s, T = 32, stereo)")
     m = 1 << 17
     oc = OracleChain(grid, rate, abi.FORMAT_CU8, [req], ring_log2=18, chan_log2=16, fine_log2=17)
     t0 = time.perf_counter()

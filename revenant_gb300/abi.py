@@ -358,7 +358,7 @@ class DeviceInfo(_S):
                 ("max_shared_per_block", U64), ("l2_bytes", U64)]
 
 
-CHAIN_BATCHED, CHAIN_PLAIN, CHAIN_FAST = 0, 1, 2
+CHAIN_BATCHED, CHAIN_PLAIN, CHAIN_FAST, CHAIN_HOISTED = 0, 1, 2, 3
 
 
 class ChainConfig(_S):

@@ -228,6 +228,8 @@ struct rv_chain {
     cudaStream_t stream = nullptr;
     rv_chain_config config{};
     bool fast = false;                 // RV_CHAIN_FAST: a batched chain with the fine stage on the tensor cores
+    bool hoisted = false;              // RV_CHAIN_HOISTED: a batched chain whose receiver stages launch per receiver
+    DeviceArray<uint32_t> hoisted_prefix;  // per receiver: its detector then audio item prefix sums
     DeviceArray<uint32_t> tc_status;   // fast mode: tensor-core waits that ran out
     uint32_t stages = 0;
     uint32_t bytes_per_sample = 0;
@@ -1084,11 +1086,14 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     if (config->format != RV_FORMAT_CS16 && config->format != RV_FORMAT_CU8)
         return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_chain_create: input format %d (cs16 and cu8 are supported)",
                              config->format);
-    if (config->mode != RV_CHAIN_BATCHED && config->mode != RV_CHAIN_PLAIN && config->mode != RV_CHAIN_FAST)
+    if (config->mode != RV_CHAIN_BATCHED && config->mode != RV_CHAIN_PLAIN && config->mode != RV_CHAIN_FAST &&
+        config->mode != RV_CHAIN_HOISTED)
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: mode %d", config->mode);
+    if (config->mode == RV_CHAIN_HOISTED && config->pipelined)
+        return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: a hoisted chain runs its launches directly (pipelined = 0)");
     rv_chain_config cfg = *config;
-    const bool fast = cfg.mode == RV_CHAIN_FAST;
-    if (fast) cfg.mode = RV_CHAIN_BATCHED;  // everything but the fine stage runs as batched
+    const bool fast = cfg.mode == RV_CHAIN_FAST, hoisted = cfg.mode == RV_CHAIN_HOISTED;
+    if (fast || hoisted) cfg.mode = RV_CHAIN_BATCHED;  // the batched chain's state and bookkeeping
     config = &cfg;
     if (config->rate <= 0 || config->rate % g.decimation != 0)
         return set_error_fmt(RV_ERR_INVALID, "rv_chain_create: rate %lld must be a positive multiple of D=%u",
@@ -1103,6 +1108,7 @@ int32_t rv_chain_create(rv_context* context, const rv_chain_config* config, rv_c
     c->stream = reinterpret_cast<cudaStream_t>(rv_context_stream(context));
     c->config = *config;
     c->fast = fast;
+    c->hoisted = hoisted;
     if (c->config.attenuation_db <= 0.0) c->config.attenuation_db = 120.0;
     rv_front_end_init(&c->fe);
     c->bytes_per_sample = config->format == RV_FORMAT_CS16 ? 4u : 2u;
@@ -1198,6 +1204,7 @@ int32_t rv_chain_destroy(rv_chain* c) {
     c->branch.release();
     c->channel.release();
     c->tc_status.release();
+    c->hoisted_prefix.release();
     c->proto.release();
     c->twiddles.release();
     c->nco.release();
@@ -1585,36 +1592,116 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
                                   "tile upload")))
                 return st;
         }
-        const WorkItem* d = S(c).items_dev.ptr;
-        const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
-        if ((st = c->fast ? launch_fine_tc(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
-                                           &S(c).queues.ptr->tiles, nullptr, c->tc_status.ptr)
-                          : launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
-                                              c->tile_shared, &S(c).queues.ptr->tiles)))
-            return st;
-        if ((st = launch_fine_units(c->stream, c->rx_table.ptr, S(c).items_dev.ptr, S(c).units_dev.ptr,
-                                    (uint32_t)units.size(), chan, c->unit_budget, &S(c).queues.ptr->units)))
-            return st;
-        const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
-        if ((st = launch_fine_batched(c->stream, c->rx_table.ptr, d, (uint32_t)fine_items.size(), chan, window,
-                                      &S(c).queues.ptr->fine)))
-            return st;
-        d += fine_items.size();
-        if ((st = launch_carrier_batched(c->stream, c->rx_table.ptr, d, (uint32_t)carrier_items.size()))) return st;
-        d += carrier_items.size();
-        mark(c, 3);
-        SpanList det_list, audio_list;
-        span_lists(c, (uint32_t)c->rx.size(), &det_list, &audio_list);
-        if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, det_list, rx_spans.det_total, kDetWindow,
-                                        &S(c).queues.ptr->detect)))
-            return st;
-        if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, audio_list, rx_spans.audio_total, S(c).audio_dev.ptr,
-                                       kDetWindow, c->weights_cap, &S(c).queues.ptr->audio)))
-            return st;
-        mark(c, 4);
-        c->stats.launches += (rx_spans.det_total ? 1 : 0) + (rx_spans.audio_total ? 1 : 0) + (fine_items.empty() ? 0 : 1) +
-                             (units.empty() ? 0 : 1) + (carrier_items.empty() ? 0 : 1) + (tiles.empty() ? 0 : 1);
-        c->stats.work_items += total + rx_spans.det_total + rx_spans.audio_total + tiles.size();
+        if (c->hoisted) {
+            // the plain recording with the detector hoisted: fine [+ carrier]
+            // per receiver through the per-dispatch kernels, then the detector
+            // and the audio per receiver through the batched kernels, each
+            // launch given only its receiver's items
+            const size_t nrx = c->rx.size();
+            for (size_t ri = 0; ri < nrx; ++ri) {
+                Receiver& r = c->rx[ri];
+                const Span& sp = spans[ri];
+                const rv_vrx_plan_info& p = r.plan;
+                const uint32_t chan_base = p.placement.channel * c->chan_blocks;
+                const uint64_t rem = (uint64_t)(p.channel_rate % p.demod_rate);
+                const uint64_t per = rem == 0 ? sp.fine_count : std::max<uint64_t>(1, (0xFFFFFFFFull - (uint64_t)p.demod_rate) / rem);
+                for (uint64_t done = 0; done < sp.fine_count;) {
+                    const uint32_t n = (uint32_t)std::min<uint64_t>({sp.fine_count - done, per, (uint64_t)r.fine_mask + 1u});
+                    rv_vrx_fine_block fb;
+                    if ((st = rv_fine_block(&p, chan_base, c->chan_blocks - 1u, r.fine_mask, sp.fine_first + done, n, &fb)))
+                        return st;
+                    if ((st = rv_vrx_fine(c->stream, &p.fine, &fb.params, c->channel.ptr, c->channel.count, r.d_taps.ptr,
+                                          r.d_taps.count, c->nco.ptr, c->nco.count, r.d_fine.ptr, r.d_fine.count)))
+                        return st;
+                    c->stats.launches += 1;
+                    done += n;
+                }
+            }
+            for (const WorkItem& it : carrier_items) {  // item: receiver, count, first fine output, reset flag (out)
+                Receiver& r = c->rx[it.rx];
+                rv_vrx_carrier_params cp;
+                if ((st = rv_carrier_block(&r.plan, r.fine_mask, it.first, it.count, it.out != 0u, 0.0f, &cp))) return st;
+                if ((st = rv_vrx_carrier(c->stream, &r.plan.carrier, &cp, c->nco.ptr, c->nco.count, r.d_fine.ptr,
+                                         r.d_fine.count, r.d_state.ptr)))
+                    return st;
+                c->stats.launches += 1;
+            }
+            mark(c, 3);
+            // receiver ri's prefix sums: zero up to ri, its count after (the
+            // kernels' search then finds ri for every item)
+            const size_t stride = 2u * (nrx + 1u);
+            std::vector<uint32_t> hp(nrx * stride, 0u);
+            for (size_t ri = 0; ri < nrx; ++ri) {
+                const uint32_t nd = rx_spans.det_prefix[ri + 1u] - rx_spans.det_prefix[ri];
+                const uint32_t na = rx_spans.audio_prefix[ri + 1u] - rx_spans.audio_prefix[ri];
+                for (size_t k = ri + 1u; k <= nrx; ++k) {
+                    hp[ri * stride + k] = nd;
+                    hp[ri * stride + nrx + 1u + k] = na;
+                }
+            }
+            if (c->hoisted_prefix.count < hp.size())
+                if ((st = c->hoisted_prefix.alloc(hp.size()))) return st;
+            if ((st = cuda_status(cudaMemcpyAsync(c->hoisted_prefix.ptr, hp.data(), hp.size() * sizeof(uint32_t),
+                                                  cudaMemcpyHostToDevice, c->stream),
+                                  "hoisted prefix upload")))
+                return st;
+            const RxRun* runs = reinterpret_cast<const RxRun*>(S(c).spans_dev.ptr);
+            for (size_t ri = 0; ri < nrx; ++ri) {
+                const uint32_t* pre = c->hoisted_prefix.ptr + ri * stride;
+                const uint32_t nd = hp[ri * stride + nrx], na = hp[ri * stride + 2u * nrx + 1u];
+                if (nd) {
+                    if ((st = cuda_status(cudaMemsetAsync(&S(c).queues.ptr->detect, 0, sizeof(uint32_t), c->stream),
+                                          "queue reset")))
+                        return st;
+                    if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, SpanList{runs, pre, (uint32_t)nrx, 0u}, nd,
+                                                    kDetWindow, &S(c).queues.ptr->detect)))
+                        return st;
+                    c->stats.launches += 1;
+                }
+                if (na) {
+                    if ((st = cuda_status(cudaMemsetAsync(&S(c).queues.ptr->audio, 0, sizeof(uint32_t), c->stream),
+                                          "queue reset")))
+                        return st;
+                    if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, SpanList{runs, pre + nrx + 1u, (uint32_t)nrx, 1u},
+                                                   na, S(c).audio_dev.ptr, kDetWindow, c->weights_cap,
+                                                   &S(c).queues.ptr->audio)))
+                        return st;
+                    c->stats.launches += 1;
+                }
+            }
+            mark(c, 4);
+        } else {
+            const WorkItem* d = S(c).items_dev.ptr;
+            const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
+            if ((st = c->fast ? launch_fine_tc(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
+                                               &S(c).queues.ptr->tiles, nullptr, c->tc_status.ptr)
+                              : launch_fine_tiles(c->stream, c->rx_table.ptr, S(c).tiles_dev.ptr, (uint32_t)tiles.size(), chan,
+                                                  c->tile_shared, &S(c).queues.ptr->tiles)))
+                return st;
+            if ((st = launch_fine_units(c->stream, c->rx_table.ptr, S(c).items_dev.ptr, S(c).units_dev.ptr,
+                                        (uint32_t)units.size(), chan, c->unit_budget, &S(c).queues.ptr->units)))
+                return st;
+            const uint32_t window = std::min<uint32_t>(kFineWindow, (fine_window + 255u) & ~255u);
+            if ((st = launch_fine_batched(c->stream, c->rx_table.ptr, d, (uint32_t)fine_items.size(), chan, window,
+                                          &S(c).queues.ptr->fine)))
+                return st;
+            d += fine_items.size();
+            if ((st = launch_carrier_batched(c->stream, c->rx_table.ptr, d, (uint32_t)carrier_items.size()))) return st;
+            d += carrier_items.size();
+            mark(c, 3);
+            SpanList det_list, audio_list;
+            span_lists(c, (uint32_t)c->rx.size(), &det_list, &audio_list);
+            if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, det_list, rx_spans.det_total, kDetWindow,
+                                            &S(c).queues.ptr->detect)))
+                return st;
+            if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, audio_list, rx_spans.audio_total, S(c).audio_dev.ptr,
+                                           kDetWindow, c->weights_cap, &S(c).queues.ptr->audio)))
+                return st;
+            mark(c, 4);
+            c->stats.launches += (rx_spans.det_total ? 1 : 0) + (rx_spans.audio_total ? 1 : 0) + (fine_items.empty() ? 0 : 1) +
+                                 (units.empty() ? 0 : 1) + (carrier_items.empty() ? 0 : 1) + (tiles.empty() ? 0 : 1);
+            c->stats.work_items += total + rx_spans.det_total + rx_spans.audio_total + tiles.size();
+        }
         }
     }
 
@@ -1649,10 +1736,10 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
 
 int32_t rv_chain_capture_graph(rv_chain* c) {
     if (c == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_capture_graph: NULL");
-    if (c->config.mode != RV_CHAIN_BATCHED)
+    if (c->config.mode != RV_CHAIN_BATCHED || c->hoisted)
         return set_error_fmt(RV_ERR_UNSUPPORTED,
-                             "rv_chain_capture_graph: a plain chain records one launch per stage per receiver; only "
-                             "the batched chain runs from a graph");
+                             "rv_chain_capture_graph: a plain or hoisted chain records one launch per stage per "
+                             "receiver; only the batched chain runs from a graph");
     if (!c->fused)
         return set_error_fmt(RV_ERR_UNSUPPORTED,
                              "rv_chain_capture_graph: no fused channelizer kernel for M=%u T=%u D=%u; this chain's "

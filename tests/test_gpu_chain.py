@@ -76,7 +76,8 @@ def test_plain_chain_matches_oracle_chain(gpu, c1_capture):
 def test_batched_chain_matches_plain_chain_and_is_blocking_invariant(gpu, c1_capture):
     reqs = c1_requests()
     out, rings = {}, {}
-    for mode, runs in ((abi.CHAIN_PLAIN, RUNS_A), (abi.CHAIN_BATCHED, RUNS_A), (abi.CHAIN_BATCHED, RUNS_B)):
+    for mode, runs in ((abi.CHAIN_PLAIN, RUNS_A), (abi.CHAIN_BATCHED, RUNS_A), (abi.CHAIN_BATCHED, RUNS_B),
+                       (abi.CHAIN_HOISTED, RUNS_A)):
         ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=mode, max_run_samples=1 << 17)
         ids = [ch.add_receiver(r) for r in reqs]
         at = 0
@@ -89,7 +90,7 @@ def test_batched_chain_matches_plain_chain_and_is_blocking_invariant(gpu, c1_cap
     plain = out[(abi.CHAIN_PLAIN, tuple(RUNS_A))]
     plain_rings = rings[(abi.CHAIN_PLAIN, tuple(RUNS_A))]
     problems = []
-    for key in ((abi.CHAIN_BATCHED, tuple(RUNS_A)), (abi.CHAIN_BATCHED, tuple(RUNS_B))):
+    for key in ((abi.CHAIN_BATCHED, tuple(RUNS_A)), (abi.CHAIN_BATCHED, tuple(RUNS_B)), (abi.CHAIN_HOISTED, tuple(RUNS_A))):
         for i, (a, b) in enumerate(zip(plain, out[key])):
             fine_same = np.array_equal(plain_rings[i].view(np.uint32), rings[key][i].view(np.uint32))
             if a.size != b.size or not np.array_equal(a.view(np.uint32), b.view(np.uint32)):
@@ -108,16 +109,17 @@ def test_batched_wideband_receivers_match_plain(gpu):
     z = signals.scene(n, rate, emitters + [("wfm", reqs[0].center, 1.0)], snr_db=30.0, seed=3)
     codes = signals.quantise(z, "cs16")
     res = []
-    for mode in (abi.CHAIN_PLAIN, abi.CHAIN_BATCHED):
+    for mode in (abi.CHAIN_PLAIN, abi.CHAIN_BATCHED, abi.CHAIN_HOISTED):
         ch = Chain(gpu, grid=(64, 17, 32), rate=rate, fmt=abi.FORMAT_CS16, mode=mode, max_run_samples=1 << 17)
         ids = [ch.add_receiver(r) for r in reqs]
         for k in range(n // (1 << 17)):
             ch.run(codes[2 * k * (1 << 17):2 * (k + 1) * (1 << 17)])
         res.append([ch.audio(i) for i in ids])
         ch.close()
-    for i, (a, b) in enumerate(zip(*res)):
-        assert a.size == b.size and a.size > 0
-        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d mode %d differs" % (i, reqs[i].demod)
+    for other in res[1:]:
+        for i, (a, b) in enumerate(zip(res[0], other)):
+            assert a.size == b.size and a.size > 0
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d mode %d differs" % (i, reqs[i].demod)
 
 
 def test_wfm_stereo_recovers_the_tone(gpu, c1_capture):
@@ -200,9 +202,10 @@ def test_captured_wideband_chain_matches_direct(gpu):
         assert a.size > 0 and np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d" % i
 
 
-def test_plain_chain_refuses_capture(gpu):
+@pytest.mark.parametrize("mode", [abi.CHAIN_PLAIN, abi.CHAIN_HOISTED])
+def test_plain_chain_refuses_capture(gpu, mode):
     from revenant_gb300.library import lib
-    ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=abi.CHAIN_PLAIN, max_run_samples=4096)
+    ch = Chain(gpu, grid=(8, 17, 4), rate=2_400_000, fmt=abi.FORMAT_CU8, mode=mode, max_run_samples=4096)
     assert lib().rv_chain_capture_graph(ch.handle) == abi.RV_ERR_UNSUPPORTED
     ch.close()
 
