@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-excision", action="store_true", help="skip the timed run with impulse excision on")
     ap.add_argument("--no-c4", action="store_true", help="skip the M = 4096 channelizer DFT comparison")
     ap.add_argument("--no-noise", action="store_true", help="skip the scene noise field measurement")
+    ap.add_argument("--no-tune", action="store_true", help="keep the rule's fine-tile shapes (no rv_chain_autotune)")
     ap.add_argument("--no-fast", action="store_true", help="skip the fast-mode (tensor-core fine stage) leg")
     ap.add_argument("--no-c1c2", action="store_true", help="skip the C1 single-receiver and C2 channelizer legs")
     ap.add_argument("--no-c5", action="store_true", help="skip the learned detection proposal (C5)")
@@ -204,11 +205,15 @@ def run_gb300(args):
     codes = capture(n)
     reqs = receivers(args.receivers)
 
-    def make_chain(mode, run_samples, profile=True, pipelined=False):
+    tune_reports = []
+
+    def make_chain(mode, run_samples, profile=True, pipelined=False, tune=False):
         ch = Chain(dev, grid=GRID, rate=RATE, fmt=abi.FORMAT_CS16, mode=mode, max_run_samples=run_samples,
                    keep_audio=False, profile=profile, pipelined=pipelined)
         for r in reqs:
             ch.add_receiver(r)
+        if tune and not args.no_tune:
+            tune_reports.append(ch.autotune(run_samples))
         return ch
 
     # replicas: every rank processes its own copy of the workload (the path
@@ -220,7 +225,9 @@ def run_gb300(args):
     # is prepared and its input copied while the previous one executes); a
     # second, directly launched batched chain (bit-identical) gives the
     # per-stage split
-    chain = make_chain(abi.CHAIN_BATCHED, min(1 << args.run_log2, n), profile=False, pipelined=True)
+    t_tune = time.perf_counter()
+    chain = make_chain(abi.CHAIN_BATCHED, min(1 << args.run_log2, n), profile=False, pipelined=True, tune=True)
+    tune_s = time.perf_counter() - t_tune
     chain.capture_graph()
     plans = [chain.info(i)[0] for i in range(len(reqs))]
     stream = torch.cuda.ExternalStream(dev.stream)
@@ -274,7 +281,7 @@ def run_gb300(args):
                                                           "graph_captures", "host_ms")}
     # per-stage device time from the direct batched chain, CUDA events between
     # stages on the chain's stream, over the same number of steps
-    sch = make_chain(abi.CHAIN_BATCHED, run_samples, profile=True)
+    sch = make_chain(abi.CHAIN_BATCHED, run_samples, profile=True, tune=True)
     for _ in range(args.warmup):
         step(sch, "device")
     sbase = sch.stats()
@@ -413,6 +420,12 @@ def run_gb300(args):
                                            "per instruction"}},
         "realtime_factor": round(value * 1e6 / RATE / max(world, 1), 1),
         "plain_path": plain,
+        "autotune": None if not tune_reports else dict(
+            tune_reports[0], default_ms=round(tune_reports[0]["default_ms"], 3),
+            tuned_ms=round(tune_reports[0]["tuned_ms"], 3), seconds=round(tune_s, 2),
+            note="rv_chain_autotune before the first run: per receiver class, every fine-tile shape that fits was "
+                 "timed on one run of its tiles; default_ms / tuned_ms: one run's fine tiles of every tiled "
+                 "receiver with the rule's shapes at 4 tiles per SM, and tuned"),
         "fast_mode": fast,
         "with_impulse_excision": excision,
         "clocks": clocks.summary(),

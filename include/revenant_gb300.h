@@ -531,6 +531,25 @@ int32_t rv_coarse_fused(void* stream, const rv_grid_params* grid, int32_t format
 
 typedef struct rv_chain rv_chain;
 
+/* rv_chain_autotune's findings: receivers of the same rates, taps and
+ * pattern period form a class; each class's fine-tile shapes that fit shared
+ * memory were timed on one run of its own tiles and the fastest kept (the
+ * rule's shape unless another was more than 3 % faster), within the shared
+ * memory of the rule's largest shape (a launch's CTAs all reserve the
+ * largest); the choices are kept only when every tiled receiver's run is
+ * faster with them together; then the tile count per SM (2, 4 or 8). Times: the fine tiles of one run of every tiled
+ * receiver, rule's shapes at 4 tiles per SM against the tuned ones. */
+typedef struct rv_chain_tune_report {
+    uint32_t receivers;        /* tiled receivers */
+    uint32_t classes;          /* receiver classes tuned */
+    uint32_t classes_changed;  /* classes whose shape differs from the rule's */
+    uint32_t shapes_timed;
+    uint32_t tiles_per_sm;     /* the chosen tile count per SM */
+    uint32_t shapes_reverted;  /* 1: the classes' choices together were not faster; the rule's kept */
+    double default_ms;
+    double tuned_ms;
+} rv_chain_tune_report;
+
 typedef struct rv_chain_config {
     rv_grid_params grid;
     uint32_t reserved;
@@ -597,6 +616,12 @@ int32_t rv_chain_get_stats(const rv_chain* chain, rv_chain_stats* stats);
  * buffer it names moved (a receiver was added). Outputs are bit-identical to
  * the direct batched run. */
 int32_t rv_chain_capture_graph(rv_chain* chain);
+/* Times the batched chain's fine-tile shapes per receiver class on
+ * `run_samples`-sample runs and keeps the fastest (outputs do not depend on
+ * the shape). Call after the receivers are added and before the first run
+ * (it writes their fine rings, then clears them); RV_ERR_UNSUPPORTED for a
+ * plain, hoisted or fast chain. */
+int32_t rv_chain_autotune(rv_chain* chain, uint32_t run_samples, rv_chain_tune_report* report);
 /* The spectrum stage (Graph::on_block's spectrum dispatch, a6): with
  * `transform` N > 0, every run that completes N or more channel blocks
  * computes one frame of the last N blocks (M * N / 2 dB bins, the central half

@@ -374,6 +374,11 @@ class ChainStats(_S):
                 ("graph_captures", U64), ("graph_ms", C.c_double), ("host_ms", C.c_double)]
 
 
+class ChainTuneReport(_S):
+    _fields_ = [("receivers", U32), ("classes", U32), ("classes_changed", U32), ("shapes_timed", U32),
+                ("tiles_per_sm", U32), ("shapes_reverted", U32), ("default_ms", C.c_double), ("tuned_ms", C.c_double)]
+
+
 class CnnTrainConfig(_S):
     _fields_ = [("learning_rate", F32), ("beta1", F32), ("beta2", F32), ("epsilon", F32), ("weight_decay", F32),
                 ("pos_weight", F32)]

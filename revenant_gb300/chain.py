@@ -85,6 +85,14 @@ class Chain:
         """Run the batched kernels from one captured CUDA graph from now on."""
         check(lib().rv_chain_capture_graph(self.handle))
 
+    def autotune(self, run_samples):
+        """Time the fine-tile shapes per receiver class on runs of
+        `run_samples` and keep the fastest (before the first run); returns
+        the report as a dict."""
+        rep = abi.ChainTuneReport()
+        check(lib().rv_chain_autotune(self.handle, int(run_samples), C.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in rep._fields_ if k != "reserved"}
+
     def set_front_end(self, dc=True, iq=True, lag=1):
         """Front-end DC / IQ-imbalance correction from the next run on."""
         check(lib().rv_chain_set_front_end(self.handle, 1 if dc else 0, 1 if iq else 0, lag))

@@ -22,6 +22,8 @@
 #include <chrono>
 #include <new>
 #include <numeric>
+#include <map>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -229,6 +231,7 @@ struct rv_chain {
     rv_chain_config config{};
     bool fast = false;                 // RV_CHAIN_FAST: a batched chain with the fine stage on the tensor cores
     bool hoisted = false;              // RV_CHAIN_HOISTED: a batched chain whose receiver stages launch per receiver
+    uint32_t tiles_per_sm = 4;         // fine tiles a run is cut into, per SM (rv_chain_autotune may change it)
     DeviceArray<uint32_t> hoisted_prefix;  // per receiver: its detector then audio item prefix sums
     DeviceArray<uint32_t> tc_status;   // fast mode: tensor-core waits that ran out
     uint32_t stages = 0;
@@ -733,17 +736,26 @@ int32_t coarse_batched(rv_chain* c, uint64_t first_sample, const uint8_t* src, u
 // The 2D tile shape of a receiver's fine stage (fine_tiles.cu): rows of P'
 // outputs (the pattern period times the smallest k making it 48 or more), cut
 // into column blocks of at most 16 R columns (16 slots of R adjacent columns),
-// chunks of 16 rows. Among R = 4..1 and one or two staged chunks whose table
-// slice and row segments fit in `budget` float2 of shared memory, the shape
-// that leaves the fewest column slots idle wins (then the larger R, then two
-// buffers). Leaves tile_cols at 0 (not tiled) when nothing fits.
-void plan_tiles(Receiver& r, uint64_t fc, uint64_t fd, uint32_t budget) {
+// chunks of 16 rows, one or two chunks staged, the block's table slice and
+// row segments in shared memory. A shape changes which thread computes which
+// output and what is staged, never an output's arithmetic.
+struct TileShape {
+    uint32_t cols = 0, block = 0, rows = 0, buffers = 0, seg = 0, stride = 0, period = 0, shared = 0;
+    uint64_t row_step = 0;
+    double score = 0.0;  // the rule's preference: column slots filled, then larger R, then two buffers
+    bool same(const TileShape& o) const {
+        return cols == o.cols && block == o.block && rows == o.rows && buffers == o.buffers && seg == o.seg &&
+               stride == o.stride && period == o.period && shared == o.shared;
+    }
+};
+
+// Every tile shape of a receiver that fits `budget` float2 of shared memory,
+// R = 4..1, two staged chunks before one.
+void tile_shapes(const Receiver& r, uint64_t fc, uint64_t fd, uint32_t budget, std::vector<TileShape>& out) {
     const uint64_t T = r.plan.fine.taps;
-    r.tile_cols = 0;
     if (r.period == 0) return;
     const uint64_t P = (uint64_t)r.period * ((48u + r.period - 1u) / r.period);
     if (P > 65535u || (P * fc) % fd != 0) return;
-    double best = 0.0;
     for (uint32_t R = 4; R >= 1; --R) {
         const uint64_t cap = (uint64_t)kTileSlots * R;
         const uint64_t nblk = (P + cap - 1u) / cap;
@@ -753,27 +765,52 @@ void plan_tiles(Receiver& r, uint64_t fc, uint64_t fd, uint32_t budget) {
             const uint64_t w = std::min<uint64_t>(A, P - a0);
             L = std::max<uint64_t>(L, (a0 + w - 1u) * fc / fd - a0 * fc / fd + T);
         }
-        const uint64_t Ap = A, Lp = L | 1u;
+        const uint64_t Lp = L | 1u;
         // every block runs all 16 slots of R columns
         const double fill = (double)P / (double)(nblk * kTileSlots * R);
         for (uint32_t nb = 2; nb >= 1; --nb) {
-            const uint64_t need = (T + 1u) / 2u * 2u * Ap + (uint64_t)nb * kTileRows * Lp;  // tap pairs + rows
+            const uint64_t need = (T + 1u) / 2u * 2u * A + (uint64_t)nb * kTileRows * Lp;  // tap pairs + rows
             if (need > budget) continue;
-            const double score = fill * (1.0 + 0.01 * R) * (nb == 2 ? 1.0 : 0.97);
-            if (score > best) {
-                best = score;
-                r.tile_cols = (uint32_t)Ap;
-                r.tile_block = (uint32_t)A;
-                r.tile_rows = R;
-                r.tile_buffers = nb;
-                r.tile_seg = (uint32_t)L;
-                r.tile_stride = (uint32_t)Lp;
-                r.row_step = P * fc / fd;
-                r.tile_period = (uint32_t)P;
-                r.tile_shared = (uint32_t)need;
-            }
+            TileShape sh;
+            sh.cols = (uint32_t)A;
+            sh.block = (uint32_t)A;
+            sh.rows = R;
+            sh.buffers = nb;
+            sh.seg = (uint32_t)L;
+            sh.stride = (uint32_t)Lp;
+            sh.period = (uint32_t)P;
+            sh.shared = (uint32_t)need;
+            sh.row_step = P * fc / fd;
+            sh.score = fill * (1.0 + 0.01 * R) * (nb == 2 ? 1.0 : 0.97);
+            out.push_back(sh);
         }
     }
+}
+
+void set_tile_shape(Receiver& r, const TileShape& sh) {
+    r.tile_cols = sh.cols;
+    r.tile_block = sh.block;
+    r.tile_rows = sh.rows;
+    r.tile_buffers = sh.buffers;
+    r.tile_seg = sh.seg;
+    r.tile_stride = sh.stride;
+    r.row_step = sh.row_step;
+    r.tile_period = sh.period;
+    r.tile_shared = sh.shared;
+}
+
+// The rule's shape: among those that fit `budget`, the one that leaves the
+// fewest column slots idle (then the larger R, then two buffers). Leaves
+// tile_cols at 0 (not tiled) when nothing fits. rv_chain_autotune replaces
+// the rule's choice by timing.
+void plan_tiles(Receiver& r, uint64_t fc, uint64_t fd, uint32_t budget) {
+    r.tile_cols = 0;
+    std::vector<TileShape> shapes;
+    tile_shapes(r, fc, fd, budget, shapes);
+    const TileShape* best = nullptr;
+    for (const TileShape& sh : shapes)
+        if (best == nullptr || sh.score > best->score) best = &sh;
+    if (best != nullptr) set_tile_shape(r, *best);
 }
 
 // Tiles covering fine outputs [first, first + count) of receiver `rx`: every
@@ -1526,7 +1563,8 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
             int sms = 0, dev = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            const uint64_t tile_target = std::max<uint64_t>(1, tile_cost_total / (uint64_t)(4 * std::max(sms, 1)));
+            const uint64_t tile_target =
+                std::max<uint64_t>(1, tile_cost_total / ((uint64_t)c->tiles_per_sm * (uint64_t)std::max(sms, 1)));
             for (const TileSpan& ts : tile_spans) push_tiles(tiles, ts.rx, c->rx[ts.rx], ts.first, ts.count, tile_target);
             // largest first, so the last tiles to start are the short ones (a
             // tensor-core tile costs its K chunks whatever its rows)
@@ -1731,6 +1769,186 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
     }
     if ((st = collect_slot(c, sl))) return st;
     collect_marks(c);
+    return clear_error();
+}
+
+namespace {
+
+// Mean device time of the fine tiles of `rxs` over one run of `outputs[i]`
+// fine outputs each (cut `per_sm` tiles per SM, the list repeated until it
+// fills the GPU `fill` times), shared memory `shared` float2s a CTA.
+int32_t time_tiles(rv_chain* c, const std::vector<uint32_t>& rxs, const std::vector<uint64_t>& outputs,
+                   uint32_t per_sm, uint32_t shared, uint32_t fill, DeviceArray<FineTile>& d_tiles,
+                   DeviceArray<uint32_t>& queue, cudaEvent_t e0, cudaEvent_t e1, double* ms) {
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t cost = 0;
+    for (size_t i = 0; i < rxs.size(); ++i) cost += outputs[i] * c->rx[rxs[i]].plan.fine.taps;
+    const uint64_t target = std::max<uint64_t>(1, cost / ((uint64_t)per_sm * (uint64_t)std::max(sms, 1)));
+    std::vector<FineTile> one, tiles;
+    for (size_t i = 0; i < rxs.size(); ++i) push_tiles(one, rxs[i], c->rx[rxs[i]], 0, outputs[i], target);
+    if (one.empty()) return set_error_fmt(RV_ERR_INVALID, "rv_chain_autotune: no tiles to time");
+    while (tiles.size() < (size_t)fill * (size_t)std::max(sms, 1)) tiles.insert(tiles.end(), one.begin(), one.end());
+    std::stable_sort(tiles.begin(), tiles.end(), [&](const FineTile& x, const FineTile& y) {
+        return (uint64_t)x.rows * x.width * c->rx[x.rx].plan.fine.taps > (uint64_t)y.rows * y.width * c->rx[y.rx].plan.fine.taps;
+    });
+    if (d_tiles.count < tiles.size())
+        if (int32_t st = d_tiles.alloc(tiles.size())) return st;
+    if (int32_t st = cuda_status(cudaMemcpy(d_tiles.ptr, tiles.data(), tiles.size() * sizeof(FineTile), cudaMemcpyHostToDevice),
+                                 "autotune tiles"))
+        return st;
+    const float2* chan = reinterpret_cast<const float2*>(c->channel.ptr);
+    const uint32_t n = (uint32_t)tiles.size();
+    constexpr int kReps = 3;
+    for (int rep = -1; rep < kReps; ++rep) {  // one untimed launch first
+        if (rep == 0)
+            if (int32_t st = cuda_status(cudaEventRecord(e0, c->stream), "autotune event")) return st;
+        if (int32_t st = cuda_status(cudaMemsetAsync(queue.ptr, 0, sizeof(uint32_t), c->stream), "autotune queue"))
+            return st;
+        if (int32_t st = launch_fine_tiles(c->stream, c->rx_table.ptr, d_tiles.ptr, n, chan, shared, queue.ptr)) return st;
+    }
+    if (int32_t st = cuda_status(cudaEventRecord(e1, c->stream), "autotune event")) return st;
+    if (int32_t st = cuda_status(cudaEventSynchronize(e1), "autotune sync")) return st;
+    float elapsed = 0.0f;
+    if (int32_t st = cuda_status(cudaEventElapsedTime(&elapsed, e0, e1), "autotune time")) return st;
+    *ms = elapsed / kReps;
+    return RV_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t rv_chain_autotune(rv_chain* c, uint32_t run_samples, rv_chain_tune_report* report) {
+    if (c == nullptr || report == nullptr) return set_error_fmt(RV_ERR_INVALID, "rv_chain_autotune: NULL argument");
+    memset(report, 0, sizeof *report);
+    if (c->config.mode != RV_CHAIN_BATCHED || c->fast || c->hoisted)
+        return set_error_fmt(RV_ERR_UNSUPPORTED, "rv_chain_autotune: tunes the batched chain's fine tiles");
+    if (run_samples == 0) return set_error_fmt(RV_ERR_INVALID, "rv_chain_autotune: run_samples is 0");
+    for (const Receiver& r : c->rx)
+        if (r.started)
+            return set_error_fmt(RV_ERR_INVALID, "rv_chain_autotune: tune before the first run (its rings are written)");
+    if (int32_t st = cuda_status(cudaStreamSynchronize(c->stream), "autotune sync")) return st;
+    // one run's fine outputs per receiver, and the classes: receivers of the
+    // same rates, taps and pattern period share their shapes
+    const uint64_t blocks = run_samples / c->config.grid.decimation;
+    std::map<std::tuple<int64_t, int64_t, uint32_t, uint32_t>, std::vector<uint32_t>> classes;
+    std::vector<uint32_t> tiled;
+    std::vector<uint64_t> outputs(c->rx.size(), 0);
+    for (uint32_t i = 0; i < (uint32_t)c->rx.size(); ++i) {
+        const Receiver& r = c->rx[i];
+        if (r.tile_cols == 0) continue;
+        outputs[i] = blocks * (uint64_t)r.plan.demod_rate / (uint64_t)r.plan.channel_rate;
+        if (outputs[i] == 0) continue;
+        tiled.push_back(i);
+        classes[std::make_tuple(r.plan.channel_rate, r.plan.demod_rate, r.plan.fine.taps, r.period)].push_back(i);
+    }
+    if (tiled.empty()) return clear_error();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    DeviceArray<FineTile> d_tiles;
+    DeviceArray<uint32_t> queue;
+    int32_t st = cuda_status(cudaEventCreate(&e0), "autotune event");
+    if (!st) st = cuda_status(cudaEventCreate(&e1), "autotune event");
+    if (!st) st = queue.alloc(1);
+    auto all_outputs = [&](const std::vector<uint32_t>& rxs) {
+        std::vector<uint64_t> o;
+        for (uint32_t i : rxs) o.push_back(outputs[i]);
+        return o;
+    };
+    auto max_shared = [&]() {
+        uint32_t m = 0;
+        for (uint32_t i : tiled) m = std::max(m, c->rx[i].tile_shared);
+        return m;
+    };
+    // the rule's shapes, 4 tiles per SM: the default. A launch's shared
+    // memory is the largest shape's, so the rule's largest bounds every
+    // candidate (a larger one would take CTAs per SM from every tile)
+    double default_ms = 0.0, tuned_ms = 0.0;
+    const uint32_t launch_shared = max_shared();
+    std::vector<TileShape> rule_shapes(c->rx.size());
+    for (uint32_t i : tiled) {
+        const Receiver& r = c->rx[i];
+        TileShape& t = rule_shapes[i];
+        t.cols = r.tile_cols, t.block = r.tile_block, t.rows = r.tile_rows, t.buffers = r.tile_buffers;
+        t.seg = r.tile_seg, t.stride = r.tile_stride, t.period = r.tile_period, t.shared = r.tile_shared;
+        t.row_step = r.row_step;
+    }
+    if (!st) st = upload_table(c);
+    if (!st) st = time_tiles(c, tiled, all_outputs(tiled), 4, launch_shared, 1, d_tiles, queue, e0, e1, &default_ms);
+    // each class: every shape within the launch's shared memory, timed on
+    // the class's tiles repeated to fill the GPU four times over
+    const uint32_t budgets[1] = {launch_shared};
+    for (auto it = classes.begin(); !st && it != classes.end(); ++it) {
+        const std::vector<uint32_t>& members = it->second;
+        Receiver& r0 = c->rx[members[0]];
+        const uint64_t fc = (uint64_t)r0.plan.channel_rate, fd = (uint64_t)r0.plan.demod_rate;
+        std::vector<TileShape> shapes, candidates;
+        for (uint32_t b : budgets) tile_shapes(r0, fc, fd, b, shapes);
+        for (const TileShape& sh : shapes) {
+            bool seen = false;
+            for (const TileShape& o : candidates) seen = seen || o.same(sh);
+            if (!seen) candidates.push_back(sh);
+        }
+        const TileShape rule = rule_shapes[members[0]];
+        const TileShape* best = nullptr;
+        double best_ms = 0.0;
+        for (const TileShape& sh : candidates) {
+            for (uint32_t i : members) set_tile_shape(c->rx[i], sh);
+            double ms = 0.0;
+            if ((st = upload_table(c))) break;
+            if ((st = time_tiles(c, members, all_outputs(members), 4, launch_shared, 4, d_tiles, queue, e0, e1, &ms))) break;
+            ++report->shapes_timed;
+            // the rule's shape unless another is clearly faster
+            const double bias = sh.same(rule) ? 0.97 : 1.0;
+            if (best == nullptr || ms * bias < best_ms) {
+                best = &sh;
+                best_ms = ms * bias;
+            }
+        }
+        if (st) break;
+        for (uint32_t i : members) set_tile_shape(c->rx[i], *best);
+        ++report->classes;
+        if (!best->same(rule)) ++report->classes_changed;
+    }
+    // the tuned shapes together: kept only when the whole run is faster
+    if (!st) st = upload_table(c);
+    double together_ms = 0.0;
+    if (!st) st = time_tiles(c, tiled, all_outputs(tiled), 4, launch_shared, 1, d_tiles, queue, e0, e1, &together_ms);
+    if (!st && !(together_ms < default_ms)) {
+        for (uint32_t i : tiled) set_tile_shape(c->rx[i], rule_shapes[i]);
+        report->classes_changed = 0;
+        report->shapes_reverted = 1;
+        st = upload_table(c);
+    }
+    // tiles per SM, on the shapes kept
+    uint32_t per_sm = 4;
+    double best_ms = 0.0;
+    for (uint32_t k : {2u, 4u, 8u}) {
+        double ms = 0.0;
+        if (st || (st = time_tiles(c, tiled, all_outputs(tiled), k, launch_shared, 1, d_tiles, queue, e0, e1, &ms))) break;
+        if (k == 2u || ms < best_ms) {
+            best_ms = ms;
+            per_sm = k;
+        }
+    }
+    tuned_ms = best_ms;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    d_tiles.release();
+    queue.release();
+    // the timed launches wrote the fine rings: back to a stream start
+    c->tile_shared = std::max(max_shared(), launch_shared);
+    for (uint32_t i : tiled) {
+        Receiver& r = c->rx[i];
+        if (!st) st = cuda_status(cudaMemsetAsync(r.d_fine.ptr, 0, r.d_fine.count * sizeof(rv_cf32), c->stream), "fine clear");
+    }
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream), "autotune sync");
+    c->table_dirty = true;
+    if (st) return st;
+    c->tiles_per_sm = per_sm;
+    report->tiles_per_sm = per_sm;
+    report->default_ms = default_ms;
+    report->tuned_ms = tuned_ms;
+    report->receivers = (uint32_t)tiled.size();
     return clear_error();
 }
 

@@ -157,6 +157,7 @@ SIGNATURES = {
     "rv_chain_read_audio": (I32, [P, U32, P, U64, ptr(U64)]),
     "rv_chain_get_stats": (I32, [P, ptr(abi.ChainStats)]),
     "rv_chain_capture_graph": (I32, [P]),
+    "rv_chain_autotune": (I32, [P, U32, ptr(abi.ChainTuneReport)]),
     "rv_chain_set_front_end": (I32, [P, I32, I32, U32]),
     "rv_chain_set_impulse_excision": (I32, [P, I32, F64, F64]),
     "rv_chain_excision_counters": (I32, [P, P]),

@@ -6,6 +6,8 @@ the batched chain (fused coarse kernel + batched receivers) must equal the
 plain chain bit for bit, for every mode, across runs of uneven sizes
 (blocking invariance, tests/reference/test_vrx.cpp:1241).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -262,3 +264,32 @@ class _At:
 
     def __init__(self, buf, offset):
         self.address = buf.address + offset
+
+
+def test_autotuned_chain_matches_the_rule(gpu):
+    """rv_chain_autotune times fine-tile shapes per receiver class and keeps
+    the fastest: the audio must not change (a shape moves work between
+    threads, never an output's arithmetic), and tuning after the first run is
+    refused."""
+    rate, n, run = 20_000_000, 1 << 19, 1 << 17
+    reqs = signals.random_receivers(24, rate, seed=5)
+    z = signals.scene(n, rate, [("am", r.center, 0.2) for r in reqs[:6]], snr_db=30.0, seed=5)
+    codes = signals.quantise(z, "cs16")
+    res = []
+    for tune in (False, True):
+        ch = Chain(gpu, grid=(64, 17, 32), rate=rate, fmt=abi.FORMAT_CS16, mode=abi.CHAIN_BATCHED, max_run_samples=run)
+        ids = [ch.add_receiver(r) for r in reqs]
+        if tune:
+            rep = ch.autotune(run)
+            assert rep["classes"] > 0 and rep["shapes_timed"] >= rep["classes"]
+            assert rep["tiles_per_sm"] in (2, 4, 8) and rep["default_ms"] > 0 and rep["tuned_ms"] > 0
+        for k in range(n // run):
+            ch.run(codes[2 * k * run:2 * (k + 1) * run])
+        res.append([ch.audio(i) for i in ids])
+        if tune:
+            from revenant_gb300.library import lib
+            assert lib().rv_chain_autotune(ch.handle, run, C.byref(abi.ChainTuneReport())) == abi.RV_ERR_INVALID
+        ch.close()
+    for i, (a, b) in enumerate(zip(*res)):
+        assert a.size == b.size and a.size > 0
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "receiver %d differs after tuning" % i
