@@ -523,7 +523,8 @@ int32_t rv_coarse_fused(void* stream, const rv_grid_params* grid, int32_t format
 #define RV_CHAIN_BATCHED 0 /* fused coarse kernel + one launch per receiver stage */
 #define RV_CHAIN_PLAIN 1   /* one launch per stage per receiver, as the reference records */
 #define RV_CHAIN_FAST 2    /* batched, the fine stage on the tensor cores (split BF16 GEMMs, FP32
-                            * accumulation): to a stated tolerance, not bit for bit */
+                            * accumulation), the DC-removal and mono audio FIRs with fused
+                            * multiply-adds: to a stated tolerance, not bit for bit */
 #define RV_CHAIN_HOISTED 3 /* the plain recording with the detector hoisted: one launch per stage per
                             * receiver (fine, carrier, detector, audio), the detector once per fine
                             * sample as the batched chain does; the same audio bit for bit (a

@@ -977,10 +977,10 @@ int32_t capture(rv_chain* c, const rv_coarse_params& coarse) {
     span_lists(c, sh.nrx, &det, &audio);
     if (!st)
         st = launch_detect_batched(c->stream, c->rx_table.ptr, det, sh.nrx, kDetWindow, &rc->queues.detect,
-                                   &rc->detect);
+                                   &rc->detect, c->fast);
     if (!st)
         st = launch_audio_batched(c->stream, c->rx_table.ptr, audio, sh.nrx, S(c).audio_dev.ptr, kDetWindow,
-                                  sh.weights_cap, &rc->queues.audio, &rc->audio);
+                                  sh.weights_cap, &rc->queues.audio, &rc->audio, c->fast);
     const int32_t end = cuda_status(cudaStreamEndCapture(c->stream, &graph), "graph capture end");
     if (st || end) {
         if (graph) cudaGraphDestroy(graph);
@@ -1730,10 +1730,10 @@ int32_t rv_chain_run(rv_chain* c, const void* samples, uint64_t count, int32_t w
             SpanList det_list, audio_list;
             span_lists(c, (uint32_t)c->rx.size(), &det_list, &audio_list);
             if ((st = launch_detect_batched(c->stream, c->rx_table.ptr, det_list, rx_spans.det_total, kDetWindow,
-                                            &S(c).queues.ptr->detect)))
+                                            &S(c).queues.ptr->detect, nullptr, c->fast)))
                 return st;
             if ((st = launch_audio_batched(c->stream, c->rx_table.ptr, audio_list, rx_spans.audio_total, S(c).audio_dev.ptr,
-                                           kDetWindow, c->weights_cap, &S(c).queues.ptr->audio)))
+                                           kDetWindow, c->weights_cap, &S(c).queues.ptr->audio, nullptr, c->fast)))
                 return st;
             mark(c, 4);
             c->stats.launches += (rx_spans.det_total ? 1 : 0) + (rx_spans.audio_total ? 1 : 0) + (fine_items.empty() ? 0 : 1) +

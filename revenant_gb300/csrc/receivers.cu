@@ -261,7 +261,17 @@ __device__ __forceinline__ void add_pair(uint64_t& acc, float lo, float hi) {
 __device__ __forceinline__ void unpack_pair(uint64_t acc, float& lo, float& hi) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc));
 }
+// fast mode: acc = (acc.lo + lo * w, acc.hi + hi * w), one fused packed
+// multiply-add (each lane rounded once)
+__device__ __forceinline__ void fma_pair(uint64_t& acc, float lo, float hi, float w) {
+    asm("{\n .reg .b64 x, y;\n mov.b64 x, {%1, %2};\n mov.b64 y, {%3, %3};\n fma.rn.ftz.f32x2 %0, x, y, %0;\n}\n"
+        : "+l"(acc)
+        : "f"(lo), "f"(hi), "f"(w));
+}
 
+// FAST (the chain's fast mode): the DC-removal FIR's products and sums as
+// fused multiply-adds, to a stated tolerance rather than the reference's bits.
+template <bool FAST>
 __global__ void __launch_bounds__(kRxThreads)
 k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, uint32_t window_cap, uint32_t* queue,
                  const uint32_t* dyn) {
@@ -325,10 +335,17 @@ k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems,
                     const float4 nz = *reinterpret_cast<const float4*>(v - (int)w - 4);
                     const float4 wt = *reinterpret_cast<const float4*>(dws + w);
                     const float y = nz.w, z = nz.z, u = nz.y;
-                    add_pair(a01, x0 * wt.x, x1 * wt.x); add_pair(a23, x2 * wt.x, x3 * wt.x);
-                    add_pair(a01, y * wt.y, x0 * wt.y); add_pair(a23, x1 * wt.y, x2 * wt.y);
-                    add_pair(a01, z * wt.z, y * wt.z); add_pair(a23, x0 * wt.z, x1 * wt.z);
-                    add_pair(a01, u * wt.w, z * wt.w); add_pair(a23, y * wt.w, x0 * wt.w);
+                    if (FAST) {
+                        fma_pair(a01, x0, x1, wt.x); fma_pair(a23, x2, x3, wt.x);
+                        fma_pair(a01, y, x0, wt.y); fma_pair(a23, x1, x2, wt.y);
+                        fma_pair(a01, z, y, wt.z); fma_pair(a23, x0, x1, wt.z);
+                        fma_pair(a01, u, z, wt.w); fma_pair(a23, y, x0, wt.w);
+                    } else {
+                        add_pair(a01, x0 * wt.x, x1 * wt.x); add_pair(a23, x2 * wt.x, x3 * wt.x);
+                        add_pair(a01, y * wt.y, x0 * wt.y); add_pair(a23, x1 * wt.y, x2 * wt.y);
+                        add_pair(a01, z * wt.z, y * wt.z); add_pair(a23, x0 * wt.z, x1 * wt.z);
+                        add_pair(a01, u * wt.w, z * wt.w); add_pair(a23, y * wt.w, x0 * wt.w);
+                    }
                     x3 = y;
                     x2 = z;
                     x1 = u;
@@ -373,6 +390,9 @@ k_detect_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems,
 
 // ---- audio FIR with decimation, mono or stereo ----------------------------
 
+// FAST (the chain's fast mode): the mono FIR's products and sums as fused
+// multiply-adds.
+template <bool FAST>
 __global__ void __launch_bounds__(kRxThreads)
 k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, float* __restrict__ audio,
                 uint32_t window_cap, uint32_t weights_cap, uint32_t* queue, const uint32_t* dyn) {
@@ -495,10 +515,17 @@ k_audio_batched(const RxDev* __restrict__ rxs, SpanList spans, uint32_t nitems, 
                 for (uint32_t k = 0; k < nq; ++k) {
                     const float4 s4 = *reinterpret_cast<const float4*>(sq - 4u * k);
                     const float4 w4 = *reinterpret_cast<const float4*>(wq + 4u * k);
-                    acc = acc + s4.w * w4.x;
-                    acc = acc + s4.z * w4.y;
-                    acc = acc + s4.y * w4.z;
-                    acc = acc + s4.x * w4.w;
+                    if (FAST) {
+                        acc = __fmaf_rn(s4.w, w4.x, acc);
+                        acc = __fmaf_rn(s4.z, w4.y, acc);
+                        acc = __fmaf_rn(s4.y, w4.z, acc);
+                        acc = __fmaf_rn(s4.x, w4.w, acc);
+                    } else {
+                        acc = acc + s4.w * w4.x;
+                        acc = acc + s4.z * w4.y;
+                        acc = acc + s4.y * w4.z;
+                        acc = acc + s4.x * w4.w;
+                    }
                 }
                 for (uint32_t t = hp + 4u * nq; t < Ta; ++t) {
                     const float term = v[-(int)t] * w[t];
@@ -585,22 +612,30 @@ int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem*
 }
 
 int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, SpanList items, uint32_t nitems,
-                              uint32_t window_cap, uint32_t* queue, const uint32_t* dyn) {
+                              uint32_t window_cap, uint32_t* queue, const uint32_t* dyn, bool fast) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)(window_cap + 4096u) * sizeof(float);  // window + DC weights
-    if (int32_t st = set_shared((const void*)k_detect_batched, shared)) return st;
-    const unsigned grid = persistent_grid((const void*)k_detect_batched, kRxThreads, shared, dyn ? ~0u : nitems);
-    k_detect_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap, queue, dyn);
+    const void* kern = fast ? (const void*)k_detect_batched<true> : (const void*)k_detect_batched<false>;
+    if (int32_t st = set_shared(kern, shared)) return st;
+    const unsigned grid = persistent_grid(kern, kRxThreads, shared, dyn ? ~0u : nitems);
+    if (fast)
+        k_detect_batched<true><<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap, queue, dyn);
+    else
+        k_detect_batched<false><<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, window_cap, queue, dyn);
     return cuda_status(cudaGetLastError(), "detect batched");
 }
 
 int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, SpanList items, uint32_t nitems, float* audio,
-                             uint32_t window_cap, uint32_t weights_cap, uint32_t* queue, const uint32_t* dyn) {
+                             uint32_t window_cap, uint32_t weights_cap, uint32_t* queue, const uint32_t* dyn, bool fast) {
     if (nitems == 0) return RV_OK;
     const size_t shared = (size_t)(window_cap + weights_cap) * sizeof(float);  // window, then the weights
-    if (int32_t st = set_shared((const void*)k_audio_batched, shared)) return st;
-    const unsigned grid = persistent_grid((const void*)k_audio_batched, kRxThreads, shared, dyn ? ~0u : nitems);
-    k_audio_batched<<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap, weights_cap, queue, dyn);
+    const void* kern = fast ? (const void*)k_audio_batched<true> : (const void*)k_audio_batched<false>;
+    if (int32_t st = set_shared(kern, shared)) return st;
+    const unsigned grid = persistent_grid(kern, kRxThreads, shared, dyn ? ~0u : nitems);
+    if (fast)
+        k_audio_batched<true><<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap, weights_cap, queue, dyn);
+    else
+        k_audio_batched<false><<<grid, kRxThreads, shared, s>>>(rxs, items, nitems, audio, window_cap, weights_cap, queue, dyn);
     return cuda_status(cudaGetLastError(), "audio batched");
 }
 

@@ -209,12 +209,13 @@ int32_t launch_fine_tc(cudaStream_t s, const RxDev* rxs, const FineTile* tiles, 
                        uint32_t* queue, const uint32_t* dyn, uint32_t* status);
 int32_t launch_carrier_batched(cudaStream_t s, const RxDev* rxs, const WorkItem* items, uint32_t nitems,
                                const uint32_t* dyn = nullptr);
+// fast: fused multiply-adds in the DC-removal FIR (the chain's fast mode)
 int32_t launch_detect_batched(cudaStream_t s, const RxDev* rxs, SpanList spans, uint32_t nitems,
-                              uint32_t window_cap, uint32_t* queue, const uint32_t* dyn = nullptr);
+                              uint32_t window_cap, uint32_t* queue, const uint32_t* dyn = nullptr, bool fast = false);
 // weights_cap: floats of demodulator weights staged per CTA (the largest
 // table among the receivers: audio taps, or the whole stereo table)
 int32_t launch_audio_batched(cudaStream_t s, const RxDev* rxs, SpanList spans, uint32_t nitems,
                              float* audio, uint32_t window_cap, uint32_t weights_cap, uint32_t* queue,
-                             const uint32_t* dyn = nullptr);
+                             const uint32_t* dyn = nullptr, bool fast = false);
 
 }  // namespace rv

@@ -1,9 +1,10 @@
 """Fast mode (rv_chain_create with RV_CHAIN_FAST): the batched chain with the
 fine stage as split-precision BF16 GEMMs on the tensor cores (hi*hi + hi*lo +
-lo*hi products accumulated in FP32). It is a tolerance mode, not a bit-exact
-one, so it is checked against the bit-exact batched chain (itself pinned to
-the oracle chain bit for bit in test_gpu_chain_c3.py) on the benchmark's own
-receiver mix, to the tolerances stated here:
+lo*hi products accumulated in FP32) and the DC-removal and mono audio FIRs as
+fused multiply-adds. It is a tolerance mode, not a bit-exact one, so it is
+checked against the bit-exact batched chain (itself pinned to the oracle
+chain bit for bit in test_gpu_chain_c3.py) on the benchmark's own receiver
+mix, to the tolerances stated here:
 
 * every receiver's fine ring within FINE_REL_MAX relative RMS;
 * per demodulation mode, the median receiver's audio within AUDIO_REL_MEDIAN
