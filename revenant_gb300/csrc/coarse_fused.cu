@@ -270,6 +270,143 @@ int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, cons
     return cuda_status(cudaGetLastError(), "coarse_fused launch");
 }
 
+// ---- any grid of up to 1024 channels and M/D <= 4 (C2's M = 1024, D = 512,
+// T = 16 among them), grid sizes given at run time. A CTA takes batches of
+// kWideB * P consecutive blocks (P = M/D block phases), one thread per branch
+// r. Block b + P is one polyphase row later than block b, so for each phase
+// the thread loads its T - 1 older samples once and then one new sample per
+// block, keeping the window in registers (each raw sample is read and
+// converted once per phase and batch, plus the warm-up). Branch outputs go
+// straight to their bit-reversed slots in shared memory; the batch's
+// transforms then run the reference's radix-2 DIT stages together (the same
+// butterflies as the plain kernel), and each channel's slots of the batch are
+// phase-corrected and written as one contiguous run of the channel-major
+// ring: every output's operations as in the plain path.
+constexpr uint32_t kWideB = 4;  // consecutive blocks of one phase in a batch
+
+template <int T, int FMT, bool FE>
+__global__ void __launch_bounds__(1024, 1)
+k_coarse_wide(const uint32_t* __restrict__ raw, const float* __restrict__ taps, const rv_cf32* __restrict__ tw_g,
+              rv_cf32* __restrict__ ring, rv_coarse_params p_arg, uint32_t M, uint32_t D, uint32_t stages,
+              const rv_coarse_params* dyn, const FrontEndTable* fe_g) {
+    const rv_coarse_params p = dyn != nullptr ? *dyn : p_arg;
+    const uint32_t P = M / D, NBB = kWideB * P;  // blocks a batch
+    const uint32_t pitch = M + 1u;               // transform rows, padded against bank conflicts
+    const uint32_t batches = (p.block_count + NBB - 1u) / NBB;
+    extern __shared__ float2 smem[];
+    float2* twd = smem;   // [M]
+    float2* x = twd + M;  // [NBB][pitch] the transforms
+    __shared__ FrontEndTable fe_s[1];
+    if (FE) {
+        for (uint32_t i = threadIdx.x; i < sizeof(FrontEndTable) / 4u; i += blockDim.x)
+            reinterpret_cast<uint32_t*>(fe_s)[i] = reinterpret_cast<const uint32_t*>(fe_g)[i];
+    }
+    const FrontEndTable* fe = fe_s;
+    for (uint32_t i = threadIdx.x; i < M; i += blockDim.x) twd[i] = ld_cf32(&tw_g[i]);
+    const uint32_t r = threadIdx.x;  // blockDim.x == M
+    const uint32_t slot_in = brev((M - r) & (M - 1u), stages);
+    const uint32_t window_start = p.base_offset - (M * (uint32_t)T - 1u);
+    float h[T];
+#pragma unroll
+    for (int q = 0; q < T; ++q) h[q] = taps[(uint32_t)q * M + r];
+    __syncthreads();
+    for (uint32_t batch = blockIdx.x; batch < batches; batch += gridDim.x) {
+        const uint32_t blk0 = batch * NBB;
+        const uint32_t nb = (p.block_count - blk0 < NBB) ? p.block_count - blk0 : NBB;
+        // ---- branch FIR, phase by phase: blocks blk0 + ph + j P, j < kWideB
+        for (uint32_t ph = 0; ph < P; ++ph) {
+            const uint32_t n0 = p.base_offset + (blk0 + ph) * D - r;  // newest sample (q = 0) of j = 0
+            float2 win[T];
+#pragma unroll
+            for (int q = 1; q < T; ++q) win[T - q] = load_sample<FMT, FE>(raw, n0 - (uint32_t)q * M, p, window_start, fe);
+#pragma unroll
+            for (int j = 0; j < (int)kWideB; ++j) {
+                win[j] = load_sample<FMT, FE>(raw, n0 + (uint32_t)j * M, p, window_start, fe);
+                float2 acc = make_float2(0.0F, 0.0F);
+#pragma unroll
+                for (int q = 0; q < T; ++q) mac(acc, win[(j - q + T) % T], h[q]);
+                const uint32_t lb = ph + (uint32_t)j * P;  // block within the batch
+                if (lb < nb) x[lb * pitch + slot_in] = acc;
+            }
+        }
+        __syncthreads();
+        // ---- the batch's transforms, each stage for all of them
+        const uint32_t half_m = M >> 1;  // butterflies a transform a stage (a power of two)
+        for (uint32_t st = 0; st < stages; ++st) {
+            const uint32_t half = 1u << st, step = M >> (st + 1u);
+            for (uint32_t u = r; u < nb * half_m; u += M) {
+                float2* xb = x + (u >> (stages - 1u)) * pitch;
+                const uint32_t bf = u & (half_m - 1u);
+                const uint32_t jj = bf & (half - 1u);
+                const uint32_t ia = ((bf >> st) << (st + 1u)) + jj;
+                butterfly(xb[ia], xb[ia + half], twd[jj * step]);
+            }
+            __syncthreads();
+        }
+        // ---- phase correction and write-out: each channel's slots together
+        // (NBB a power of two: kWideB times a power-of-two P)
+        const uint32_t nbb_log2 = 31u - (uint32_t)__clz(NBB);
+        for (uint32_t e = r; e < M * NBB; e += M) {
+            const uint32_t k = e >> nbb_log2, lb = e & (NBB - 1u);
+            if (lb >= nb) continue;
+            const uint32_t m_abs = p.block_base + blk0 + lb;
+            const uint32_t dm = ((m_abs & (M - 1u)) * D) & (M - 1u);
+            float2 v = x[lb * pitch + k];
+            if (D != M) v = cmul(v, twd[(k * dm) & (M - 1u)]);
+            st_cf32(&ring[(uint64_t)k * p.out_ring_blocks + (m_abs & p.out_ring_mask)], v);
+        }
+        __syncthreads();  // the transforms are read before the next batch's branch outputs land
+    }
+}
+
+bool coarse_wide_supported(const rv_grid_params& g) {
+    const uint32_t M = g.channels;
+    return M >= 32u && M <= 1024u && (M & (M - 1u)) == 0u && g.decimation != 0u && M % g.decimation == 0u &&
+           M / g.decimation <= 4u && (g.taps_per_branch == 16u || g.taps_per_branch == 17u);
+}
+
+template <int T, int FMT, bool FE>
+int32_t launch_wide(cudaStream_t stream, const rv_grid_params& g, const uint32_t* raw, const float* taps,
+                    const rv_cf32* tw, rv_cf32* ring, const rv_coarse_params& p, const rv_coarse_params* dyn,
+                    const FrontEndTable* fe) {
+    const uint32_t M = g.channels, D = g.decimation, P = M / D;
+    uint32_t stages = 0;
+    while ((1u << stages) < M) ++stages;
+    const size_t shared = sizeof(float2) * ((size_t)M + (size_t)kWideB * P * (M + 1u));
+    auto kern = k_coarse_wide<T, FMT, FE>;
+    if (shared > 48u * 1024u)
+        if (int32_t st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared),
+                                     "coarse wide shared"))
+            return st;
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (int32_t st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)M, shared),
+                                 "coarse wide occupancy"))
+        return st;
+    const uint32_t max_grid = (uint32_t)(per_sm > 0 ? per_sm : 1) * (uint32_t)sms;
+    const uint32_t NBB = kWideB * P;
+    const uint32_t batches = (p.block_count + NBB - 1u) / NBB;
+    const uint32_t grid = dyn != nullptr ? max_grid : (batches < max_grid ? batches : max_grid);
+    kern<<<grid, M, shared, stream>>>(raw, taps, tw, ring, p, M, D, stages, dyn, fe);
+    return cuda_status(cudaGetLastError(), "coarse wide launch");
+}
+
+template <int T>
+int32_t dispatch_wide(cudaStream_t stream, const rv_grid_params& g, int32_t format, const uint32_t* raw,
+                      const float* taps, const rv_cf32* tw, rv_cf32* ring, const rv_coarse_params& p,
+                      const rv_coarse_params* dyn, const FrontEndTable* fe) {
+    if (format == RV_FORMAT_CS16)
+        return fe ? launch_wide<T, RV_FORMAT_CS16, true>(stream, g, raw, taps, tw, ring, p, dyn, fe)
+                  : launch_wide<T, RV_FORMAT_CS16, false>(stream, g, raw, taps, tw, ring, p, dyn, fe);
+    if (format == RV_FORMAT_CU8)
+        return fe ? launch_wide<T, RV_FORMAT_CU8, true>(stream, g, raw, taps, tw, ring, p, dyn, fe)
+                  : launch_wide<T, RV_FORMAT_CU8, false>(stream, g, raw, taps, tw, ring, p, dyn, fe);
+    if (format == kFormatCf32Ring && fe == nullptr)
+        return launch_wide<T, kFormatCf32Ring, false>(stream, g, raw, taps, tw, ring, p, dyn, fe);
+    return set_error_fmt(RV_ERR_UNSUPPORTED, "coarse_fused: format %d", format);
+}
+
 // Source samples [from, from + count) of the raw ring converted into the cf32
 // ring at the same slots, each corrected with the parameters of the run it
 // arrived in (the table's entries are relative to window_start), exactly as
@@ -322,7 +459,7 @@ int32_t launch_convert_ring(cudaStream_t stream, int32_t format, const void* raw
 bool coarse_fused_supported(const rv_grid_params& g) {
     return (g.channels == 64 && g.taps_per_branch == 17 && g.decimation == 32) ||
            (g.channels == 8 && g.taps_per_branch == 17 && g.decimation == 4) ||
-           (g.channels == 64 && g.taps_per_branch == 17 && g.decimation == 64);
+           (g.channels == 64 && g.taps_per_branch == 17 && g.decimation == 64) || coarse_wide_supported(g);
 }
 
 // Dispatch over the instantiated grids. Returns RV_ERR_UNSUPPORTED for a
@@ -346,6 +483,10 @@ int32_t launch_coarse_fused(cudaStream_t stream, const rv_grid_params& g, int32_
     RV_COARSE_CASE(8, 17, 4, 8)
     RV_COARSE_CASE(64, 17, 64, 2)
 #undef RV_COARSE_CASE
+    if (coarse_wide_supported(g)) {
+        if (g.taps_per_branch == 16u) return dispatch_wide<16>(stream, g, format, w, taps, tw, ring, p, dyn, fe);
+        return dispatch_wide<17>(stream, g, format, w, taps, tw, ring, p, dyn, fe);
+    }
     return set_error_fmt(RV_ERR_UNSUPPORTED,
                          "coarse_fused: no fused kernel for M=%u T=%u D=%u format %d in this build (use the plain launches)",
                          g.channels, g.taps_per_branch, g.decimation, format);

@@ -1,10 +1,10 @@
 """C2's grid in the chain: M = 1024 channels, D = 512, T = 16 (a 16,384-tap
-prototype) at 61.44 MS/s cs16, a grid no fused channelizer kernel is built
-for. The batched chain then runs the reference's branch and FFT dispatches
-over its cf32 ring and keeps the receivers batched; its audio must equal the
+prototype) at 61.44 MS/s cs16, which the generic fused channelizer kernel
+covers (grids sized at run time). The batched chain's audio must equal the
 plain chain's bit for bit, and the plain chain's the oracle chain's, across
-runs of uneven sizes; with impulse excision on as well. A captured graph is
-refused for this grid.
+runs of uneven sizes; with impulse excision on as well (the fused kernel then
+reads the cleaned cf32 ring); and the chain replayed from a captured graph
+must equal it directly launched.
 """
 import numpy as np
 import pytest
@@ -83,8 +83,13 @@ def test_c2_batched_chain_matches_plain(gpu, capture, excise_at):
     assert_same(outs[0], outs[1], "batched vs plain")
 
 
-def test_c2_capture_graph_is_refused(gpu):
-    ch, _ = make(gpu, abi.CHAIN_BATCHED)
-    with pytest.raises(Exception):
-        ch.capture_graph()
-    ch.close()
+def test_c2_captured_chain_matches_direct(gpu, capture):
+    outs = []
+    for graph in (False, True):
+        ch, ids = make(gpu, abi.CHAIN_BATCHED)
+        if graph:
+            ch.capture_graph()
+        feed(ch, capture)
+        outs.append(audio_of(ch, ids))
+        ch.close()
+    assert_same(outs[0], outs[1], "captured vs direct")

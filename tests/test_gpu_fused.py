@@ -75,6 +75,12 @@ CASES = [
     (8, 17, 4, abi.FORMAT_CU8, 16, 9000, (1 << 16) - 3, 11),
     (8, 17, 4, abi.FORMAT_CS16, 14, 3000, 17, 0),
     (64, 17, 64, abi.FORMAT_CS16, 17, 1500, 4321, 5),
+    # grids without a hand-instantiated kernel: the generic one (C2's grid first)
+    (1024, 16, 512, abi.FORMAT_CS16, 18, 300, 777, 5),
+    (1024, 16, 512, abi.FORMAT_CU8, 18, 257, (1 << 18) - 1000, 0xFFFFFFF0, 16383),
+    (128, 17, 64, abi.FORMAT_CU8, 16, 500, 0, 0, 2175),
+    (256, 16, 256, abi.FORMAT_CS16, 17, 203, 100, 3),
+    (32, 17, 16, abi.FORMAT_CS16, 15, 1000, 9, 1),
 ]
 
 
@@ -127,9 +133,12 @@ def test_coarse_fused_rejects_and_reports(gpu):
     st = lib().rv_coarse_fused(gpu.stream, C.byref(g), abi.FORMAT_CS16, C.byref(p), d_raw.ptr, raw.nbytes,
                                d_taps.ptr, taps.size, d_tw.ptr, 64, d_out.ptr, 64 * 256)
     assert st == abi.RV_ERR_INVALID and b"history" in lib().rv_last_error()
-    g2 = abi.GridParams(32, 17, 16)
-    st = lib().rv_coarse_fused(gpu.stream, C.byref(g2), abi.FORMAT_CS16, C.byref(abi.CoarseParams(4095, 0, 1, 0, 1, 0)),
-                               d_raw.ptr, raw.nbytes, d_taps.ptr, 32 * 17, d_tw.ptr, 32, d_out.ptr, 64 * 256)
+    # more channels than a CTA has threads: no fused kernel (checked on the
+    # host before anything is launched)
+    g2 = abi.GridParams(2048, 16, 1024)
+    big = gpu.zeros(4 << 16)
+    st = lib().rv_coarse_fused(gpu.stream, C.byref(g2), abi.FORMAT_CS16, C.byref(abi.CoarseParams((1 << 16) - 1, 0, 1, 0, 1, 0)),
+                               big.ptr, 4 << 16, d_taps.ptr, 2048 * 16, d_tw.ptr, 2048, d_out.ptr, 2048)
     assert st == abi.RV_ERR_UNSUPPORTED
 
 
