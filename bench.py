@@ -358,14 +358,15 @@ def run_gb300(args):
                         "chain per receiver (tests/test_gpu_chain_fast.py)"}
 
     plain = None
-    if not args.no_plain:
+    if not args.no_plain and n >= 1 << 21:
         # the reference's recording, one launch per stage per receiver (it
         # recomputes the detector inside every audio tap, as the reference's
         # demodulator does), and the same with the detector hoisted (once per
         # fine sample, still one launch per stage per receiver): the second
         # isolates what batching adds. Both on the same 2^22 samples after a
         # 2^20-sample warm-up, CUDA events on the chain's stream.
-        pn, blk = 1 << 22, 1 << 20
+        blk = 1 << 20
+        pn = min(1 << 22, (n - blk) // blk * blk)  # within the capture
 
         def plain_leg(mode):
             pch = make_chain(mode, blk)
@@ -384,7 +385,7 @@ def run_gb300(args):
                     "launches_per_run": round(pst.launches / max(pst.runs, 1), 1)}
 
         plain = plain_leg(abi.CHAIN_PLAIN)
-        plain["sample"] = "2^22 samples after a 2^20 warm-up, same 256 receivers, CUDA events"
+        plain["sample"] = "%d samples after a 2^20 warm-up, same 256 receivers, CUDA events" % pn
         hoisted = plain_leg(abi.CHAIN_HOISTED)
         hoisted["note"] = ("RV_CHAIN_HOISTED: one launch per stage per receiver with the detector once per fine "
                            "sample; the same audio bit for bit")
@@ -738,7 +739,10 @@ def c2_channelizer(dev, stream, d_codes, reps, hbm_gbs):
     import torch
     from revenant_gb300 import abi
     from revenant_gb300.library import check, lib
-    M, T, D, n = 1024, 16, 512, 1 << 26
+    # 2^26 samples, or the whole capture when it is shorter (a power of two:
+    # the raw ring's mask)
+    M, T, D = 1024, 16, 512
+    n = min(1 << 26, 1 << ((d_codes.nbytes // 4).bit_length() - 1))
     g = abi.GridParams(M, T, D)
     taps = np.zeros(M * T, np.float32)
     check(lib().rv_design_prototype(C.byref(g), 120.0, taps.ctypes.data, taps.size, None, None))
@@ -783,7 +787,8 @@ def c2_channelizer(dev, stream, d_codes, reps, hbm_gbs):
     for b in (d_taps, d_tw, ring, branch, chan):
         b.free()
     gbs, gbs_d = 20.0 * n / ms / 1e6, 20.0 * n / ms_d / 1e6
-    return {"workload": "M=1024 D=512 T=16 over 2^26 cs16 samples: the fused channelizer (rv_coarse_fused)",
+    return {"workload": "M=1024 D=512 T=16 over 2^%d cs16 samples: the fused channelizer (rv_coarse_fused)"
+                        % (n.bit_length() - 1),
             "ms": round(ms, 3), "value": round(n / ms / 1e3, 1), "unit": "MS/s", "roofline": {
                 "bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_gbs, "unit": "GB/s",
                 "frac": round(gbs / hbm_gbs, 4), "algorithmic_bytes_per_sample": 20},
