@@ -501,15 +501,8 @@ constexpr uint32_t fwd_smem() {
 
 template <uint32_t NT>
 int32_t launch_fwd(cudaStream_t s, const FwdArgs& f) {
-    static bool configured = false;
-    if (!configured) {
-        if (int32_t st = cuda_status(cudaFuncSetAttribute((const void*)k_gemm_fwd<NT>,
-                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)fwd_smem<NT>()),
-                                     "cnn forward shared memory"))
-            return st;
-        configured = true;
-    }
+    if (int32_t st = ensure_shared((const void*)k_gemm_fwd<NT>, fwd_smem<NT>(), "cnn forward shared memory"))
+        return st;
     const dim3 grid((f.m + kRows - 1u) / kRows, (f.n + NT - 1u) / NT, 1);
     k_gemm_fwd<NT><<<grid, kThreads, fwd_smem<NT>(), s>>>(f);
     return cuda_status(cudaGetLastError(), "cnn forward gemm");
@@ -533,15 +526,7 @@ constexpr uint32_t gemm_smem() {
 
 template <uint32_t NT>
 int32_t launch_gemm(cudaStream_t s, const GemmArgs& g, uint32_t splits) {
-    static bool configured = false;  // per process: the attribute is per function
-    if (!configured) {
-        if (int32_t st = cuda_status(cudaFuncSetAttribute((const void*)k_gemm<NT>,
-                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)gemm_smem<NT>()),
-                                     "cnn gemm shared memory"))
-            return st;
-        configured = true;
-    }
+    if (int32_t st = ensure_shared((const void*)k_gemm<NT>, gemm_smem<NT>(), "cnn gemm shared memory")) return st;
     const dim3 grid((g.m + kRows - 1u) / kRows, (g.n + NT - 1u) / NT, splits);
     k_gemm<NT><<<grid, kThreads, gemm_smem<NT>(), s>>>(g);
     return cuda_status(cudaGetLastError(), "cnn gemm");

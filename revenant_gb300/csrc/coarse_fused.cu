@@ -248,21 +248,14 @@ int32_t launch(cudaStream_t stream, const uint32_t* raw, const float* taps, cons
     constexpr int TILE = S * CB * kChunksPerTile;
     const size_t shared = sizeof(float2) * (M + 2 * S * CB * M);
     auto kern = k_coarse<M, T, D, FMT, S, FE>;
-    static int max_grid = 0;
-    if (max_grid == 0) {
-        if (shared > 48 * 1024) {
-            if (int32_t st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared),
-                                         "coarse shared"))
-                return st;
-        }
-        int per_sm = 0, dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (int32_t st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, shared),
-                                     "coarse occupancy"))
-            return st;
-        max_grid = (per_sm > 0 ? per_sm : 1) * sms;
-    }
+    if (int32_t st = ensure_shared((const void*)kern, shared, "coarse shared")) return st;
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (int32_t st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, shared),
+                                 "coarse occupancy"))
+        return st;
+    const int max_grid = (per_sm > 0 ? per_sm : 1) * sms;
     const uint32_t tiles = (p.block_count + TILE - 1) / TILE;
     // captured: the full resident grid, for whatever block count the run has
     const uint32_t grid = dyn != nullptr ? (uint32_t)max_grid : (tiles < (uint32_t)max_grid ? tiles : (uint32_t)max_grid);
@@ -374,10 +367,7 @@ int32_t launch_wide(cudaStream_t stream, const rv_grid_params& g, const uint32_t
     while ((1u << stages) < M) ++stages;
     const size_t shared = sizeof(float2) * ((size_t)M + (size_t)kWideB * P * (M + 1u));
     auto kern = k_coarse_wide<T, FMT, FE>;
-    if (shared > 48u * 1024u)
-        if (int32_t st = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared),
-                                     "coarse wide shared"))
-            return st;
+    if (int32_t st = ensure_shared((const void*)kern, shared, "coarse wide shared")) return st;
     int per_sm = 0, dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -24,6 +24,15 @@ int32_t clear_error();
 int32_t cuda_status(cudaError_t err, const char* what);
 
 inline bool is_pow2(uint64_t v) { return v != 0 && (v & (v - 1)) == 0; }
+
+// Raises a kernel's dynamic shared memory limit on the current device to
+// `bytes` when it is lower (the attribute is per device and per function).
+inline int32_t ensure_shared(const void* kern, size_t bytes, const char* what) {
+    cudaFuncAttributes attr;
+    if (int32_t st = cuda_status(cudaFuncGetAttributes(&attr, kern), what)) return st;
+    if ((size_t)attr.maxDynamicSharedSizeBytes >= bytes) return 0;
+    return cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes), what);
+}
 inline uint32_t ilog2(uint32_t v) {
     uint32_t s = 0;
     while (s < 31 && (1u << s) < v) ++s;

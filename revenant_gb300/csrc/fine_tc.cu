@@ -435,14 +435,7 @@ int32_t launch_fine_tc_tables(cudaStream_t s, const float2* lerped, uint32_t T, 
 int32_t launch_fine_tc(cudaStream_t s, const RxDev* rxs, const FineTile* tiles, uint32_t ntiles, const float2* chan,
                        uint32_t* queue, const uint32_t* dyn, uint32_t* status) {
     if (ntiles == 0) return RV_OK;
-    static bool configured = false;
-    if (!configured) {
-        if (int32_t st = cuda_status(cudaFuncSetAttribute((const void*)k_fine_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)kSmemWs),
-                                     "fine tc shared memory"))
-            return st;
-        configured = true;
-    }
+    if (int32_t st = ensure_shared((const void*)k_fine_tc, kSmemWs, "fine tc shared memory")) return st;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
