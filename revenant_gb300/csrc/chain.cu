@@ -858,21 +858,6 @@ void push_tiles(std::vector<FineTile>& list, uint32_t rx, const Receiver& r, uin
     }
 }
 
-void push_items(std::vector<WorkItem>& list, uint32_t rx, uint64_t first, uint64_t count, uint32_t per_item,
-                uint64_t out, uint32_t out_stride) {
-    uint64_t done = 0;
-    while (done < count) {
-        const uint32_t n = (uint32_t)std::min<uint64_t>(count - done, per_item);
-        WorkItem w{};
-        w.rx = rx;
-        w.count = n;
-        w.first = first + done;
-        w.out = out + done * out_stride;
-        list.push_back(w);
-        done += n;
-    }
-}
-
 // Fine items carry the exact input index of their first output and its
 // resampler fraction (resample_block, core/dsp/vrx_reference.cpp:2786-2810)
 // so the device does no 64-bit division. Returns the largest window.
